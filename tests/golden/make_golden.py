@@ -1,0 +1,216 @@
+"""Generate golden fixtures by running the reference renderer itself.
+
+The reference (FROL256/diffrender_tutorials) has no golden vectors of its
+own; its tests compare against finite differences only (src/tests.cpp).  This
+script compiles the reference's CPU path (oracle/ref/build_ref.py), runs it
+through oracle/ref/ref_driver.cpp on small seeded scenes and stores inputs and
+outputs as tests/golden/*.npz.  It needs the reference source tree and runs
+in the development container only; the fixtures it writes are committed and
+are all that the tests read.
+
+    python tests/golden/make_golden.py
+"""
+import math
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
+
+import build_ref  # noqa: E402
+import kvio  # noqa: E402
+from diffrender_tutorials_gb300.scene import (Scene, TriangleMesh, Texture, make_cube, make_icosphere,  # noqa: E402
+                                              perturb_vertices, identity4)
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+SIL, VC, TEX, LAMBERT = 1, 2, 3, 4
+
+
+def scene_items(scene):
+    it = {"n_meshes": np.array([len(scene.meshes)], np.int32)}
+    for i, m in enumerate(scene.meshes):
+        p = f"m{i}."
+        it[p + "vertices"] = m.vertices.reshape(-1)
+        it[p + "indices"] = m.indices
+        for name in ("colors", "tc", "normals", "tangents"):
+            a = getattr(m, name)
+            if a is not None:
+                it[p + name] = a.reshape(-1)
+        if m.textures:
+            t = m.textures[0]
+            it[p + "tex"] = t.data
+            it[p + "tex_shape"] = np.array([t.w, t.h, t.channels], np.int32)
+        it[p + "transforms"] = scene.transforms_colmajor(i)
+    return it
+
+
+def cam_items(cams):
+    la = np.array([[*c.origin, *c.target, *c.up, c.width, c.height] for c in cams], np.float32).reshape(-1)
+    fov = np.array([c.fov_rad for c in cams], np.float32)
+    return {"cams_lookat": la, "cams_fov": fov}
+
+
+def run(items):
+    exe = build_ref.build()
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.kv"), os.path.join(d, "out.kv")
+        kvio.save(fin, items)
+        subprocess.check_call([exe, fin, fout])
+        return kvio.load(fout)
+
+
+class Cam:
+    def __init__(self, origin, width, height, fov=math.pi / 4, target=(0, 0, 0), up=(0, 1, 0)):
+        self.origin, self.target, self.up = origin, target, up
+        self.width, self.height, self.fov_rad = width, height, fov
+
+
+def textured_sphere(sub=2, tex_size=16, seed=3):
+    m = make_icosphere(sub, seed=seed)
+    P = m.vertices.astype(np.float64)
+    u = 0.5 + np.arctan2(P[:, 0], P[:, 2]) / (2 * math.pi)
+    v = np.arccos(np.clip(P[:, 1], -1, 1)) / math.pi
+    rng = np.random.default_rng(seed)
+    tex = rng.uniform(0.1, 0.9, size=(tex_size, tex_size, 3)).astype(np.float32)
+    return TriangleMesh(m.vertices, m.indices, tc=np.stack([u, v], 1).astype(np.float32), normals=m.normals,
+                        textures=[Texture(tex_size, tex_size, 3, tex.reshape(-1))])
+
+
+def save(name, **arrays):
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def prefixed(prefix, d):
+    return {prefix + k: v for k, v in d.items()}
+
+
+def main():
+    build_ref.build(verbose=True)
+
+    # -- cameras (CamInfo, common_src/camera.h) ---------------------------
+    cams = [Cam((0, 0, 3), 256, 256), Cam((3 * math.sin(math.pi / 4), 0, 3 * math.cos(math.pi / 4)), 512, 512),
+            Cam((0.3, 1.2, -2.5), 64, 48, fov=0.9), Cam((-3, 0, 0), 1024, 1024)]
+    items = {"task": np.array([0], np.int32), **cam_items(cams)}
+    out = run(items)
+    save("camera", **items, **prefixed("out.", out))
+
+    # -- random streams and Hammersley points -----------------------------
+    seeds = np.array([7777 + k * k + 1 for k in range(14)] + [1, 7, 100], np.int32)
+    items = {"task": np.array([6], np.int32), "prng_seeds": seeds, "prng_count": np.array([64], np.int32)}
+    out = run(items)
+    ham = {}
+    for n in (1, 4, 8, 16, 25, 32):
+        ham[f"ham{n}"] = run({"task": np.array([7], np.int32), "ham_n": np.array([n], np.int32)})["ham"]
+    save("random", **items, **prefixed("out.", out), **ham)
+
+    # -- per-sample nearest hits ------------------------------------------
+    cube = make_cube(seed=1)
+    scene = Scene()
+    scene.add_mesh(cube)
+    tetra = TriangleMesh(np.array([[0, 0, 0], [0.6, 0, 0], [0, 0.6, 0], [0, 0, 0.6]], np.float32) + np.float32(0.2),
+                         np.array([0, 2, 1, 0, 1, 3, 0, 3, 2, 1, 2, 3], np.uint32),
+                         colors=np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0]], np.float32))
+    t1 = identity4(); t1[0, 3] = 0.9; t1[1, 3] = -0.2
+    t2 = identity4(); t2[0, 3] = -1.1; t2[2, 3] = 0.4
+    scene.add_mesh(tetra, [t1, t2])
+    cam = Cam((0.4, 0.7, 3.0), 64, 64)
+    rng = np.random.default_rng(5)
+    g = (np.arange(64) + 0.5)
+    grid = np.stack(np.meshgrid(g, g), -1).reshape(-1, 2)
+    xy = np.concatenate([grid, rng.uniform(0, 64, size=(4096, 2))]).astype(np.float32)
+    items = {"task": np.array([1], np.int32), **scene_items(scene), **cam_items([cam]), "hit_xy": xy.reshape(-1)}
+    out = run(items)
+    save("hits_cube_instanced", **items, **prefixed("out.", out))
+
+    ico = make_icosphere(3, seed=2)
+    scene = Scene()
+    scene.add_mesh(ico)
+    cam = Cam((0.0, 0.5, 2.8), 96, 96)
+    xy = rng.uniform(0, 96, size=(12000, 2)).astype(np.float32)
+    items = {"task": np.array([1], np.int32), **scene_items(scene), **cam_items([cam]), "hit_xy": xy.reshape(-1)}
+    out = run(items)
+    save("hits_icosphere3", **items, **prefixed("out.", out))
+
+    # -- forward render ---------------------------------------------------
+    scene = Scene()
+    scene.add_mesh(make_cube(seed=1))
+    cams = [Cam((0, 0, 3), 64, 64), Cam((2.0, 1.0, 2.0), 48, 40)]
+    for mode, spp in ((VC, 16), (SIL, 9), (VC, 8)):
+        items = {"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([spp], np.int32),
+                 **scene_items(scene), **cam_items(cams)}
+        out = run(items)
+        save(f"render_cube_m{mode}_spp{spp}", **items, **prefixed("out.", out))
+    ts = Scene()
+    ts.add_mesh(textured_sphere())
+    for mode in (TEX, LAMBERT):
+        items = {"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),
+                 **scene_items(ts), **cam_items([Cam((0.5, 0.8, 2.6), 48, 48)])}
+        out = run(items)
+        save(f"render_sphere_m{mode}", **items, **prefixed("out.", out))
+
+    # -- derivatives ------------------------------------------------------
+    true_cube = make_cube(seed=1)
+    init_cube = perturb_vertices(true_cube, 0.1, seed=11)
+    init_cube.colors = np.clip(true_cube.colors + np.random.default_rng(12).normal(0, 0.1, (8, 3)), 0, 1).astype(np.float32)
+    tscene, iscene = Scene(), Scene()
+    tscene.add_mesh(true_cube)
+    iscene.add_mesh(init_cube)
+    cams = [Cam((0, 0, 3), 64, 64)]
+    tgt = run({"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+               **scene_items(tscene), **cam_items(cams)})["images"]
+    for mode in (VC, SIL):
+        items = {"task": np.array([4], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([16], np.int32),
+                 **scene_items(iscene), **cam_items(cams), "targets": tgt, "edge_samples": np.array([64 * 64], np.int32),
+                 "dmesh_ids": np.array([0], np.int32)}
+        out = run(items)
+        save(f"drc_cube_m{mode}", **items, **prefixed("out.", out))
+
+    # two views, d_render with a given adjoint (accumulation over views)
+    cams2 = [Cam((0, 0, 3), 48, 48), Cam((2.2, 1.0, 1.8), 48, 48)]
+    adj = np.random.default_rng(13).normal(0, 0.5, size=2 * 48 * 48 * 3).astype(np.float32)
+    items = {"task": np.array([3], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+             **scene_items(iscene), **cam_items(cams2), "adjoints": adj, "edge_samples": np.array([3000], np.int32),
+             "dmesh_ids": np.array([0], np.int32)}
+    out = run(items)
+    save("drender_cube_2views", **items, **prefixed("out.", out))
+
+    # textured sphere: texture derivatives (TEXTURE_COLOR) and Lambert
+    tsph = textured_sphere()
+    isph = tsph.copy()
+    isph.textures[0].data[:] = 0.5
+    isph.vertices = perturb_vertices(tsph, 0.02, seed=21).vertices
+    tsc, isc = Scene(), Scene()
+    tsc.add_mesh(tsph)
+    isc.add_mesh(isph)
+    cams = [Cam((0.5, 0.8, 2.6), 40, 40)]
+    for mode in (TEX, LAMBERT):
+        tg = run({"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),
+                  **scene_items(tsc), **cam_items(cams)})["images"]
+        items = {"task": np.array([4], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),
+                 **scene_items(isc), **cam_items(cams), "targets": tg, "edge_samples": np.array([1600], np.int32),
+                 "dmesh_ids": np.array([0], np.int32)}
+        out = run(items)
+        save(f"drc_sphere_m{mode}", **items, **prefixed("out.", out))
+
+    # -- optimiser trajectory ("Adam" variant, optimizer_simple.cpp) -------
+    cams = [Cam((0, 0, 3), 32, 32)]
+    tgt = run({"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+               **scene_items(tscene), **cam_items(cams)})["images"]
+    items = {"task": np.array([5], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+             **scene_items(iscene), **cam_items(cams), "targets": tgt, "iters": np.array([6], np.int32),
+             "opt_alg": np.array([4], np.int32), "opt_pos_lr": np.array([0.01], np.float32),
+             "opt_base_lr": np.array([0.01], np.float32), "opt_flags": np.array([1 | 4], np.int32),
+             "dmesh_ids": np.array([0], np.int32)}
+    out = run(items)
+    save("optimize_cube_vc", **items, **prefixed("out.", out))
+
+
+if __name__ == "__main__":
+    main()
