@@ -1,0 +1,336 @@
+#!/usr/bin/env python3
+"""Benchmark: forward+adjoint optimisation iterations per second.
+
+Workload (default): the icosphere configuration -- 2,562 vertices / 5,120
+triangles, point light (3,3,3) intensity 10 with per-vertex albedo, 8 ring
+cameras at distance 3, 512x512, 16 spp, W*H edge samples per view, FP32.
+One step = one optimiser iteration over all 8 views: forward render, MSE
+loss + adjoint, interior adjoint, edge sampling, the reference's "Adam"
+update and the LBVH refit (d_render_and_compare + OptStep + OptUpdateScene
+of src/optimizer_simple.cpp).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl drgb|reference]
+                    [--workload icosphere|cube]
+
+value: iterations/s with everything resident on the GPU (optimiser graph
+replays timed with CUDA events on the renderer stream; L2 flushed before
+every step).  e2e: the same metric through the public C-ABI call
+drgb_d_render_and_compare with host buffers (targets H2D, gradient + loss
+D2H inside the timed region).  The reference arm times the reference
+algorithm's CPU implementation (the oracle port; the reference itself cannot
+be built on the GPU host) on a bounded sample and extrapolates linearly in
+pixels x views.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "icosphere": dict(name="icosphere5120_pointlight_8views_512x512_16spp", sub=4, mode=16, spp=16, res=512,
+                      views=8, sample_res=64, sample_views=1),
+    "cube": dict(name="cube12_vertexcolor_1view_256x256_16spp", sub=None, mode=2, spp=16, res=256, views=1,
+                 sample_res=256, sample_views=1),
+}
+
+
+def make_problem(w):
+    import diffrender_tutorials_gb300 as D
+    if w["sub"] is None:
+        true = D.make_cube(seed=1)
+        init = D.perturb_vertices(true, 0.1, seed=2)
+        init.colors = np.clip(true.colors + np.random.default_rng(3).normal(0, 0.1, (8, 3)), 0, 1).astype(np.float32)
+        cams = [D.CamInfo(origin=(0, 0, 3), width=w["res"], height=w["res"])]
+    else:
+        true = D.make_icosphere(w["sub"], seed=1)
+        init = D.perturb_vertices(true, 0.02, seed=2, radial=True)
+        cams = D.ring_cameras(w["views"], 3.0, w["res"], w["res"])
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(true)
+    isc.add_mesh(init)
+    return ts, isc, cams
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)])
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(w, reps=1):
+    """Oracle (CPU port of the reference algorithm) on a bounded sample:
+    returns (seconds per full-workload iteration, extrapolation factor, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    import diffrender_tutorials_gb300 as D
+    ts, isc, cams = make_problem(w)
+    sres, sv = w["sample_res"], w["sample_views"]
+    scams = [D.CamInfo(origin=c.origin, target=c.target, up=c.up, width=sres, height=sres) for c in cams[:sv]]
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    tgt = O.render(ts, scams, w["mode"], w["spp"])
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.d_render_and_compare(isc, scams, w["mode"], w["spp"], tgt, sres * sres)
+    dt = (time.perf_counter() - t0) / reps
+    factor = (w["res"] * w["res"] * w["views"]) / (sres * sres * sv)
+    return dt * factor, factor, cores, f"{sv} view(s) at {sres}x{sres} of the same scene, extrapolated x{factor:g}"
+
+
+def reference_arm(args, w, ws, rank, pg):
+    if rank != 0:
+        return
+    # warm-up then timed samples; each step is one bounded sample
+    for _ in range(args.warmup):
+        cpu_sample(w)
+    times = []
+    for _ in range(args.steps):
+        t, factor, cores, desc = cpu_sample(w)
+        times.append(t)
+    mean = sum(times) / len(times)
+    val = 1.0 / mean
+    line = {"impl": "reference", "metric": "fwd+adjoint iters/s", "value": val, "unit": "iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["name"], "parallelism": "replicas"},
+            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": cores, "kind": "port",
+                             "sample": desc + " (brute-force caster, 14-block reduction replay)"},
+            "e2e": {"value": val, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def read_traffic():
+    """Per-launch DRAM bytes of the pixel kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_pixels_icosphere_traffic.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def drgb_arm(args, w, ws, rank, local, pg):
+    import torch
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(local)
+    ts, isc, cams = make_problem(w)
+    S = D.SHADING_MODEL(w["mode"])
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
+    r.commit(ts)
+    targets = r.render(ts, cams)
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.01)
+    p.base_lr = 0.01
+    p.flags = D.OptimizerParameters._OPT_POS | D.OptimizerParameters._OPT_COL
+    opt = D.CreateSimpleOptimizer()
+    opt.Init(isc, r, cams, targets, p)
+    stream = torch.cuda.ExternalStream(r.stream(), device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        opt.run_async(1)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(pg)
+    torch.cuda.synchronize()
+    k0 = D.kernel_launches()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.zero_()  # L2 flush (256 MiB write) outside the timed events
+                starts[i].record(stream)
+                opt.run_async(1)
+                ends[i].record(stream)
+        torch.cuda.synchronize()
+    launches = D.kernel_launches() - k0 - 0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = allmax(pg, sum(step_ms))
+    barrier(pg)
+    value = ws * args.steps / (total_ms / 1e3)
+    losses = opt.losses
+
+    # e2e: the public C-ABI call with host buffers (pinned), one call per step
+    r2 = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
+    r2.commit(isc)
+    tg_pinned = torch.empty(targets.size, dtype=torch.float32, pin_memory=True).numpy()
+    tg_pinned[:] = targets.reshape(-1)
+    ds = D.DScene(r2, [0])
+    ds.data = torch.zeros(ds.data.size, dtype=torch.float32, pin_memory=True).numpy()
+    edge_samples = w["res"] * w["res"]
+    for _ in range(max(1, args.warmup)):
+        r2.d_render_and_compare(isc, cams, tg_pinned, edge_samples, ds)
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r2.d_render_and_compare(isc, cams, tg_pinned, edge_samples, ds)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = allmax(pg, sum(e2e_ms))
+    e2e_value = ws * args.steps / (e2e_total / 1e3)
+    h2d = tg_pinned.nbytes + 168 * len(cams)
+    d2h = ds.data.nbytes + 4
+
+    # roofline of the dominant kernel (fused forward/adjoint pixel kernel)
+    prof = opt.profile(3)
+    work = opt.count_work()
+    clocks = clk.summary()
+    import json as _j
+    peaks = {}
+    try:
+        peaks = _j.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    npix = w["res"] * w["res"] * w["views"]
+    # algorithmic bytes of one pixel-kernel launch: targets read (12 B/px),
+    # adjoint written (16 B/px), scene data read once (pos/col/nrm/tc 56 B/vertex,
+    # triangles+indices 64 B/triangle, nodes 64 B/node), gradients written
+    n_tri = sum(m.face_count for m in isc.meshes)
+    n_v = sum(m.vertex_count for m in isc.meshes)
+    alg_bytes = npix * (12 + 16) + n_v * 56 + n_tri * (64 + 64) + n_v * 24
+    px_s = prof["pixels"] / 1e3
+    ach = alg_bytes / px_s / 1e9
+    traffic = read_traffic()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clocks.get("sm_mhz") or 1900.0
+    fp32_peak = sms * 128 * sm_mhz * 1e6 / 1e12  # T lane-ops/s, FMA counted once
+    # FP32 lane-ops: 18 per slab test, 61 per Moller-Trumbore test, ~60 per
+    # ray for generation/shading, ~120 per shaded edge sample (edge_grad etc.)
+    ops = 18 * work["box_tests"] + 61 * work["tri_tests"] + 60 * work["rays"] + 120 * work["edge_samples"]
+    iter_s = prof["total"] / 1e3
+    line = {
+        "metric": "fwd+adjoint iters/s", "value": value, "unit": "iters/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere/cube, rendered targets)",
+        "config": {"workload": w["name"], "triangles": n_tri, "vertices": n_v, "resolution": w["res"],
+                   "views": w["views"], "spp": w["spp"], "edge_samples_per_view": edge_samples,
+                   "shading": S.name, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": "replicas", "step": "d_render_and_compare + Adam + LBVH refit (CUDA graph)"},
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "api": "drgb_d_render_and_compare (host pointers, pinned)",
+                "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
+        "gpu_launches": int(launches),
+        "phases_ms": prof,
+        "work_per_iter": work,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                     "traffic": traffic, "kernel": "k_pixels (forward+loss+interior adjoint)",
+                     "note": "algorithmic bytes / CUDA-event time of the pixel phase; the kernel is bound by FP32 "
+                             "issue and latency, see roofline_fp32"},
+        "roofline_fp32": {"bound": "fp32", "achieved": ops / iter_s / 1e12, "peak": fp32_peak, "unit": "Tops/s",
+                          "frac": ops / iter_s / 1e12 / fp32_peak,
+                          "peak_source": "nominal: SMs x 128 FP32 lanes x median sampled SM clock "
+                                         "(MEASURED_PEAKS.json has no FP32 figure)",
+                          "ops_per_iter": ops},
+        "final_loss": losses[-1] if losses else None,
+    }
+    if ws == 1 and rank == 0 and not args.no_cpu_baseline:
+        t, factor, cores, desc = cpu_sample(w)
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "iters/s", "cores": cores, "kind": "port",
+                                "sample": desc + " (oracle: brute-force caster, CPU port of the reference path)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="drgb", choices=["drgb", "reference"])
+    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 1)
+    w = WORKLOADS[args.workload]
+    ws, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, w, ws, rank, pg)
+    else:
+        drgb_arm(args, w, ws, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

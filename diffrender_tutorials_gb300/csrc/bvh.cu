@@ -1,0 +1,370 @@
+// Scene flattening and the device-built LBVH.
+//
+// prepare_scene() is the device counterpart of Scene::prepare_for_render
+// (common_src/scene_utils.cpp:98-173): it applies each instance transform to
+// its mesh, transforms normals by the inverse transpose, and then writes the
+// triangles the caster tests.  Those are transformed once more by their
+// instance transform, as BruteForce3D::GetNearestHit does
+// (raytrace_src/raytrace3d_bf.cpp:116-125); for identity transforms this is
+// exact.  Each triangle is stored as (A, B-A, C-A): the same differences the
+// caster forms, so the intersection arithmetic is unchanged.
+//
+// build_bvh() builds a linear BVH (Karras 2012: Morton codes of triangle
+// centroids, LSD radix sort, binary radix tree).  Only the topology is built
+// here; refit_bvh() recomputes every box bottom-up and is run after each
+// parameter update, since vertex positions move but the mesh topology does
+// not.  Boxes are padded so that the traversal never culls a triangle the
+// brute-force test would accept.
+#include <algorithm>
+#include <climits>
+
+#include "engine.h"
+
+namespace drgb {
+
+// Per block: its transform and the inverse transpose used for normals.
+__global__ void k_block_tr(const BlockDev* blocks, int n_blocks, const float* const* mesh_tr, float* block_tr) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_blocks) return;
+  const BlockDev bd = blocks[b];
+  const float* tr = mesh_tr[bd.mesh] + 16 * bd.inst;
+  float inv[16];
+  mat_inverse44(tr, inv);
+  float* o = block_tr + 32 * b;
+  for (int i = 0; i < 16; i++) o[i] = tr[i];
+  for (int r = 0; r < 4; r++)
+    for (int c = 0; c < 4; c++) o[16 + 4 * c + r] = inv[4 * r + c];  // transpose
+}
+
+// Flattened vertex arrays (prepare_for_render's per-instance loop).
+__global__ void k_flatten(const int* vblock, int n, const BlockDev* blocks, const MeshSrc* src, const float* block_tr,
+                          float4* pos, float4* orig, float4* col, float4* nrm, float2* tc) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const int b = vblock[g];
+  const BlockDev bd = blocks[b];
+  const int k = g - bd.vert_off;
+  const MeshSrc s = src[bd.mesh];
+  const float* tr = block_tr + 32 * b;
+  const f3 v = mk(s.v[3 * k], s.v[3 * k + 1], s.v[3 * k + 2]);
+  const f3 p = mat_pt(tr, v);
+  pos[g] = make_float4(p.x, p.y, p.z, 0.0f);
+  orig[g] = make_float4(v.x, v.y, v.z, 0.0f);
+  col[g] = s.col ? make_float4(s.col[3 * k], s.col[3 * k + 1], s.col[3 * k + 2], 0.0f) : make_float4(0, 0, 0, 0);
+  if (s.nrm) {
+    const f3 nn = mat_pt(tr + 16, mk(s.nrm[3 * k], s.nrm[3 * k + 1], s.nrm[3 * k + 2]));
+    nrm[g] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+  } else {
+    nrm[g] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  }
+  tc[g] = s.tc ? make_float2(s.tc[2 * k], s.tc[2 * k + 1]) : make_float2(0.0f, 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// LBVH topology.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ f3 traced_vertex(const float4* pos, const float* block_tr, int b, int g) {
+  return mat_pt(block_tr + 32 * b, ld3(pos, g));
+}
+
+__global__ void k_centroid_bounds(const int4* tri_v, int n, const float4* pos, const float* block_tr, float* bounds) {
+  __shared__ float smin[3][256], smax[3][256];
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int4 tv = tri_v[t];
+    const f3 a = traced_vertex(pos, block_tr, tv.w, tv.x);
+    const f3 b = traced_vertex(pos, block_tr, tv.w, tv.y);
+    const f3 c = traced_vertex(pos, block_tr, tv.w, tv.z);
+    const float cx = (a.x + b.x + c.x) * (1.0f / 3.0f), cy = (a.y + b.y + c.y) * (1.0f / 3.0f),
+                cz = (a.z + b.z + c.z) * (1.0f / 3.0f);
+    lo[0] = fminf(lo[0], cx); lo[1] = fminf(lo[1], cy); lo[2] = fminf(lo[2], cz);
+    hi[0] = fmaxf(hi[0], cx); hi[1] = fmaxf(hi[1], cy); hi[2] = fmaxf(hi[2], cz);
+  }
+  for (int a = 0; a < 3; a++) { smin[a][threadIdx.x] = lo[a]; smax[a][threadIdx.x] = hi[a]; }
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int a = 0; a < 3; a++) {
+        smin[a][threadIdx.x] = fminf(smin[a][threadIdx.x], smin[a][threadIdx.x + s]);
+        smax[a][threadIdx.x] = fmaxf(smax[a][threadIdx.x], smax[a][threadIdx.x + s]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int a = 0; a < 3; a++) { bounds[a] = smin[a][0]; bounds[3 + a] = smax[a][0]; }
+}
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__global__ void k_morton(const int4* tri_v, int n, const float4* pos, const float* block_tr, const float* bounds,
+                         uint32_t* keys, int* vals) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int4 tv = tri_v[t];
+  const f3 a = traced_vertex(pos, block_tr, tv.w, tv.x);
+  const f3 b = traced_vertex(pos, block_tr, tv.w, tv.y);
+  const f3 c = traced_vertex(pos, block_tr, tv.w, tv.z);
+  float q[3] = {(a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f), (a.z + b.z + c.z) * (1.0f / 3.0f)};
+  uint32_t code = 0;
+  for (int k = 0; k < 3; k++) {
+    const float ext = bounds[3 + k] - bounds[k];
+    float f = ext > 0.0f ? (q[k] - bounds[k]) / ext : 0.5f;
+    f = fminf(fmaxf(f, 0.0f), 1.0f);
+    const uint32_t xi = min((uint32_t)(f * 1024.0f), 1023u);
+    code |= expand_bits(xi) << (2 - k);
+  }
+  keys[t] = code;
+  vals[t] = t;
+}
+
+// LSD radix sort of (key, value) pairs, 8-bit digits, stable.
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* keys, int n, int shift, uint32_t* hist) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * RS_TILE;
+  for (int i = threadIdx.x; i < RS_TILE; i += RS_THREADS)
+    if (base + i < n) atomicAdd(&h[(keys[base + i] >> shift) & 255u], 1u);
+  __syncthreads();
+  hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of m counts by one block.
+__global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* hist, int m) {
+  __shared__ uint32_t part[1024];
+  const int per = (m + 1023) / 1024;
+  const int b = threadIdx.x * per, e = min(m, b + per);
+  uint32_t s = 0;
+  for (int i = b; i < e; i++) s += hist[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (int i = b; i < e; i++) {
+    const uint32_t v = hist[i];
+    hist[i] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* kin, const int* vin, uint32_t* kout,
+                                                           int* vout, int n, int shift, const uint32_t* hist) {
+  __shared__ uint32_t offs[256];
+  __shared__ uint32_t wcnt[RS_THREADS / 32][257];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  offs[tid] = hist[tid * gridDim.x + blockIdx.x];
+  const int base = blockIdx.x * RS_TILE;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int r = 0; r < RS_ITEMS; r++) {
+    for (int i = tid; i < (RS_THREADS / 32) * 257; i += RS_THREADS) (&wcnt[0][0])[i] = 0u;
+    __syncthreads();
+    const int idx = base + r * RS_THREADS + tid;
+    const bool valid = idx < n;
+    const uint32_t key = valid ? kin[idx] : 0u;
+    const int val = valid ? vin[idx] : 0;
+    const uint32_t digit = valid ? ((key >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t rank = __popc(peers & lt);
+    if ((__ffs(peers) - 1) == lane) wcnt[warp][digit] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t off = offs[digit] + rank;
+      for (int w = 0; w < warp; w++) off += wcnt[w][digit];
+      kout[off] = key;
+      vout[off] = val;
+    }
+    __syncthreads();
+    uint32_t tot = 0;
+    for (int w = 0; w < RS_THREADS / 32; w++) tot += wcnt[w][tid];
+    offs[tid] += tot;
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int lbvh_delta(const uint32_t* keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const unsigned long long a = ((unsigned long long)keys[i] << 32) | (unsigned)i;
+  const unsigned long long b = ((unsigned long long)keys[j] << 32) | (unsigned)j;
+  return __clzll(a ^ b);
+}
+
+// Binary radix tree (Karras 2012, Algorithm 4): internal node i, leaves ~k.
+__global__ void k_karras(const uint32_t* keys, int n, float4* nodes, int* leaf_parent, int* node_parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (lbvh_delta(keys, n, i, i + 1) - lbvh_delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = lbvh_delta(keys, n, i, i - d);
+  int lmax = 2;
+  while (lbvh_delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (lbvh_delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = lbvh_delta(keys, n, i, j);
+  int s = 0;
+  for (int div = 2;; div <<= 1) {
+    const int t = (l + div - 1) / div;
+    if (lbvh_delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t == 1) break;
+  }
+  const int gamma = i + s * d + min(d, 0);
+  const int left = (min(i, j) == gamma) ? ~gamma : gamma;
+  const int right = (max(i, j) == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  nodes[4 * i + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.0f, 0.0f);
+  if (left < 0) leaf_parent[~left] = i; else node_parent[left] = i;
+  if (right < 0) leaf_parent[~right] = i; else node_parent[right] = i;
+  if (i == 0) node_parent[0] = -1;
+}
+
+// ---------------------------------------------------------------------------
+// Leaf triangles + bottom-up refit.
+// ---------------------------------------------------------------------------
+struct Box {
+  float lx, hx, ly, hy, lz, hz;
+};
+
+__device__ __forceinline__ void write_child(float4* nodes, int parent, int slot, const Box& b) {
+  float* n = reinterpret_cast<float*>(nodes + 4 * parent);
+  if (slot == 0) {
+    n[0] = b.lx; n[1] = b.hx; n[2] = b.ly; n[3] = b.hy; n[8] = b.lz; n[9] = b.hz;
+  } else {
+    n[4] = b.lx; n[5] = b.hx; n[6] = b.ly; n[7] = b.hy; n[10] = b.lz; n[11] = b.hz;
+  }
+}
+
+__global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const float4* pos, const float* block_tr,
+                               float4* tri, float4* nodes, const int* leaf_parent, const int* node_parent,
+                               int* counters) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int t = perm[k];
+  const int4 tv = tri_v[t];
+  const f3 A = traced_vertex(pos, block_tr, tv.w, tv.x);
+  const f3 B = traced_vertex(pos, block_tr, tv.w, tv.y);
+  const f3 C = traced_vertex(pos, block_tr, tv.w, tv.z);
+  const f3 e1 = B - A, e2 = C - A;
+  tri[3 * k + 0] = make_float4(A.x, A.y, A.z, __int_as_float(t));
+  tri[3 * k + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+  tri[3 * k + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+  if (n == 1) return;
+  Box b;
+  b.lx = fminf(A.x, fminf(B.x, C.x)); b.hx = fmaxf(A.x, fmaxf(B.x, C.x));
+  b.ly = fminf(A.y, fminf(B.y, C.y)); b.hy = fmaxf(A.y, fmaxf(B.y, C.y));
+  b.lz = fminf(A.z, fminf(B.z, C.z)); b.hz = fmaxf(A.z, fmaxf(B.z, C.z));
+  const float ext = fmaxf(b.hx - b.lx, fmaxf(b.hy - b.ly, b.hz - b.lz));
+  const float mag = fmaxf(fmaxf(fmaxf(fabsf(b.lx), fabsf(b.hx)), fmaxf(fabsf(b.ly), fabsf(b.hy))),
+                          fmaxf(fabsf(b.lz), fabsf(b.hz)));
+  const float pad = ext * 1e-5f + mag * 2e-6f + 1e-20f;
+  b.lx -= pad; b.ly -= pad; b.lz -= pad; b.hx += pad; b.hy += pad; b.hz += pad;
+  int child = ~k;
+  int p = leaf_parent[k];
+  while (p >= 0) {
+    const float4 c = __ldcg(nodes + 4 * p + 3);
+    const int slot = (__float_as_int(c.x) == child) ? 0 : 1;
+    write_child(nodes, p, slot, b);
+    __threadfence();
+    if (atomicAdd(counters + p, 1) == 0) return;  // the sibling finishes this node
+    __threadfence();
+    const float4 n0 = __ldcg(nodes + 4 * p + 0), n1 = __ldcg(nodes + 4 * p + 1), n2 = __ldcg(nodes + 4 * p + 2);
+    b.lx = fminf(n0.x, n1.x); b.hx = fmaxf(n0.y, n1.y);
+    b.ly = fminf(n0.z, n1.z); b.hy = fmaxf(n0.w, n1.w);
+    b.lz = fminf(n2.x, n2.z); b.hz = fmaxf(n2.y, n2.w);
+    child = p;
+    p = node_parent[p];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+void flatten_scene(Job& J, cudaStream_t s) {
+  if (J.n_vertices == 0) return;
+  k_block_tr<<<(J.n_blocks + 63) / 64, 64, 0, s>>>(J.blocks.p, J.n_blocks, J.tr_tab.p, J.block_tr.p);
+  k_flatten<<<(J.n_vertices + 255) / 256, 256, 0, s>>>(J.vblock.p, J.n_vertices, J.blocks.p, J.src_tab.p,
+                                                      J.block_tr.p, J.pos.p, J.orig.p, J.col.p, J.nrm.p, J.tc.p);
+  count_launch(2);
+}
+
+void prepare_scene(Job& J, cudaStream_t s) {
+  flatten_scene(J, s);
+  refit_bvh(J, s);
+}
+
+void commit_scene(Job& J, cudaStream_t s) {
+  flatten_scene(J, s);
+  build_bvh(J, s);
+  refit_bvh(J, s);
+}
+
+void refit_bvh(Job& J, cudaStream_t s) {
+  const int n = J.n_tris;
+  if (n == 0) return;
+  if (n > 1) DRGB_CUDA(cudaMemsetAsync(J.counters.p, 0, sizeof(int) * (n - 1), s));
+  k_leaves_refit<<<(n + 127) / 128, 128, 0, s>>>(J.perm.p, n, J.tri_v.p, J.pos.p, J.block_tr.p, J.tri.p, J.nodes.p,
+                                                 J.leaf_parent.p, J.node_parent.p, J.counters.p);
+  count_launch();
+}
+
+void build_bvh(Job& J, cudaStream_t s) {
+  const int n = J.n_tris;
+  J.tri.alloc(3 * (size_t)std::max(n, 1));
+  J.perm.alloc(std::max(n, 1));
+  J.leaf_parent.alloc(std::max(n, 1));
+  J.nodes.alloc(4 * (size_t)std::max(n - 1, 1));
+  J.node_parent.alloc(std::max(n - 1, 1));
+  J.counters.alloc(std::max(n - 1, 1));
+  if (n == 0) {
+    J.root = INT_MIN;
+    return;
+  }
+  if (n == 1) {
+    J.root = ~0;
+    const int zero = 0, minus1 = -1;
+    DRGB_CUDA(cudaMemcpyAsync(J.perm.p, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.leaf_parent.p, &minus1, sizeof(int), cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  J.root = 0;
+  for (int b = 0; b < 2; b++) {
+    J.sort_keys[b].alloc(n);
+    J.sort_vals[b].alloc(n);
+  }
+  const int tiles = (n + RS_TILE - 1) / RS_TILE;
+  J.sort_hist.alloc(256 * (size_t)tiles);
+  J.bounds.alloc(6);
+  k_centroid_bounds<<<1, 256, 0, s>>>(J.tri_v.p, n, J.pos.p, J.block_tr.p, J.bounds.p);
+  k_morton<<<(n + 255) / 256, 256, 0, s>>>(J.tri_v.p, n, J.pos.p, J.block_tr.p, J.bounds.p, J.sort_keys[0].p,
+                                           J.sort_vals[0].p);
+  count_launch(2);
+  int cur = 0;
+  for (int shift = 0; shift < 32; shift += 8) {
+    k_rs_hist<<<tiles, RS_THREADS, 0, s>>>(J.sort_keys[cur].p, n, shift, J.sort_hist.p);
+    k_rs_scan<<<1, 1024, 0, s>>>(J.sort_hist.p, 256 * tiles);
+    k_rs_scatter<<<tiles, RS_THREADS, 0, s>>>(J.sort_keys[cur].p, J.sort_vals[cur].p, J.sort_keys[cur ^ 1].p,
+                                             J.sort_vals[cur ^ 1].p, n, shift, J.sort_hist.p);
+    count_launch(3);
+    cur ^= 1;
+  }
+  DRGB_CUDA(cudaMemcpyAsync(J.perm.p, J.sort_vals[cur].p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  DRGB_CUDA(cudaMemsetAsync(J.nodes.p, 0, sizeof(float4) * 4 * (n - 1), s));
+  k_karras<<<(n - 1 + 255) / 256, 256, 0, s>>>(J.sort_keys[cur].p, n, J.nodes.p, J.leaf_parent.p, J.node_parent.p);
+  count_launch();
+}
+
+}  // namespace drgb

@@ -1,0 +1,644 @@
+// C ABI of the renderer (include/drgb.h).  Each drgb_renderer owns one job
+// (scene, LBVH, views, gradient and optimiser state) and one CUDA stream.
+// Errors never escape as exceptions: they become negative return codes
+// with a per-thread message (drgb_last_error).
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <memory>
+#include <string>
+
+#include "engine.h"
+
+namespace drgb {
+static std::atomic<int64_t> g_launches{0};
+static thread_local int64_t t_capture_count = 0;
+static thread_local bool t_capturing = false;
+void count_launch(int n) {
+  if (t_capturing) t_capture_count += n;
+  else g_launches += n;
+}
+void add_launches(int64_t n) { g_launches += n; }
+}  // namespace drgb
+
+using namespace drgb;
+
+static thread_local std::string t_err;
+static void set_error(const std::string& m) { t_err = m; }
+
+template <class F>
+static int guard(F&& f) {
+  try {
+    f();
+    return DRGB_OK;
+  } catch (const CudaError& e) {
+    set_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return DRGB_ERR_OOM;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return DRGB_ERR_INVALID;
+  }
+}
+
+static void require(bool c, const char* msg, int code = DRGB_ERR_INVALID) {
+  if (!c) throw CudaError(msg, code);
+}
+
+struct drgb_renderer {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Job job;
+  DevBuf<JobDev> d_job;
+  DevBuf<int4> d_items;
+  DevBuf<int> d_counter;
+  DevBuf<CamDev> d_cam1;
+  DevBuf<float> d_xy;
+  DevBuf<uint32_t> d_u32;
+  DevBuf<float> d_f32;
+  int sm_count = 1;
+  int use_graph = 1;
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_kernels = 0;
+  bool graph_valid = false;
+
+  ~drgb_renderer() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void set_device() const { DRGB_CUDA(cudaSetDevice(device)); }
+  void require_commit() const { require(job.committed, "no scene committed (call drgb_commit first)", DRGB_ERR_STATE); }
+  int px_grid() const { return sm_count * 8; }
+  int edge_grid() const { return sm_count * 8; }
+
+  // Pixel work items for the current views: view-major, tiles row-major.
+  void make_items() {
+    Job& J = job;
+    std::vector<int4> items;
+    for (int v = 0; v < J.n_views; v++) {
+      const int W = (int)J.h_cams[v].width, H = (int)J.h_cams[v].height;
+      for (int y = 0; y < H; y += J.tile_h)
+        for (int x = 0; x < W; x += J.tile_w) items.push_back(make_int4(0, v, x, y));
+    }
+    J.h_pixel_items = items;
+    d_items.upload(items.data(), items.size(), stream);
+    J.loss_part.reserve(std::max<size_t>(1, items.size()));
+    J.dev.item_base = 0;
+    J.dev.item_count = (int)items.size();
+  }
+
+  void views(const drgb_camera* cams, int n, bool same_size) {
+    require(cams != nullptr && n > 0, "need at least one camera");
+    if (same_size)
+      for (int i = 1; i < n; i++)
+        require((int)cams[i].width == (int)cams[0].width && (int)cams[i].height == (int)cams[0].height,
+                "gradient calls need all views of the same size");
+    setup_views(job, cams, n);
+    job.cams.upload(job.h_cams.data(), job.h_cams.size(), stream);
+    std::vector<int64_t> off(n + 1, 0);
+    for (int i = 0; i < n; i++) off[i + 1] = off[i] + (int64_t)cams[i].width * (int64_t)cams[i].height;
+    job.img_off.upload(off.data(), off.size(), stream);
+    make_items();
+  }
+
+  int64_t n_pixels() const {
+    int64_t s = 0;
+    for (auto& c : job.h_cams) s += (int64_t)c.width * (int64_t)c.height;
+    return s;
+  }
+
+  // Buffers of a gradient call over the current views.
+  void gradient_buffers(int edge_samples) {
+    Job& J = job;
+    require(edge_samples >= 0, "edge sample count must be >= 0");
+    const size_t npix = (size_t)J.n_views * J.W * J.H;
+    J.adj.reserve(std::max<size_t>(1, npix));
+    build_edges(J);
+    J.proj.reserve(std::max<size_t>(1, (size_t)J.n_views * J.n_vertices));
+    J.pmf.reserve(std::max<size_t>(1, (size_t)J.n_views * J.n_edges));
+    J.cdf.reserve(std::max<size_t>(1, (size_t)J.n_views * (J.n_edges + 1)));
+    J.queue.reserve(std::max<size_t>(1, (size_t)J.n_views * std::max(edge_samples, 1)));
+    J.dev.edge_samples = edge_samples;
+    J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
+  }
+
+  void push_dev() {
+    JobDev keep = job.dev;
+    sync_dev(job);
+    job.dev.item_base = keep.item_base;
+    job.dev.item_count = keep.item_count;
+    job.dev.edge_samples = keep.edge_samples;
+    job.dev.rnd = keep.rnd;
+    d_job.alloc(1);
+    DRGB_CUDA(cudaMemcpyAsync(d_job.p, &job.dev, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
+  }
+
+  void check_flags() {
+    uint32_t f = 0;
+    DRGB_CUDA(cudaMemcpyAsync(&f, job.err.p, sizeof(f), cudaMemcpyDeviceToHost, stream));
+    DRGB_CUDA(cudaStreamSynchronize(stream));
+    if (f) {
+      DRGB_CUDA(cudaMemsetAsync(job.err.p, 0, sizeof(uint32_t), stream));
+      DRGB_CUDA(cudaStreamSynchronize(stream));
+      std::string m = "kernel error flags " + std::to_string(f);
+      if (f & ERR_STACK_OVERFLOW) m += " (traversal stack overflow)";
+      if (f & ERR_TRAVERSAL_LIMIT) m += " (traversal step limit)";
+      throw CudaError(m, DRGB_ERR_KERNEL);
+    }
+  }
+
+  // Forward + loss + interior adjoint + edges of the current views; grad is
+  // cleared first.  Everything is enqueued on the stream.
+  void enqueue_iteration(bool want_images) {
+    Job& J = job;
+    const bool interior = J.mode != SILHOUETTE;
+    DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
+    int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
+    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream);
+    launch_loss_finalize(d_job.p, 1, stream);
+    if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
+  }
+};
+
+static void check_renderer(drgb_renderer* r) { require(r != nullptr, "null renderer"); }
+
+extern "C" {
+
+int drgb_abi_version(void) { return DRGB_ABI_VERSION; }
+
+int drgb_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return DRGB_ERR_INVALID;
+  std::snprintf(buf, len, "%s", t_err.c_str());
+  return DRGB_OK;
+}
+
+int64_t drgb_kernel_launches(void) { return g_launches.load(); }
+
+int drgb_camera_look_at(const float origin[3], const float target[3], const float up[3], float width, float height,
+                        float fov_rad, float znear, float zfar, drgb_camera* out) {
+  return guard([&] {
+    require(origin && target && up && out, "null argument");
+    camera_look_at(origin, target, up, width, height, fov_rad, znear, zfar, out);
+  });
+}
+
+int drgb_renderer_create(int shading_model, int spp, int device, drgb_renderer** out) {
+  return guard([&] {
+    require(out != nullptr, "null output pointer");
+    *out = nullptr;
+    switch (shading_model) {
+      case DRGB_SILHOUETTE: case DRGB_VERTEX_COLOR: case DRGB_TEXTURE_COLOR: case DRGB_LAMBERT:
+      case DRGB_LAMBERT_POINT_VCOLOR: case DRGB_PATH_DIFFUSE: break;
+      default: throw CudaError("unknown shading model " + std::to_string(shading_model), DRGB_ERR_UNSUPPORTED);
+    }
+    require(spp >= 1 && spp <= 64, "spp must be in [1, 64]");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw CudaError("no CUDA device", DRGB_ERR_NO_DEVICE);
+    require(device >= 0 && device < n, "device index out of range");
+    auto r = std::make_unique<drgb_renderer>();
+    r->device = device;
+    DRGB_CUDA(cudaSetDevice(device));
+    DRGB_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    DRGB_CUDA(cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, device));
+    init_job_model(r->job, shading_model, spp);
+    r->d_counter.alloc(1);
+    *out = r.release();
+  });
+}
+
+int drgb_renderer_destroy(drgb_renderer* r) {
+  if (!r) return DRGB_ERR_INVALID;
+  return guard([&] {
+    cudaSetDevice(r->device);
+    cudaStreamSynchronize(r->stream);
+    delete r;
+  });
+}
+
+void* drgb_renderer_stream(drgb_renderer* r) { return r ? (void*)r->stream : nullptr; }
+
+int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
+  return guard([&] {
+    check_renderer(r);
+    switch (option) {
+      case DRGB_OPT_TRACE_BRUTEFORCE: r->job.trace_bruteforce = value ? 1 : 0; break;
+      case DRGB_OPT_TILE_W:
+      case DRGB_OPT_TILE_H: {
+        const int v = (int)value;
+        require(v >= 1, "tile size must be >= 1");
+        const int tw = option == DRGB_OPT_TILE_W ? v : r->job.tile_w;
+        const int th = option == DRGB_OPT_TILE_H ? v : r->job.tile_h;
+        require(tw * th * r->job.S <= 256, "tile_w*tile_h*samples must be <= 256");
+        r->job.tile_w = tw;
+        r->job.tile_h = th;
+        break;
+      }
+      case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
+      default: throw CudaError("unknown option", DRGB_ERR_INVALID);
+    }
+    r->graph_valid = false;
+  });
+}
+
+int drgb_renderer_set_model_params(drgb_renderer* r, const drgb_model_params* p) {
+  return guard([&] {
+    check_renderer(r);
+    require(p != nullptr, "null params");
+    for (int i = 0; i < 3; i++) r->job.mp.light_pos[i] = p->light_pos[i];
+    r->job.mp.light_intensity = p->light_intensity;
+    r->job.mp.ambient = p->ambient;
+    r->job.mp.path_depth = std::max(0, std::min(16, (int)p->path_depth));
+    r->job.mp.seed = p->seed;
+    r->graph_valid = false;
+  });
+}
+
+int drgb_commit(drgb_renderer* r, const drgb_scene_desc* scene) {
+  return guard([&] {
+    check_renderer(r);
+    r->set_device();
+    Job& J = r->job;
+    upload_scene(J, scene, r->stream);
+    J.opt.active = false;
+    r->graph_valid = false;
+    set_dscene(J, nullptr, 0);
+    commit_scene(J, r->stream);
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int drgb_render(drgb_renderer* r, const drgb_camera* cams, int n_views, float* images) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(images != nullptr, "null image buffer");
+    r->set_device();
+    Job& J = r->job;
+    r->views(cams, n_views, false);
+    const int64_t npx = r->n_pixels();
+    J.images.reserve(3 * (size_t)npx);
+    r->push_dev();
+    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_FWD | PX_IMG,
+                  r->px_grid(), r->stream);
+    DRGB_CUDA(cudaMemcpyAsync(images, J.images.p, sizeof(float) * 3 * npx, cudaMemcpyDeviceToHost, r->stream));
+    r->check_flags();
+  });
+}
+
+int drgb_dscene_layout(drgb_renderer* r, const int32_t* ids, int n_ids, int32_t* layout, int64_t* total) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    std::vector<DLayout> L;
+    const int64_t t = compute_layout(r->job, ids, n_ids, L);
+    if (layout)
+      for (size_t k = 0; k < L.size(); k++) {
+        int32_t* o = layout + 9 * k;
+        o[0] = L[k].vertices; o[1] = L[k].instances; o[2] = L[k].pos_off; o[3] = L[k].color_off;
+        o[4] = L[k].tex_off; o[5] = L[k].tr_off; o[6] = -1; o[7] = L[k].full; o[8] = L[k].mesh_id;
+      }
+    if (total) *total = t;
+  });
+}
+
+int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoints, int n_views,
+                  int edge_samples_in_total, const int32_t* ids, int n_ids, float* dscene) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(adjoints && dscene, "null adjoint or gradient buffer");
+    r->set_device();
+    Job& J = r->job;
+    r->views(cams, n_views, true);
+    set_dscene(J, ids, n_ids);
+    r->gradient_buffers(edge_samples_in_total);
+    const size_t npix = (size_t)n_views * J.W * J.H;
+    J.adj_in.reserve(3 * npix);
+    DRGB_CUDA(cudaMemcpyAsync(J.adj_in.p, adjoints, sizeof(float) * 3 * npix, cudaMemcpyHostToDevice, r->stream));
+    if (J.grad_total > 0)
+      DRGB_CUDA(cudaMemcpyAsync(J.grad.p, dscene, sizeof(float) * J.grad_total, cudaMemcpyHostToDevice, r->stream));
+    r->push_dev();
+    launch_adj_convert(r->d_job.p, (int64_t)npix, r->stream);
+    if (J.mode != SILHOUETTE)
+      launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_ADJ, r->px_grid(),
+                    r->stream);
+    if (edge_samples_in_total > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
+    if (J.grad_total > 0)
+      DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, cudaMemcpyDeviceToHost, r->stream));
+    r->check_flags();
+  });
+}
+
+static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams, const float* targets, int n_views,
+                                      int edge_samples, const int32_t* ids, int n_ids, float* dscene,
+                                      float* out_images, float* loss, bool device_ptrs) {
+  check_renderer(r);
+  r->require_commit();
+  require(targets && dscene, "null target or gradient buffer");
+  r->set_device();
+  Job& J = r->job;
+  r->views(cams, n_views, true);
+  set_dscene(J, ids, n_ids);
+  r->gradient_buffers(edge_samples);
+  const size_t npix = (size_t)n_views * J.W * J.H;
+  const cudaMemcpyKind h2d = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind d2h = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  J.targets.reserve(3 * npix);
+  DRGB_CUDA(cudaMemcpyAsync(J.targets.p, targets, sizeof(float) * 3 * npix, h2d, r->stream));
+  if (out_images) J.images.reserve(3 * npix);
+  r->push_dev();
+  // images are only written when requested
+  JobDev d = J.dev;
+  if (!out_images) d.images = nullptr;
+  DRGB_CUDA(cudaMemcpyAsync(r->d_job.p, &d, sizeof(JobDev), cudaMemcpyHostToDevice, r->stream));
+  r->enqueue_iteration(out_images != nullptr);
+  if (J.grad_total > 0) DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, d2h, r->stream));
+  if (out_images)
+    DRGB_CUDA(cudaMemcpyAsync(out_images, J.images.p, sizeof(float) * 3 * npix, d2h, r->stream));
+  if (loss) DRGB_CUDA(cudaMemcpyAsync(loss, J.loss_out.p, sizeof(float), d2h, r->stream));
+  if (!device_ptrs) r->check_flags();
+  else DRGB_CUDA(cudaStreamSynchronize(r->stream));  // the JobDev staging copy above reads host memory
+}
+
+int drgb_d_render_and_compare(drgb_renderer* r, const drgb_camera* cams, const float* targets, int n_views,
+                              int edge_samples, const int32_t* ids, int n_ids, float* dscene, float* out_images,
+                              float* loss) {
+  return guard([&] {
+    d_render_and_compare_impl(r, cams, targets, n_views, edge_samples, ids, n_ids, dscene, out_images, loss, false);
+  });
+}
+
+int drgb_d_render_and_compare_device(drgb_renderer* r, const drgb_camera* cams, const float* d_targets, int n_views,
+                                     int edge_samples, const int32_t* ids, int n_ids, float* d_dscene,
+                                     float* d_out_images, float* d_loss) {
+  return guard([&] {
+    d_render_and_compare_impl(r, cams, d_targets, n_views, edge_samples, ids, n_ids, d_dscene, d_out_images, d_loss,
+                              true);
+  });
+}
+
+int drgb_cast_rays(drgb_renderer* r, const drgb_camera* cam, const float* xy, int64_t n, uint32_t* prim,
+                   uint32_t* inst, uint32_t* geom, float* t, float* u, float* v) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(cam && xy && prim && inst && geom && t && u && v && n >= 0, "null argument");
+    r->set_device();
+    if (n == 0) return;
+    const CamDev c = make_cam(*cam);
+    r->d_cam1.upload(&c, 1, r->stream);
+    r->d_xy.upload(xy, 2 * (size_t)n, r->stream);
+    r->d_u32.reserve(3 * (size_t)n);
+    r->d_f32.reserve(3 * (size_t)n);
+    r->push_dev();
+    uint32_t* U = r->d_u32.p;
+    float* F = r->d_f32.p;
+    launch_cast(r->d_job.p, r->d_cam1.p, r->d_xy.p, n, U, U + n, U + 2 * n, F, F + n, F + 2 * n, r->stream);
+    DRGB_CUDA(cudaMemcpyAsync(prim, U, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(inst, U + n, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(geom, U + 2 * n, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(t, F, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(u, F + n, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(v, F + 2 * n, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    r->check_flags();
+  });
+}
+
+// ---- optimiser ----------------------------------------------------------------
+
+int drgb_opt_params_default(int alg, drgb_opt_params* p) {
+  return guard([&] {
+    require(p != nullptr, "null params");
+    std::memset(p, 0, sizeof(*p));
+    p->alg = alg;
+    p->decay_period = alg == DRGB_GD_ADAM ? 100 : 25;  // set_default, optimizer_simple.cpp:13-23
+    p->decay_mult = 0.75f;
+    p->base_lr = p->position_lr = p->textures_lr = p->transforms_lr = 0.1f;
+    p->flags = DRGB_OPT_POS | DRGB_OPT_TFM | DRGB_OPT_COL | DRGB_OPT_TEX;
+    p->n_dmesh_ids = 1;
+    p->dmesh_ids[0] = 0;
+  });
+}
+
+int drgb_optimizer_init(drgb_renderer* r, const drgb_scene_desc* scene, const drgb_camera* cams, const float* targets,
+                        int n_views, const drgb_opt_params* p) {
+  return guard([&] {
+    check_renderer(r);
+    require(scene && cams && targets && p, "null argument");
+    require(p->alg >= DRGB_GD_NAIVE && p->alg <= DRGB_GD_ADAM, "unknown optimiser algorithm");
+    require(p->n_dmesh_ids >= 1 && p->n_dmesh_ids <= 16, "need 1..16 differentiable meshes");
+    r->set_device();
+    Job& J = r->job;
+    upload_scene(J, scene, r->stream);
+    set_dscene(J, p->dmesh_ids, p->n_dmesh_ids);
+    commit_scene(J, r->stream);
+    r->views(cams, n_views, true);
+    const size_t npix = (size_t)n_views * J.W * J.H;
+    J.targets.reserve(3 * npix);
+    DRGB_CUDA(cudaMemcpyAsync(J.targets.p, targets, sizeof(float) * 3 * npix, cudaMemcpyHostToDevice, r->stream));
+    // EvalFunction passes targets[0].width*height edge samples (optimizer_simple.cpp:241)
+    r->gradient_buffers(J.W * J.H);
+    OptState& O = J.opt;
+    O.params = *p;
+    O.active = true;
+    O.host_iter = 0;
+    O.m.alloc(std::max<int64_t>(1, J.grad_total));
+    O.G.alloc(std::max<int64_t>(1, J.grad_total));
+    DRGB_CUDA(cudaMemsetAsync(O.m.p, 0, sizeof(float) * O.m.n, r->stream));
+    DRGB_CUDA(cudaMemsetAsync(O.G.p, 0, sizeof(float) * O.G.n, r->stream));
+    std::vector<float> lr;
+    for (size_t k = 0; k < J.dlay.size(); k++) {
+      lr.push_back(p->position_lr);
+      lr.push_back(p->base_lr);
+      lr.push_back(p->textures_lr);
+      lr.push_back(p->transforms_lr);
+    }
+    O.lr.upload(lr.data(), lr.size(), r->stream);
+    const int zero = 0;
+    O.iter.upload(&zero, 1, r->stream);
+    O.losses.alloc(1024);
+    r->push_dev();
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+    r->graph_valid = false;
+  });
+}
+
+static void enqueue_opt_iteration(drgb_renderer* r) {
+  Job& J = r->job;
+  r->enqueue_iteration(false);
+  launch_opt_record(J, r->stream);
+  launch_opt_step(J, r->stream);
+  prepare_scene(J, r->stream);
+}
+
+int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters) {
+  return guard([&] {
+    check_renderer(r);
+    require(r->job.opt.active, "optimiser not initialised", DRGB_ERR_STATE);
+    require(n_iters >= 0, "negative iteration count");
+    r->set_device();
+    Job& J = r->job;
+    OptState& O = J.opt;
+    const int64_t need = O.host_iter + n_iters;
+    if ((int64_t)O.losses.n < need) {
+      size_t cap = O.losses.n;
+      while ((int64_t)cap < need) cap *= 2;
+      DevBuf<float> nb;
+      nb.alloc(cap);
+      DRGB_CUDA(cudaMemcpyAsync(nb.p, O.losses.p, sizeof(float) * O.losses.n, cudaMemcpyDeviceToDevice, r->stream));
+      DRGB_CUDA(cudaStreamSynchronize(r->stream));
+      O.losses = std::move(nb);
+      r->graph_valid = false;
+    }
+    if (r->use_graph) {
+      if (!r->graph_valid) {
+        if (r->graph) {
+          cudaGraphExecDestroy(r->graph);
+          r->graph = nullptr;
+        }
+        cudaGraph_t g;
+        t_capturing = true;
+        t_capture_count = 0;
+        DRGB_CUDA(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+          enqueue_opt_iteration(r);
+        } catch (...) {
+          cudaStreamEndCapture(r->stream, &g);
+          t_capturing = false;
+          throw;
+        }
+        DRGB_CUDA(cudaStreamEndCapture(r->stream, &g));
+        t_capturing = false;
+        r->graph_kernels = t_capture_count;
+        DRGB_CUDA(cudaGraphInstantiate(&r->graph, g, 0));
+        cudaGraphDestroy(g);
+        r->graph_valid = true;
+      }
+      for (int64_t i = 0; i < n_iters; i++) DRGB_CUDA(cudaGraphLaunch(r->graph, r->stream));
+      add_launches(r->graph_kernels * n_iters);
+    } else {
+      for (int64_t i = 0; i < n_iters; i++) enqueue_opt_iteration(r);
+    }
+    O.host_iter += n_iters;
+  });
+}
+
+int drgb_optimizer_run(drgb_renderer* r, int64_t n_iters, float* final_error, float* losses) {
+  const int64_t start = r ? r->job.opt.host_iter : 0;
+  int rc = drgb_optimizer_run_async(r, n_iters);
+  if (rc != DRGB_OK) return rc;
+  return guard([&] {
+    Job& J = r->job;
+    std::vector<float> h((size_t)std::max<int64_t>(1, n_iters));
+    if (n_iters > 0)
+      DRGB_CUDA(cudaMemcpyAsync(h.data(), J.opt.losses.p + start, sizeof(float) * n_iters, cudaMemcpyDeviceToHost,
+                                r->stream));
+    r->check_flags();
+    if (losses && n_iters > 0) std::memcpy(losses, h.data(), sizeof(float) * n_iters);
+    if (final_error && n_iters > 0) *final_error = h[n_iters - 1];
+  });
+}
+
+int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
+  return guard([&] {
+    check_renderer(r);
+    require(r->job.opt.active, "optimiser not initialised", DRGB_ERR_STATE);
+    require(n_iters >= 1 && out_ms, "bad arguments");
+    r->set_device();
+    Job& J = r->job;
+    cudaEvent_t ev[5];
+    for (auto& e : ev) DRGB_CUDA(cudaEventCreate(&e));
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int it = 0; it < n_iters; it++) {
+      DRGB_CUDA(cudaEventRecord(ev[0], r->stream));
+      DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), r->stream));
+      const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
+      launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
+                    r->stream);
+      launch_loss_finalize(r->d_job.p, 1, r->stream);
+      DRGB_CUDA(cudaEventRecord(ev[1], r->stream));
+      if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
+      DRGB_CUDA(cudaEventRecord(ev[2], r->stream));
+      launch_opt_record(J, r->stream);
+      launch_opt_step(J, r->stream);
+      DRGB_CUDA(cudaEventRecord(ev[3], r->stream));
+      prepare_scene(J, r->stream);
+      DRGB_CUDA(cudaEventRecord(ev[4], r->stream));
+      DRGB_CUDA(cudaEventSynchronize(ev[4]));
+      float ms;
+      for (int k = 0; k < 4; k++) {
+        DRGB_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+        acc[k] += ms;
+      }
+      DRGB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[4]));
+      acc[4] += ms;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    J.opt.host_iter += n_iters;
+    for (int k = 0; k < 5; k++) out_ms[k] = (float)(acc[k] / n_iters);
+    r->check_flags();
+  });
+}
+
+int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(counts != nullptr, "null counts");
+    require(r->job.n_views > 0 && r->job.targets.p, "run a gradient call or optimiser init first", DRGB_ERR_STATE);
+    r->set_device();
+    Job& J = r->job;
+    DevBuf<unsigned long long> w;
+    w.alloc(4);
+    DRGB_CUDA(cudaMemsetAsync(w.p, 0, 4 * sizeof(unsigned long long), r->stream));
+    JobDev d = J.dev;
+    d.work = w.p;
+    DRGB_CUDA(cudaMemcpyAsync(r->d_job.p, &d, sizeof(JobDev), cudaMemcpyHostToDevice, r->stream));
+    const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
+    // gradients of this replay are discarded: save and restore the buffer
+    DevBuf<float> save;
+    save.alloc(std::max<int64_t>(1, J.grad_total));
+    DRGB_CUDA(cudaMemcpyAsync(save.p, J.grad.p, save.bytes(), cudaMemcpyDeviceToDevice, r->stream));
+    DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, save.bytes(), r->stream));
+    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
+                  r->stream);
+    if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
+    int shaded = 0;
+    DRGB_CUDA(cudaMemcpyAsync(&shaded, J.queue_count.p, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(J.grad.p, save.p, save.bytes(), cudaMemcpyDeviceToDevice, r->stream));
+    unsigned long long h[4];
+    DRGB_CUDA(cudaMemcpyAsync(h, w.p, sizeof(h), cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaMemcpyAsync(r->d_job.p, &J.dev, sizeof(JobDev), cudaMemcpyHostToDevice, r->stream));
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+    counts[0] = h[0];
+    counts[1] = h[1];
+    counts[2] = h[2];
+    counts[3] = (uint64_t)std::max(0, shaded);
+    r->check_flags();
+  });
+}
+
+int drgb_optimizer_get_mesh(drgb_renderer* r, int mesh_id, float* vertices, float* colors, float* texture,
+                            float* transforms) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(mesh_id >= 0 && mesh_id < (int)r->job.meshes.size(), "mesh id out of range");
+    r->set_device();
+    const MeshState& M = r->job.meshes[mesh_id];
+    if (vertices)
+      DRGB_CUDA(cudaMemcpyAsync(vertices, M.vertices.p, sizeof(float) * 3 * M.nv, cudaMemcpyDeviceToHost, r->stream));
+    if (colors && M.has_colors)
+      DRGB_CUDA(cudaMemcpyAsync(colors, M.colors.p, sizeof(float) * 3 * M.nv, cudaMemcpyDeviceToHost, r->stream));
+    if (texture && M.texture.p)
+      DRGB_CUDA(cudaMemcpyAsync(texture, M.texture.p, M.texture.bytes(), cudaMemcpyDeviceToHost, r->stream));
+    if (transforms)
+      DRGB_CUDA(cudaMemcpyAsync(transforms, M.transforms.p, M.transforms.bytes(), cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+}  // extern "C"

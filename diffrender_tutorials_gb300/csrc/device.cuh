@@ -1,0 +1,643 @@
+// Device-side data layout and math shared by the renderer kernels.
+//
+// Every translation unit that includes this header is compiled with
+// -fmad=false: the reference's CPU arithmetic (x86-64, no FMA contraction) is
+// reproduced operation by operation, so that camera rays, hit distances,
+// barycentrics and shaded colours are bit-identical to the reference's
+// brute-force caster.  Where rounding does not have to match (BVH slab
+// tests), fused multiply-adds are requested explicitly with __fmaf_rn.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace drgb {
+
+// ---------------------------------------------------------------------------
+// Shading models: numbering of SHADING_MODEL (src/dmesh.h:16-23) plus two
+// models without a reference counterpart.
+// ---------------------------------------------------------------------------
+enum Model : int {
+  SILHOUETTE = 1,
+  VERTEX_COLOR = 2,
+  TEXTURE_COLOR = 3,
+  LAMBERT = 4,
+  LAMBERT_POINT_VCOLOR = 16,
+  PATH_DIFFUSE = 17,
+};
+
+__host__ __device__ inline bool model_has_color(int m) {
+  return m == VERTEX_COLOR || m == LAMBERT_POINT_VCOLOR || m == PATH_DIFFUSE;
+}
+__host__ __device__ inline bool model_has_tex(int m) { return m == TEXTURE_COLOR || m == LAMBERT; }
+
+constexpr int kStackSize = 64;
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+
+// Error flags raised by kernels (never trap): the host reads them after a call.
+enum ErrFlag : uint32_t {
+  ERR_STACK_OVERFLOW = 1u,
+  ERR_TRAVERSAL_LIMIT = 2u,
+  ERR_BAD_INDEX = 4u,
+};
+
+// Camera block: the 82 floats of the oracle's layout (world_view, proj, wvp,
+// proj_inv, wv_inv, width, height), computed on the host like CamInfo.
+struct CamDev {
+  float wv[16];
+  float proj[16];
+  float wvp[16];
+  float proj_inv[16];
+  float wv_inv[16];
+  float width, height;
+};
+
+// A (mesh, instance) pair: where its vertices start in the flattened arrays.
+struct BlockDev {
+  int vert_off;   // first flattened vertex
+  int tri_off;    // first flattened triangle
+  int mesh;       // mesh id (geomId)
+  int inst;       // instance id (instId)
+};
+
+// Per-mesh data used by shading and gradient scatter.
+struct MeshDev {
+  const float* tex;   // w*h*c texture or null
+  int tex_w, tex_h, tex_c;
+  int dslot;          // differentiable slot, -1 if the mesh is static
+  int64_t g_base;     // offset of this mesh's DMesh block in the flat gradient
+  int pos_off, color_off, tex_off, tr_off;
+  int n_vertices, n_instances;
+};
+
+struct ModelParams {
+  float light_pos[3];
+  float light_intensity;
+  float ambient;
+  int path_depth;
+  uint32_t seed;
+};
+
+// One render job: a committed scene, its BVH, views and buffers.  All
+// pointers are device pointers.
+struct JobDev {
+  // flattened prepared scene (Scene::prepare_for_render, scene_utils.cpp:98-173)
+  int n_vertices;
+  int n_tris;
+  int n_blocks;
+  int n_meshes;
+  const float4* pos;     // world positions
+  const float4* orig;    // untransformed positions
+  const float4* col;
+  const float4* nrm;
+  const float2* tc;
+  const int4* tri_v;     // per flattened triangle: global ids A,B,C and block index
+  const BlockDev* blocks;
+  const MeshDev* meshes;
+  const float* tr_inv0;  // inverse transforms of mesh 0 (16 per instance)
+  // BVH: internal nodes (4 float4 each) and leaf triangles in leaf order
+  const float4* nodes;
+  const float4* tri;     // 3 float4 per leaf: (A, id bits), (e1), (e2)
+  int root;              // >= 0 internal node, < 0 leaf ~k, INT_MIN if empty
+  int trace_bruteforce;  // 1: test every triangle (reference loop order)
+  // model
+  int mode;
+  int spp;               // requested spp (Hammersley count)
+  int sq;                // floor(sqrt(spp))
+  int S;                 // sq*sq samples per pixel
+  const float* ham;      // 2*spp Hammersley offsets
+  ModelParams mp;
+  // views
+  int n_views;
+  const CamDev* cams;
+  int W, H;              // view size (all views of a gradient call share it)
+  // gradient buffer (DScene layout, all differentiable meshes concatenated)
+  float* grad;
+  uint32_t* err;
+  // per-call I/O of the pixel kernel
+  float* images;            // 3 floats per pixel (null: not written)
+  const int64_t* img_off;   // first pixel of each view in images/targets
+  const float* targets;     // 3 floats per pixel
+  float4* adj;              // adjoint image, W*H per view
+  const float* adj_in;      // caller-supplied adjoint images (d_render), 3 floats per pixel
+  double* loss_part;        // one partial sum per pixel item of this job
+  float* loss_out;          // final loss of the last call
+  int tile_w, tile_h;
+  int item_base, item_count;  // pixel items of this job in the launch's item list
+  // edge sampling (edge_derivatives, drender.h:235-425)
+  const int4* edges;        // v0, v1 (global ids), vn0, vn1 (mesh-local ids)
+  const int2* edge_mi;      // mesh, instance
+  int n_edges;
+  float4* proj;             // per view per vertex: pixel x, pixel y, world z
+  float* pmf;               // per view n_edges
+  float* cdf;               // per view n_edges + 1
+  int4* queue;              // surviving samples: view, sample index, edge id
+  int* queue_count;
+  int queue_cap;
+  int edge_samples;
+  const float* rnd;         // 2 * edge_samples replayed random numbers
+  // optional work counters (rays, box tests, triangle tests); null normally
+  unsigned long long* work;
+};
+
+// ---------------------------------------------------------------------------
+// Exact float3 helpers (LiteMath operation order).
+// ---------------------------------------------------------------------------
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float length(f3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) {
+  float inv = 1.0f / length(a);
+  return a * inv;
+}
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+  float dx = a.x * b.y - a.y * b.x;
+  float dy = a.y * b.z - a.z * b.y;
+  float dz = a.z * b.x - a.x * b.z;
+  return mk(dy, dz, dx);
+}
+__device__ __forceinline__ float ref_sign(float x) { return x == 0.0f ? 0.0f : (x < 0.0f ? -1.0f : 1.0f); }
+__device__ __forceinline__ float ref_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float ref_min(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float ref_clamp(float u, float a, float b) { return ref_min(ref_max(a, u), b); }
+__device__ __forceinline__ int clampi(int u, int a, int b) {
+  int m = (a < u) ? u : a;
+  return (b < m) ? b : m;
+}
+__device__ __forceinline__ f3 ld3(const float4* p, int i) {
+  float4 v = __ldg(p + i);
+  return mk(v.x, v.y, v.z);
+}
+__device__ __forceinline__ f3 f4to3(float4 v) { return mk(v.x, v.y, v.z); }
+
+// mat4_colmajor_mul_vec4 with w = 1 (LiteMath.h:1342-1348, 1451-1457)
+__device__ __forceinline__ f3 mat_pt(const float* m, f3 p) {
+  return mk(p.x * m[0] + p.y * m[4] + p.z * m[8] + 1.0f * m[12], p.x * m[1] + p.y * m[5] + p.z * m[9] + 1.0f * m[13],
+            p.x * m[2] + p.y * m[6] + p.z * m[10] + 1.0f * m[14]);
+}
+
+// Barycentric interpolation a*(1-u-v) + b*v + u*c (shade_simple.cpp:36).
+__device__ __forceinline__ f3 interp(f3 a, f3 b, f3 c, float u, float v) {
+  const float w0 = 1.0f - u - v;
+  return (a * w0 + b * v) + c * u;
+}
+
+// ---------------------------------------------------------------------------
+// 4x4 inverse with the cofactor pairing of LiteMath.h:1551-1633 (column-major
+// storage, element (r,c) at m[4c+r]).  Used on the host for camera inverses
+// and on the device for the normal transform.
+// ---------------------------------------------------------------------------
+#define MM(m, r, c) ((m)[4 * (c) + (r)])
+__host__ __device__ inline void mat_inverse44(const float* m1, float* out) {
+  float tmp[12], m[16];
+  tmp[0] = MM(m1, 2, 2) * MM(m1, 3, 3);
+  tmp[1] = MM(m1, 2, 3) * MM(m1, 3, 2);
+  tmp[2] = MM(m1, 2, 1) * MM(m1, 3, 3);
+  tmp[3] = MM(m1, 2, 3) * MM(m1, 3, 1);
+  tmp[4] = MM(m1, 2, 1) * MM(m1, 3, 2);
+  tmp[5] = MM(m1, 2, 2) * MM(m1, 3, 1);
+  tmp[6] = MM(m1, 2, 0) * MM(m1, 3, 3);
+  tmp[7] = MM(m1, 2, 3) * MM(m1, 3, 0);
+  tmp[8] = MM(m1, 2, 0) * MM(m1, 3, 2);
+  tmp[9] = MM(m1, 2, 2) * MM(m1, 3, 0);
+  tmp[10] = MM(m1, 2, 0) * MM(m1, 3, 1);
+  tmp[11] = MM(m1, 2, 1) * MM(m1, 3, 0);
+  MM(m, 0, 0) = tmp[0] * MM(m1, 1, 1) + tmp[3] * MM(m1, 1, 2) + tmp[4] * MM(m1, 1, 3);
+  MM(m, 0, 0) -= tmp[1] * MM(m1, 1, 1) + tmp[2] * MM(m1, 1, 2) + tmp[5] * MM(m1, 1, 3);
+  MM(m, 1, 0) = tmp[1] * MM(m1, 1, 0) + tmp[6] * MM(m1, 1, 2) + tmp[9] * MM(m1, 1, 3);
+  MM(m, 1, 0) -= tmp[0] * MM(m1, 1, 0) + tmp[7] * MM(m1, 1, 2) + tmp[8] * MM(m1, 1, 3);
+  MM(m, 2, 0) = tmp[2] * MM(m1, 1, 0) + tmp[7] * MM(m1, 1, 1) + tmp[10] * MM(m1, 1, 3);
+  MM(m, 2, 0) -= tmp[3] * MM(m1, 1, 0) + tmp[6] * MM(m1, 1, 1) + tmp[11] * MM(m1, 1, 3);
+  MM(m, 3, 0) = tmp[5] * MM(m1, 1, 0) + tmp[8] * MM(m1, 1, 1) + tmp[11] * MM(m1, 1, 2);
+  MM(m, 3, 0) -= tmp[4] * MM(m1, 1, 0) + tmp[9] * MM(m1, 1, 1) + tmp[10] * MM(m1, 1, 2);
+  MM(m, 0, 1) = tmp[1] * MM(m1, 0, 1) + tmp[2] * MM(m1, 0, 2) + tmp[5] * MM(m1, 0, 3);
+  MM(m, 0, 1) -= tmp[0] * MM(m1, 0, 1) + tmp[3] * MM(m1, 0, 2) + tmp[4] * MM(m1, 0, 3);
+  MM(m, 1, 1) = tmp[0] * MM(m1, 0, 0) + tmp[7] * MM(m1, 0, 2) + tmp[8] * MM(m1, 0, 3);
+  MM(m, 1, 1) -= tmp[1] * MM(m1, 0, 0) + tmp[6] * MM(m1, 0, 2) + tmp[9] * MM(m1, 0, 3);
+  MM(m, 2, 1) = tmp[3] * MM(m1, 0, 0) + tmp[6] * MM(m1, 0, 1) + tmp[11] * MM(m1, 0, 3);
+  MM(m, 2, 1) -= tmp[2] * MM(m1, 0, 0) + tmp[7] * MM(m1, 0, 1) + tmp[10] * MM(m1, 0, 3);
+  MM(m, 3, 1) = tmp[4] * MM(m1, 0, 0) + tmp[9] * MM(m1, 0, 1) + tmp[10] * MM(m1, 0, 2);
+  MM(m, 3, 1) -= tmp[5] * MM(m1, 0, 0) + tmp[8] * MM(m1, 0, 1) + tmp[11] * MM(m1, 0, 2);
+  tmp[0] = MM(m1, 0, 2) * MM(m1, 1, 3);
+  tmp[1] = MM(m1, 0, 3) * MM(m1, 1, 2);
+  tmp[2] = MM(m1, 0, 1) * MM(m1, 1, 3);
+  tmp[3] = MM(m1, 0, 3) * MM(m1, 1, 1);
+  tmp[4] = MM(m1, 0, 1) * MM(m1, 1, 2);
+  tmp[5] = MM(m1, 0, 2) * MM(m1, 1, 1);
+  tmp[6] = MM(m1, 0, 0) * MM(m1, 1, 3);
+  tmp[7] = MM(m1, 0, 3) * MM(m1, 1, 0);
+  tmp[8] = MM(m1, 0, 0) * MM(m1, 1, 2);
+  tmp[9] = MM(m1, 0, 2) * MM(m1, 1, 0);
+  tmp[10] = MM(m1, 0, 0) * MM(m1, 1, 1);
+  tmp[11] = MM(m1, 0, 1) * MM(m1, 1, 0);
+  MM(m, 0, 2) = tmp[0] * MM(m1, 3, 1) + tmp[3] * MM(m1, 3, 2) + tmp[4] * MM(m1, 3, 3);
+  MM(m, 0, 2) -= tmp[1] * MM(m1, 3, 1) + tmp[2] * MM(m1, 3, 2) + tmp[5] * MM(m1, 3, 3);
+  MM(m, 1, 2) = tmp[1] * MM(m1, 3, 0) + tmp[6] * MM(m1, 3, 2) + tmp[9] * MM(m1, 3, 3);
+  MM(m, 1, 2) -= tmp[0] * MM(m1, 3, 0) + tmp[7] * MM(m1, 3, 2) + tmp[8] * MM(m1, 3, 3);
+  MM(m, 2, 2) = tmp[2] * MM(m1, 3, 0) + tmp[7] * MM(m1, 3, 1) + tmp[10] * MM(m1, 3, 3);
+  MM(m, 2, 2) -= tmp[3] * MM(m1, 3, 0) + tmp[6] * MM(m1, 3, 1) + tmp[11] * MM(m1, 3, 3);
+  MM(m, 3, 2) = tmp[5] * MM(m1, 3, 0) + tmp[8] * MM(m1, 3, 1) + tmp[11] * MM(m1, 3, 2);
+  MM(m, 3, 2) -= tmp[4] * MM(m1, 3, 0) + tmp[9] * MM(m1, 3, 1) + tmp[10] * MM(m1, 3, 2);
+  MM(m, 0, 3) = tmp[2] * MM(m1, 2, 2) + tmp[5] * MM(m1, 2, 3) + tmp[1] * MM(m1, 2, 1);
+  MM(m, 0, 3) -= tmp[4] * MM(m1, 2, 3) + tmp[0] * MM(m1, 2, 1) + tmp[3] * MM(m1, 2, 2);
+  MM(m, 1, 3) = tmp[8] * MM(m1, 2, 3) + tmp[0] * MM(m1, 2, 0) + tmp[7] * MM(m1, 2, 2);
+  MM(m, 1, 3) -= tmp[6] * MM(m1, 2, 2) + tmp[9] * MM(m1, 2, 3) + tmp[1] * MM(m1, 2, 0);
+  MM(m, 2, 3) = tmp[6] * MM(m1, 2, 1) + tmp[11] * MM(m1, 2, 3) + tmp[3] * MM(m1, 2, 0);
+  MM(m, 2, 3) -= tmp[10] * MM(m1, 2, 3) + tmp[2] * MM(m1, 2, 0) + tmp[7] * MM(m1, 2, 1);
+  MM(m, 3, 3) = tmp[10] * MM(m1, 2, 2) + tmp[4] * MM(m1, 2, 0) + tmp[9] * MM(m1, 2, 1);
+  MM(m, 3, 3) -= tmp[8] * MM(m1, 2, 1) + tmp[11] * MM(m1, 2, 2) + tmp[5] * MM(m1, 2, 0);
+  const float k = 1.0f / (MM(m1, 0, 0) * MM(m, 0, 0) + MM(m1, 0, 1) * MM(m, 1, 0) + MM(m1, 0, 2) * MM(m, 2, 0) +
+                          MM(m1, 0, 3) * MM(m, 3, 0));
+  for (int i = 0; i < 16; i++) out[i] = m[i] * k;
+}
+
+#undef MM
+
+// ---------------------------------------------------------------------------
+// Camera rays: EyeRayDirNormalized + transform_ray3f (raytrace.h:49-76) as
+// used by BruteForce3D::CastSingleRay (raytrace3d_bf.cpp:158-174).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void camera_ray(const CamDev& c, float x, float y, f3& ro, f3& rd) {
+  const float xn = x / c.width, yn = y / c.height;
+  const float V0 = 2.0f * xn - 1.0f, V1 = -2.0f * yn + 1.0f, V2 = 0.0f, V3 = 1.0f;
+  const float* B = c.proj_inv;
+  float r0 = V0 * B[0] + V1 * B[4] + V2 * B[8] + V3 * B[12];
+  float r1 = V0 * B[1] + V1 * B[5] + V2 * B[9] + V3 * B[13];
+  float r2 = V0 * B[2] + V1 * B[6] + V2 * B[10] + V3 * B[14];
+  float r3 = V0 * B[3] + V1 * B[7] + V2 * B[11] + V3 * B[15];
+  r0 /= r3;
+  r1 /= r3;
+  r2 /= r3;
+  const f3 dir = normalize(mk(r0, r1, r2));
+  const f3 p0 = mk(0.0f, 0.0f, 0.0f);
+  const f3 pos = mat_pt(c.wv_inv, p0);
+  const f3 pos2 = mat_pt(c.wv_inv, p0 + dir * 100.0f);
+  ro = pos;
+  rd = normalize(pos2 - pos);
+}
+
+// ---------------------------------------------------------------------------
+// Ray/triangle test in the operation order of raytrace3d_bf.cpp:127-140.
+// Returns true when the brute-force caster would accept the hit for the
+// current best distance; u, v, t are bit-identical to the caster's.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool mt_test(f3 pos, f3 dir, f3 A, f3 edge1, f3 edge2, float tNear, float& t, float& u,
+                                        float& v) {
+  const f3 pvec = cross(dir, edge2);
+  const f3 tvec = pos - A;
+  const float e1dpv = dot(edge1, pvec);
+  const float signv = ref_sign(e1dpv);
+  const float invDet = signv / ref_max(signv * e1dpv, 1e-6f);
+  v = dot(tvec, pvec) * invDet;
+  if (!(v > 0.0f)) return false;
+  const f3 qvec = cross(tvec, edge1);
+  u = dot(qvec, dir) * invDet;
+  if (!(u > 0.0f) || !(u + v < 1.0f)) return false;
+  t = dot(edge2, qvec) * invDet;
+  return t > tNear;
+}
+
+struct Hit {
+  float t, u, v;
+  int tri;  // flattened triangle index, -1 = miss
+};
+
+// Ray/box slab test with precomputed inverse direction; returns the entry
+// distance (or +inf when the box is missed within [lo_t, hi_t]).
+__device__ __forceinline__ float slab(float lx, float hx, float ly, float hy, float lz, float hz, f3 inv, f3 oi,
+                                      float lo_t, float hi_t) {
+  const float tx0 = __fmaf_rn(lx, inv.x, -oi.x), tx1 = __fmaf_rn(hx, inv.x, -oi.x);
+  const float ty0 = __fmaf_rn(ly, inv.y, -oi.y), ty1 = __fmaf_rn(hy, inv.y, -oi.y);
+  const float tz0 = __fmaf_rn(lz, inv.z, -oi.z), tz1 = __fmaf_rn(hz, inv.z, -oi.z);
+  const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), lo_t));
+  const float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), hi_t));
+  return tmin <= tmax ? tmin : __int_as_float(0x7f800000);
+}
+
+__device__ __forceinline__ float safe_inv(float d) {
+  const float eps = 1e-20f;
+  if (fabsf(d) < eps) d = copysignf(eps, d);
+  return 1.0f / d;
+}
+
+// Slack on the culling distance so that no box whose triangle the
+// brute-force test would accept is skipped (boxes are also padded).
+__device__ __forceinline__ float cull_bound(float t) { return t + fabsf(t) * 4e-6f + 1e-6f; }
+
+// Nearest hit (ANY=false) or any hit (ANY=true) in [tNear, tFar).  Equal
+// distances resolve to the lowest flattened triangle index, which is the
+// triangle the reference's in-order brute-force loop keeps.
+__device__ __forceinline__ void add_work(const JobDev& J, unsigned boxes, unsigned tris) {
+  if (J.work) {
+    atomicAdd(J.work + 0, 1ull);
+    atomicAdd(J.work + 1, (unsigned long long)boxes);
+    atomicAdd(J.work + 2, (unsigned long long)tris);
+  }
+}
+
+template <bool ANY>
+__device__ __forceinline__ bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best) {
+  best.t = tFar;
+  best.tri = -1;
+  best.u = 0.0f;
+  best.v = 0.0f;
+  if (J.n_tris <= 0) return false;
+  unsigned n_box = 0, n_tri = 0;
+  if (J.trace_bruteforce) {
+    for (int k = 0; k < J.n_tris; k++) {
+      const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+      const int id = __float_as_int(a.w);
+      float t, u, v;
+      if (mt_test(o, d, f4to3(a), f4to3(e1), f4to3(e2), tNear, t, u, v)) {
+        if (t < best.t || (t == best.t && id < best.tri)) {
+          best.t = t;
+          best.u = u;
+          best.v = v;
+          best.tri = id;
+          if (ANY) {
+            add_work(J, 0, k + 1);
+            return true;
+          }
+        }
+      }
+    }
+    add_work(J, 0, J.n_tris);
+    return best.tri >= 0;
+  }
+  const f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  const f3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const float lo_t = tNear - fabsf(tNear) * 4e-6f - 1e-6f;
+  int stack[kStackSize];
+  int sp = 0;
+  int node = J.root;
+  int guard = 0;
+  while (true) {
+    if (node >= 0) {
+      const float4 n0 = __ldg(J.nodes + 4 * node + 0);
+      const float4 n1 = __ldg(J.nodes + 4 * node + 1);
+      const float4 n2 = __ldg(J.nodes + 4 * node + 2);
+      const float4 n3 = __ldg(J.nodes + 4 * node + 3);
+      const float hi_t = cull_bound(best.t);
+      n_box += 2;
+      const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, inv, oi, lo_t, hi_t);
+      const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, inv, oi, lo_t, hi_t);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      const bool h0 = t0 <= hi_t, h1 = t1 <= hi_t;
+      if (h0 && h1) {
+        const bool first0 = t0 <= t1;
+        if (sp >= kStackSize) {
+          atomicOr(J.err, ERR_STACK_OVERFLOW);
+          add_work(J, n_box, n_tri);
+          return best.tri >= 0;
+        }
+        stack[sp++] = first0 ? c1 : c0;
+        node = first0 ? c0 : c1;
+        continue;
+      } else if (h0) {
+        node = c0;
+        continue;
+      } else if (h1) {
+        node = c1;
+        continue;
+      }
+    } else {
+      const int k = ~node;
+      const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+      const int id = __float_as_int(a.w);
+      float t, u, v;
+      n_tri++;
+      if (mt_test(o, d, f4to3(a), f4to3(e1), f4to3(e2), tNear, t, u, v)) {
+        if (t < best.t || (t == best.t && id < best.tri)) {
+          best.t = t;
+          best.u = u;
+          best.v = v;
+          best.tri = id;
+          if (ANY) {
+            add_work(J, n_box, n_tri);
+            return true;
+          }
+        }
+      }
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+    if (++guard > (1 << 24)) {
+      atomicOr(J.err, ERR_TRAVERSAL_LIMIT);
+      break;
+    }
+  }
+  add_work(J, n_box, n_tri);
+  return best.tri >= 0;
+}
+
+// Surface record of a camera ray (SurfaceInfo, raytrace.h:21-29, plus ids).
+struct Surf {
+  Hit h;
+  int A, B, C;  // global vertex ids
+  int block;
+  f3 ro, rd;
+};
+
+__device__ __forceinline__ bool cast(const JobDev& J, const CamDev& cam, float x, float y, Surf& s) {
+  camera_ray(cam, x, y, s.ro, s.rd);
+  if (!trace<false>(J, s.ro, s.rd, 0.0f, 1e9f, s.h)) return false;
+  const int4 tv = __ldg(J.tri_v + s.h.tri);
+  s.A = tv.x;
+  s.B = tv.y;
+  s.C = tv.z;
+  s.block = tv.w;
+  return true;
+}
+
+// sample_bilinear_clamp_3f (shade_common.cpp:3-21)
+__device__ __forceinline__ f3 sample_bilinear(float tx, float ty, int w, int h, const float* data) {
+  tx = ref_clamp(tx, 0.0f, 1.0f);
+  ty = ref_clamp(ty, 0.0f, 1.0f);
+  tx *= (float)w;
+  ty *= (float)h;
+  const int ix = (int)tx, iy = (int)ty;
+  const int x0 = clampi(ix, 0, w - 1), y0 = clampi(iy, 0, h - 1);
+  const int x1 = clampi(ix + 1, 0, w - 1), y1 = clampi(iy + 1, 0, h - 1);
+  const float dx = tx - (float)x0, dy = ty - (float)y0;
+  const float* p00 = data + 3 * (y0 * w + x0);
+  const float* p01 = data + 3 * (y1 * w + x0);
+  const float* p10 = data + 3 * (y0 * w + x1);
+  const float* p11 = data + 3 * (y1 * w + x1);
+  float r[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    r[i] = (1 - dx) * (1 - dy) * __ldg(p00 + i) + (1 - dx) * dy * __ldg(p01 + i) + dx * (1 - dy) * __ldg(p10 + i) +
+           dx * dy * __ldg(p11 + i);
+  return mk(r[0], r[1], r[2]);
+}
+
+__device__ __forceinline__ float2 interp_tc(const JobDev& J, const Surf& s) {
+  const float2 a = __ldg(J.tc + s.A), b = __ldg(J.tc + s.B), c = __ldg(J.tc + s.C);
+  const float w0 = 1.0f - s.h.u - s.h.v;
+  return make_float2((a.x * w0 + b.x * s.h.v) + s.h.u * c.x, (a.y * w0 + b.y * s.h.v) + s.h.u * c.y);
+}
+
+// Lighting factor of the point-light vertex-albedo model:
+// vis * I * max(0, n.l) / d^2 + ambient, with the reference Lambert's bias.
+__device__ __forceinline__ float lpv_factor(const JobDev& J, const Surf& s) {
+  const float u = s.h.u, v = s.h.v;
+  const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
+  const f3 p = s.ro + s.rd * (s.h.t - 1e-5f);
+  const f3 L = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]) - p;
+  const float d2 = dot(L, L);
+  const float dist = sqrtf(d2);
+  const f3 l = L / dist;
+  Hit sh;
+  const float vis = trace<true>(J, p, l, 0.0f, dist, sh) ? 0.0f : 1.0f;
+  const float ndl = ref_max(0.0f, dot(n, l));
+  return vis * J.mp.light_intensity * ndl / d2 + J.mp.ambient;
+}
+
+// Counter-based hash for the path model.
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
+  uint32_t state = x * 747796405u + 2891336453u;
+  uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+__device__ __forceinline__ float rnd01(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t h = pcg_hash(a ^ pcg_hash(b ^ pcg_hash(c)));
+  return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+// Fixed-depth diffuse path tracer (same definition as the oracle's
+// path_diffuse): point light, Lambert BRDF, cosine-weighted bounces.
+__device__ inline f3 path_diffuse(const JobDev& J, const Surf& first, uint32_t key, f3* d_alb0) {
+  const f3 lp = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]);
+  const float I = J.mp.light_intensity;
+  f3 L = mk(0, 0, 0), beta = mk(1, 1, 1), beta_na = mk(1, 1, 1), dL0 = mk(0, 0, 0);
+  Surf sf = first;
+  f3 ro = first.ro, rd = first.rd;
+  for (int bounce = 0; bounce <= J.mp.path_depth; bounce++) {
+    if (bounce > 0) {
+      if (!trace<false>(J, ro, rd, 0.0f, 1e9f, sf.h)) {
+        L = L + beta * J.mp.ambient;
+        dL0 = dL0 + beta_na * J.mp.ambient;
+        break;
+      }
+      const int4 tv = __ldg(J.tri_v + sf.h.tri);
+      sf.A = tv.x;
+      sf.B = tv.y;
+      sf.C = tv.z;
+    }
+    const float u = sf.h.u, v = sf.h.v;
+    const f3 alb = interp(ld3(J.col, sf.A), ld3(J.col, sf.B), ld3(J.col, sf.C), u, v);
+    f3 n = normalize(interp(ld3(J.nrm, sf.A), ld3(J.nrm, sf.B), ld3(J.nrm, sf.C), u, v));
+    const f3 pa = ld3(J.pos, sf.A);
+    const f3 ng = normalize(cross(ld3(J.pos, sf.B) - pa, ld3(J.pos, sf.C) - pa));
+    if (dot(ng, rd) > 0.0f) n = n * -1.0f;
+    const f3 ngf = dot(ng, n) < 0.0f ? ng * -1.0f : ng;
+    const f3 p = (ro + rd * sf.h.t) + ngf * 1e-4f;
+    const f3 Lv = lp - p;
+    const float d2 = dot(Lv, Lv);
+    const float dist = sqrtf(d2);
+    const f3 l = Lv / dist;
+    const float ndl = ref_max(0.0f, dot(n, l));
+    Hit sh;
+    if (ndl > 0.0f && !trace<true>(J, p, l, 0.0f, dist, sh)) {
+      const float k = I * ndl / (d2 * 3.14159265f);
+      L = L + (beta * alb) * k;
+      dL0 = dL0 + (bounce == 0 ? beta_na : beta_na * alb) * k;
+    }
+    if (bounce == J.mp.path_depth) break;
+    const float r1 = rnd01(key, (uint32_t)bounce, J.mp.seed);
+    const float r2 = rnd01(key, (uint32_t)bounce + 1000u, J.mp.seed);
+    const float phi = 6.28318531f * r1;
+    const float sr = sqrtf(r2);
+    const f3 a = fabsf(n.x) > 0.5f ? mk(0, 1, 0) : mk(1, 0, 0);
+    const f3 ex = normalize(cross(a, n));
+    const f3 ey = cross(n, ex);
+    const float lx = sr * cosf(phi), ly = sr * sinf(phi), lz = sqrtf(ref_max(0.0f, 1.0f - r2));
+    rd = normalize((ex * lx + ey * ly) + n * lz);
+    ro = p;
+    beta_na = bounce == 0 ? beta_na : beta_na * alb;
+    beta = beta * alb;
+  }
+  if (d_alb0) *d_alb0 = dL0;
+  return L;
+}
+
+// shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).
+__device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
+  Surf s;
+  if (!cast(J, cam, x, y, s)) {
+    if (J.mode == PATH_DIFFUSE) return mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
+    return mk(0.0f, 0.0f, 0.0f);
+  }
+  const float u = s.h.u, v = s.h.v;
+  switch (J.mode) {
+    case SILHOUETTE:
+      return mk(1.0f, 1.0f, 1.0f);
+    case VERTEX_COLOR:
+      return interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v);
+    case TEXTURE_COLOR: {
+      const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
+      const float2 tc = interp_tc(J, s);
+      return sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+    }
+    case LAMBERT: {
+      // light_dir = normalize(-1,-1,0), colour (1,0.5,0.2), ambient 0.1, BIAS 1e-5
+      const f3 light_dir = normalize(mk(-1.0f, -1.0f, 0.0f));
+      const f3 to_light = light_dir * -1.0f;
+      const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
+      const float2 tc = interp_tc(J, s);
+      const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
+      const f3 diffuse = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+      const f3 surf_pos = s.ro + s.rd * (s.h.t - 1e-5f);
+      Hit sh;
+      const float shv = trace<true>(J, surf_pos, to_light, 0.0f, 1e9f, sh) ? 0.0f : 1.0f;
+      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * shv) * ref_max(0.0f, dot(n, to_light));
+      return (lit + mk(1.0f, 1.0f, 1.0f) * 0.1f) * diffuse;
+    }
+    case LAMBERT_POINT_VCOLOR: {
+      const f3 alb = interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v);
+      return alb * lpv_factor(J, s);
+    }
+    case PATH_DIFFUSE:
+      return path_diffuse(J, s, key, nullptr);
+    default:
+      return mk(0.0f, 0.0f, 0.0f);
+  }
+}
+
+// VertexShader (functions.h:5-13): pixel x,y of a world point.
+__device__ __forceinline__ void vertex_shader(const CamDev& c, float vx, float vy, float vz, float& ox, float& oy) {
+  const float* m = c.wvp;
+  const float W = vx * m[3] + vy * m[7] + vz * m[11] + m[15];
+  const float xNDC = (vx * m[0] + vy * m[4] + vz * m[8] + m[12]) / W;
+  const float yNDC = -(vx * m[1] + vy * m[5] + vz * m[9] + m[13]) / W;
+  ox = (xNDC * 0.5f + 0.5f) * c.width;
+  oy = (yNDC * 0.5f + 0.5f) * c.height;
+}
+
+// VS_X_grad / VS_Y_grad (functions.cpp:21-163), same evaluation order.
+__device__ __forceinline__ f3 vs_grad(const CamDev& c, f3 V, bool y) {
+  const float* m = c.wvp;
+  const float t1 = V.x, t0 = m[3], t3 = V.y, t2 = m[7], t5 = V.z, t4 = m[11];
+  const float W = t1 * t0 + t3 * t2 + t5 * t4 + m[15];
+  const float t7 = y ? m[1] : m[0];
+  const float t9 = y ? m[5] : m[4];
+  const float t11 = y ? m[9] : m[8];
+  const float t13r = V.x * t7 + V.y * t9 + V.z * t11 + (y ? m[13] : m[12]);
+  const float t13 = y ? -t13r : t13r;
+  const float t6 = W;
+  const float t14 = y ? c.height : c.width;
+  const float d_xNDC = (1 * t14) * 0.5f;
+  const float r6 = d_xNDC / t6;
+  const float s6 = y ? -r6 : r6;
+  const float d_W = d_xNDC * -t13 / (t6 * t6);
+  return mk(s6 * t7 + d_W * t0, s6 * t9 + d_W * t2, s6 * t11 + d_W * t4);
+}
+
+}  // namespace drgb

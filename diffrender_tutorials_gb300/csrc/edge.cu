@@ -1,0 +1,220 @@
+// Edge-sampling boundary term (DiffRender::edge_derivatives,
+// src/drender.h:235-425; build_edge_sampler / sample / edge_grad,
+// src/drender.cpp:5-87; VS_X_grad / VS_Y_grad, src/functions.cpp:21-163).
+//
+//   k_edge_project : VertexShader of every flattened vertex, per view
+//   k_edge_pmf     : edge weights = 3-D length of the projected endpoints
+//   k_edge_cdf     : the sampler's CDF, summed sequentially in edge order so
+//                    that it is bit-identical to the reference's
+//   k_edge_select  : replayed random numbers -> edge (upper_bound) -> point
+//                    -> off-image / small-adjoint rejection; survivors are
+//                    appended to a queue with one atomic per warp (ballot)
+//   k_edge_shade   : two-sided shading at p -/+ 1e-3 n, (f_in - f_out).dL/dI,
+//                    chain rule to the world vertices and the instance
+//                    matrix, scattered with atomics (transform terms summed
+//                    across the warp first)
+#include "engine.h"
+
+namespace drgb {
+
+__global__ void k_edge_project(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int view = blockIdx.y;
+  if (v >= J.n_vertices) return;
+  const CamDev& c = J.cams[view];
+  const float4 p = __ldg(J.pos + v);
+  float ox, oy;
+  vertex_shader(c, p.x, p.y, p.z, ox, oy);
+  J.proj[(int64_t)view * J.n_vertices + v] = make_float4(ox, oy, p.z, 0.0f);
+}
+
+__global__ void k_edge_pmf(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int view = blockIdx.y;
+  if (e >= J.n_edges) return;
+  const int4 ed = __ldg(J.edges + e);
+  const float4* P = J.proj + (int64_t)view * J.n_vertices;
+  const float4 a = P[ed.x], b = P[ed.y];
+  J.pmf[(int64_t)view * J.n_edges + e] = length(mk(b.x - a.x, b.y - a.y, b.z - a.z));
+}
+
+// One warp per view: cdf[k+1] = pmf[k] + cdf[k] in edge order, then both
+// divided by the total (drender.cpp:5-22).
+__global__ void k_edge_cdf(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int view = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int E = J.n_edges;
+  float* pmf = J.pmf + (int64_t)view * E;
+  float* cdf = J.cdf + (int64_t)view * (E + 1);
+  float run = 0.0f;
+  if (lane == 0) cdf[0] = 0.0f;
+  for (int base = 0; base < E; base += 32) {
+    const float v = (base + lane < E) ? pmf[base + lane] : 0.0f;
+    const int cnt = min(32, E - base);
+    float out = 0.0f;
+    for (int j = 0; j < cnt; j++) {
+      const float pj = __shfl_sync(0xffffffffu, v, j);
+      run = pj + run;
+      if (lane == j) out = run;
+    }
+    if (lane < cnt) cdf[base + lane + 1] = out;
+  }
+  __syncwarp();
+  const float total = __shfl_sync(0xffffffffu, run, 0);
+  for (int k = lane; k < E; k += 32) pmf[k] = pmf[k] / total;
+  for (int k = lane; k <= E; k += 32) cdf[k] = cdf[k] / total;
+}
+
+__device__ __forceinline__ int upper_bound_idx(const float* cdf, int n, float u) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (u < cdf[mid]) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+__global__ void k_edge_select(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int view = blockIdx.y;
+  bool keep = false;
+  int edge_id = 0;
+  if (i < J.edge_samples && J.n_edges > 0) {
+    const float rnd0 = __ldg(J.rnd + 2 * i), rnd1 = __ldg(J.rnd + 2 * i + 1);
+    const float* cdf = J.cdf + (int64_t)view * (J.n_edges + 1);
+    edge_id = clampi(upper_bound_idx(cdf, J.n_edges + 1, rnd0) - 1, 0, J.n_edges - 1);
+    const int4 ed = __ldg(J.edges + edge_id);
+    const float4* P = J.proj + (int64_t)view * J.n_vertices;
+    const float4 a = P[ed.x], b = P[ed.y];
+    const float t = rnd1;
+    const float px = a.x + t * (b.x - a.x), py = a.y + t * (b.y - a.y);
+    const int xi = (int)px, yi = (int)py;
+    if (!(xi < 0 || yi < 0 || xi >= J.W || yi >= J.H)) {
+      const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
+      keep = !(length(mk(ad.x, ad.y, ad.z)) < 1e-3f);
+    }
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+  if (!ballot) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == __ffs(ballot) - 1) base = atomicAdd(J.queue_count, __popc(ballot));
+  base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+  if (keep) {
+    const int slot = base + __popc(ballot & ((1u << lane) - 1u));
+    if (slot < J.queue_cap) J.queue[slot] = make_int4(view, i, edge_id, 0);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_edge_shade(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int n = min(*J.queue_count, J.queue_cap);
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  // iterate in whole warps so that the warp reductions below see every lane
+  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride) {
+    const int q = q0 + lane;
+    float tr[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) tr[k] = 0.0f;
+    int key = -1;
+    if (q < n) {
+      const int4 it = J.queue[q];
+      const int view = it.x, i = it.y, edge_id = it.z;
+      const CamDev& cam = J.cams[view];
+      const int4 ed = __ldg(J.edges + edge_id);
+      const int2 mi = __ldg(J.edge_mi + edge_id);
+      const float pm = J.pmf[(int64_t)view * J.n_edges + edge_id];
+      const float4* P = J.proj + (int64_t)view * J.n_vertices;
+      const float4 pa = P[ed.x], pb = P[ed.y];
+      const float t = __ldg(J.rnd + 2 * i + 1);
+      const float dx0 = pb.x - pa.x, dy0 = pb.y - pa.y;
+      const float px = pa.x + t * dx0, py = pa.y + t * dy0;
+      const int xi = (int)px, yi = (int)py;
+      const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
+      const float dl = sqrtf(dx0 * dx0 + dy0 * dy0);
+      const float nx = -(dy0 / dl), ny = dx0 / dl;  // normal2D of the unit edge direction
+      const float cinx = px - 1e-3f * nx, ciny = py - 1e-3f * ny;
+      const float coutx = px + 1e-3f * nx, couty = py + 1e-3f * ny;
+      const uint32_t key_in = 0xA511E9B3u ^ ((uint32_t)(i * 2u) * 2654435761u);
+      const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
+      const f3 color_in = shade(J, cam, cinx, ciny, key_in);
+      const f3 color_out = shade(J, cam, coutx, couty, key_out);
+      const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
+      const float weight = 1.0f / (pdf * (float)J.edge_samples);
+      const float adjv = dot(color_in - color_out, mk(ad.x, ad.y, ad.z));
+      if (adjv * adjv > 0.0f) {
+        const float d0x = (1 - t) * nx * adjv * weight, d0y = (1 - t) * ny * adjv * weight;
+        const float d1x = t * nx * adjv * weight, d1y = t * ny * adjv * weight;
+        const f3 v0 = ld3(J.pos, ed.x), v1 = ld3(J.pos, ed.y);
+        const f3 g0x = vs_grad(cam, v0, false), g0y = vs_grad(cam, v0, true);
+        const f3 g1x = vs_grad(cam, v1, false), g1y = vs_grad(cam, v1, true);
+        const float dv0_dx = g0x.x * d0x, dv0_dy = g0y.y * d0y, dv0_dz = (g0x.z * d0x + g0y.z * d0y);
+        const float dv1_dx = g1x.x * d1x, dv1_dy = g1y.y * d1y, dv1_dz = (g1x.z * d1x + g1y.z * d1y);
+        const MeshDev& md = J.meshes[mi.x];
+        if (md.dslot >= 0) {
+          const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
+          float* g = J.grad + md.g_base + md.pos_off;
+          atomicAdd(g + ed.z * 3 + 0, M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz);
+          atomicAdd(g + ed.z * 3 + 1, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz);
+          atomicAdd(g + ed.z * 3 + 2, M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
+          atomicAdd(g + ed.w * 3 + 0, M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz);
+          atomicAdd(g + ed.w * 3 + 1, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz);
+          atomicAdd(g + ed.w * 3 + 2, M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+          const f3 o0 = ld3(J.orig, ed.x), o1 = ld3(J.orig, ed.y);
+          tr[0] = o0.x * dv0_dx + o1.x * dv1_dx;
+          tr[1] = o0.y * dv0_dx + o1.y * dv1_dx;
+          tr[2] = o0.z * dv0_dx + o1.z * dv1_dx;
+          tr[3] = 1 * dv0_dx + 1 * dv1_dx;
+          tr[4] = o0.x * dv0_dy + o1.x * dv1_dy;
+          tr[5] = o0.y * dv0_dy + o1.y * dv1_dy;
+          tr[6] = o0.z * dv0_dy + o1.z * dv1_dy;
+          tr[7] = 1 * dv0_dy + 1 * dv1_dy;
+          tr[8] = o0.x * dv0_dz + o1.x * dv1_dz;
+          tr[9] = o0.y * dv0_dz + o1.y * dv1_dz;
+          tr[10] = o0.z * dv0_dz + o1.z * dv1_dz;
+          tr[11] = 1 * dv0_dz + 1 * dv1_dz;
+          key = (int)(md.g_base + md.tr_off) + 12 * mi.y;
+        }
+      }
+    }
+    // transform gradient: one atomic per warp when every contributing lane
+    // targets the same instance, per lane otherwise
+    const unsigned any = __ballot_sync(0xffffffffu, key >= 0);
+    if (!any) continue;
+    const int lead_key = __shfl_sync(0xffffffffu, key, __ffs(any) - 1);
+    const bool uniform = __all_sync(0xffffffffu, key < 0 || key == lead_key);
+    if (uniform) {
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        float v = tr[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        tr[k] = v;
+      }
+      if (lane == 0)
+        for (int k = 0; k < 12; k++) atomicAdd(J.grad + lead_key + k, tr[k]);
+    } else if (key >= 0) {
+      for (int k = 0; k < 12; k++) atomicAdd(J.grad + key + k, tr[k]);
+    }
+  }
+}
+
+void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s) {
+  if (J.n_edges <= 0 || J.n_views <= 0) return;
+  const dim3 gp((J.n_vertices + 255) / 256, J.n_views);
+  k_edge_project<<<gp, 256, 0, s>>>(d_jobs, job);
+  const dim3 ge((J.n_edges + 255) / 256, J.n_views);
+  k_edge_pmf<<<ge, 256, 0, s>>>(d_jobs, job);
+  k_edge_cdf<<<J.n_views, 32, 0, s>>>(d_jobs, job);
+  DRGB_CUDA(cudaMemsetAsync(J.queue_count.p, 0, sizeof(int), s));
+  const dim3 gs((J.dev.edge_samples + 255) / 256, J.n_views);
+  k_edge_select<<<gs, 256, 0, s>>>(d_jobs, job);
+  k_edge_shade<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  count_launch(5);
+}
+
+}  // namespace drgb

@@ -1,0 +1,208 @@
+// Host-side engine: device-resident state of one render job and the launch
+// sequences over it.  A job is one committed scene (meshes, instances,
+// textures), its LBVH, its views and its gradient/optimiser state.  Kernels
+// take an array of jobs so that the same launch serves one job (the plain
+// path) or many (the batched path).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/drgb.h"
+#include "device.cuh"
+
+namespace drgb {
+
+struct CudaError : std::runtime_error {
+  int code;
+  CudaError(const std::string& m, int c) : std::runtime_error(m), code(c) {}
+};
+
+#define DRGB_CUDA(x)                                                                                  \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess)                                                                            \
+      throw ::drgb::CudaError(std::string(#x) + ": " + cudaGetErrorString(e_),                       \
+                              e_ == cudaErrorMemoryAllocation ? DRGB_ERR_OOM : DRGB_ERR_CUDA);       \
+  } while (0)
+
+// Owning device allocation.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    reset();
+    if (count == 0) return;
+    DRGB_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  // grow-only allocation (keeps the pointer when large enough)
+  void reserve(size_t count) {
+    if (count <= n && p) return;
+    alloc(count);
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) DRGB_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Gradient layout of one differentiable mesh (DMesh, dmesh.h:35-85).
+struct DLayout {
+  int mesh_id = -1;
+  int vertices = 0, instances = 0;
+  int pos_off = 0, color_off = -1, tex_off = -1, tr_off = 0;
+  int full = 0;
+  int64_t base = 0;  // offset in the concatenated vector
+};
+
+// Source arrays of one mesh read by the flattening kernel.
+struct MeshSrc {
+  const float* v;
+  const float* col;
+  const float* nrm;
+  const float* tc;
+};
+
+// Count of kernels launched by this library (reported by drgb_kernel_launches).
+void count_launch(int n = 1);
+
+struct MeshState {
+  int nv = 0, ni = 0, n_inst = 1;
+  DevBuf<float> vertices, colors, tc, normals, tangents, transforms, texture;
+  DevBuf<uint32_t> indices;
+  int tex_w = 0, tex_h = 0, tex_c = 0;
+  bool has_colors = false, has_tc = false, has_normals = false, has_tangents = false;
+  std::vector<uint32_t> h_indices;
+};
+
+struct OptState {
+  bool active = false;
+  drgb_opt_params params{};
+  DevBuf<float> m, G;
+  DevBuf<float> lr;       // per dmesh 4 lr values (pos, color, tex, transform)
+  DevBuf<int> iter;       // device iteration counter
+  DevBuf<float> losses;   // per-iteration loss history (ring)
+  int64_t host_iter = 0;
+};
+
+struct Job {
+  // model
+  int mode = VERTEX_COLOR;
+  int spp = 1, sq = 1, S = 1;
+  ModelParams mp{};
+  int trace_bruteforce = 0;
+  int tile_w = 4, tile_h = 4;
+  // scene
+  bool committed = false;
+  std::vector<MeshState> meshes;
+  int n_vertices = 0, n_tris = 0, n_blocks = 0;
+  std::vector<BlockDev> h_blocks;
+  DevBuf<float4> pos, orig, col, nrm;
+  DevBuf<float2> tc;
+  DevBuf<int4> tri_v;
+  DevBuf<BlockDev> blocks;
+  DevBuf<MeshDev> meshdev;
+  DevBuf<float> block_tr;  // 32 floats per block: transform, inverse-transpose
+  DevBuf<int> vblock;      // block of each flattened vertex
+  DevBuf<MeshSrc> src_tab;
+  DevBuf<const float*> tr_tab;
+  DevBuf<float> tr_inv0;   // inverse transforms of mesh 0 at the first commit
+  // BVH
+  DevBuf<float4> nodes, tri;
+  DevBuf<int> perm, leaf_parent, node_parent, counters;
+  DevBuf<uint32_t> sort_keys[2], sort_hist;
+  DevBuf<int> sort_vals[2];
+  DevBuf<float> bounds;
+  int root = 0;
+  // edges (topology; one list per differentiable-mesh set)
+  DevBuf<int4> edges;   // v0, v1, vn0, vn1
+  DevBuf<int2> edge_mi; // mesh, instance
+  int n_edges = 0;
+  std::vector<int> edge_ids_key;  // dmesh ids the list was built for
+  // views
+  int n_views = 0, W = 0, H = 0;
+  std::vector<CamDev> h_cams;
+  DevBuf<CamDev> cams;
+  DevBuf<float> ham;
+  // per-call buffers
+  DevBuf<float> images, targets, adj_in;
+  DevBuf<int64_t> img_off;
+  DevBuf<float4> adj;
+  DevBuf<double> loss_part;
+  DevBuf<float> loss_out;  // 1 float: last loss
+  DevBuf<float4> proj;     // per view per vertex projected position
+  DevBuf<float> pmf, cdf;  // per view
+  DevBuf<int4> queue;      // surviving edge samples
+  DevBuf<int> queue_count;
+  // gradients
+  std::vector<DLayout> dlay;
+  std::vector<int> dmesh_ids;
+  int64_t grad_total = 0;
+  DevBuf<float> grad;
+  DevBuf<uint32_t> err;
+  OptState opt;
+  // work items
+  std::vector<int4> h_pixel_items;
+  int n_tiles_x = 0, n_tiles_y = 0;
+
+  JobDev dev{};  // device view, refreshed by sync_dev()
+};
+
+// ---- launch helpers (implemented in the .cu files) --------------------------
+void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s);
+void flatten_scene(Job& J, cudaStream_t s);            // instance transforms -> flattened arrays
+void prepare_scene(Job& J, cudaStream_t s);            // flatten + traced triangles + refit
+void commit_scene(Job& J, cudaStream_t s);             // flatten + LBVH build + refit
+void build_bvh(Job& J, cudaStream_t s);                // topology (Morton, sort, Karras)
+void refit_bvh(Job& J, cudaStream_t s);
+void setup_views(Job& J, const drgb_camera* cams, int n_views);
+void sync_dev(Job& J);
+void set_dscene(Job& J, const int32_t* ids, int n_ids);
+void build_edges(Job& J);
+int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out);
+
+void init_job_model(Job& J, int mode, int spp);
+void choose_tile(int S, int& tw, int& th);
+void camera_look_at(const float* o, const float* t, const float* u, float width, float height, float fov_rad,
+                    float znear, float zfar, drgb_camera* out);
+CamDev make_cam(const drgb_camera& c);
+
+// Pixel kernel flags
+enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8 };
+void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
+                   cudaStream_t s);
+void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
+void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s);
+void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, int64_t n, uint32_t* prim,
+                 uint32_t* inst, uint32_t* geom, float* t, float* u, float* v, cudaStream_t s);
+void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s);
+void launch_opt_step(Job& J, cudaStream_t s);
+void launch_opt_record(Job& J, cudaStream_t s);
+
+// edge random table shared by every job with the same sample count
+const float* edge_random_table(int n, cudaStream_t s);
+
+}  // namespace drgb

@@ -1,0 +1,121 @@
+"""ctypes binding of libdrgb.so (include/drgb.h).
+
+The library is built in-tree (diffrender_tutorials_gb300/_build/libdrgb.so)
+by build.py.  There is no fallback: every renderer call goes through the
+CUDA library, and loading fails loudly when it is missing.
+"""
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdrgb.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "drgb.h")
+
+DRGB_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
+          -5: "kernel error flag", -6: "unsupported", -7: "no CUDA device"}
+
+
+class DrgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"drgb error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Camera(C.Structure):
+    _fields_ = [("world_view", C.c_float * 16), ("proj", C.c_float * 16), ("width", C.c_float), ("height", C.c_float)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("n_vertices", C.c_int32), ("n_indices", C.c_int32), ("vertices", C.c_void_p),
+                ("colors", C.c_void_p), ("tc", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p),
+                ("indices", C.c_void_p), ("n_instances", C.c_int32), ("transforms", C.c_void_p),
+                ("tex_w", C.c_int32), ("tex_h", C.c_int32), ("tex_channels", C.c_int32), ("texture", C.c_void_p)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("n_meshes", C.c_int32), ("meshes", C.POINTER(MeshDesc))]
+
+
+class ModelParams(C.Structure):
+    _fields_ = [("light_pos", C.c_float * 3), ("light_intensity", C.c_float), ("ambient", C.c_float),
+                ("path_depth", C.c_int32), ("seed", C.c_uint32)]
+
+
+class OptParams(C.Structure):
+    _fields_ = [("alg", C.c_int32), ("decay_period", C.c_int32), ("decay_mult", C.c_float),
+                ("base_lr", C.c_float), ("position_lr", C.c_float), ("textures_lr", C.c_float),
+                ("transforms_lr", C.c_float), ("flags", C.c_int32), ("n_dmesh_ids", C.c_int32),
+                ("dmesh_ids", C.c_int32 * 16)]
+
+
+VP = C.c_void_p
+_SIGS = {
+    "drgb_abi_version": (C.c_int, []),
+    "drgb_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "drgb_kernel_launches": (C.c_int64, []),
+    "drgb_camera_look_at": (C.c_int, [VP, VP, VP, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                      C.POINTER(Camera)]),
+    "drgb_renderer_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(VP)]),
+    "drgb_renderer_destroy": (C.c_int, [VP]),
+    "drgb_renderer_set_option": (C.c_int, [VP, C.c_int, C.c_int64]),
+    "drgb_renderer_set_model_params": (C.c_int, [VP, C.POINTER(ModelParams)]),
+    "drgb_renderer_stream": (VP, [VP]),
+    "drgb_commit": (C.c_int, [VP, C.POINTER(SceneDesc)]),
+    "drgb_render": (C.c_int, [VP, C.POINTER(Camera), C.c_int, VP]),
+    "drgb_dscene_layout": (C.c_int, [VP, VP, C.c_int, VP, C.POINTER(C.c_int64)]),
+    "drgb_d_render": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP]),
+    "drgb_d_render_and_compare": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP, VP, VP]),
+    "drgb_d_render_and_compare_device": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP,
+                                                   VP, VP]),
+    "drgb_cast_rays": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int64, VP, VP, VP, VP, VP, VP]),
+    "drgb_opt_params_default": (C.c_int, [C.c_int, C.POINTER(OptParams)]),
+    "drgb_optimizer_init": (C.c_int, [VP, C.POINTER(SceneDesc), C.POINTER(Camera), VP, C.c_int,
+                                      C.POINTER(OptParams)]),
+    "drgb_optimizer_run": (C.c_int, [VP, C.c_int64, VP, VP]),
+    "drgb_optimizer_run_async": (C.c_int, [VP, C.c_int64]),
+    "drgb_optimizer_get_mesh": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+    "drgb_optimizer_profile": (C.c_int, [VP, C.c_int, VP]),
+    "drgb_count_work": (C.c_int, [VP, VP]),
+}
+
+_lib = None
+
+
+def header_functions():
+    """Names of the functions declared in include/drgb.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(drgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def load(path=None):
+    """Load libdrgb.so (building it first when it is absent) and set signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(path):
+        raise OSError(f"libdrgb.so not found at {path}; run diffrender_tutorials_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    load().drgb_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(code):
+    if code != DRGB_OK:
+        raise DrgbError(code, last_error())
+    return code

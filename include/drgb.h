@@ -1,0 +1,207 @@
+/* drgb: GB300-native differentiable mesh renderer -- C ABI.
+ *
+ * This is the drop-in boundary for the hot path of the reference renderer
+ * (FROL256/diffrender_tutorials): IDiffRender (src/virtual_drender.h:14-26)
+ * over Scene/DScene/CamInfo, and the OptSimple optimiser
+ * (src/optimizer.h:52-61, src/optimizer_simple.cpp:25-309).  Every entry point
+ * takes plain pointers and sizes.  Unless a function says otherwise, data
+ * pointers are HOST pointers and the call returns when the results are in
+ * host memory; the *_device variants take DEVICE pointers and enqueue work
+ * on the renderer's stream without synchronising.
+ *
+ * All functions return DRGB_OK (0) or a negative error code; the message of
+ * the last error on the calling thread is available from drgb_last_error.
+ */
+#ifndef DRGB_H
+#define DRGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DRGB_ABI_VERSION 1
+
+/* Error codes. */
+enum {
+  DRGB_OK = 0,
+  DRGB_ERR_INVALID = -1,      /* bad argument (sizes, ids, null pointers) */
+  DRGB_ERR_CUDA = -2,         /* a CUDA call failed */
+  DRGB_ERR_OOM = -3,          /* device allocation failed */
+  DRGB_ERR_STATE = -4,        /* call out of order (e.g. render before commit) */
+  DRGB_ERR_KERNEL = -5,       /* a kernel raised an error flag (traversal stack/limit) */
+  DRGB_ERR_UNSUPPORTED = -6,  /* feature not available in this build */
+  DRGB_ERR_NO_DEVICE = -7     /* no CUDA device */
+};
+
+/* Shading models: the numbering of SHADING_MODEL (src/dmesh.h:16-23) plus two
+ * models without a reference counterpart. */
+enum {
+  DRGB_SILHOUETTE = 1,
+  DRGB_VERTEX_COLOR = 2,
+  DRGB_TEXTURE_COLOR = 3,
+  DRGB_LAMBERT = 4,
+  DRGB_LAMBERT_POINT_VCOLOR = 16, /* point light, per-vertex albedo, ambient; no reference counterpart */
+  DRGB_PATH_DIFFUSE = 17          /* fixed-depth diffuse path tracer with counter RNG; no reference counterpart */
+};
+
+/* Optimiser algorithms (OptimizerParameters::OPT_ALGORITHM, src/optimizer.h:11). */
+enum { DRGB_GD_NAIVE = 1, DRGB_GD_ADAGRAD = 2, DRGB_GD_RMSPROP = 3, DRGB_GD_ADAM = 4 };
+/* Optimiser flags (src/optimizer.h:12-18). */
+enum { DRGB_OPT_POS = 1, DRGB_OPT_TFM = 2, DRGB_OPT_COL = 4, DRGB_OPT_TEX = 8 };
+
+/* Renderer options (drgb_renderer_set_option). */
+enum {
+  DRGB_OPT_TRACE_BRUTEFORCE = 1, /* 1: test every triangle in the reference's loop order instead of the LBVH */
+  DRGB_OPT_TILE_W = 2,           /* pixel tile width of the fused forward/adjoint kernel */
+  DRGB_OPT_TILE_H = 3,
+  DRGB_OPT_USE_GRAPH = 4         /* 1 (default): optimiser iterations replay a CUDA graph */
+};
+
+/* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
+ * order (column major); mWVP and the inverses used by the caster are derived
+ * by the library. */
+typedef struct drgb_camera {
+  float world_view[16];
+  float proj[16];
+  float width, height;
+} drgb_camera;
+
+/* Fills a camera like CamInfo(origin, target, up, w, h, fov_rad, znear, zfar)
+ * (common_src/camera.h:9-22; lookAt/perspectiveMatrix, LiteMath.h:1679-1729). */
+int drgb_camera_look_at(const float origin[3], const float target[3], const float up[3], float width, float height,
+                        float fov_rad, float znear, float zfar, drgb_camera* out);
+
+/* One mesh and its instances (TriangleMesh + transforms, common_src/scene.h:40-70, 130-138). */
+typedef struct drgb_mesh_desc {
+  int32_t n_vertices;
+  int32_t n_indices;       /* multiple of 3 */
+  const float* vertices;   /* 3*n_vertices */
+  const float* colors;     /* 3*n_vertices or NULL */
+  const float* tc;         /* 2*n_vertices or NULL */
+  const float* normals;    /* 3*n_vertices or NULL */
+  const float* tangents;   /* 3*n_vertices or NULL */
+  const uint32_t* indices; /* n_indices */
+  int32_t n_instances;     /* >= 1 */
+  const float* transforms; /* 16*n_instances, column major; NULL = one identity instance */
+  int32_t tex_w, tex_h, tex_channels; /* first texture; 0 when absent */
+  const float* texture;    /* tex_w*tex_h*tex_channels or NULL */
+} drgb_mesh_desc;
+
+typedef struct drgb_scene_desc {
+  int32_t n_meshes;
+  const drgb_mesh_desc* meshes;
+} drgb_scene_desc;
+
+/* Constants of the two models without a reference counterpart. */
+typedef struct drgb_model_params {
+  float light_pos[3];
+  float light_intensity;
+  float ambient;
+  int32_t path_depth;
+  uint32_t seed;
+} drgb_model_params;
+
+/* OptimizerParameters (src/optimizer.h:9-50). */
+typedef struct drgb_opt_params {
+  int32_t alg;
+  int32_t decay_period;
+  float decay_mult;
+  float base_lr, position_lr, textures_lr, transforms_lr;
+  int32_t flags;
+  int32_t n_dmesh_ids;
+  int32_t dmesh_ids[16];
+} drgb_opt_params;
+
+typedef struct drgb_renderer drgb_renderer;
+
+/* ---- library ------------------------------------------------------------ */
+int drgb_abi_version(void);
+/* Message of the last failed call on this thread (always NUL-terminated). */
+int drgb_last_error(char* buf, size_t len);
+/* Number of kernels this library launched since load (all threads). */
+int64_t drgb_kernel_launches(void);
+
+/* ---- renderer: IDiffRender (src/virtual_drender.h:14-26) ----------------- */
+
+/* MakeDifferentialRenderer(DiffRenderSettings{mode, spp}) + init
+ * (src/drender.cpp:89-147, src/drender.h:79-88). */
+int drgb_renderer_create(int shading_model, int spp, int device, drgb_renderer** out);
+int drgb_renderer_destroy(drgb_renderer* r);
+int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value);
+int drgb_renderer_set_model_params(drgb_renderer* r, const drgb_model_params* p);
+/* CUDA stream (cudaStream_t) the renderer enqueues on. */
+void* drgb_renderer_stream(drgb_renderer* r);
+
+/* IDiffRender::commit (src/drender.h:91-96): uploads the scene, flattens it
+ * and builds the LBVH on the device. */
+int drgb_commit(drgb_renderer* r, const drgb_scene_desc* scene);
+
+/* IDiffRender::render (src/drender.h:98-141): images are width*height*3
+ * floats per view, concatenated in view order. */
+int drgb_render(drgb_renderer* r, const drgb_camera* cams, int n_views, float* images);
+
+/* Layout of the gradient vector of DScene(scene, mode, dmesh_ids)
+ * (src/dmesh.h:35-85, 155-222): 9 ints per differentiable mesh
+ * [vertices, instances, pos_off, color_off, tex_off, transform_off,
+ *  restricted_off(-1), full_size, mesh_id]; *total = sum of full sizes. */
+int drgb_dscene_layout(drgb_renderer* r, const int32_t* dmesh_ids, int n_ids, int32_t* layout, int64_t* total);
+
+/* IDiffRender::d_render (src/drender.h:144-167): accumulates (+=) into the
+ * gradient vector dscene (layout of drgb_dscene_layout). */
+int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoints, int n_views,
+                  int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids, float* dscene);
+
+/* IDiffRender::d_render_and_compare (src/drender.h:169-191): renders, forms
+ * the MSE loss and its adjoint 2*(I-T), clears dscene and fills it with the
+ * interior + edge gradient; out_images may be NULL. */
+int drgb_d_render_and_compare(drgb_renderer* r, const drgb_camera* cams, const float* targets, int n_views,
+                              int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids, float* dscene,
+                              float* out_images, float* loss);
+
+/* Same with device pointers (targets, dscene, out_images, loss may be device
+ * memory the caller owns); enqueued on the renderer stream, no host sync. */
+int drgb_d_render_and_compare_device(drgb_renderer* r, const drgb_camera* cams, const float* d_targets, int n_views,
+                                     int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids, float* d_dscene,
+                                     float* d_out_images, float* d_loss);
+
+/* Per-sample nearest hits of camera rays through (x,y) pixel positions
+ * (IRayTracer::CastSingleRay, raytrace_src/raytrace.h:31-41): prim, inst,
+ * geom, t, u, v arrays of n entries (host). */
+int drgb_cast_rays(drgb_renderer* r, const drgb_camera* cam, const float* xy, int64_t n, uint32_t* prim,
+                   uint32_t* inst, uint32_t* geom, float* t, float* u, float* v);
+
+/* ---- optimiser: IOptimizer / OptSimple (src/optimizer.h:52-61) ---------- */
+int drgb_opt_params_default(int alg, drgb_opt_params* out);
+/* IOptimizer::Init: scene, views and target images (host). */
+int drgb_optimizer_init(drgb_renderer* r, const drgb_scene_desc* scene, const drgb_camera* cams, const float* targets,
+                        int n_views, const drgb_opt_params* p);
+/* IOptimizer::Run: iterations of d_render_and_compare + OptStep +
+ * OptUpdateScene + StepDecay, all on the device; final_error = loss of the
+ * last iteration (optimizer_simple.cpp:272-309).  losses (n_iters floats,
+ * may be NULL) receives every iteration's loss. */
+int drgb_optimizer_run(drgb_renderer* r, int64_t n_iters, float* final_error, float* losses);
+/* Enqueue n_iters iterations without synchronising (device-resident loop). */
+int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters);
+/* Current optimised parameters of one mesh (host arrays, may be NULL). */
+int drgb_optimizer_get_mesh(drgb_renderer* r, int mesh_id, float* vertices, float* colors, float* texture,
+                            float* transforms);
+
+/* ---- measurement (no reference counterpart: the reference prints wall-clock
+ * ms/iter only, src/main.cpp:218-224, src/tests.cpp:136-203) -------------- */
+/* Runs n_iters optimiser iterations phase by phase (no graph) and returns the
+ * mean CUDA-event time of each phase on the renderer stream, in ms:
+ * out_ms[0] forward+loss+interior adjoint, [1] edge sampling, [2] optimiser
+ * step, [3] flatten+LBVH refit, [4] whole iteration. */
+int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms);
+/* Work of one optimiser iteration's pixel and edge passes, counted by an
+ * instrumented replay: counts[0] rays traced, [1] ray/box tests,
+ * [2] ray/triangle tests, [3] edge samples shaded. */
+int drgb_count_work(drgb_renderer* r, uint64_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DRGB_H */
