@@ -8,7 +8,7 @@
 #include <memory>
 #include <string>
 
-#include "engine.h"
+#include "renderer.h"
 
 namespace drgb {
 static std::atomic<int64_t> g_launches{0};
@@ -21,147 +21,8 @@ void count_launch(int n) {
 void add_launches(int64_t n) { g_launches += n; }
 }  // namespace drgb
 
-using namespace drgb;
-
 static thread_local std::string t_err;
-static void set_error(const std::string& m) { t_err = m; }
-
-template <class F>
-static int guard(F&& f) {
-  try {
-    f();
-    return DRGB_OK;
-  } catch (const CudaError& e) {
-    set_error(e.what());
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    set_error("host allocation failed");
-    return DRGB_ERR_OOM;
-  } catch (const std::exception& e) {
-    set_error(e.what());
-    return DRGB_ERR_INVALID;
-  }
-}
-
-static void require(bool c, const char* msg, int code = DRGB_ERR_INVALID) {
-  if (!c) throw CudaError(msg, code);
-}
-
-struct drgb_renderer {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  Job job;
-  DevBuf<JobDev> d_job;
-  DevBuf<int4> d_items;
-  DevBuf<int> d_counter;
-  DevBuf<CamDev> d_cam1;
-  DevBuf<float> d_xy;
-  DevBuf<uint32_t> d_u32;
-  DevBuf<float> d_f32;
-  int sm_count = 1;
-  int use_graph = 1;
-  cudaGraphExec_t graph = nullptr;
-  int64_t graph_kernels = 0;
-  bool graph_valid = false;
-
-  ~drgb_renderer() {
-    if (graph) cudaGraphExecDestroy(graph);
-    if (stream) cudaStreamDestroy(stream);
-  }
-
-  void set_device() const { DRGB_CUDA(cudaSetDevice(device)); }
-  void require_commit() const { require(job.committed, "no scene committed (call drgb_commit first)", DRGB_ERR_STATE); }
-  int px_grid() const { return sm_count * 8; }
-  int edge_grid() const { return sm_count * 8; }
-
-  // Pixel work items for the current views: view-major, tiles row-major.
-  void make_items() {
-    Job& J = job;
-    std::vector<int4> items;
-    for (int v = 0; v < J.n_views; v++) {
-      const int W = (int)J.h_cams[v].width, H = (int)J.h_cams[v].height;
-      for (int y = 0; y < H; y += J.tile_h)
-        for (int x = 0; x < W; x += J.tile_w) items.push_back(make_int4(0, v, x, y));
-    }
-    J.h_pixel_items = items;
-    d_items.upload(items.data(), items.size(), stream);
-    J.loss_part.reserve(std::max<size_t>(1, items.size()));
-    J.dev.item_base = 0;
-    J.dev.item_count = (int)items.size();
-  }
-
-  void views(const drgb_camera* cams, int n, bool same_size) {
-    require(cams != nullptr && n > 0, "need at least one camera");
-    if (same_size)
-      for (int i = 1; i < n; i++)
-        require((int)cams[i].width == (int)cams[0].width && (int)cams[i].height == (int)cams[0].height,
-                "gradient calls need all views of the same size");
-    setup_views(job, cams, n);
-    job.cams.upload(job.h_cams.data(), job.h_cams.size(), stream);
-    std::vector<int64_t> off(n + 1, 0);
-    for (int i = 0; i < n; i++) off[i + 1] = off[i] + (int64_t)cams[i].width * (int64_t)cams[i].height;
-    job.img_off.upload(off.data(), off.size(), stream);
-    make_items();
-  }
-
-  int64_t n_pixels() const {
-    int64_t s = 0;
-    for (auto& c : job.h_cams) s += (int64_t)c.width * (int64_t)c.height;
-    return s;
-  }
-
-  // Buffers of a gradient call over the current views.
-  void gradient_buffers(int edge_samples) {
-    Job& J = job;
-    require(edge_samples >= 0, "edge sample count must be >= 0");
-    const size_t npix = (size_t)J.n_views * J.W * J.H;
-    J.adj.reserve(std::max<size_t>(1, npix));
-    build_edges(J);
-    J.proj.reserve(std::max<size_t>(1, (size_t)J.n_views * J.n_vertices));
-    J.pmf.reserve(std::max<size_t>(1, (size_t)J.n_views * J.n_edges));
-    J.cdf.reserve(std::max<size_t>(1, (size_t)J.n_views * (J.n_edges + 1)));
-    J.queue.reserve(std::max<size_t>(1, (size_t)J.n_views * std::max(edge_samples, 1)));
-    J.dev.edge_samples = edge_samples;
-    J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
-  }
-
-  void push_dev() {
-    JobDev keep = job.dev;
-    sync_dev(job);
-    job.dev.item_base = keep.item_base;
-    job.dev.item_count = keep.item_count;
-    job.dev.edge_samples = keep.edge_samples;
-    job.dev.rnd = keep.rnd;
-    d_job.alloc(1);
-    DRGB_CUDA(cudaMemcpyAsync(d_job.p, &job.dev, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
-  }
-
-  void check_flags() {
-    uint32_t f = 0;
-    DRGB_CUDA(cudaMemcpyAsync(&f, job.err.p, sizeof(f), cudaMemcpyDeviceToHost, stream));
-    DRGB_CUDA(cudaStreamSynchronize(stream));
-    if (f) {
-      DRGB_CUDA(cudaMemsetAsync(job.err.p, 0, sizeof(uint32_t), stream));
-      DRGB_CUDA(cudaStreamSynchronize(stream));
-      std::string m = "kernel error flags " + std::to_string(f);
-      if (f & ERR_STACK_OVERFLOW) m += " (traversal stack overflow)";
-      if (f & ERR_TRAVERSAL_LIMIT) m += " (traversal step limit)";
-      throw CudaError(m, DRGB_ERR_KERNEL);
-    }
-  }
-
-  // Forward + loss + interior adjoint + edges of the current views; grad is
-  // cleared first.  Everything is enqueued on the stream.
-  void enqueue_iteration(bool want_images) {
-    Job& J = job;
-    const bool interior = J.mode != SILHOUETTE;
-    DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
-    int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
-    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream);
-    launch_loss_finalize(d_job.p, 1, stream);
-    if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
-  }
-};
+void drgb_set_last_error(const std::string& m) { t_err = m; }
 
 static void check_renderer(drgb_renderer* r) { require(r != nullptr, "null renderer"); }
 

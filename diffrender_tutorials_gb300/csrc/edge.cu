@@ -203,6 +203,20 @@ __global__ void __launch_bounds__(256) k_edge_shade(const JobDev* jobs, int job)
   }
 }
 
+// Same launch sequence with every size and the sample-queue counter passed
+// explicitly (for callers whose buffers are not owned by a Job).
+void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
+                      int* queue_count, int shade_grid, cudaStream_t s) {
+  if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
+  k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  k_edge_cdf<<<n_views, 32, 0, s>>>(d_jobs, job);
+  DRGB_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int), s));
+  k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  k_edge_shade<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  count_launch(5);
+}
+
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s) {
   if (J.n_edges <= 0 || J.n_views <= 0) return;
   const dim3 gp((J.n_vertices + 255) / 256, J.n_views);

@@ -1,0 +1,297 @@
+// drgb_d_render_and_compare_noalloc: forward + loss + interior adjoint + edge
+// term without allocating GPU memory during the call.
+//
+// Who needs it: callers that may not call cudaMalloc while they run -- code
+// that records work into a CUDA stream capture (a cudaMalloc during capture
+// invalidates it), engines that hand out all device memory from their own
+// pool or budget and forbid allocations after start-up, and latency-bound
+// loops where an allocation (and the device synchronisation it can cause)
+// is too costly.  drgb_d_render_and_compare_device grows its per-call
+// buffers with cudaMalloc on first use; this variant takes every per-call
+// buffer from one fixed array compiled into the library instead.
+//
+// Limits and sharing:
+//  * the array holds kScratchBytes (32 MiB).  A call whose buffers (adjoint
+//    images, edge-sample queue, tile partials, projected vertices, edge
+//    sampler, random streams) need more is rejected with DRGB_ERR_INVALID;
+//    roughly one 512x512 view with 262,144 edge samples fits;
+//  * every GPU that loads the library reserves the array until the process
+//    exits;
+//  * all calls share the one array and it keeps the previous call's
+//    contents: each call clears what must start at zero (the caller's
+//    gradient vector, the sample-queue and work-queue counters) and rewrites
+//    the rest, so calls that overlap on the GPU -- from two host threads, or
+//    enqueued on different streams without ordering -- race on it;
+//  * the first call on a device looks the array's device address up with
+//    cudaGetSymbolAddress; make that first call before any stream capture.
+// The renderer itself (scene, LBVH, model constants) must have been committed
+// beforehand; that set-up allocates as usual.
+#include <mutex>
+
+#include "renderer.h"
+
+namespace drgb {
+
+void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
+                      int* queue_count, int shade_grid, cudaStream_t s);
+
+constexpr size_t kScratchBytes = 32u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+namespace {
+
+// Device address of the scratch array, looked up once per device.
+unsigned char* scratch_address(int device) {
+  static std::mutex mu;
+  static std::vector<unsigned char*> addr;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)addr.size() <= device) addr.resize(device + 1, nullptr);
+  if (!addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      throw CudaError(std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e), DRGB_ERR_CUDA);
+    addr[device] = static_cast<unsigned char*>(p);
+  }
+  return addr[device];
+}
+
+// Bump allocator over the scratch array (256-byte aligned regions).
+struct Carve {
+  size_t used = 0;
+  template <class T>
+  size_t take(size_t count) {
+    const size_t off = (used + 255) & ~size_t(255);
+    used = off + count * sizeof(T);
+    return off;
+  }
+};
+
+// Unique edges of the differentiable meshes ordered by (v0, v1), the first
+// inserted kept (same list as the allocating path builds).
+void host_edges(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi) {
+  std::vector<int> key;
+  for (auto& L : lay) key.push_back(L.mesh_id);
+  std::sort(key.begin(), key.end());
+  struct E {
+    int v0, v1, vn0, vn1, mesh, inst;
+  };
+  std::vector<E> all;
+  for (int b = 0; b < J.n_blocks; b++) {
+    const BlockDev& bd = J.h_blocks[b];
+    if (!std::binary_search(key.begin(), key.end(), bd.mesh)) continue;
+    const MeshState& M = J.meshes[bd.mesh];
+    for (int k = 0; k + 2 < M.ni; k += 3) {
+      const int n[3] = {(int)M.h_indices[k], (int)M.h_indices[k + 1], (int)M.h_indices[k + 2]};
+      for (int e = 0; e < 3; e++) {
+        const int a = n[e], c = n[(e + 1) % 3];
+        const int ga = bd.vert_off + a, gc = bd.vert_off + c;
+        if (ga < gc) all.push_back(E{ga, gc, a, c, bd.mesh, bd.inst});
+        else all.push_back(E{gc, ga, c, a, bd.mesh, bd.inst});
+      }
+    }
+  }
+  std::stable_sort(all.begin(), all.end(), [](const E& x, const E& y) {
+    return x.v0 != y.v0 ? x.v0 < y.v0 : x.v1 < y.v1;
+  });
+  ed.clear();
+  mi.clear();
+  for (const E& e : all) {
+    if (!ed.empty() && ed.back().x == e.v0 && ed.back().y == e.v1) continue;
+    ed.push_back(make_int4(e.v0, e.v1, e.vn0, e.vn1));
+    mi.push_back(make_int2(e.mesh, e.inst));
+  }
+}
+
+// Replayed edge-sampler streams (prng stream 7777+k^2+1 of each of the 14
+// static OpenMP blocks), written into a host vector.
+void host_random_table(int n, std::vector<float>& out) {
+  out.assign(2 * (size_t)std::max(n, 1), 0.0f);
+  const int T = 14;
+  const int64_t q = n / T, r = n % T;
+  for (int k = 0; k < T; k++) {
+    const int64_t b = q * k + std::min<int64_t>(k, r);
+    const int64_t cnt = q + (k < r ? 1 : 0);
+    const uint32_t us = (uint32_t)(7777 + k * k + 1);
+    uint32_t sx = us * (us * us * 15731u + 74323u) + 871483u;
+    uint32_t sy = us * (us * us * 13734u + 37828u) + 234234u;
+    for (int i = 0; i < (int)(us % 7u); i++) {
+      const uint32_t x = sx * 17u + sy * 13123u;
+      sx = (x << 13) ^ x;
+      sy ^= (x << 7);
+    }
+    for (int64_t j = 0; j < 2 * cnt; j++) {
+      const uint32_t x = sx * 17u + sy * 13123u;
+      sx = (x << 13) ^ x;
+      sy ^= (x << 7);
+      const uint32_t tmp = (x * (x * x * 15731u + 74323u) + 871483u);
+      out[2 * b + j] = (float)tmp * (1.0f / 4294967296.0f);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace drgb
+
+extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_camera* cams, const float* d_targets,
+                                                 int n_views, int edge_samples, const int32_t* ids, int n_ids,
+                                                 float* d_dscene, float* d_loss) {
+  return guard([&] {
+    require(r != nullptr, "null renderer");
+    r->require_commit();
+    require(cams && d_targets && d_dscene && d_loss && n_views > 0, "null argument");
+    require(edge_samples >= 0, "edge sample count must be >= 0");
+    for (int i = 1; i < n_views; i++)
+      require((int)cams[i].width == (int)cams[0].width && (int)cams[i].height == (int)cams[0].height,
+              "gradient calls need all views of the same size");
+    r->set_device();
+    Job& J = r->job;
+    unsigned char* base = scratch_address(r->device);
+
+    // ---- host-side description of the call (no device memory involved) ----
+    const int W = (int)cams[0].width, H = (int)cams[0].height;
+    require(W >= 1 && H >= 1, "camera size must be positive");
+    std::vector<CamDev> hc(n_views);
+    for (int i = 0; i < n_views; i++) hc[i] = make_cam(cams[i]);
+    std::vector<int64_t> off(n_views + 1, 0);
+    for (int i = 0; i < n_views; i++) off[i + 1] = off[i] + (int64_t)W * H;
+    std::vector<int4> items;
+    for (int v = 0; v < n_views; v++)
+      for (int y = 0; y < H; y += J.tile_h)
+        for (int x = 0; x < W; x += J.tile_w) items.push_back(make_int4(0, v, x, y));
+    std::vector<DLayout> lay;
+    const int64_t grad_total = compute_layout(J, ids, n_ids, lay);
+    std::vector<MeshDev> md(J.meshes.size());
+    for (size_t m = 0; m < J.meshes.size(); m++) {
+      const MeshState& M = J.meshes[m];
+      md[m] = MeshDev{M.texture.p, M.tex_w, M.tex_h, M.tex_c, -1, 0, 0, -1, -1, 0, M.nv, M.n_inst};
+    }
+    for (size_t k = 0; k < lay.size(); k++) {
+      MeshDev& d = md[lay[k].mesh_id];
+      d.dslot = (int)k;
+      d.g_base = lay[k].base;
+      d.pos_off = lay[k].pos_off;
+      d.color_off = lay[k].color_off;
+      d.tex_off = lay[k].tex_off;
+      d.tr_off = lay[k].tr_off;
+    }
+    std::vector<int4> ed;
+    std::vector<int2> emi;
+    host_edges(J, lay, ed, emi);
+    const int E = (int)ed.size();
+    std::vector<float> rnd;
+    if (edge_samples > 0) host_random_table(edge_samples, rnd);
+
+    // ---- carve the scratch array ----
+    Carve c;
+    const size_t o_job = c.take<JobDev>(1);
+    const size_t o_cams = c.take<CamDev>(n_views);
+    const size_t o_off = c.take<int64_t>(n_views + 1);
+    const size_t o_items = c.take<int4>(items.size());
+    const size_t o_part = c.take<double>(items.size());
+    const size_t o_md = c.take<MeshDev>(std::max<size_t>(1, md.size()));
+    const size_t o_adj = c.take<float4>((size_t)n_views * W * H);
+    const size_t o_proj = c.take<float4>((size_t)n_views * std::max(1, J.n_vertices));
+    const size_t o_pmf = c.take<float>((size_t)n_views * std::max(1, E));
+    const size_t o_cdf = c.take<float>((size_t)n_views * (E + 1));
+    const size_t o_queue = c.take<int4>((size_t)n_views * std::max(1, edge_samples));
+    const size_t o_edges = c.take<int4>(std::max(1, E));
+    const size_t o_emi = c.take<int2>(std::max(1, E));
+    const size_t o_rnd = c.take<float>(std::max<size_t>(1, rnd.size()));
+    const size_t o_cnt = c.take<int>(2);
+    if (c.used > kScratchBytes)
+      throw CudaError("drgb_d_render_and_compare_noalloc: this call needs " + std::to_string(c.used) +
+                          " bytes of scratch; the fixed array holds " + std::to_string(kScratchBytes) +
+                          " bytes (use drgb_d_render_and_compare_device for larger calls)",
+                      DRGB_ERR_INVALID);
+
+    // ---- device view of the job: scene from the committed renderer, every
+    // per-call buffer inside the scratch array, inputs/outputs from the caller
+    JobDev d{};
+    d.n_vertices = J.n_vertices;
+    d.n_tris = J.n_tris;
+    d.n_blocks = J.n_blocks;
+    d.n_meshes = (int)J.meshes.size();
+    d.pos = J.pos.p;
+    d.orig = J.orig.p;
+    d.col = J.col.p;
+    d.nrm = J.nrm.p;
+    d.tc = J.tc.p;
+    d.tri_v = J.tri_v.p;
+    d.blocks = J.blocks.p;
+    d.meshes = reinterpret_cast<const MeshDev*>(base + o_md);
+    d.tr_inv0 = J.tr_inv0.p;
+    d.nodes = J.nodes.p;
+    d.tri = J.tri.p;
+    d.root = J.root;
+    d.trace_bruteforce = J.trace_bruteforce;
+    d.mode = J.mode;
+    d.spp = J.spp;
+    d.sq = J.sq;
+    d.S = J.S;
+    d.ham = J.ham.p;
+    d.mp = J.mp;
+    d.n_views = n_views;
+    d.cams = reinterpret_cast<const CamDev*>(base + o_cams);
+    d.W = W;
+    d.H = H;
+    d.grad = d_dscene;
+    d.err = J.err.p;
+    d.images = nullptr;
+    d.img_off = reinterpret_cast<const int64_t*>(base + o_off);
+    d.targets = d_targets;
+    d.adj = reinterpret_cast<float4*>(base + o_adj);
+    d.adj_in = nullptr;
+    d.loss_part = reinterpret_cast<double*>(base + o_part);
+    d.loss_out = d_loss;
+    d.tile_w = J.tile_w;
+    d.tile_h = J.tile_h;
+    d.item_base = 0;
+    d.item_count = (int)items.size();
+    d.edges = reinterpret_cast<const int4*>(base + o_edges);
+    d.edge_mi = reinterpret_cast<const int2*>(base + o_emi);
+    d.n_edges = E;
+    d.proj = reinterpret_cast<float4*>(base + o_proj);
+    d.pmf = reinterpret_cast<float*>(base + o_pmf);
+    d.cdf = reinterpret_cast<float*>(base + o_cdf);
+    d.queue = reinterpret_cast<int4*>(base + o_queue);
+    int* counters = reinterpret_cast<int*>(base + o_cnt);  // [0] sample queue, [1] work queue
+    d.queue_count = counters;
+    d.queue_cap = n_views * std::max(1, edge_samples);
+    d.edge_samples = edge_samples;
+    d.rnd = reinterpret_cast<const float*>(base + o_rnd);
+    d.work = nullptr;
+
+    // ---- copies into the scratch array (pageable host sources; the copies
+    // complete their host reads before returning) and the launches ----
+    cudaStream_t s = r->stream;
+    auto put = [&](size_t o, const void* src, size_t bytes) {
+      if (bytes) DRGB_CUDA(cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, s));
+    };
+    put(o_job, &d, sizeof(JobDev));
+    put(o_cams, hc.data(), sizeof(CamDev) * hc.size());
+    put(o_off, off.data(), sizeof(int64_t) * off.size());
+    put(o_items, items.data(), sizeof(int4) * items.size());
+    put(o_md, md.data(), sizeof(MeshDev) * md.size());
+    put(o_edges, ed.data(), sizeof(int4) * ed.size());
+    put(o_emi, emi.data(), sizeof(int2) * emi.size());
+    if (edge_samples > 0) put(o_rnd, rnd.data(), sizeof(float) * rnd.size());
+    if (grad_total > 0) DRGB_CUDA(cudaMemsetAsync(d_dscene, 0, sizeof(float) * grad_total, s));
+    DRGB_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), s));
+    const JobDev* d_job = reinterpret_cast<const JobDev*>(base + o_job);
+    const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
+    launch_pixels(d_job, reinterpret_cast<const int4*>(base + o_items), (int)items.size(), counters + 1, flags,
+                  r->px_grid(), s);
+    launch_loss_finalize(d_job, 1, s);
+    if (edge_samples > 0)
+      launch_edges_raw(d_job, 0, E, n_views, J.n_vertices, edge_samples, counters, r->edge_grid(), s);
+    uint32_t f = 0;
+    DRGB_CUDA(cudaMemcpyAsync(&f, J.err.p, sizeof(f), cudaMemcpyDeviceToHost, s));
+    DRGB_CUDA(cudaStreamSynchronize(s));
+    if (f) {
+      DRGB_CUDA(cudaMemsetAsync(J.err.p, 0, sizeof(uint32_t), s));
+      DRGB_CUDA(cudaStreamSynchronize(s));
+      throw CudaError("kernel error flags " + std::to_string(f), DRGB_ERR_KERNEL);
+    }
+  });
+}

@@ -69,6 +69,8 @@ _SIGS = {
     "drgb_d_render_and_compare": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP, VP, VP]),
     "drgb_d_render_and_compare_device": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP,
                                                    VP, VP]),
+    "drgb_d_render_and_compare_noalloc": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int, C.c_int, VP, C.c_int, VP,
+                                                    VP]),
     "drgb_cast_rays": (C.c_int, [VP, C.POINTER(Camera), VP, C.c_int64, VP, VP, VP, VP, VP, VP]),
     "drgb_opt_params_default": (C.c_int, [C.c_int, C.POINTER(OptParams)]),
     "drgb_optimizer_init": (C.c_int, [VP, C.POINTER(SceneDesc), C.POINTER(Camera), VP, C.c_int,

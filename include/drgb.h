@@ -167,6 +167,23 @@ int drgb_d_render_and_compare_device(drgb_renderer* r, const drgb_camera* cams, 
                                      int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids, float* d_dscene,
                                      float* d_out_images, float* d_loss);
 
+/* No counterpart in the reference.  The same computation and outputs as
+ * drgb_d_render_and_compare_device (gradient vector and loss written to
+ * caller-owned device memory), for callers that cannot allocate GPU memory
+ * while they run: code recording into a CUDA stream capture, engines that
+ * own all device memory through a fixed pool, latency-bound loops.  The call
+ * itself makes no cudaMalloc/cudaFree; its per-call buffers come from one
+ * 32 MiB array compiled into the library (reserved on every GPU that loads
+ * it, until exit).  Calls needing more (roughly: beyond one 512x512 view
+ * with 262,144 edge samples) return DRGB_ERR_INVALID.  All calls share that
+ * array, so calls that overlap on the GPU race; the first call on a device
+ * looks its address up and should come before any stream capture.  The
+ * scene must have been committed (drgb_commit) beforehand; returns after
+ * the results are in device memory. */
+int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_camera* cams, const float* d_targets,
+                                      int n_views, int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids,
+                                      float* d_dscene, float* d_loss);
+
 /* Per-sample nearest hits of camera rays through (x,y) pixel positions
  * (IRayTracer::CastSingleRay, raytrace_src/raytrace.h:31-41): prim, inst,
  * geom, t, u, v arrays of n entries (host). */
