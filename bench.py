@@ -41,6 +41,9 @@ WORKLOADS = {
                       views=8, sample_res=64, sample_views=1),
     "cube": dict(name="cube12_vertexcolor_1view_256x256_16spp", sub=None, mode=2, spp=16, res=256, views=1,
                  sample_res=256, sample_views=1),
+    # small case of the icosphere kernels for ncu section captures
+    "icosphere_small": dict(name="icosphere5120_pointlight_2views_256x256_16spp", sub=4, mode=16, spp=16, res=256,
+                            views=2, sample_res=32, sample_views=1),
 }
 
 

@@ -39,18 +39,22 @@ def _stale(lib, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, extra_flags=(), out=None):
+    """Compile the library; `out` names another output path (and object
+    directory) for builds with different `extra_flags`."""
+    lib = out or LIB
+    objdir = os.path.dirname(os.path.abspath(lib))
+    os.makedirs(objdir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "drgb.h"))
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    if not force and not _stale(LIB, srcs + headers + [__file__]):
-        return LIB
+    if not force and not _stale(lib, srcs + headers + [__file__]):
+        return lib
     cc = nvcc()
     objs = []
 
     def comp(src):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
         cmd = [cc, *flags(), *extra_flags, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
@@ -61,13 +65,13 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(comp, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

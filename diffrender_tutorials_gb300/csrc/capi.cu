@@ -92,7 +92,7 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         require(v >= 1, "tile size must be >= 1");
         const int tw = option == DRGB_OPT_TILE_W ? v : r->job.tile_w;
         const int th = option == DRGB_OPT_TILE_H ? v : r->job.tile_h;
-        require(tw * th * r->job.S <= 256, "tile_w*tile_h*samples must be <= 256");
+        require(tw * th <= 32 && tw * th * r->job.S <= 64, "a tile holds at most 32 pixels and 64 samples");
         r->job.tile_w = tw;
         r->job.tile_h = th;
         break;
@@ -143,7 +143,7 @@ int drgb_render(drgb_renderer* r, const drgb_camera* cams, int n_views, float* i
     J.images.reserve(3 * (size_t)npx);
     r->push_dev();
     launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_FWD | PX_IMG,
-                  r->px_grid(), r->stream);
+                  r->px_grid(), r->stream, J.mode);
     DRGB_CUDA(cudaMemcpyAsync(images, J.images.p, sizeof(float) * 3 * npx, cudaMemcpyDeviceToHost, r->stream));
     r->check_flags();
   });
@@ -185,7 +185,7 @@ int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoin
     launch_adj_convert(r->d_job.p, (int64_t)npix, r->stream);
     if (J.mode != SILHOUETTE)
       launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_ADJ, r->px_grid(),
-                    r->stream);
+                    r->stream, J.mode);
     if (edge_samples_in_total > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
     if (J.grad_total > 0)
       DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, cudaMemcpyDeviceToHost, r->stream));
@@ -418,7 +418,7 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
       DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), r->stream));
       const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
       launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
-                    r->stream);
+                    r->stream, J.mode);
       launch_loss_finalize(r->d_job.p, 1, r->stream);
       DRGB_CUDA(cudaEventRecord(ev[1], r->stream));
       if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
@@ -465,7 +465,7 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
     DRGB_CUDA(cudaMemcpyAsync(save.p, J.grad.p, save.bytes(), cudaMemcpyDeviceToDevice, r->stream));
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, save.bytes(), r->stream));
     launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
-                  r->stream);
+                  r->stream, J.mode);
     if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
     int shaded = 0;
     DRGB_CUDA(cudaMemcpyAsync(&shaded, J.queue_count.p, sizeof(int), cudaMemcpyDeviceToHost, r->stream));

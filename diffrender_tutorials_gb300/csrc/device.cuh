@@ -342,8 +342,17 @@ __device__ __forceinline__ void add_work(const JobDev& J, unsigned boxes, unsign
   }
 }
 
+// Traversal is kept out of line by default: it is called from several
+// places per kernel (camera hits, shadow rays, re-traced adjoint samples),
+// and one shared copy of the loop keeps the kernels' code within the
+// instruction cache.  Build with -DDRGB_TRACE_INLINE to inline it instead.
+#ifdef DRGB_TRACE_INLINE
+#define DRGB_TRACE_ATTR __forceinline__
+#else
+#define DRGB_TRACE_ATTR __noinline__
+#endif
 template <bool ANY>
-__device__ __forceinline__ bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best) {
+__device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best) {
   best.t = tFar;
   best.tri = -1;
   best.u = 0.0f;
@@ -494,9 +503,10 @@ __device__ __forceinline__ float lpv_factor(const JobDev& J, const Surf& s) {
   const float d2 = dot(L, L);
   const float dist = sqrtf(d2);
   const f3 l = L / dist;
-  Hit sh;
-  const float vis = trace<true>(J, p, l, 0.0f, dist, sh) ? 0.0f : 1.0f;
   const float ndl = ref_max(0.0f, dot(n, l));
+  // with n.l <= 0 the lit term is 0 whatever the visibility: no shadow ray
+  Hit sh;
+  const float vis = (ndl > 0.0f && trace<true>(J, p, l, 0.0f, dist, sh)) ? 0.0f : 1.0f;
   return vis * J.mp.light_intensity * ndl / d2 + J.mp.ambient;
 }
 
@@ -568,15 +578,19 @@ __device__ inline f3 path_diffuse(const JobDev& J, const Surf& first, uint32_t k
   return L;
 }
 
-// shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).
+// shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).  MODE != 0
+// compiles a single model (no code, hence no registers, for the others);
+// MODE == 0 switches on the job's model at run time.
+template <int MODE = 0>
 __device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
+  const int mode = MODE ? MODE : J.mode;
   Surf s;
   if (!cast(J, cam, x, y, s)) {
-    if (J.mode == PATH_DIFFUSE) return mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
+    if (mode == PATH_DIFFUSE) return mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
     return mk(0.0f, 0.0f, 0.0f);
   }
   const float u = s.h.u, v = s.h.v;
-  switch (J.mode) {
+  switch (mode) {
     case SILHOUETTE:
       return mk(1.0f, 1.0f, 1.0f);
     case VERTEX_COLOR:
@@ -595,9 +609,11 @@ __device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y,
       const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
       const f3 diffuse = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
       const f3 surf_pos = s.ro + s.rd * (s.h.t - 1e-5f);
+      const float ndl = ref_max(0.0f, dot(n, to_light));
+      // (colour * vis) * 0 is 0 for either visibility: trace only when lit
       Hit sh;
-      const float shv = trace<true>(J, surf_pos, to_light, 0.0f, 1e9f, sh) ? 0.0f : 1.0f;
-      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * shv) * ref_max(0.0f, dot(n, to_light));
+      const float shv = (ndl > 0.0f && trace<true>(J, surf_pos, to_light, 0.0f, 1e9f, sh)) ? 0.0f : 1.0f;
+      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * shv) * ndl;
       return (lit + mk(1.0f, 1.0f, 1.0f) * 0.1f) * diffuse;
     }
     case LAMBERT_POINT_VCOLOR: {

@@ -329,9 +329,10 @@ void set_dscene(Job& J, const int32_t* ids, int n_ids) {
   DRGB_CUDA(cudaStreamSynchronize(0));
 }
 
-// Pixel tile with at most 256 samples: maximise pixels, prefer square.
+// Pixel tile of one warp: at most 32 samples (one pixel when a pixel has
+// more); maximise pixels, prefer square.
 void choose_tile(int S, int& tw, int& th) {
-  const int P = std::max(1, 256 / std::max(1, S));
+  const int P = std::max(1, 32 / std::max(1, S));
   int best = 0;
   tw = th = 1;
   for (int h = 1; h <= P; h++) {

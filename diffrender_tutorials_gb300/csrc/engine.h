@@ -193,7 +193,7 @@ CamDev make_cam(const drgb_camera& c);
 // Pixel kernel flags
 enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8 };
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
-                   cudaStream_t s);
+                   cudaStream_t s, int mode);
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
 void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s);
 void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, int64_t n, uint32_t* prim,

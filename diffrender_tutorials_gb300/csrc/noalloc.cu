@@ -281,7 +281,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     const JobDev* d_job = reinterpret_cast<const JobDev*>(base + o_job);
     const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
     launch_pixels(d_job, reinterpret_cast<const int4*>(base + o_items), (int)items.size(), counters + 1, flags,
-                  r->px_grid(), s);
+                  r->px_grid(), s, J.mode);
     launch_loss_finalize(d_job, 1, s);
     if (edge_samples > 0)
       launch_edges_raw(d_job, 0, E, n_views, J.n_vertices, edge_samples, counters, r->edge_grid(), s);

@@ -74,13 +74,16 @@ __device__ __forceinline__ void texture_grad(f3 val, float tx, float ty, int w, 
   atomicAdd(d11 + 0, w11 * val.x); atomicAdd(d11 + 1, w11 * val.y); atomicAdd(d11 + 2, w11 * val.z);
 }
 
-// shade_grad<M> for one sample; every lane of the warp must call it.
+// shade_grad<M> for one sample; every lane of the warp must call it.  MODE
+// as for shade().
+template <int MODE>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
                                            uint32_t key, float* wscr) {
+  const int mode = MODE ? MODE : J.mode;
   Surf s;
   bool hit = false;
   if (active) hit = cast(J, cam, x, y, s);
-  if (model_has_color(J.mode)) {
+  if (model_has_color(mode)) {
     float c[9];
     int tri = -1, gA = 0, gB = 0, gC = 0;
 #pragma unroll
@@ -88,11 +91,11 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
     if (hit) {
       const float u = s.h.u, v = s.h.v;
       f3 ca, cb, cc;
-      if (J.mode == VERTEX_COLOR) {
+      if (mode == VERTEX_COLOR) {
         ca = val * (1.0f - u - v);
         cb = val * v;
         cc = val * u;
-      } else if (J.mode == LAMBERT_POINT_VCOLOR) {
+      } else if (mode == LAMBERT_POINT_VCOLOR) {
         const float k = lpv_factor(J, s);
         ca = val * ((1.0f - u - v) * k);
         cb = val * (v * k);
@@ -112,7 +115,7 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
       gA = s.A; gB = s.B; gC = s.C;
     }
     scatter_vertex_colors(J, tri, gA, gB, gC, c, wscr);
-  } else if (model_has_tex(J.mode) && hit) {
+  } else if (model_has_tex(mode) && hit) {
     const BlockDev bd = J.blocks[s.block];
     const MeshDev& md = J.meshes[bd.mesh];
     if (md.dslot >= 0 && md.tex_off >= 0) {
@@ -122,149 +125,177 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
   }
 }
 
-template <int FLAGS>
+// One warp per work item: a tile of tile_w x tile_h pixels whose samples
+// fill at most 64 lanes (two passes of 32).  Warps take items from an atomic
+// queue on their own and synchronise only within themselves, so no warp
+// waits for a slower one.
+constexpr int PX_WARPS = PX_THREADS / 32;
+constexpr int PX_MAX_SAMPLES = 64;
+
+template <int MODE>
 __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
-                                                       int n_items, int* counter) {
-  __shared__ JobDev sJ;
-  __shared__ CamDev sC;
-  __shared__ float s_col[PX_THREADS * 3];
-  __shared__ float4 s_adj[PX_THREADS];
-  __shared__ double s_loss[PX_THREADS];
-  __shared__ float s_ham[2 * 64];
-  __shared__ float wscr_all[PX_THREADS / 32][9 * 32];
-  __shared__ int s_item;
-  __shared__ int s_job;
-  const int tid = threadIdx.x;
-  float* wscr = wscr_all[tid >> 5];
-  if (tid == 0) s_job = -1;
-  __syncthreads();
+                                                       int n_items, int* counter, const int flags) {
+  __shared__ JobDev sJ_all[PX_WARPS];
+  __shared__ CamDev sC_all[PX_WARPS];
+  __shared__ float s_col_all[PX_WARPS][PX_MAX_SAMPLES * 3];
+  __shared__ float4 s_adj_all[PX_WARPS][32];
+  __shared__ float s_ham_all[PX_WARPS][2 * 64];
+  __shared__ float wscr_all[PX_WARPS][9 * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  JobDev& J = sJ_all[warp];
+  CamDev& C = sC_all[warp];
+  float* s_col = s_col_all[warp];
+  float4* s_adj = s_adj_all[warp];
+  float* s_ham = s_ham_all[warp];
+  float* wscr = wscr_all[warp];
+  int cur_job = -1, cur_view = -1;
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int it = s_item;
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
     if (it >= n_items) break;
     const int4 item = items[it];
-    if (item.x != s_job) {
+    if (item.x != cur_job) {
       const int* src = reinterpret_cast<const int*>(jobs + item.x);
-      int* dst = reinterpret_cast<int*>(&sJ);
-      for (int i = tid; i < (int)(sizeof(JobDev) / sizeof(int)); i += PX_THREADS) dst[i] = src[i];
-      __syncthreads();
-      for (int i = tid; i < 2 * sJ.spp && i < 128; i += PX_THREADS) s_ham[i] = sJ.ham[i];
-      if (tid == 0) s_job = item.x;
+      int* dst = reinterpret_cast<int*>(&J);
+      for (int i = lane; i < (int)(sizeof(JobDev) / sizeof(int)); i += 32) dst[i] = src[i];
+      __syncwarp();
+      for (int i = lane; i < 2 * J.spp && i < 128; i += 32) s_ham[i] = J.ham[i];
+      cur_job = item.x;
+      cur_view = -1;
     }
-    {
-      const int* src = reinterpret_cast<const int*>(sJ.cams + item.y);
-      int* dst = reinterpret_cast<int*>(&sC);
-      for (int i = tid; i < (int)(sizeof(CamDev) / sizeof(int)); i += PX_THREADS) dst[i] = src[i];
+    if (item.y != cur_view) {
+      const int* src = reinterpret_cast<const int*>(J.cams + item.y);
+      int* dst = reinterpret_cast<int*>(&C);
+      for (int i = lane; i < (int)(sizeof(CamDev) / sizeof(int)); i += 32) dst[i] = src[i];
+      cur_view = item.y;
     }
-    __syncthreads();
-    const JobDev& J = sJ;
+    __syncwarp();
     const int view = item.y, x0 = item.z, y0 = item.w;
-    const int W = (int)sC.width, H = (int)sC.height;
-    const int tw = J.tile_w, th = J.tile_h;
-    const int P = tw * th;
+    const int W = (int)C.width, H = (int)C.height;
+    const int tw = J.tile_w;
+    const int P = tw * J.tile_h;
     const int S = J.S, sq = J.sq;
     const int NS = P * S;
-    // sample of this thread (samples of a pixel are consecutive threads)
-    const int p = tid / S, k = tid - p * S;
-    const int px = x0 + p % tw, py = y0 + p / tw;
-    const bool valid = tid < NS && px < W && py < H;
-    const int64_t pix = valid ? (int64_t)py * W + px : 0;
-    if (FLAGS & PX_FWD) {
-      f3 c = mk(0.0f, 0.0f, 0.0f);
-      if (valid) {
-        const int dy = k / sq, dx = k - dy * sq;
-        const float xoff = (dx + 0.5f) / (float)sq;
-        const float yoff = (dy + 0.5f) / (float)sq;
-        const uint32_t key = ((uint32_t)view * 0x9E3779B9u) ^
-                             ((uint32_t)(pix * 64 + dy * sq + dx) * 2654435761u);
-        c = shade(J, sC, (float)px + xoff, (float)py + yoff, key) / (float)S;
+    if (flags & PX_FWD) {
+      for (int base = 0; base < NS; base += 32) {
+        const int s = base + lane;
+        const int p = s / S, k = s - p * S;
+        const int px = x0 + p % tw, py = y0 + p / tw;
+        f3 c = mk(0.0f, 0.0f, 0.0f);
+        if (s < NS && px < W && py < H) {
+          const int dy = k / sq, dx = k - dy * sq;
+          const float xoff = (dx + 0.5f) / (float)sq;
+          const float yoff = (dy + 0.5f) / (float)sq;
+          const int64_t pix = (int64_t)py * W + px;
+          const uint32_t key = ((uint32_t)view * 0x9E3779B9u) ^
+                               ((uint32_t)(pix * 64 + dy * sq + dx) * 2654435761u);
+          c = shade<MODE>(J, C, (float)px + xoff, (float)py + yoff, key) / (float)S;
+        }
+        if (s < NS) {
+          s_col[3 * s + 0] = c.x;
+          s_col[3 * s + 1] = c.y;
+          s_col[3 * s + 2] = c.z;
+        }
       }
-      if (tid < NS) {
-        s_col[3 * tid + 0] = c.x;
-        s_col[3 * tid + 1] = c.y;
-        s_col[3 * tid + 2] = c.z;
-      }
-      __syncthreads();
+      __syncwarp();
       double lsum = 0.0;
-      if (tid < P) {
-        const int qx = x0 + tid % tw, qy = y0 + tid / tw;
+      if (lane < P) {
+        const int qx = x0 + lane % tw, qy = y0 + lane / tw;
         if (qx < W && qy < H) {
           float ax = 0.0f, ay = 0.0f, az = 0.0f;
-          for (int j = 0; j < S; j++) {
-            ax += s_col[3 * (tid * S + j) + 0];
-            ay += s_col[3 * (tid * S + j) + 1];
-            az += s_col[3 * (tid * S + j) + 2];
+          for (int j = 0; j < S; j++) {  // the reference's summation order
+            ax += s_col[3 * (lane * S + j) + 0];
+            ay += s_col[3 * (lane * S + j) + 1];
+            az += s_col[3 * (lane * S + j) + 2];
           }
           const int64_t q = (int64_t)qy * W + qx;
-          if ((FLAGS & PX_IMG) && J.images) {
+          if ((flags & PX_IMG) && J.images) {
             float* o = J.images + 3 * (J.img_off[view] + q);
             o[0] = ax; o[1] = ay; o[2] = az;
           }
-          if (FLAGS & PX_LOSS) {
+          if (flags & PX_LOSS) {
             const float* t = J.targets + 3 * (J.img_off[view] + q);
             const float dx = ax - t[0], dy = ay - t[1], dz = az - t[2];
             const float4 a = make_float4(2.0f * dx, 2.0f * dy, 2.0f * dz, 0.0f);
-            s_adj[tid] = a;
+            s_adj[lane] = a;
             J.adj[(int64_t)view * J.W * J.H + q] = a;
             lsum = (double)(dx * dx + dy * dy + dz * dz);
           }
         }
-        s_loss[tid] = lsum;
       }
-      __syncthreads();
-      if ((FLAGS & PX_LOSS) && tid == 0) {
+      if (flags & PX_LOSS) {
+        // pixel order within the tile
         double acc = 0.0;
-        for (int j = 0; j < P; j++) acc += s_loss[j];
-        J.loss_part[it - J.item_base] = acc;
+        for (int j = 0; j < P; j++) acc += __shfl_sync(0xffffffffu, lsum, j);
+        if (lane == 0) J.loss_part[it - J.item_base] = acc;
       }
     }
-    if (FLAGS & PX_ADJ) {
-      if (!(FLAGS & PX_LOSS)) {
-        if (tid < P) {
-          const int qx = x0 + tid % tw, qy = y0 + tid / tw;
+    if (flags & PX_ADJ) {
+      if (!(flags & PX_LOSS)) {
+        if (lane < P) {
+          const int qx = x0 + lane % tw, qy = y0 + lane / tw;
           float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
           if (qx < W && qy < H) {
             const float* src = J.adj_in + 3 * ((int64_t)view * J.W * J.H + (int64_t)qy * W + qx);
             a = make_float4(src[0], src[1], src[2], 0.0f);
           }
-          s_adj[tid] = a;
+          s_adj[lane] = a;
         }
-        __syncthreads();
       }
-      // each warp runs its samples together (the scatter is warp-collective)
-      f3 val = mk(0.0f, 0.0f, 0.0f);
-      bool act = false;
-      float sx = 0.0f, sy = 0.0f;
-      uint32_t key = 0;
-      if (valid) {
-        const float4 a = s_adj[p];
-        val = mk(a.x, a.y, a.z) / (float)S;
-        act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
-        sx = (float)px + s_ham[2 * k];
-        sy = (float)py + s_ham[2 * k + 1];
-        key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
+      __syncwarp();
+      for (int base = 0; base < NS; base += 32) {
+        const int s = base + lane;
+        const int p = s / S, k = s - p * S;
+        const int px = x0 + p % tw, py = y0 + p / tw;
+        f3 val = mk(0.0f, 0.0f, 0.0f);
+        bool act = false;
+        float sx = 0.0f, sy = 0.0f;
+        uint32_t key = 0;
+        if (s < NS && px < W && py < H) {
+          const float4 a = s_adj[p];
+          val = mk(a.x, a.y, a.z) / (float)S;
+          act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
+          sx = (float)px + s_ham[2 * k];
+          sy = (float)py + s_ham[2 * k + 1];
+          const int64_t pix = (int64_t)py * W + px;
+          key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
+        }
+        shade_grad<MODE>(J, C, act, sx, sy, val, key, wscr);
       }
-      shade_grad(J, sC, act, sx, sy, val, key, wscr);
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
-// Loss of each job: per view, double sum of its items' partials -> float;
-// float sum over views; divided by views*W*H (drender.h:184-190).
-__global__ void k_loss_finalize(const JobDev* jobs, int n_jobs) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+// Loss of each job (one block per job): per view, the double sum of its
+// items' partials -> float; float sum over views in view order; divided by
+// views*W*H (drender.h:184-190).  Each thread sums a contiguous run of items
+// and the 256 run sums are added in run order, so the result does not
+// depend on scheduling.
+constexpr int LOSS_THREADS = 256;
+__global__ void __launch_bounds__(LOSS_THREADS) k_loss_finalize(const JobDev* jobs, int n_jobs) {
+  __shared__ double part[LOSS_THREADS];
+  const int j = blockIdx.x;
   if (j >= n_jobs) return;
   const JobDev& J = jobs[j];
   const int per_view = J.item_count / J.n_views;
+  const int chunk = (per_view + LOSS_THREADS - 1) / LOSS_THREADS;
   float mse = 0.0f;
   for (int v = 0; v < J.n_views; v++) {
+    const int b = threadIdx.x * chunk, e = min(per_view, b + chunk);
     double acc = 0.0;
-    for (int i = 0; i < per_view; i++) acc += J.loss_part[v * per_view + i];
-    mse += (float)acc;
+    for (int i = b; i < e; i++) acc += J.loss_part[v * per_view + i];
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int t = 0; t < LOSS_THREADS; t++) s += part[t];
+      mse += (float)s;
+    }
+    __syncthreads();
   }
-  J.loss_out[0] = mse / (float)(J.n_views * J.W * J.H);
+  if (threadIdx.x == 0) J.loss_out[0] = mse / (float)(J.n_views * J.W * J.H);
 }
 
 // Caller-supplied adjoint images (3 floats per pixel) -> float4 adjoint.
@@ -307,38 +338,30 @@ void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, in
   count_launch();
 }
 
+// `mode` selects the kernel compiled for one shading model; 0 (a launch whose
+// jobs mix models) runs the generic kernel that switches per job.
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
-                   cudaStream_t s) {
+                   cudaStream_t s, int mode) {
   if (n_items <= 0) return;
+  if ((flags & PX_LOSS) && !(flags & PX_FWD)) throw CudaError("loss needs the forward pass", DRGB_ERR_INVALID);
   DRGB_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int), s));
   if (grid <= 0 || grid > n_items) grid = n_items;
-  switch (flags) {
-    case PX_FWD | PX_IMG:
-      k_pixels<PX_FWD | PX_IMG><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
+  switch (mode) {
+    case SILHOUETTE: k_pixels<SILHOUETTE><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case VERTEX_COLOR: k_pixels<VERTEX_COLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT: k_pixels<LAMBERT><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT_POINT_VCOLOR:
+      k_pixels<LAMBERT_POINT_VCOLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
       break;
-    case PX_FWD | PX_LOSS | PX_ADJ | PX_IMG:
-      k_pixels<PX_FWD | PX_LOSS | PX_ADJ | PX_IMG><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
-      break;
-    case PX_FWD | PX_LOSS | PX_ADJ:
-      k_pixels<PX_FWD | PX_LOSS | PX_ADJ><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
-      break;
-    case PX_FWD | PX_LOSS | PX_IMG:
-      k_pixels<PX_FWD | PX_LOSS | PX_IMG><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
-      break;
-    case PX_FWD | PX_LOSS:
-      k_pixels<PX_FWD | PX_LOSS><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
-      break;
-    case PX_ADJ:
-      k_pixels<PX_ADJ><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter);
-      break;
-    default:
-      throw CudaError("unsupported pixel kernel flags", DRGB_ERR_INVALID);
+    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    default: k_pixels<0><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
   }
   count_launch();
 }
 
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s) {
-  k_loss_finalize<<<(n_jobs + 63) / 64, 64, 0, s>>>(d_jobs, n_jobs);
+  k_loss_finalize<<<n_jobs, LOSS_THREADS, 0, s>>>(d_jobs, n_jobs);
   count_launch();
 }
 

@@ -149,7 +149,7 @@ struct drgb_renderer {
     const bool interior = J.mode != SILHOUETTE;
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
     int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
-    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream);
+    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream, J.mode);
     launch_loss_finalize(d_job.p, 1, stream);
     if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
   }

@@ -96,7 +96,7 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("DRGB_LIB") or LIB_PATH
     if not os.path.exists(path):
         from . import build as _build
         _build.build()

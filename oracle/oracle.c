@@ -521,8 +521,9 @@ static float lpv_factor(const ctx_t* c, const surf_t* sf) {
   const float d2 = dot3(L, L);
   const float dist = sqrtf(d2);
   const f3 l = div3s(L, dist);
-  const float vis = any_hit(s, p, l, 0.0f, dist) ? 0.0f : 1.0f;
   const float ndl = maxf_ref(0.0f, dot3(n, l));
+  /* the lit term is 0 when n.l <= 0 whatever the visibility */
+  const float vis = (ndl > 0.0f && any_hit(s, p, l, 0.0f, dist)) ? 0.0f : 1.0f;
   return vis * c->mp->light_intensity * ndl / d2 + c->mp->ambient;
 }
 
@@ -618,8 +619,10 @@ static f3 shade(const ctx_t* c, f2 sp) {
       f3 diffuse = sample_bilinear(tc, m->tex_w, m->tex_h, m->texture);
       f3 surf_pos = add3(sf.ro, scl3(sf.rd, sf.h.t - BIAS));
       const f3 to_light = scl3(light_dir, -1.0f);
-      float sh = nearest_hit(s, surf_pos, to_light, 0.0f, 1e9f).prim == 0xFFFFFFFFu ? 1.0f : 0.0f;
-      f3 lit = scl3(scl3(light_color, sh), maxf_ref(0.0f, dot3(n, to_light)));
+      const float ndl = maxf_ref(0.0f, dot3(n, to_light));
+      /* (colour * vis) * 0 is 0 for either visibility: trace only when lit */
+      float sh = (ndl > 0.0f && nearest_hit(s, surf_pos, to_light, 0.0f, 1e9f).prim != 0xFFFFFFFFu) ? 0.0f : 1.0f;
+      f3 lit = scl3(scl3(light_color, sh), ndl);
       return mul3(add3(lit, ambient), diffuse);
     }
     case ORC_LAMBERT_POINT_VCOLOR: {
