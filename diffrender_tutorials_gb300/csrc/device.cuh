@@ -446,186 +446,11 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   return best.tri >= 0;
 }
 
-// Surface record of a camera ray (SurfaceInfo, raytrace.h:21-29, plus ids).
-struct Surf {
-  Hit h;
-  int A, B, C;  // global vertex ids
-  int block;
-  f3 ro, rd;
-};
+}  // namespace drgb
 
-__device__ __forceinline__ bool cast(const JobDev& J, const CamDev& cam, float x, float y, Surf& s) {
-  camera_ray(cam, x, y, s.ro, s.rd);
-  if (!trace<false>(J, s.ro, s.rd, 0.0f, 1e9f, s.h)) return false;
-  const int4 tv = __ldg(J.tri_v + s.h.tri);
-  s.A = tv.x;
-  s.B = tv.y;
-  s.C = tv.z;
-  s.block = tv.w;
-  return true;
-}
+#include "shading.cuh"
 
-// sample_bilinear_clamp_3f (shade_common.cpp:3-21)
-__device__ __forceinline__ f3 sample_bilinear(float tx, float ty, int w, int h, const float* data) {
-  tx = ref_clamp(tx, 0.0f, 1.0f);
-  ty = ref_clamp(ty, 0.0f, 1.0f);
-  tx *= (float)w;
-  ty *= (float)h;
-  const int ix = (int)tx, iy = (int)ty;
-  const int x0 = clampi(ix, 0, w - 1), y0 = clampi(iy, 0, h - 1);
-  const int x1 = clampi(ix + 1, 0, w - 1), y1 = clampi(iy + 1, 0, h - 1);
-  const float dx = tx - (float)x0, dy = ty - (float)y0;
-  const float* p00 = data + 3 * (y0 * w + x0);
-  const float* p01 = data + 3 * (y1 * w + x0);
-  const float* p10 = data + 3 * (y0 * w + x1);
-  const float* p11 = data + 3 * (y1 * w + x1);
-  float r[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-    r[i] = (1 - dx) * (1 - dy) * __ldg(p00 + i) + (1 - dx) * dy * __ldg(p01 + i) + dx * (1 - dy) * __ldg(p10 + i) +
-           dx * dy * __ldg(p11 + i);
-  return mk(r[0], r[1], r[2]);
-}
-
-__device__ __forceinline__ float2 interp_tc(const JobDev& J, const Surf& s) {
-  const float2 a = __ldg(J.tc + s.A), b = __ldg(J.tc + s.B), c = __ldg(J.tc + s.C);
-  const float w0 = 1.0f - s.h.u - s.h.v;
-  return make_float2((a.x * w0 + b.x * s.h.v) + s.h.u * c.x, (a.y * w0 + b.y * s.h.v) + s.h.u * c.y);
-}
-
-// Lighting factor of the point-light vertex-albedo model:
-// vis * I * max(0, n.l) / d^2 + ambient, with the reference Lambert's bias.
-__device__ __forceinline__ float lpv_factor(const JobDev& J, const Surf& s) {
-  const float u = s.h.u, v = s.h.v;
-  const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
-  const f3 p = s.ro + s.rd * (s.h.t - 1e-5f);
-  const f3 L = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]) - p;
-  const float d2 = dot(L, L);
-  const float dist = sqrtf(d2);
-  const f3 l = L / dist;
-  const float ndl = ref_max(0.0f, dot(n, l));
-  // with n.l <= 0 the lit term is 0 whatever the visibility: no shadow ray
-  Hit sh;
-  const float vis = (ndl > 0.0f && trace<true>(J, p, l, 0.0f, dist, sh)) ? 0.0f : 1.0f;
-  return vis * J.mp.light_intensity * ndl / d2 + J.mp.ambient;
-}
-
-// Counter-based hash for the path model.
-__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
-  uint32_t state = x * 747796405u + 2891336453u;
-  uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
-  return (word >> 22u) ^ word;
-}
-__device__ __forceinline__ float rnd01(uint32_t a, uint32_t b, uint32_t c) {
-  uint32_t h = pcg_hash(a ^ pcg_hash(b ^ pcg_hash(c)));
-  return (float)(h >> 8) * (1.0f / 16777216.0f);
-}
-
-// Fixed-depth diffuse path tracer (same definition as the oracle's
-// path_diffuse): point light, Lambert BRDF, cosine-weighted bounces.
-__device__ inline f3 path_diffuse(const JobDev& J, const Surf& first, uint32_t key, f3* d_alb0) {
-  const f3 lp = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]);
-  const float I = J.mp.light_intensity;
-  f3 L = mk(0, 0, 0), beta = mk(1, 1, 1), beta_na = mk(1, 1, 1), dL0 = mk(0, 0, 0);
-  Surf sf = first;
-  f3 ro = first.ro, rd = first.rd;
-  for (int bounce = 0; bounce <= J.mp.path_depth; bounce++) {
-    if (bounce > 0) {
-      if (!trace<false>(J, ro, rd, 0.0f, 1e9f, sf.h)) {
-        L = L + beta * J.mp.ambient;
-        dL0 = dL0 + beta_na * J.mp.ambient;
-        break;
-      }
-      const int4 tv = __ldg(J.tri_v + sf.h.tri);
-      sf.A = tv.x;
-      sf.B = tv.y;
-      sf.C = tv.z;
-    }
-    const float u = sf.h.u, v = sf.h.v;
-    const f3 alb = interp(ld3(J.col, sf.A), ld3(J.col, sf.B), ld3(J.col, sf.C), u, v);
-    f3 n = normalize(interp(ld3(J.nrm, sf.A), ld3(J.nrm, sf.B), ld3(J.nrm, sf.C), u, v));
-    const f3 pa = ld3(J.pos, sf.A);
-    const f3 ng = normalize(cross(ld3(J.pos, sf.B) - pa, ld3(J.pos, sf.C) - pa));
-    if (dot(ng, rd) > 0.0f) n = n * -1.0f;
-    const f3 ngf = dot(ng, n) < 0.0f ? ng * -1.0f : ng;
-    const f3 p = (ro + rd * sf.h.t) + ngf * 1e-4f;
-    const f3 Lv = lp - p;
-    const float d2 = dot(Lv, Lv);
-    const float dist = sqrtf(d2);
-    const f3 l = Lv / dist;
-    const float ndl = ref_max(0.0f, dot(n, l));
-    Hit sh;
-    if (ndl > 0.0f && !trace<true>(J, p, l, 0.0f, dist, sh)) {
-      const float k = I * ndl / (d2 * 3.14159265f);
-      L = L + (beta * alb) * k;
-      dL0 = dL0 + (bounce == 0 ? beta_na : beta_na * alb) * k;
-    }
-    if (bounce == J.mp.path_depth) break;
-    const float r1 = rnd01(key, (uint32_t)bounce, J.mp.seed);
-    const float r2 = rnd01(key, (uint32_t)bounce + 1000u, J.mp.seed);
-    const float phi = 6.28318531f * r1;
-    const float sr = sqrtf(r2);
-    const f3 a = fabsf(n.x) > 0.5f ? mk(0, 1, 0) : mk(1, 0, 0);
-    const f3 ex = normalize(cross(a, n));
-    const f3 ey = cross(n, ex);
-    const float lx = sr * cosf(phi), ly = sr * sinf(phi), lz = sqrtf(ref_max(0.0f, 1.0f - r2));
-    rd = normalize((ex * lx + ey * ly) + n * lz);
-    ro = p;
-    beta_na = bounce == 0 ? beta_na : beta_na * alb;
-    beta = beta * alb;
-  }
-  if (d_alb0) *d_alb0 = dL0;
-  return L;
-}
-
-// shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).  MODE != 0
-// compiles a single model (no code, hence no registers, for the others);
-// MODE == 0 switches on the job's model at run time.
-template <int MODE = 0>
-__device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
-  const int mode = MODE ? MODE : J.mode;
-  Surf s;
-  if (!cast(J, cam, x, y, s)) {
-    if (mode == PATH_DIFFUSE) return mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
-    return mk(0.0f, 0.0f, 0.0f);
-  }
-  const float u = s.h.u, v = s.h.v;
-  switch (mode) {
-    case SILHOUETTE:
-      return mk(1.0f, 1.0f, 1.0f);
-    case VERTEX_COLOR:
-      return interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v);
-    case TEXTURE_COLOR: {
-      const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
-      const float2 tc = interp_tc(J, s);
-      return sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
-    }
-    case LAMBERT: {
-      // light_dir = normalize(-1,-1,0), colour (1,0.5,0.2), ambient 0.1, BIAS 1e-5
-      const f3 light_dir = normalize(mk(-1.0f, -1.0f, 0.0f));
-      const f3 to_light = light_dir * -1.0f;
-      const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
-      const float2 tc = interp_tc(J, s);
-      const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
-      const f3 diffuse = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
-      const f3 surf_pos = s.ro + s.rd * (s.h.t - 1e-5f);
-      const float ndl = ref_max(0.0f, dot(n, to_light));
-      // (colour * vis) * 0 is 0 for either visibility: trace only when lit
-      Hit sh;
-      const float shv = (ndl > 0.0f && trace<true>(J, surf_pos, to_light, 0.0f, 1e9f, sh)) ? 0.0f : 1.0f;
-      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * shv) * ndl;
-      return (lit + mk(1.0f, 1.0f, 1.0f) * 0.1f) * diffuse;
-    }
-    case LAMBERT_POINT_VCOLOR: {
-      const f3 alb = interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v);
-      return alb * lpv_factor(J, s);
-    }
-    case PATH_DIFFUSE:
-      return path_diffuse(J, s, key, nullptr);
-    default:
-      return mk(0.0f, 0.0f, 0.0f);
-  }
-}
+namespace drgb {
 
 // VertexShader (functions.h:5-13): pixel x,y of a world point.
 __device__ __forceinline__ void vertex_shader(const CamDev& c, float vx, float vy, float vz, float& ox, float& oy) {

@@ -21,6 +21,15 @@ namespace drgb {
 
 constexpr int PX_THREADS = 256;
 
+// Traversal policy of the pixel kernel: per-ray by default (measured faster
+// on GB300 for the icosphere workload: 78 vs 73 iterations/s); build with
+// -DDRGB_PIXEL_WARP_TRACE for the warp-coherent traversal.
+#ifdef DRGB_PIXEL_WARP_TRACE
+constexpr bool kPixelWarp = true;
+#else
+constexpr bool kPixelWarp = false;
+#endif
+
 // Warp-aggregated scatter of per-vertex colour gradients.  All 32 lanes
 // must call it; lanes without a contribution pass tri = -1.
 __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
@@ -81,13 +90,17 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
                                            uint32_t key, float* wscr) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
-  bool hit = false;
-  if (active) hit = cast(J, cam, x, y, s);
+  const bool hit = cast_p<kPixelWarp>(J, cam, x, y, active, s);
   if (model_has_color(mode)) {
     float c[9];
     int tri = -1, gA = 0, gB = 0, gC = 0;
 #pragma unroll
     for (int i = 0; i < 9; i++) c[i] = 0.0f;
+    // warp-collective traversals first, then the per-lane arithmetic
+    float k = 1.0f;
+    f3 d0 = mk(0.0f, 0.0f, 0.0f);
+    if (mode == LAMBERT_POINT_VCOLOR) k = lpv_factor_p<kPixelWarp>(J, s, hit);
+    if (mode == PATH_DIFFUSE) path_diffuse_p<kPixelWarp>(J, s, key, hit, &d0);
     if (hit) {
       const float u = s.h.u, v = s.h.v;
       f3 ca, cb, cc;
@@ -96,13 +109,10 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
         cb = val * v;
         cc = val * u;
       } else if (mode == LAMBERT_POINT_VCOLOR) {
-        const float k = lpv_factor(J, s);
         ca = val * ((1.0f - u - v) * k);
         cb = val * (v * k);
         cc = val * (u * k);
       } else {
-        f3 d0;
-        path_diffuse(J, s, key, &d0);
         const f3 vd = val * d0;
         ca = vd * (1.0f - u - v);
         cb = vd * v;
@@ -183,15 +193,21 @@ __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict_
         const int p = s / S, k = s - p * S;
         const int px = x0 + p % tw, py = y0 + p / tw;
         f3 c = mk(0.0f, 0.0f, 0.0f);
-        if (s < NS && px < W && py < H) {
+        const bool act = s < NS && px < W && py < H;
+        float fx = 0.0f, fy = 0.0f;
+        uint32_t key = 0;
+        if (act) {
           const int dy = k / sq, dx = k - dy * sq;
           const float xoff = (dx + 0.5f) / (float)sq;
           const float yoff = (dy + 0.5f) / (float)sq;
           const int64_t pix = (int64_t)py * W + px;
-          const uint32_t key = ((uint32_t)view * 0x9E3779B9u) ^
-                               ((uint32_t)(pix * 64 + dy * sq + dx) * 2654435761u);
-          c = shade<MODE>(J, C, (float)px + xoff, (float)py + yoff, key) / (float)S;
+          key = ((uint32_t)view * 0x9E3779B9u) ^ ((uint32_t)(pix * 64 + dy * sq + dx) * 2654435761u);
+          fx = (float)px + xoff;
+          fy = (float)py + yoff;
         }
+        // every lane calls it (required by the warp-coherent policy)
+        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act);
+        if (act) c = sc / (float)S;
         if (s < NS) {
           s_col[3 * s + 0] = c.x;
           s_col[3 * s + 1] = c.y;

@@ -1,0 +1,355 @@
+// Shading models and the two traversal policies they run on.
+//
+// Per-ray policy (WARP = false): each thread traverses the LBVH on its own
+// (trace<ANY>).  Used where a warp's rays are unrelated -- the edge-sample
+// pass, which draws samples at random over all edges.
+//
+// Warp-coherent policy (WARP = true): the 32 rays of a warp traverse the
+// LBVH together (trace_warp<ANY>).  Used by the pixel kernel, whose warps
+// hold the samples of one or two adjacent pixels, so their camera rays,
+// shadow rays and re-traced adjoint rays visit nearly the same nodes.  The
+// node to visit is the same for the whole warp (one broadcast load), a child
+// is entered when any lane's ray reaches it before that lane's current hit
+// distance, the order of two hit children follows the majority of lanes,
+// and the traversal stack lives one entry per lane, read back with a
+// shuffle.  Every lane still tests every leaf its own ray reaches, so the
+// result per lane is the same as with the per-ray policy.
+//
+// The shading code below is written in masked form: lanes without a hit
+// carry an inactive flag through the traversal calls instead of leaving
+// early, so that in the warp policy all 32 lanes reach every traversal call.
+#pragma once
+
+namespace drgb {
+
+template <bool ANY>
+__device__ DRGB_TRACE_ATTR bool trace_warp(const JobDev& J, f3 o, f3 d, float tNear, float tFar, bool active,
+                                           Hit& best) {
+  best.t = tFar;
+  best.tri = -1;
+  best.u = 0.0f;
+  best.v = 0.0f;
+  const unsigned FULL = 0xffffffffu;
+  if (J.n_tris <= 0) return false;
+  if (J.trace_bruteforce) return active ? trace<ANY>(J, o, d, tNear, tFar, best) : false;
+  bool live = active;
+  if (!__any_sync(FULL, live)) return false;
+  const int lane = threadIdx.x & 31;
+  const f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  const f3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const float lo_t = tNear - fabsf(tNear) * 4e-6f - 1e-6f;
+  unsigned n_box = 0, n_tri = 0;
+  int s0 = 0, s1 = 0;  // stack entry i is held by lane i%32 in slot i/32
+  int sp = 0;
+  int node = J.root;
+  int guard = 0;
+  while (true) {
+    if (node >= 0) {
+      const float4 n0 = __ldg(J.nodes + 4 * node + 0);
+      const float4 n1 = __ldg(J.nodes + 4 * node + 1);
+      const float4 n2 = __ldg(J.nodes + 4 * node + 2);
+      const float4 n3 = __ldg(J.nodes + 4 * node + 3);
+      bool h0 = false, h1 = false;
+      float t0 = 0.0f, t1 = 0.0f;
+      if (live) {
+        const float hi_t = cull_bound(best.t);
+        t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, inv, oi, lo_t, hi_t);
+        t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, inv, oi, lo_t, hi_t);
+        h0 = t0 <= hi_t;
+        h1 = t1 <= hi_t;
+        n_box += 2;
+      }
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      const unsigned b0 = __ballot_sync(FULL, h0), b1 = __ballot_sync(FULL, h1);
+      if (b0 && b1) {
+        const unsigned p0 = __ballot_sync(FULL, h0 && (!h1 || t0 <= t1));
+        const bool first0 = 2 * __popc(p0) >= __popc(b0 | b1);
+        if (sp >= 64) {
+          if (lane == 0) atomicOr(J.err, ERR_STACK_OVERFLOW);
+          break;
+        }
+        const int far = first0 ? c1 : c0;
+        if (lane == (sp & 31)) {
+          if (sp < 32) s0 = far;
+          else s1 = far;
+        }
+        sp++;
+        node = first0 ? c0 : c1;
+        continue;
+      } else if (b0) {
+        node = c0;
+        continue;
+      } else if (b1) {
+        node = c1;
+        continue;
+      }
+    } else {
+      const int k = ~node;
+      const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+      const int id = __float_as_int(a.w);
+      if (live) {
+        float t, u, v;
+        n_tri++;
+        if (mt_test(o, d, f4to3(a), f4to3(e1), f4to3(e2), tNear, t, u, v) &&
+            (t < best.t || (t == best.t && id < best.tri))) {
+          best.t = t;
+          best.u = u;
+          best.v = v;
+          best.tri = id;
+          if (ANY) live = false;
+        }
+      }
+      if (ANY && !__any_sync(FULL, live)) break;
+    }
+    if (sp == 0) break;
+    sp--;
+    node = __shfl_sync(FULL, sp < 32 ? s0 : s1, sp & 31);
+    if (++guard > (1 << 24)) {
+      if (lane == 0) atomicOr(J.err, ERR_TRAVERSAL_LIMIT);
+      break;
+    }
+  }
+  if (active) add_work(J, n_box, n_tri);
+  return best.tri >= 0;
+}
+
+// Traversal under a policy; inactive lanes report a miss.
+template <bool ANY, bool WARP>
+__device__ __forceinline__ bool trace_p(const JobDev& J, f3 o, f3 d, float tNear, float tFar, bool active, Hit& h) {
+  if (WARP) return trace_warp<ANY>(J, o, d, tNear, tFar, active, h);
+  if (!active) {
+    h.t = tFar;
+    h.tri = -1;
+    h.u = h.v = 0.0f;
+    return false;
+  }
+  return trace<ANY>(J, o, d, tNear, tFar, h);
+}
+
+// Surface record of a camera ray (SurfaceInfo, raytrace.h:21-29, plus ids).
+// Without a hit the vertex ids are 0, so masked loads stay in bounds.
+struct Surf {
+  Hit h;
+  int A, B, C;  // global vertex ids
+  int block;
+  f3 ro, rd;
+};
+
+template <bool WARP>
+__device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float x, float y, bool active, Surf& s) {
+  camera_ray(cam, x, y, s.ro, s.rd);
+  const bool hit = trace_p<false, WARP>(J, s.ro, s.rd, 0.0f, 1e9f, active, s.h);
+  s.A = s.B = s.C = 0;
+  s.block = 0;
+  if (hit) {
+    const int4 tv = __ldg(J.tri_v + s.h.tri);
+    s.A = tv.x;
+    s.B = tv.y;
+    s.C = tv.z;
+    s.block = tv.w;
+  }
+  return hit;
+}
+
+__device__ __forceinline__ bool cast(const JobDev& J, const CamDev& cam, float x, float y, Surf& s) {
+  return cast_p<false>(J, cam, x, y, true, s);
+}
+
+// sample_bilinear_clamp_3f (shade_common.cpp:3-21)
+__device__ __forceinline__ f3 sample_bilinear(float tx, float ty, int w, int h, const float* data) {
+  tx = ref_clamp(tx, 0.0f, 1.0f);
+  ty = ref_clamp(ty, 0.0f, 1.0f);
+  tx *= (float)w;
+  ty *= (float)h;
+  const int ix = (int)tx, iy = (int)ty;
+  const int x0 = clampi(ix, 0, w - 1), y0 = clampi(iy, 0, h - 1);
+  const int x1 = clampi(ix + 1, 0, w - 1), y1 = clampi(iy + 1, 0, h - 1);
+  const float dx = tx - (float)x0, dy = ty - (float)y0;
+  const float* p00 = data + 3 * (y0 * w + x0);
+  const float* p01 = data + 3 * (y1 * w + x0);
+  const float* p10 = data + 3 * (y0 * w + x1);
+  const float* p11 = data + 3 * (y1 * w + x1);
+  float r[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    r[i] = (1 - dx) * (1 - dy) * __ldg(p00 + i) + (1 - dx) * dy * __ldg(p01 + i) + dx * (1 - dy) * __ldg(p10 + i) +
+           dx * dy * __ldg(p11 + i);
+  return mk(r[0], r[1], r[2]);
+}
+
+__device__ __forceinline__ float2 interp_tc(const JobDev& J, const Surf& s) {
+  const float2 a = __ldg(J.tc + s.A), b = __ldg(J.tc + s.B), c = __ldg(J.tc + s.C);
+  const float w0 = 1.0f - s.h.u - s.h.v;
+  return make_float2((a.x * w0 + b.x * s.h.v) + s.h.u * c.x, (a.y * w0 + b.y * s.h.v) + s.h.u * c.y);
+}
+
+// Lighting factor of the point-light vertex-albedo model:
+// vis * I * max(0, n.l) / d^2 + ambient, with the reference Lambert's bias.
+// With n.l <= 0 the lit term is 0 whatever the visibility: no shadow ray.
+template <bool WARP>
+__device__ __forceinline__ float lpv_factor_p(const JobDev& J, const Surf& s, bool hit) {
+  f3 p = mk(0.0f, 0.0f, 0.0f), l = mk(0.0f, 0.0f, 1.0f);
+  float d2 = 1.0f, dist = 0.0f, ndl = 0.0f;
+  if (hit) {
+    const float u = s.h.u, v = s.h.v;
+    const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
+    p = s.ro + s.rd * (s.h.t - 1e-5f);
+    const f3 L = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]) - p;
+    d2 = dot(L, L);
+    dist = sqrtf(d2);
+    l = L / dist;
+    ndl = ref_max(0.0f, dot(n, l));
+  }
+  Hit sh;
+  const float vis = trace_p<true, WARP>(J, p, l, 0.0f, dist, hit && ndl > 0.0f, sh) ? 0.0f : 1.0f;
+  return vis * J.mp.light_intensity * ndl / d2 + J.mp.ambient;
+}
+
+__device__ __forceinline__ float lpv_factor(const JobDev& J, const Surf& s) { return lpv_factor_p<false>(J, s, true); }
+
+// Counter-based hash for the path model.
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
+  uint32_t state = x * 747796405u + 2891336453u;
+  uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+__device__ __forceinline__ float rnd01(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t h = pcg_hash(a ^ pcg_hash(b ^ pcg_hash(c)));
+  return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+// Fixed-depth diffuse path tracer (same definition as the oracle's
+// path_diffuse): point light, Lambert BRDF, cosine-weighted bounces.
+// `alive` = the camera ray hit; the bounce loop runs the same number of
+// times on every lane.
+template <bool WARP>
+__device__ inline f3 path_diffuse_p(const JobDev& J, const Surf& first, uint32_t key, bool alive, f3* d_alb0) {
+  const f3 lp = mk(J.mp.light_pos[0], J.mp.light_pos[1], J.mp.light_pos[2]);
+  const float I = J.mp.light_intensity;
+  f3 L = mk(0, 0, 0), beta = mk(1, 1, 1), beta_na = mk(1, 1, 1), dL0 = mk(0, 0, 0);
+  Surf sf = first;
+  f3 ro = first.ro, rd = first.rd;
+  for (int bounce = 0; bounce <= J.mp.path_depth; bounce++) {
+    bool hitb = alive;
+    if (bounce > 0) {
+      Hit hh;
+      hitb = trace_p<false, WARP>(J, ro, rd, 0.0f, 1e9f, alive, hh);
+      if (alive && !hitb) {
+        L = L + beta * J.mp.ambient;
+        dL0 = dL0 + beta_na * J.mp.ambient;
+      }
+      if (hitb) {
+        sf.h = hh;
+        const int4 tv = __ldg(J.tri_v + hh.tri);
+        sf.A = tv.x;
+        sf.B = tv.y;
+        sf.C = tv.z;
+      }
+    }
+    f3 alb = mk(0, 0, 0), n = mk(0, 0, 1), p = mk(0, 0, 0), l = mk(0, 0, 1);
+    float d2 = 1.0f, dist = 0.0f, ndl = 0.0f;
+    if (hitb) {
+      const float u = sf.h.u, v = sf.h.v;
+      alb = interp(ld3(J.col, sf.A), ld3(J.col, sf.B), ld3(J.col, sf.C), u, v);
+      n = normalize(interp(ld3(J.nrm, sf.A), ld3(J.nrm, sf.B), ld3(J.nrm, sf.C), u, v));
+      const f3 pa = ld3(J.pos, sf.A);
+      const f3 ng = normalize(cross(ld3(J.pos, sf.B) - pa, ld3(J.pos, sf.C) - pa));
+      if (dot(ng, rd) > 0.0f) n = n * -1.0f;
+      const f3 ngf = dot(ng, n) < 0.0f ? ng * -1.0f : ng;
+      p = (ro + rd * sf.h.t) + ngf * 1e-4f;
+      const f3 Lv = lp - p;
+      d2 = dot(Lv, Lv);
+      dist = sqrtf(d2);
+      l = Lv / dist;
+      ndl = ref_max(0.0f, dot(n, l));
+    }
+    Hit sh;
+    const bool occluded = trace_p<true, WARP>(J, p, l, 0.0f, dist, hitb && ndl > 0.0f, sh);
+    if (hitb && ndl > 0.0f && !occluded) {
+      const float k = I * ndl / (d2 * 3.14159265f);
+      L = L + (beta * alb) * k;
+      dL0 = dL0 + (bounce == 0 ? beta_na : beta_na * alb) * k;
+    }
+    if (bounce == J.mp.path_depth) break;
+    if (hitb) {
+      const float r1 = rnd01(key, (uint32_t)bounce, J.mp.seed);
+      const float r2 = rnd01(key, (uint32_t)bounce + 1000u, J.mp.seed);
+      const float phi = 6.28318531f * r1;
+      const float sr = sqrtf(r2);
+      const f3 a = fabsf(n.x) > 0.5f ? mk(0, 1, 0) : mk(1, 0, 0);
+      const f3 ex = normalize(cross(a, n));
+      const f3 ey = cross(n, ex);
+      const float lx = sr * cosf(phi), ly = sr * sinf(phi), lz = sqrtf(ref_max(0.0f, 1.0f - r2));
+      rd = normalize((ex * lx + ey * ly) + n * lz);
+      ro = p;
+      beta_na = bounce == 0 ? beta_na : beta_na * alb;
+      beta = beta * alb;
+    }
+    alive = hitb;
+  }
+  if (d_alb0) *d_alb0 = dL0;
+  return L;
+}
+
+// shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).  MODE != 0
+// compiles a single model (no code, hence no registers, for the others);
+// MODE == 0 switches on the job's model at run time.  Inactive lanes return
+// the background.
+template <int MODE, bool WARP>
+__device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active) {
+  const int mode = MODE ? MODE : J.mode;
+  Surf s;
+  const bool hit = cast_p<WARP>(J, cam, x, y, active, s);
+  const float u = s.h.u, v = s.h.v;
+  switch (mode) {
+    case SILHOUETTE:
+      return hit ? mk(1.0f, 1.0f, 1.0f) : mk(0.0f, 0.0f, 0.0f);
+    case VERTEX_COLOR:
+      return hit ? interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v) : mk(0.0f, 0.0f, 0.0f);
+    case TEXTURE_COLOR: {
+      if (!hit) return mk(0.0f, 0.0f, 0.0f);
+      const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
+      const float2 tc = interp_tc(J, s);
+      return sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+    }
+    case LAMBERT: {
+      // light_dir = normalize(-1,-1,0), colour (1,0.5,0.2), ambient 0.1, BIAS 1e-5
+      const f3 light_dir = normalize(mk(-1.0f, -1.0f, 0.0f));
+      const f3 to_light = light_dir * -1.0f;
+      f3 diffuse = mk(0.0f, 0.0f, 0.0f), surf_pos = mk(0.0f, 0.0f, 0.0f);
+      float ndl = 0.0f;
+      if (hit) {
+        const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
+        const float2 tc = interp_tc(J, s);
+        const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
+        diffuse = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+        surf_pos = s.ro + s.rd * (s.h.t - 1e-5f);
+        ndl = ref_max(0.0f, dot(n, to_light));
+      }
+      // (colour * vis) * 0 is 0 for either visibility: trace only when lit
+      Hit sh;
+      const bool occ = trace_p<true, WARP>(J, surf_pos, to_light, 0.0f, 1e9f, hit && ndl > 0.0f, sh);
+      if (!hit) return mk(0.0f, 0.0f, 0.0f);
+      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * (occ ? 0.0f : 1.0f)) * ndl;
+      return (lit + mk(1.0f, 1.0f, 1.0f) * 0.1f) * diffuse;
+    }
+    case LAMBERT_POINT_VCOLOR: {
+      const float k = lpv_factor_p<WARP>(J, s, hit);
+      if (!hit) return mk(0.0f, 0.0f, 0.0f);
+      return interp(ld3(J.col, s.A), ld3(J.col, s.B), ld3(J.col, s.C), u, v) * k;
+    }
+    case PATH_DIFFUSE: {
+      const f3 r = path_diffuse_p<WARP>(J, s, key, hit, nullptr);
+      return hit ? r : mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
+    }
+    default:
+      return mk(0.0f, 0.0f, 0.0f);
+  }
+}
+
+template <int MODE = 0>
+__device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
+  return shade_p<MODE, false>(J, cam, x, y, key, true);
+}
+
+}  // namespace drgb
