@@ -7,4 +7,5 @@ a Python mirror of the reference's IDiffRender / IOptimizer interfaces.
 from .scene import (CamInfo, Scene, Texture, TriangleMesh, displace_radially, make_cube, make_icosphere,  # noqa: F401
                     make_uv_sphere, perturb_vertices, ring_cameras)
 from .api import (SHADING_MODEL, CreateSimpleOptimizer, DiffRenderSettings, DMesh, DScene, IDiffRender,  # noqa: F401
-                  IOptimizer, MakeDifferentialRenderer, ModelParams, OptimizerParameters, kernel_launches)
+                  IOptimizer, MakeDifferentialRenderer, ModelParams, OptimizerParameters, kernel_launches,
+                  BatchOptimizer)

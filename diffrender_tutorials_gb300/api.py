@@ -372,5 +372,95 @@ def CreateSimpleOptimizer() -> IOptimizer:
     return IOptimizer()
 
 
+def _model_params_native(p: Optional[ModelParams]):
+    if p is None:
+        return None
+    mp = N.ModelParams()
+    mp.light_pos[:] = [float(x) for x in p.light_pos]
+    mp.light_intensity, mp.ambient, mp.path_depth, mp.seed = p.light_intensity, p.ambient, p.path_depth, p.seed
+    return mp
+
+
+class BatchOptimizer:
+    """Many independent optimisation jobs advanced by one fused launch
+    sequence per iteration (drgb_batch_*).  Each job is the equivalent of
+    IOptimizer.Init + Run on its own renderer."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        N.check(N.load().drgb_batch_create(int(device), C.byref(self._h)))
+        self._scenes = {}
+
+    def __del__(self):
+        try:
+            if self._h:
+                N.load().drgb_batch_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def add_job(self, scene: Scene, cams: Sequence[CamInfo], targets: np.ndarray, settings: DiffRenderSettings,
+                params: OptimizerParameters, model_params: Optional[ModelParams] = None) -> int:
+        h = _SceneHandle(scene)
+        tg = np.ascontiguousarray(np.asarray(targets, np.float32).reshape(-1))
+        p = params.native()
+        mp = _model_params_native(model_params)
+        jid = C.c_int32(0)
+        N.check(N.load().drgb_batch_add_job(self._h, int(settings.mode), int(settings.spp),
+                                            C.byref(mp) if mp is not None else None, C.byref(h.desc),
+                                            make_cameras(list(cams)), _ptr(tg), len(cams), C.byref(p),
+                                            C.byref(jid)))
+        self._scenes[int(jid.value)] = scene.copy()
+        return int(jid.value)
+
+    def remove_job(self, job_id: int):
+        N.check(N.load().drgb_batch_remove_job(self._h, int(job_id)))
+        self._scenes.pop(job_id, None)
+
+    def size(self) -> int:
+        return int(N.load().drgb_batch_size(self._h))
+
+    def set_option(self, option: int, value: int):
+        N.check(N.load().drgb_batch_set_option(self._h, option, int(value)))
+
+    def run(self, num_iters: int):
+        N.check(N.load().drgb_batch_run(self._h, int(num_iters)))
+
+    def run_async(self, num_iters: int):
+        N.check(N.load().drgb_batch_run_async(self._h, int(num_iters)))
+
+    def sync(self):
+        N.check(N.load().drgb_batch_sync(self._h))
+
+    def stream(self) -> int:
+        return N.load().drgb_batch_stream(self._h) or 0
+
+    def losses(self, job_id: int) -> np.ndarray:
+        done = C.c_int64(0)
+        N.check(N.load().drgb_batch_job_losses(self._h, int(job_id), 0, 0, None, C.byref(done)))
+        out = np.zeros(max(1, done.value), np.float32)
+        N.check(N.load().drgb_batch_job_losses(self._h, int(job_id), 0, done.value, _ptr(out), C.byref(done)))
+        return out[:done.value]
+
+    def device_bytes(self, job_id: int) -> int:
+        return int(N.load().drgb_batch_job_device_bytes(self._h, int(job_id)))
+
+    def job_scene(self, job_id: int) -> Scene:
+        s = self._scenes[job_id].copy()
+        for i, m in enumerate(s.meshes):
+            v = np.zeros_like(m.vertices)
+            col = np.zeros_like(m.colors) if m.colors is not None else None
+            tex = np.zeros_like(m.textures[0].data) if m.textures else None
+            tr = np.zeros(16 * len(s.transforms[i]), np.float32)
+            N.check(N.load().drgb_batch_get_mesh(self._h, int(job_id), i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
+            m.vertices = v
+            if col is not None:
+                m.colors = col
+            if tex is not None:
+                m.textures[0].data = tex
+            s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
+        return s
+
+
 def kernel_launches() -> int:
     return int(N.load().drgb_kernel_launches())

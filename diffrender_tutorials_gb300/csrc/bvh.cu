@@ -23,9 +23,8 @@
 namespace drgb {
 
 // Per block: its transform and the inverse transpose used for normals.
-__global__ void k_block_tr(const BlockDev* blocks, int n_blocks, const float* const* mesh_tr, float* block_tr) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= n_blocks) return;
+__device__ __forceinline__ void block_tr_body(const BlockDev* blocks, int b, const float* const* mesh_tr,
+                                              float* block_tr) {
   const BlockDev bd = blocks[b];
   const float* tr = mesh_tr[bd.mesh] + 16 * bd.inst;
   float inv[16];
@@ -36,11 +35,16 @@ __global__ void k_block_tr(const BlockDev* blocks, int n_blocks, const float* co
     for (int c = 0; c < 4; c++) o[16 + 4 * c + r] = inv[4 * r + c];  // transpose
 }
 
+__global__ void k_block_tr(const BlockDev* blocks, int n_blocks, const float* const* mesh_tr, float* block_tr) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_blocks) return;
+  block_tr_body(blocks, b, mesh_tr, block_tr);
+}
+
 // Flattened vertex arrays (prepare_for_render's per-instance loop).
-__global__ void k_flatten(const int* vblock, int n, const BlockDev* blocks, const MeshSrc* src, const float* block_tr,
-                          float4* pos, float4* orig, float4* col, float4* nrm, float2* tc) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n) return;
+__device__ __forceinline__ void flatten_body(int g, const int* vblock, const BlockDev* blocks, const MeshSrc* src,
+                                             const float* block_tr, float4* pos, float4* orig, float4* col,
+                                             float4* nrm, float2* tc) {
   const int b = vblock[g];
   const BlockDev bd = blocks[b];
   const int k = g - bd.vert_off;
@@ -58,6 +62,13 @@ __global__ void k_flatten(const int* vblock, int n, const BlockDev* blocks, cons
     nrm[g] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
   }
   tc[g] = s.tc ? make_float2(s.tc[2 * k], s.tc[2 * k + 1]) : make_float2(0.0f, 0.0f);
+}
+
+__global__ void k_flatten(const int* vblock, int n, const BlockDev* blocks, const MeshSrc* src, const float* block_tr,
+                          float4* pos, float4* orig, float4* col, float4* nrm, float2* tc) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  flatten_body(g, vblock, blocks, src, block_tr, pos, orig, col, nrm, tc);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,11 +258,9 @@ __device__ __forceinline__ void write_child(float4* nodes, int parent, int slot,
   }
 }
 
-__global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const float4* pos, const float* block_tr,
-                               float4* tri, float4* nodes, const int* leaf_parent, const int* node_parent,
-                               int* counters) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+__device__ __forceinline__ void leaf_refit_body(int k, const int* perm, int n, const int4* tri_v, const float4* pos,
+                                                const float* block_tr, float4* tri, float4* nodes,
+                                                const int* leaf_parent, const int* node_parent, int* counters) {
   const int t = perm[k];
   const int4 tv = tri_v[t];
   const f3 A = traced_vertex(pos, block_tr, tv.w, tv.x);
@@ -287,6 +296,60 @@ __global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const 
     child = p;
     p = node_parent[p];
   }
+}
+
+__global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const float4* pos, const float* block_tr,
+                               float4* tri, float4* nodes, const int* leaf_parent, const int* node_parent,
+                               int* counters) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  leaf_refit_body(k, perm, n, tri_v, pos, block_tr, tri, nodes, leaf_parent, node_parent, counters);
+}
+
+// ---- batched forms: one launch over the scenes of many jobs --------------
+// The segment tables give, per job, the number of blocks / vertices /
+// internal nodes / triangles (Seg::count) and the first chunk of 256.
+__global__ void k_b_block_tr(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int b = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (b >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  block_tr_body(A.blocks, b, A.tr_tab, A.block_tr);
+}
+
+__global__ void k_b_flatten(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int g = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (g >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  flatten_body(g, A.vblock, A.blocks, A.src, A.block_tr, A.pos, A.orig, A.col, A.nrm, A.tc);
+}
+
+__global__ void k_b_zero_counters(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int i = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (i >= sg.count) return;
+  aux[sg.job].counters[i] = 0;
+}
+
+__global__ void k_b_refit(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int k = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (k >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  leaf_refit_body(k, A.perm, A.n_tris, A.tri_v, A.pos, A.block_tr, A.tri, A.nodes, A.leaf_parent, A.node_parent,
+                  A.counters);
+}
+
+// Flatten + refit of every job of a batch (segment tables built by the host:
+// blocks, vertices, internal nodes and triangles per job).
+void launch_b_prepare(const JobAux* d_aux, const Seg* segs[4], const int nsegs[4], const int chunks[4],
+                      cudaStream_t s) {
+  if (chunks[0] > 0) k_b_block_tr<<<chunks[0], 256, 0, s>>>(d_aux, segs[0], nsegs[0]);
+  if (chunks[1] > 0) k_b_flatten<<<chunks[1], 256, 0, s>>>(d_aux, segs[1], nsegs[1]);
+  if (chunks[2] > 0) k_b_zero_counters<<<chunks[2], 256, 0, s>>>(d_aux, segs[2], nsegs[2]);
+  if (chunks[3] > 0) k_b_refit<<<chunks[3], 256, 0, s>>>(d_aux, segs[3], nsegs[3]);
+  count_launch(4);
 }
 
 // ---------------------------------------------------------------------------

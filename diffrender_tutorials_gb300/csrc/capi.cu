@@ -23,6 +23,7 @@ void add_launches(int64_t n) { g_launches += n; }
 
 static thread_local std::string t_err;
 void drgb_set_last_error(const std::string& m) { t_err = m; }
+std::string t_err_message() { return t_err; }
 
 static void check_renderer(drgb_renderer* r) { require(r != nullptr, "null renderer"); }
 

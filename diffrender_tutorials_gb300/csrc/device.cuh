@@ -139,6 +139,78 @@ struct JobDev {
   unsigned long long* work;
 };
 
+// Source arrays of one mesh read by the flattening kernel.
+struct MeshSrc {
+  const float* v;
+  const float* col;
+  const float* nrm;
+  const float* tc;
+};
+
+// One differentiable mesh as the optimiser updates it.
+struct OptMesh {
+  int64_t base;
+  int full;
+  int pos_off, color_off, tex_off, tr_off;
+  int nv, n_inst;
+  float* vertices;
+  float* colors;
+  float* texture;
+  float* transforms;
+};
+
+constexpr int kBatchMaxDMeshes = 4;
+
+// Everything the per-iteration maintenance passes of one job touch (scene
+// flattening, LBVH refit, optimiser), for launches that cover many jobs.
+struct JobAux {
+  int n_vertices, n_tris, n_blocks;
+  const int* vblock;
+  const BlockDev* blocks;
+  const MeshSrc* src;
+  const float* const* tr_tab;
+  float* block_tr;
+  float4 *pos, *orig, *col, *nrm;
+  float2* tc;
+  const int4* tri_v;
+  const int* perm;
+  float4* tri;
+  float4* nodes;
+  const int* leaf_parent;
+  const int* node_parent;
+  int* counters;
+  float* grad;
+  int64_t grad_total;
+  float *m, *G, *lr;
+  int* iter;
+  float* losses;
+  int losses_cap;
+  const float* loss_out;
+  int alg, flags, mode, decay_period;
+  float decay_mult;
+  int n_dmesh;
+  OptMesh dm[kBatchMaxDMeshes];
+};
+
+// A contiguous run of work of one job (and one view or sub-range): global
+// chunk indices [begin, begin + ceil(count / chunk)) map to it.
+struct Seg {
+  int job;
+  int sub;
+  int begin;
+  int count;
+};
+
+// Segment of a global chunk index (segments sorted by begin).
+__device__ __forceinline__ int find_seg(const Seg* segs, int n, int chunk) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&segs[mid].begin) <= chunk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---------------------------------------------------------------------------
 // Exact float3 helpers (LiteMath operation order).
 // ---------------------------------------------------------------------------

@@ -2,26 +2,25 @@
 // src/drender.h:235-425; build_edge_sampler / sample / edge_grad,
 // src/drender.cpp:5-87; VS_X_grad / VS_Y_grad, src/functions.cpp:21-163).
 //
-//   k_edge_project : VertexShader of every flattened vertex, per view
-//   k_edge_pmf     : edge weights = 3-D length of the projected endpoints
-//   k_edge_cdf     : the sampler's CDF, summed sequentially in edge order so
-//                    that it is bit-identical to the reference's
-//   k_edge_select  : replayed random numbers -> edge (upper_bound) -> point
-//                    -> off-image / small-adjoint rejection; survivors are
-//                    appended to a queue with one atomic per warp (ballot)
-//   k_edge_shade   : two-sided shading at p -/+ 1e-3 n, (f_in - f_out).dL/dI,
-//                    chain rule to the world vertices and the instance
-//                    matrix, scattered with atomics (transform terms summed
-//                    across the warp first)
+//   project : VertexShader of every flattened vertex, per view
+//   pmf     : edge weights = 3-D length of the projected endpoints
+//   cdf     : the sampler's CDF, summed sequentially in edge order so that it
+//             is bit-identical to the reference's
+//   select  : replayed random numbers -> edge (upper_bound) -> point ->
+//             off-image / small-adjoint rejection; survivors are appended to
+//             a queue with one atomic per warp (ballot compaction)
+//   shade   : two-sided shading at p -/+ 1e-3 n, (f_in - f_out).dL/dI, chain
+//             rule to the world vertices and the instance matrix, scattered
+//             with atomics (transform terms summed across the warp first)
+//
+// Every pass exists in a single-job form (grid over views of one job) and a
+// batched form (segment table over the (job, view) pairs of many jobs); both
+// run the same per-element code.  Queue entries carry their job index.
 #include "engine.h"
 
 namespace drgb {
 
-__global__ void k_edge_project(const JobDev* jobs, int job) {
-  const JobDev& J = jobs[job];
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  const int view = blockIdx.y;
-  if (v >= J.n_vertices) return;
+__device__ __forceinline__ void edge_project_body(const JobDev& J, int view, int v) {
   const CamDev& c = J.cams[view];
   const float4 p = __ldg(J.pos + v);
   float ox, oy;
@@ -29,23 +28,17 @@ __global__ void k_edge_project(const JobDev* jobs, int job) {
   J.proj[(int64_t)view * J.n_vertices + v] = make_float4(ox, oy, p.z, 0.0f);
 }
 
-__global__ void k_edge_pmf(const JobDev* jobs, int job) {
-  const JobDev& J = jobs[job];
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  const int view = blockIdx.y;
-  if (e >= J.n_edges) return;
+__device__ __forceinline__ void edge_pmf_body(const JobDev& J, int view, int e) {
   const int4 ed = __ldg(J.edges + e);
   const float4* P = J.proj + (int64_t)view * J.n_vertices;
   const float4 a = P[ed.x], b = P[ed.y];
   J.pmf[(int64_t)view * J.n_edges + e] = length(mk(b.x - a.x, b.y - a.y, b.z - a.z));
 }
 
-// One warp per view: cdf[k+1] = pmf[k] + cdf[k] in edge order, then both
-// divided by the total (drender.cpp:5-22).
-__global__ void k_edge_cdf(const JobDev* jobs, int job) {
-  const JobDev& J = jobs[job];
-  const int view = blockIdx.x;
-  const int lane = threadIdx.x;
+// One warp: cdf[k+1] = pmf[k] + cdf[k] in edge order, then both divided by
+// the total (drender.cpp:5-22).
+__device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view) {
+  const int lane = threadIdx.x & 31;
   const int E = J.n_edges;
   float* pmf = J.pmf + (int64_t)view * E;
   float* cdf = J.cdf + (int64_t)view * (E + 1);
@@ -77,130 +70,198 @@ __device__ __forceinline__ int upper_bound_idx(const float* cdf, int n, float u)
   return lo;
 }
 
+// Sample i of a view: edge choice and rejection (drender.h:326-345).
+__device__ __forceinline__ bool edge_select_test(const JobDev& J, int view, int i, int& edge_id) {
+  edge_id = 0;
+  if (i >= J.edge_samples || J.n_edges <= 0) return false;
+  const float rnd0 = __ldg(J.rnd + 2 * i), rnd1 = __ldg(J.rnd + 2 * i + 1);
+  const float* cdf = J.cdf + (int64_t)view * (J.n_edges + 1);
+  edge_id = clampi(upper_bound_idx(cdf, J.n_edges + 1, rnd0) - 1, 0, J.n_edges - 1);
+  const int4 ed = __ldg(J.edges + edge_id);
+  const float4* P = J.proj + (int64_t)view * J.n_vertices;
+  const float4 a = P[ed.x], b = P[ed.y];
+  const float t = rnd1;
+  const float px = a.x + t * (b.x - a.x), py = a.y + t * (b.y - a.y);
+  const int xi = (int)px, yi = (int)py;
+  if (xi < 0 || yi < 0 || xi >= J.W || yi >= J.H) return false;
+  const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
+  return !(length(mk(ad.x, ad.y, ad.z)) < 1e-3f);
+}
+
+// Warp-aggregated append (all 32 lanes call it).
+__device__ __forceinline__ void queue_append(int4* queue, int* count, int cap, bool keep, int4 entry) {
+  const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+  if (!ballot) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(ballot) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(ballot));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (keep) {
+    const int slot = base + __popc(ballot & ((1u << lane) - 1u));
+    if (slot < cap) queue[slot] = entry;
+  }
+}
+
+// Shading and chain rule of queue entries [q0, q0+32) (one per lane).
+__device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* queue, int n, int q0) {
+  const int lane = threadIdx.x & 31;
+  const int q = q0 + lane;
+  float tr[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) tr[k] = 0.0f;
+  float* target = nullptr;  // transform-gradient block this lane adds to
+  if (q < n) {
+    const int4 it = queue[q];
+    const int view = it.x, i = it.y, edge_id = it.z;
+    const JobDev& J = jobs[it.w];
+    const CamDev& cam = J.cams[view];
+    const int4 ed = __ldg(J.edges + edge_id);
+    const int2 mi = __ldg(J.edge_mi + edge_id);
+    const float pm = J.pmf[(int64_t)view * J.n_edges + edge_id];
+    const float4* P = J.proj + (int64_t)view * J.n_vertices;
+    const float4 pa = P[ed.x], pb = P[ed.y];
+    const float t = __ldg(J.rnd + 2 * i + 1);
+    const float dx0 = pb.x - pa.x, dy0 = pb.y - pa.y;
+    const float px = pa.x + t * dx0, py = pa.y + t * dy0;
+    const int xi = (int)px, yi = (int)py;
+    const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
+    const float dl = sqrtf(dx0 * dx0 + dy0 * dy0);
+    const float nx = -(dy0 / dl), ny = dx0 / dl;  // normal2D of the unit edge direction
+    const float cinx = px - 1e-3f * nx, ciny = py - 1e-3f * ny;
+    const float coutx = px + 1e-3f * nx, couty = py + 1e-3f * ny;
+    const uint32_t key_in = 0xA511E9B3u ^ ((uint32_t)(i * 2u) * 2654435761u);
+    const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
+    const f3 color_in = shade(J, cam, cinx, ciny, key_in);
+    const f3 color_out = shade(J, cam, coutx, couty, key_out);
+    const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
+    const float weight = 1.0f / (pdf * (float)J.edge_samples);
+    const float adjv = dot(color_in - color_out, mk(ad.x, ad.y, ad.z));
+    if (adjv * adjv > 0.0f) {
+      const float d0x = (1 - t) * nx * adjv * weight, d0y = (1 - t) * ny * adjv * weight;
+      const float d1x = t * nx * adjv * weight, d1y = t * ny * adjv * weight;
+      const f3 v0 = ld3(J.pos, ed.x), v1 = ld3(J.pos, ed.y);
+      const f3 g0x = vs_grad(cam, v0, false), g0y = vs_grad(cam, v0, true);
+      const f3 g1x = vs_grad(cam, v1, false), g1y = vs_grad(cam, v1, true);
+      const float dv0_dx = g0x.x * d0x, dv0_dy = g0y.y * d0y, dv0_dz = (g0x.z * d0x + g0y.z * d0y);
+      const float dv1_dx = g1x.x * d1x, dv1_dy = g1y.y * d1y, dv1_dz = (g1x.z * d1x + g1y.z * d1y);
+      const MeshDev& md = J.meshes[mi.x];
+      if (md.dslot >= 0) {
+        const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
+        float* g = J.grad + md.g_base + md.pos_off;
+        atomicAdd(g + ed.z * 3 + 0, M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz);
+        atomicAdd(g + ed.z * 3 + 1, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz);
+        atomicAdd(g + ed.z * 3 + 2, M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
+        atomicAdd(g + ed.w * 3 + 0, M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz);
+        atomicAdd(g + ed.w * 3 + 1, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz);
+        atomicAdd(g + ed.w * 3 + 2, M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+        const f3 o0 = ld3(J.orig, ed.x), o1 = ld3(J.orig, ed.y);
+        tr[0] = o0.x * dv0_dx + o1.x * dv1_dx;
+        tr[1] = o0.y * dv0_dx + o1.y * dv1_dx;
+        tr[2] = o0.z * dv0_dx + o1.z * dv1_dx;
+        tr[3] = 1 * dv0_dx + 1 * dv1_dx;
+        tr[4] = o0.x * dv0_dy + o1.x * dv1_dy;
+        tr[5] = o0.y * dv0_dy + o1.y * dv1_dy;
+        tr[6] = o0.z * dv0_dy + o1.z * dv1_dy;
+        tr[7] = 1 * dv0_dy + 1 * dv1_dy;
+        tr[8] = o0.x * dv0_dz + o1.x * dv1_dz;
+        tr[9] = o0.y * dv0_dz + o1.y * dv1_dz;
+        tr[10] = o0.z * dv0_dz + o1.z * dv1_dz;
+        tr[11] = 1 * dv0_dz + 1 * dv1_dz;
+        target = J.grad + md.g_base + md.tr_off + 12 * mi.y;
+      }
+    }
+  }
+  // transform gradient: one atomic per warp when every contributing lane
+  // targets the same block, per lane otherwise
+  const unsigned any = __ballot_sync(0xffffffffu, target != nullptr);
+  if (!any) return;
+  const unsigned long long mine = (unsigned long long)target;
+  const unsigned long long lead = __shfl_sync(0xffffffffu, mine, __ffs(any) - 1);
+  const bool uniform = __all_sync(0xffffffffu, target == nullptr || mine == lead);
+  if (uniform) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      float v = tr[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      tr[k] = v;
+    }
+    if (lane == 0)
+      for (int k = 0; k < 12; k++) atomicAdd(reinterpret_cast<float*>(lead) + k, tr[k]);
+  } else if (target) {
+    for (int k = 0; k < 12; k++) atomicAdd(target + k, tr[k]);
+  }
+}
+
+// ---- single job: blockIdx.y = view -----------------------------------------
+__global__ void k_edge_project(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < J.n_vertices) edge_project_body(J, blockIdx.y, v);
+}
+
+__global__ void k_edge_pmf(const JobDev* jobs, int job) {
+  const JobDev& J = jobs[job];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < J.n_edges) edge_pmf_body(J, blockIdx.y, e);
+}
+
+__global__ void k_edge_cdf(const JobDev* jobs, int job) { edge_cdf_body(jobs[job], blockIdx.x); }
+
 __global__ void k_edge_select(const JobDev* jobs, int job) {
   const JobDev& J = jobs[job];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int view = blockIdx.y;
-  bool keep = false;
-  int edge_id = 0;
-  if (i < J.edge_samples && J.n_edges > 0) {
-    const float rnd0 = __ldg(J.rnd + 2 * i), rnd1 = __ldg(J.rnd + 2 * i + 1);
-    const float* cdf = J.cdf + (int64_t)view * (J.n_edges + 1);
-    edge_id = clampi(upper_bound_idx(cdf, J.n_edges + 1, rnd0) - 1, 0, J.n_edges - 1);
-    const int4 ed = __ldg(J.edges + edge_id);
-    const float4* P = J.proj + (int64_t)view * J.n_vertices;
-    const float4 a = P[ed.x], b = P[ed.y];
-    const float t = rnd1;
-    const float px = a.x + t * (b.x - a.x), py = a.y + t * (b.y - a.y);
-    const int xi = (int)px, yi = (int)py;
-    if (!(xi < 0 || yi < 0 || xi >= J.W || yi >= J.H)) {
-      const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
-      keep = !(length(mk(ad.x, ad.y, ad.z)) < 1e-3f);
-    }
-  }
-  const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-  if (!ballot) return;
-  const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == __ffs(ballot) - 1) base = atomicAdd(J.queue_count, __popc(ballot));
-  base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
-  if (keep) {
-    const int slot = base + __popc(ballot & ((1u << lane) - 1u));
-    if (slot < J.queue_cap) J.queue[slot] = make_int4(view, i, edge_id, 0);
-  }
+  int edge_id;
+  const bool keep = edge_select_test(J, view, i, edge_id);
+  queue_append(J.queue, J.queue_count, J.queue_cap, keep, make_int4(view, i, edge_id, job));
 }
 
-__global__ void __launch_bounds__(256) k_edge_shade(const JobDev* jobs, int job) {
+// Persistent over the queue, in whole warps (the reductions need every lane).
+__global__ void __launch_bounds__(256) k_edge_shade_q(const JobDev* jobs, const int4* queue, const int* count,
+                                                      int cap) {
+  const int n = min(*count, cap);
+  const int stride = gridDim.x * blockDim.x;
+  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
+    edge_shade_warp(jobs, queue, n, q0);
+}
+
+// Single job: the queue, its counter and its capacity are the job's own.
+__global__ void __launch_bounds__(256) k_edge_shade_job(const JobDev* jobs, int job) {
   const JobDev& J = jobs[job];
   const int n = min(*J.queue_count, J.queue_cap);
-  const int lane = threadIdx.x & 31;
   const int stride = gridDim.x * blockDim.x;
-  // iterate in whole warps so that the warp reductions below see every lane
-  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride) {
-    const int q = q0 + lane;
-    float tr[12];
-#pragma unroll
-    for (int k = 0; k < 12; k++) tr[k] = 0.0f;
-    int key = -1;
-    if (q < n) {
-      const int4 it = J.queue[q];
-      const int view = it.x, i = it.y, edge_id = it.z;
-      const CamDev& cam = J.cams[view];
-      const int4 ed = __ldg(J.edges + edge_id);
-      const int2 mi = __ldg(J.edge_mi + edge_id);
-      const float pm = J.pmf[(int64_t)view * J.n_edges + edge_id];
-      const float4* P = J.proj + (int64_t)view * J.n_vertices;
-      const float4 pa = P[ed.x], pb = P[ed.y];
-      const float t = __ldg(J.rnd + 2 * i + 1);
-      const float dx0 = pb.x - pa.x, dy0 = pb.y - pa.y;
-      const float px = pa.x + t * dx0, py = pa.y + t * dy0;
-      const int xi = (int)px, yi = (int)py;
-      const float4 ad = J.adj[(int64_t)view * J.W * J.H + (int64_t)yi * J.W + xi];
-      const float dl = sqrtf(dx0 * dx0 + dy0 * dy0);
-      const float nx = -(dy0 / dl), ny = dx0 / dl;  // normal2D of the unit edge direction
-      const float cinx = px - 1e-3f * nx, ciny = py - 1e-3f * ny;
-      const float coutx = px + 1e-3f * nx, couty = py + 1e-3f * ny;
-      const uint32_t key_in = 0xA511E9B3u ^ ((uint32_t)(i * 2u) * 2654435761u);
-      const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
-      const f3 color_in = shade(J, cam, cinx, ciny, key_in);
-      const f3 color_out = shade(J, cam, coutx, couty, key_out);
-      const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
-      const float weight = 1.0f / (pdf * (float)J.edge_samples);
-      const float adjv = dot(color_in - color_out, mk(ad.x, ad.y, ad.z));
-      if (adjv * adjv > 0.0f) {
-        const float d0x = (1 - t) * nx * adjv * weight, d0y = (1 - t) * ny * adjv * weight;
-        const float d1x = t * nx * adjv * weight, d1y = t * ny * adjv * weight;
-        const f3 v0 = ld3(J.pos, ed.x), v1 = ld3(J.pos, ed.y);
-        const f3 g0x = vs_grad(cam, v0, false), g0y = vs_grad(cam, v0, true);
-        const f3 g1x = vs_grad(cam, v1, false), g1y = vs_grad(cam, v1, true);
-        const float dv0_dx = g0x.x * d0x, dv0_dy = g0y.y * d0y, dv0_dz = (g0x.z * d0x + g0y.z * d0y);
-        const float dv1_dx = g1x.x * d1x, dv1_dy = g1y.y * d1y, dv1_dz = (g1x.z * d1x + g1y.z * d1y);
-        const MeshDev& md = J.meshes[mi.x];
-        if (md.dslot >= 0) {
-          const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
-          float* g = J.grad + md.g_base + md.pos_off;
-          atomicAdd(g + ed.z * 3 + 0, M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz);
-          atomicAdd(g + ed.z * 3 + 1, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz);
-          atomicAdd(g + ed.z * 3 + 2, M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
-          atomicAdd(g + ed.w * 3 + 0, M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz);
-          atomicAdd(g + ed.w * 3 + 1, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz);
-          atomicAdd(g + ed.w * 3 + 2, M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
-          const f3 o0 = ld3(J.orig, ed.x), o1 = ld3(J.orig, ed.y);
-          tr[0] = o0.x * dv0_dx + o1.x * dv1_dx;
-          tr[1] = o0.y * dv0_dx + o1.y * dv1_dx;
-          tr[2] = o0.z * dv0_dx + o1.z * dv1_dx;
-          tr[3] = 1 * dv0_dx + 1 * dv1_dx;
-          tr[4] = o0.x * dv0_dy + o1.x * dv1_dy;
-          tr[5] = o0.y * dv0_dy + o1.y * dv1_dy;
-          tr[6] = o0.z * dv0_dy + o1.z * dv1_dy;
-          tr[7] = 1 * dv0_dy + 1 * dv1_dy;
-          tr[8] = o0.x * dv0_dz + o1.x * dv1_dz;
-          tr[9] = o0.y * dv0_dz + o1.y * dv1_dz;
-          tr[10] = o0.z * dv0_dz + o1.z * dv1_dz;
-          tr[11] = 1 * dv0_dz + 1 * dv1_dz;
-          key = (int)(md.g_base + md.tr_off) + 12 * mi.y;
-        }
-      }
-    }
-    // transform gradient: one atomic per warp when every contributing lane
-    // targets the same instance, per lane otherwise
-    const unsigned any = __ballot_sync(0xffffffffu, key >= 0);
-    if (!any) continue;
-    const int lead_key = __shfl_sync(0xffffffffu, key, __ffs(any) - 1);
-    const bool uniform = __all_sync(0xffffffffu, key < 0 || key == lead_key);
-    if (uniform) {
-#pragma unroll
-      for (int k = 0; k < 12; k++) {
-        float v = tr[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        tr[k] = v;
-      }
-      if (lane == 0)
-        for (int k = 0; k < 12; k++) atomicAdd(J.grad + lead_key + k, tr[k]);
-    } else if (key >= 0) {
-      for (int k = 0; k < 12; k++) atomicAdd(J.grad + key + k, tr[k]);
-    }
-  }
+  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
+    edge_shade_warp(jobs, J.queue, n, q0);
+}
+
+// ---- batched: segment tables over (job, view) pairs --------------------------
+__global__ void k_b_edge_project(const JobDev* jobs, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int v = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (v < sg.count) edge_project_body(jobs[sg.job], sg.sub, v);
+}
+
+__global__ void k_b_edge_pmf(const JobDev* jobs, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int e = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (e < sg.count) edge_pmf_body(jobs[sg.job], sg.sub, e);
+}
+
+// one warp per (job, view) pair: segs[w].job / .sub
+__global__ void k_b_edge_cdf(const JobDev* jobs, const Seg* pairs, int n_pairs) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n_pairs) return;
+  const Seg sg = pairs[w];
+  edge_cdf_body(jobs[sg.job], sg.sub);
+}
+
+__global__ void k_b_edge_select(const JobDev* jobs, const Seg* segs, int nseg, int4* queue, int* count, int cap) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int i = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  int edge_id = 0;
+  const bool keep = i < sg.count && edge_select_test(jobs[sg.job], sg.sub, i, edge_id);
+  queue_append(queue, count, cap, keep, make_int4(sg.sub, i, edge_id, sg.job));
 }
 
 // Same launch sequence with every size and the sample-queue counter passed
@@ -213,21 +274,29 @@ void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, i
   k_edge_cdf<<<n_views, 32, 0, s>>>(d_jobs, job);
   DRGB_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int), s));
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
-  k_edge_shade<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  // the queue, its counter and capacity are read from the job on the device
+  k_edge_shade_job<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
   count_launch(5);
 }
 
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s) {
   if (J.n_edges <= 0 || J.n_views <= 0) return;
-  const dim3 gp((J.n_vertices + 255) / 256, J.n_views);
-  k_edge_project<<<gp, 256, 0, s>>>(d_jobs, job);
-  const dim3 ge((J.n_edges + 255) / 256, J.n_views);
-  k_edge_pmf<<<ge, 256, 0, s>>>(d_jobs, job);
-  k_edge_cdf<<<J.n_views, 32, 0, s>>>(d_jobs, job);
-  DRGB_CUDA(cudaMemsetAsync(J.queue_count.p, 0, sizeof(int), s));
-  const dim3 gs((J.dev.edge_samples + 255) / 256, J.n_views);
-  k_edge_select<<<gs, 256, 0, s>>>(d_jobs, job);
-  k_edge_shade<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  launch_edges_raw(d_jobs, job, J.n_edges, J.n_views, J.n_vertices, J.dev.edge_samples, J.queue_count.p, shade_grid,
+                   s);
+}
+
+// Edge pass of every job of a batch; the shared queue holds (view, sample,
+// edge, job) entries of all jobs.
+void launch_b_edges(const JobDev* d_jobs, const Seg* proj_segs, int n_proj, int proj_chunks, const Seg* pmf_segs,
+                    int n_pmf, int pmf_chunks, const Seg* pairs, int n_pairs, const Seg* sel_segs, int n_sel,
+                    int sel_chunks, int4* queue, int* count, int cap, int shade_grid, cudaStream_t s) {
+  if (n_pairs <= 0) return;
+  if (proj_chunks > 0) k_b_edge_project<<<proj_chunks, 256, 0, s>>>(d_jobs, proj_segs, n_proj);
+  if (pmf_chunks > 0) k_b_edge_pmf<<<pmf_chunks, 256, 0, s>>>(d_jobs, pmf_segs, n_pmf);
+  k_b_edge_cdf<<<(n_pairs + 7) / 8, 256, 0, s>>>(d_jobs, pairs, n_pairs);
+  DRGB_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
+  if (sel_chunks > 0) k_b_edge_select<<<sel_chunks, 256, 0, s>>>(d_jobs, sel_segs, n_sel, queue, count, cap);
+  k_edge_shade_q<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, queue, count, cap);
   count_launch(5);
 }
 

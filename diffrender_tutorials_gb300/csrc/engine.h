@@ -78,14 +78,6 @@ struct DLayout {
   int64_t base = 0;  // offset in the concatenated vector
 };
 
-// Source arrays of one mesh read by the flattening kernel.
-struct MeshSrc {
-  const float* v;
-  const float* col;
-  const float* nrm;
-  const float* tc;
-};
-
 // Count of kernels launched by this library (reported by drgb_kernel_launches).
 void count_launch(int n = 1);
 

@@ -13,17 +13,6 @@
 
 namespace drgb {
 
-struct OptMesh {
-  int64_t base;
-  int full;
-  int pos_off, color_off, tex_off, tr_off;
-  int nv, n_inst;
-  float* vertices;
-  float* colors;
-  float* texture;
-  float* transforms;
-};
-
 struct OptDev {
   int n;  // differentiable meshes
   OptMesh m[16];
@@ -32,9 +21,7 @@ struct OptDev {
   float decay_mult;
 };
 
-__global__ void k_opt_moments(float* grad, float* m, float* G, int64_t n, int alg) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ void opt_moment_body(float* grad, float* m, float* G, int64_t i, int alg) {
   const float g = grad[i];
   if (alg == DRGB_GD_ADAGRAD) {
     G[i] += (g * g);
@@ -50,14 +37,18 @@ __global__ void k_opt_moments(float* grad, float* m, float* G, int64_t n, int al
   }
 }
 
-__global__ void k_opt_apply(float* grad, const float* G, const float* lr, OptDev o) {
-  const int k = blockIdx.y;
-  if (k >= o.n) return;
-  const OptMesh& M = o.m[k];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= M.full) return;
+__global__ void k_opt_moments(float* grad, float* m, float* G, int64_t n, int alg) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  opt_moment_body(grad, m, G, i, alg);
+}
+
+// Step of element j of differentiable mesh k: scale, then subtract from the
+// scene parameter it belongs to (OptStep + OptUpdateScene).
+__device__ __forceinline__ void opt_apply_body(float* grad, const float* G, const float* lr, const OptMesh& M, int k,
+                                               int j, int alg, int flags, int mode) {
   float v = grad[M.base + j];
-  if (o.alg >= DRGB_GD_ADAGRAD) v = v / (sqrtf(G[j] + 1e-8f));
+  if (alg >= DRGB_GD_ADAGRAD) v = v / (sqrtf(G[j] + 1e-8f));
   // segment of j: positions [0, color|tex|tr), colours, texture, transforms
   int seg;
   if (j >= M.tr_off) seg = 3;
@@ -67,18 +58,64 @@ __global__ void k_opt_apply(float* grad, const float* G, const float* lr, OptDev
   v *= lr[4 * k + seg];
   grad[M.base + j] = v;
   if (seg == 0) {
-    if (o.flags & DRGB_OPT_POS) M.vertices[j - M.pos_off] -= v;
+    if (flags & DRGB_OPT_POS) M.vertices[j - M.pos_off] -= v;
   } else if (seg == 1) {
-    if ((o.flags & DRGB_OPT_COL) && M.colors) M.colors[j - M.color_off] -= v;
+    if ((flags & DRGB_OPT_COL) && M.colors) M.colors[j - M.color_off] -= v;
   } else if (seg == 2) {
-    if ((o.flags & DRGB_OPT_TEX) && o.mode != SILHOUETTE && o.mode != VERTEX_COLOR && M.texture)
+    if ((flags & DRGB_OPT_TEX) && mode != SILHOUETTE && mode != VERTEX_COLOR && M.texture)
       M.texture[j - M.tex_off] -= v;
   } else {
-    if (o.flags & DRGB_OPT_TFM) {
+    if (flags & DRGB_OPT_TFM) {
       const int l = j - M.tr_off, inst = l / 12, r = (l % 12) / 4, c = l % 4;
       M.transforms[16 * inst + 4 * c + r] -= v;
     }
   }
+}
+
+__global__ void k_opt_apply(float* grad, const float* G, const float* lr, OptDev o) {
+  const int k = blockIdx.y;
+  if (k >= o.n) return;
+  const OptMesh& M = o.m[k];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M.full) return;
+  opt_apply_body(grad, G, lr, M, k, j, o.alg, o.flags, o.mode);
+}
+
+// ---- batched forms: one launch over the parameters of many jobs ----------
+__global__ void k_b_opt_moments(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int64_t i = (int64_t)(blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (i >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  if (A.alg >= DRGB_GD_ADAGRAD) opt_moment_body(A.grad, A.m, A.G, i, A.alg);
+}
+
+__global__ void k_b_opt_apply(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int j = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (j >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  opt_apply_body(A.grad, A.G, A.lr, A.dm[sg.sub], sg.sub, j, A.alg, A.flags, A.mode);
+}
+
+// Per job: losses[iter] = loss, StepDecay(iter), iter++.
+__global__ void k_b_opt_tail(const JobAux* aux, int n_jobs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_jobs) return;
+  const JobAux& A = aux[j];
+  const int it = *A.iter;
+  if (it >= 0 && it < A.losses_cap) A.losses[it] = *A.loss_out;
+  if (it > 0 && it % max(1, A.decay_period) == 0)
+    for (int i = 0; i < 4 * A.n_dmesh; i++) A.lr[i] *= A.decay_mult;
+  *A.iter = it + 1;
+}
+
+void launch_b_opt(const JobAux* d_aux, int n_jobs, const Seg* d_moment_segs, int n_moment_segs, int moment_chunks,
+                  const Seg* d_apply_segs, int n_apply_segs, int apply_chunks, cudaStream_t s) {
+  if (moment_chunks > 0) k_b_opt_moments<<<moment_chunks, 256, 0, s>>>(d_aux, d_moment_segs, n_moment_segs);
+  if (apply_chunks > 0) k_b_opt_apply<<<apply_chunks, 256, 0, s>>>(d_aux, d_apply_segs, n_apply_segs);
+  k_b_opt_tail<<<(n_jobs + 127) / 128, 128, 0, s>>>(d_aux, n_jobs);
+  count_launch(3);
 }
 
 // StepDecay(iter) then iter++ (optimizer_simple.cpp:82-90, 293-301).

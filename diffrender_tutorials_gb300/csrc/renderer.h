@@ -12,8 +12,9 @@ namespace drgb {
 void add_launches(int64_t n);
 }  // namespace drgb
 
-// Records the message returned by drgb_last_error on this thread.
+// Records / returns the message returned by drgb_last_error on this thread.
 void drgb_set_last_error(const std::string& m);
+std::string t_err_message();
 
 template <class F>
 static int guard(F&& f) {

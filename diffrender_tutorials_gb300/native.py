@@ -78,6 +78,20 @@ _SIGS = {
     "drgb_optimizer_run": (C.c_int, [VP, C.c_int64, VP, VP]),
     "drgb_optimizer_run_async": (C.c_int, [VP, C.c_int64]),
     "drgb_optimizer_get_mesh": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+    "drgb_batch_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
+    "drgb_batch_destroy": (C.c_int, [VP]),
+    "drgb_batch_stream": (VP, [VP]),
+    "drgb_batch_add_job": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(ModelParams), C.POINTER(SceneDesc),
+                                     C.POINTER(Camera), VP, C.c_int, C.POINTER(OptParams), C.POINTER(C.c_int32)]),
+    "drgb_batch_remove_job": (C.c_int, [VP, C.c_int32]),
+    "drgb_batch_size": (C.c_int, [VP]),
+    "drgb_batch_set_option": (C.c_int, [VP, C.c_int, C.c_int64]),
+    "drgb_batch_run_async": (C.c_int, [VP, C.c_int64]),
+    "drgb_batch_run": (C.c_int, [VP, C.c_int64]),
+    "drgb_batch_sync": (C.c_int, [VP]),
+    "drgb_batch_job_losses": (C.c_int, [VP, C.c_int32, C.c_int64, C.c_int64, VP, C.POINTER(C.c_int64)]),
+    "drgb_batch_get_mesh": (C.c_int, [VP, C.c_int32, C.c_int, VP, VP, VP, VP]),
+    "drgb_batch_job_device_bytes": (C.c_int64, [VP, C.c_int32]),
     "drgb_optimizer_profile": (C.c_int, [VP, C.c_int, VP]),
     "drgb_count_work": (C.c_int, [VP, VP]),
 }

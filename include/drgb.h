@@ -206,6 +206,37 @@ int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters);
 int drgb_optimizer_get_mesh(drgb_renderer* r, int mesh_id, float* vertices, float* colors, float* texture,
                             float* transforms);
 
+/* ---- batched optimisation (no reference counterpart: the reference runs one
+ * OptSimple at a time, src/tests.cpp:125-204).  A batch advances many
+ * independent optimisation jobs -- each one the equivalent of
+ * IOptimizer::Init + Run (src/optimizer.h:52-61) -- with one fused launch
+ * sequence per iteration, replayed from a CUDA graph.  Every job is set up
+ * exactly as drgb_optimizer_init sets up a plain optimiser, so a job computes
+ * the same alone and in a batch (up to the order of floating-point atomic
+ * additions). ------------------------------------------------------------- */
+typedef struct drgb_batch drgb_batch;
+int drgb_batch_create(int device, drgb_batch** out);
+int drgb_batch_destroy(drgb_batch* b);
+void* drgb_batch_stream(drgb_batch* b);
+/* Adds a job (scene, views, host target images, optimiser parameters;
+ * model_params may be NULL).  Returns its id in *job_id. */
+int drgb_batch_add_job(drgb_batch* b, int shading_model, int spp, const drgb_model_params* model_params,
+                       const drgb_scene_desc* scene, const drgb_camera* cams, const float* targets, int n_views,
+                       const drgb_opt_params* p, int32_t* job_id);
+int drgb_batch_remove_job(drgb_batch* b, int32_t job_id);
+int drgb_batch_size(drgb_batch* b);
+int drgb_batch_set_option(drgb_batch* b, int option, int64_t value); /* DRGB_OPT_USE_GRAPH */
+/* n_iters iterations of every job: enqueue only / enqueue and wait. */
+int drgb_batch_run_async(drgb_batch* b, int64_t n_iters);
+int drgb_batch_run(drgb_batch* b, int64_t n_iters);
+int drgb_batch_sync(drgb_batch* b);
+/* Losses of iterations [first, first+n) of a job; *iters_done = iterations run. */
+int drgb_batch_job_losses(drgb_batch* b, int32_t job_id, int64_t first, int64_t n, float* out, int64_t* iters_done);
+int drgb_batch_get_mesh(drgb_batch* b, int32_t job_id, int mesh_id, float* vertices, float* colors, float* texture,
+                        float* transforms);
+/* Device memory held by a job (for admission against a memory budget). */
+int64_t drgb_batch_job_device_bytes(drgb_batch* b, int32_t job_id);
+
 /* ---- measurement (no reference counterpart: the reference prints wall-clock
  * ms/iter only, src/main.cpp:218-224, src/tests.cpp:136-203) -------------- */
 /* Runs n_iters optimiser iterations phase by phase (no graph) and returns the
