@@ -409,20 +409,168 @@ def batch_arm(args, ws, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def serve_setups(args, local):
+    """The Poisson trace with its target images rendered from the true meshes."""
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import workloads as WL
+    specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate)
+    out = []
+    for sp in specs:
+        ts, isc = D.Scene(), D.Scene()
+        ts.add_mesh(sp.true_mesh)
+        isc.add_mesh(sp.init_mesh)
+        st = D.DiffRenderSettings(D.SHADING_MODEL(sp.mode), sp.spp)
+        r = D.MakeDifferentialRenderer(st, device=local)
+        r.commit(ts)
+        out.append((isc, sp.cams, r.render(ts, sp.cams), st, sp))
+        del r
+    return out
+
+
+def serve_params(sp):
+    import diffrender_tutorials_gb300 as D
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.002)
+    p.base_lr = 0.01
+    p.flags = D.OptimizerParameters._OPT_POS | D.OptimizerParameters._OPT_COL
+    return p
+
+
+def serve_arm(args, ws, rank, local, pg):
+    """Poisson arrivals of optimisation jobs (wall clock): the serving loop
+    (continuous batching, admission by memory budget) against the plain path
+    (each job alone with its own optimiser, first come first served), on the
+    same trace.  Per-iteration latency = device time of the step that ran the
+    iteration; per-job latency = completion - arrival."""
+    import torch
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(local)
+    setups = serve_setups(args, local)
+    n = len(setups)
+    total_iters = sum(sp.steps for *_, sp in setups)
+    # warm-up: load the kernels and the graph path once
+    warm = D.OptimizationServer(device=local)
+    for isc, cams, tgt, st, sp in setups[:2]:
+        warm.submit(isc, cams, tgt, st, serve_params(sp), args.warmup)
+    warm.wait(0)
+    warm.close()
+    torch.cuda.synchronize()
+
+    # served
+    srv = D.OptimizationServer(device=local, hbm_budget_bytes=int(args.budget_gb * 1e9), max_jobs=args.slots)
+    k0 = D.kernel_launches()
+    h2d = 0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        tickets = []
+        for isc, cams, tgt, st, sp in setups:
+            dt = t0 + sp.arrival - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(isc, cams, tgt, st, serve_params(sp), sp.steps))
+            h2d += tgt.nbytes + sum(m.vertices.nbytes + m.indices.nbytes + (m.colors.nbytes if m.colors is not None
+                                                                              else 0) for m in isc.meshes)
+        srv.wait(0)
+    launches = D.kernel_launches() - k0
+    stats = srv.stats()
+    infos = [srv.info(t) for t in tickets]
+    assert all(i["state"] == "done" for i in infos), [i["state"] for i in infos]
+    ms, resident = srv.step_times()
+    d2h = sum(sum(m.vertices.nbytes + (m.colors.nbytes if m.colors is not None else 0) for m in s[0].meshes) +
+              4 * sp.steps for s, sp in zip(setups, [x[4] for x in setups]))
+    first = min(i["t_submit"] for i in infos)
+    makespan = max(i["t_done"] for i in infos) - first
+    served = total_iters / makespan
+    job_lat = [i["t_done"] - i["t_submit"] for i in infos]
+    it_lat = np.repeat(ms, resident)  # every resident job's iteration took the step's time
+    srv.close()
+
+    # plain: one job at a time in arrival order, each with its own optimiser
+    plain_it, plain_job = [], []
+    plain_busy = 0.0
+    t0 = time.perf_counter()
+    for isc, cams, tgt, st, sp in setups:
+        dt = t0 + sp.arrival - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        r = D.MakeDifferentialRenderer(st, device=local)
+        o = D.CreateSimpleOptimizer()
+        o.Init(isc, r, cams, tgt, serve_params(sp))
+        s = torch.cuda.ExternalStream(r.stream(), device=local)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(sp.steps)]
+        with torch.cuda.stream(s):
+            for e0, e1 in ev:
+                e0.record(s)
+                o.run_async(1)
+                e1.record(s)
+        ev[-1][1].synchronize()
+        o.current_scene()  # results back on the host, as the server does
+        plain_job.append(time.perf_counter() - t0 - sp.arrival)
+        its = [e0.elapsed_time(e1) for e0, e1 in ev]
+        plain_busy += sum(its) / 1e3
+        plain_it += its
+        del o, r
+    plain_makespan = time.perf_counter() - t0 - setups[0][4].arrival
+    plain = total_iters / plain_makespan
+
+    pct = lambda xs, q: float(np.percentile(np.asarray(xs, np.float64), q))  # noqa: E731
+    tris = [sp.triangles for *_, sp in setups]
+    res = [sp.cams[0].width for *_, sp in setups]
+    line = {
+        "metric": "served fwd+adjoint iters/s", "value": served, "unit": "iters/s", "n_gpus": ws,
+        "steps": total_iters, "warmup": args.warmup, "ms_per_step": 1e3 / served, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Poisson trace of displaced-sphere optimisation jobs)",
+        "config": {"workload": f"serve{n}_poisson{args.rate:g}_displaced_spheres", "jobs": n, "rate_per_s": args.rate,
+                   "triangles": [min(tris), max(tris)], "resolution": [min(res), max(res)],
+                   "views": [min(len(sp.cams) for *_, sp in setups), max(len(sp.cams) for *_, sp in setups)],
+                   "steps_per_job": [min(sp.steps for *_, sp in setups), max(sp.steps for *_, sp in setups)],
+                   "models": sorted({D.SHADING_MODEL(sp.mode).name for *_, sp in setups}),
+                   "hbm_budget_gb": args.budget_gb, "slots": args.slots or "unlimited",
+                   "l2": f"not flushed: back-to-back steps over a resident working set of "
+                         f"{stats['bytes_peak'] / 1e9:.2f} GB (> L2)",
+                   "parallelism": "replicas"},
+        "latency_ms": {"iteration_p50": pct(it_lat, 50), "iteration_p99": pct(it_lat, 99),
+                       "job_p50": 1e3 * pct(job_lat, 50), "job_p99": 1e3 * pct(job_lat, 99)},
+        "plain": {"value": plain, "unit": "iters/s", "how": "each job alone with its own optimiser graph, "
+                  "first come first served, same arrivals",
+                  "latency_ms": {"iteration_p50": pct(plain_it, 50), "iteration_p99": pct(plain_it, 99),
+                                 "job_p50": 1e3 * pct(plain_job, 50), "job_p99": 1e3 * pct(plain_job, 99)},
+                  "gpu_busy_s": plain_busy, "makespan_s": plain_makespan},
+        "speedup_vs_plain": served / plain,
+        "makespan_s": makespan, "gpu_busy_s": stats["busy_seconds"], "batched_steps": int(stats["batch_steps"]),
+        "resident_jobs": {"max": int(resident.max()), "mean": float(resident.mean())},
+        "hbm_peak_gb": stats["bytes_peak"] / 1e9,
+        "e2e": {"value": served, "unit": "iters/s", "h2d_bytes_per_step": int(h2d / total_iters),
+                "d2h_bytes_per_step": int(d2h / total_iters),
+                "api": "drgb_server_submit/wait (host inputs copied at submission, results copied back)"},
+        "clocks": clk.summary(), "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="drgb", choices=["drgb", "reference"])
-    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch"])
-    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve"])
+    ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
+    ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device memory budget")
+    ap.add_argument("--slots", type=int, default=0, help="serving: resident jobs at most (0: no limit)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)
     ws, rank, local, pg = dist_setup()
-    if args.workload == "batch":
-        batch_arm(args, ws, rank, local, pg)
+    if args.workload in ("batch", "serve"):
+        if args.jobs is None:
+            args.jobs = 64 if args.workload == "batch" else 16
+        (batch_arm if args.workload == "batch" else serve_arm)(args, ws, rank, local, pg)
         if pg is not None:
             pg.destroy_process_group()
         return

@@ -8,4 +8,4 @@ from .scene import (CamInfo, Scene, Texture, TriangleMesh, displace_radially, ma
                     make_uv_sphere, perturb_vertices, ring_cameras)
 from .api import (SHADING_MODEL, CreateSimpleOptimizer, DiffRenderSettings, DMesh, DScene, IDiffRender,  # noqa: F401
                   IOptimizer, MakeDifferentialRenderer, ModelParams, OptimizerParameters, kernel_launches,
-                  BatchOptimizer)
+                  BatchOptimizer, OptimizationServer, estimate_job_bytes)

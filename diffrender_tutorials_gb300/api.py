@@ -462,5 +462,109 @@ class BatchOptimizer:
         return s
 
 
+JOB_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
+
+class OptimizationServer:
+    """Serving loop over the batched engine (drgb_server_*): jobs are
+    submitted at any time, admitted in arrival order by a device-memory budget
+    and a slot count, and advanced together one iteration per batched step
+    (continuous batching).  With worker=True a native worker thread steps the
+    batch; otherwise call step()."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 150 * 10**9, max_jobs: int = 0,
+                 worker: bool = True, deterministic: bool = False):
+        cfg = N.ServerConfig(int(device), int(max_jobs), int(hbm_budget_bytes), 1 if worker else 0,
+                             1 if deterministic else 0)
+        self._h = C.c_void_p()
+        N.check(N.load().drgb_server_create(C.byref(cfg), C.byref(self._h)))
+        self._scenes = {}
+
+    def close(self):
+        if self._h:
+            N.load().drgb_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scene: Scene, cams: Sequence[CamInfo], targets: np.ndarray, settings: DiffRenderSettings,
+               params: OptimizerParameters, steps: int, model_params: Optional[ModelParams] = None) -> int:
+        h = _SceneHandle(scene)
+        tg = np.ascontiguousarray(np.asarray(targets, np.float32).reshape(-1))
+        p = params.native()
+        mp = _model_params_native(model_params)
+        t = C.c_int32(0)
+        N.check(N.load().drgb_server_submit(self._h, int(settings.mode), int(settings.spp),
+                                            C.byref(mp) if mp is not None else None, C.byref(h.desc),
+                                            make_cameras(list(cams)), _ptr(tg), len(cams), C.byref(p), int(steps),
+                                            C.byref(t)))
+        self._scenes[int(t.value)] = scene.copy()
+        return int(t.value)
+
+    def step(self) -> int:
+        n = C.c_int32(0)
+        N.check(N.load().drgb_server_step(self._h, C.byref(n)))
+        return int(n.value)
+
+    def wait(self, ticket: int = 0, timeout: float = -1.0):
+        """Until the job (or, with ticket 0, every submitted job) is finished."""
+        N.check(N.load().drgb_server_wait(self._h, int(ticket), float(timeout)))
+
+    def info(self, ticket: int) -> dict:
+        i = N.JobInfo()
+        N.check(N.load().drgb_server_job_info(self._h, int(ticket), C.byref(i)))
+        return {"state": JOB_STATES.get(i.state, str(i.state)), "error": i.error, "steps": i.steps,
+                "steps_done": i.steps_done, "t_submit": i.t_submit, "t_admit": i.t_admit, "t_done": i.t_done,
+                "device_bytes": i.device_bytes, "final_loss": i.final_loss}
+
+    def losses(self, ticket: int) -> np.ndarray:
+        n = self.info(ticket)["steps_done"]
+        out = np.zeros(max(1, n), np.float32)
+        N.check(N.load().drgb_server_job_losses(self._h, int(ticket), 0, n, _ptr(out)))
+        return out[:n]
+
+    def result_scene(self, ticket: int) -> Scene:
+        s = self._scenes[ticket].copy()
+        for i, m in enumerate(s.meshes):
+            v = np.zeros_like(m.vertices)
+            col = np.zeros_like(m.colors) if m.colors is not None else None
+            tex = np.zeros_like(m.textures[0].data) if m.textures else None
+            tr = np.zeros(16 * len(s.transforms[i]), np.float32)
+            N.check(N.load().drgb_server_get_mesh(self._h, int(ticket), i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
+            m.vertices = v
+            if col is not None:
+                m.colors = col
+            if tex is not None:
+                m.textures[0].data = tex
+            s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
+        return s
+
+    def release(self, ticket: int):
+        N.check(N.load().drgb_server_release(self._h, int(ticket)))
+        self._scenes.pop(ticket, None)
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.load().drgb_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}
+
+    def step_times(self):
+        """(device ms, resident jobs) of every batched step so far."""
+        n = self.stats()["batch_steps"]
+        ms = np.zeros(max(1, n), np.float32)
+        jobs = np.zeros(max(1, n), np.int32)
+        N.check(N.load().drgb_server_step_times(self._h, 0, n, _ptr(ms), _ptr(jobs)))
+        return ms[:n], jobs[:n]
+
+
+def estimate_job_bytes(scene: Scene, cams: Sequence[CamInfo], mode: int = 0) -> int:
+    h = _SceneHandle(scene)
+    return int(N.load().drgb_estimate_job_bytes(int(mode), C.byref(h.desc), make_cameras(list(cams)), len(cams)))
+
+
 def kernel_launches() -> int:
     return int(N.load().drgb_kernel_launches())

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdrgb.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["bvh.cu", "render.cu", "edge.cu", "optim.cu", "engine.cu", "capi.cu", "noalloc.cu", "batch.cu"]
+SOURCES = ["bvh.cu", "render.cu", "edge.cu", "optim.cu", "engine.cu", "capi.cu", "noalloc.cu", "batch.cu", "serve.cu", "detsum.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

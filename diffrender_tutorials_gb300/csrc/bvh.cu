@@ -173,6 +173,11 @@ __global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* hist, int m) {
   }
 }
 
+void launch_rs_scan(uint32_t* hist, int m, cudaStream_t s) {
+  k_rs_scan<<<1, 1024, 0, s>>>(hist, m);
+  count_launch();
+}
+
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* kin, const int* vin, uint32_t* kout,
                                                            int* vout, int n, int shift, const uint32_t* hist) {
   __shared__ uint32_t offs[256];

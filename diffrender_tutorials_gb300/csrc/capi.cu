@@ -99,6 +99,19 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         break;
       }
       case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
+      case DRGB_OPT_DETERMINISTIC: {
+        Job& J = r->job;
+        J.det = value ? 1 : 0;
+        J.dev.det = 0;
+        // an initialised optimiser gets its record buffers now; other calls
+        // allocate them with their per-call buffers
+        if (J.det && J.opt.active) {
+          r->set_device();
+          det_buffers(J, r->stream);
+        }
+        if (r->d_job.p) r->push_dev();
+        break;
+      }
       default: throw CudaError("unknown option", DRGB_ERR_INVALID);
     }
     r->graph_valid = false;
@@ -184,10 +197,12 @@ int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoin
       DRGB_CUDA(cudaMemcpyAsync(J.grad.p, dscene, sizeof(float) * J.grad_total, cudaMemcpyHostToDevice, r->stream));
     r->push_dev();
     launch_adj_convert(r->d_job.p, (int64_t)npix, r->stream);
+    r->det_begin();
     if (J.mode != SILHOUETTE)
       launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_ADJ, r->px_grid(),
-                    r->stream, J.mode);
+                    r->stream, J.mode, J.det);
     if (edge_samples_in_total > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
+    r->det_end();
     if (J.grad_total > 0)
       DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, cudaMemcpyDeviceToHost, r->stream));
     r->check_flags();
@@ -417,12 +432,14 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
     for (int it = 0; it < n_iters; it++) {
       DRGB_CUDA(cudaEventRecord(ev[0], r->stream));
       DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), r->stream));
+      r->det_begin();
       const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
       launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
-                    r->stream, J.mode);
+                    r->stream, J.mode, J.det);
       launch_loss_finalize(r->d_job.p, 1, r->stream);
       DRGB_CUDA(cudaEventRecord(ev[1], r->stream));
       if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
+      r->det_end();  // deterministic mode: the record reduction is timed with the edge phase
       DRGB_CUDA(cudaEventRecord(ev[2], r->stream));
       launch_opt_record(J, r->stream);
       launch_opt_step(J, r->stream);

@@ -137,7 +137,32 @@ struct JobDev {
   const float* rnd;         // 2 * edge_samples replayed random numbers
   // optional work counters (rays, box tests, triangle tests); null normally
   unsigned long long* work;
+  // deterministic reduction: gradient contributions become records
+  // {gradient index of 3 consecutive floats, value} in slots fixed by their
+  // producer (work item / pass / lane, or view / edge sample), summed later
+  // in a fixed order instead of by float atomics
+  int det;
+  int rec_item_cap;          // record slots of one pixel work item
+  uint32_t* rec_key;
+  float4* rec_val;
+  int* rec_count;            // records per region: work items, then (view, sample) edge regions
 };
+
+// Record slots a work item of NS samples may fill (deterministic mode):
+// per pass of 32 samples, 3 per lane for vertex colours, 4 for texture taps.
+__host__ __device__ inline int item_record_cap(int mode, int NS) {
+  const int passes = (NS + 31) / 32;
+  return passes * 32 * (model_has_tex(mode) ? 4 : 3);
+}
+
+// Record slots of the edge region of sample i of a view.
+constexpr int kEdgeRecords = 6;  // two vertex positions, four rows of the instance matrix
+__device__ __forceinline__ int64_t edge_region(const JobDev& J, int view, int i) {
+  return (int64_t)J.item_count + (int64_t)view * J.edge_samples + i;
+}
+__device__ __forceinline__ int64_t edge_rec_slot(const JobDev& J, int view, int i) {
+  return (int64_t)J.item_count * J.rec_item_cap + ((int64_t)view * J.edge_samples + i) * kEdgeRecords;
+}
 
 // Source arrays of one mesh read by the flattening kernel.
 struct MeshSrc {

@@ -103,7 +103,9 @@ __device__ __forceinline__ void queue_append(int4* queue, int* count, int cap, b
   }
 }
 
-// Shading and chain rule of queue entries [q0, q0+32) (one per lane).
+// Shading and chain rule of queue entries [q0, q0+32) (one per lane).  DET:
+// the deterministic-mode variant (records for jobs that have record buffers).
+template <bool DET>
 __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* queue, int n, int q0) {
   const int lane = threadIdx.x & 31;
   const int q = q0 + lane;
@@ -149,12 +151,18 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
       if (md.dslot >= 0) {
         const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
         float* g = J.grad + md.g_base + md.pos_off;
-        atomicAdd(g + ed.z * 3 + 0, M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz);
-        atomicAdd(g + ed.z * 3 + 1, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz);
-        atomicAdd(g + ed.z * 3 + 2, M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
-        atomicAdd(g + ed.w * 3 + 0, M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz);
-        atomicAdd(g + ed.w * 3 + 1, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz);
-        atomicAdd(g + ed.w * 3 + 2, M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+        const f3 d0 = mk(M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz,
+                         M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
+        const f3 d1 = mk(M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz,
+                         M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+        if (!(DET && J.det)) {
+          atomicAdd(g + ed.z * 3 + 0, d0.x);
+          atomicAdd(g + ed.z * 3 + 1, d0.y);
+          atomicAdd(g + ed.z * 3 + 2, d0.z);
+          atomicAdd(g + ed.w * 3 + 0, d1.x);
+          atomicAdd(g + ed.w * 3 + 1, d1.y);
+          atomicAdd(g + ed.w * 3 + 2, d1.z);
+        }
         const f3 o0 = ld3(J.orig, ed.x), o1 = ld3(J.orig, ed.y);
         tr[0] = o0.x * dv0_dx + o1.x * dv1_dx;
         tr[1] = o0.y * dv0_dx + o1.y * dv1_dx;
@@ -169,6 +177,22 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
         tr[10] = o0.z * dv0_dz + o1.z * dv1_dz;
         tr[11] = 1 * dv0_dz + 1 * dv1_dz;
         target = J.grad + md.g_base + md.tr_off + 12 * mi.y;
+        if (DET && J.det) {
+          // six records in the sample's own slots, in a fixed order
+          const int64_t slot = edge_rec_slot(J, view, i);
+          const uint32_t kp = (uint32_t)(g - J.grad), kt = (uint32_t)(target - J.grad);
+          J.rec_key[slot + 0] = kp + 3 * ed.z;
+          J.rec_val[slot + 0] = make_float4(d0.x, d0.y, d0.z, 0.0f);
+          J.rec_key[slot + 1] = kp + 3 * ed.w;
+          J.rec_val[slot + 1] = make_float4(d1.x, d1.y, d1.z, 0.0f);
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            J.rec_key[slot + 2 + k] = kt + 3 * k;
+            J.rec_val[slot + 2 + k] = make_float4(tr[3 * k], tr[3 * k + 1], tr[3 * k + 2], 0.0f);
+          }
+          J.rec_count[edge_region(J, view, i)] = kEdgeRecords;
+          target = nullptr;
+        }
       }
     }
   }
@@ -218,21 +242,23 @@ __global__ void k_edge_select(const JobDev* jobs, int job) {
 }
 
 // Persistent over the queue, in whole warps (the reductions need every lane).
+template <bool DET>
 __global__ void __launch_bounds__(256) k_edge_shade_q(const JobDev* jobs, const int4* queue, const int* count,
                                                       int cap) {
   const int n = min(*count, cap);
   const int stride = gridDim.x * blockDim.x;
   for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
-    edge_shade_warp(jobs, queue, n, q0);
+    edge_shade_warp<DET>(jobs, queue, n, q0);
 }
 
 // Single job: the queue, its counter and its capacity are the job's own.
+template <bool DET>
 __global__ void __launch_bounds__(256) k_edge_shade_job(const JobDev* jobs, int job) {
   const JobDev& J = jobs[job];
   const int n = min(*J.queue_count, J.queue_cap);
   const int stride = gridDim.x * blockDim.x;
   for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
-    edge_shade_warp(jobs, J.queue, n, q0);
+    edge_shade_warp<DET>(jobs, J.queue, n, q0);
 }
 
 // ---- batched: segment tables over (job, view) pairs --------------------------
@@ -267,7 +293,7 @@ __global__ void k_b_edge_select(const JobDev* jobs, const Seg* segs, int nseg, i
 // Same launch sequence with every size and the sample-queue counter passed
 // explicitly (for callers whose buffers are not owned by a Job).
 void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
-                      int* queue_count, int shade_grid, cudaStream_t s) {
+                      int* queue_count, int shade_grid, cudaStream_t s, bool det) {
   if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
   k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
@@ -275,28 +301,30 @@ void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, i
   DRGB_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int), s));
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   // the queue, its counter and capacity are read from the job on the device
-  k_edge_shade_job<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  if (det) k_edge_shade_job<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
+  else k_edge_shade_job<false><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job);
   count_launch(5);
 }
 
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s) {
   if (J.n_edges <= 0 || J.n_views <= 0) return;
   launch_edges_raw(d_jobs, job, J.n_edges, J.n_views, J.n_vertices, J.dev.edge_samples, J.queue_count.p, shade_grid,
-                   s);
+                   s, J.det != 0);
 }
 
 // Edge pass of every job of a batch; the shared queue holds (view, sample,
 // edge, job) entries of all jobs.
 void launch_b_edges(const JobDev* d_jobs, const Seg* proj_segs, int n_proj, int proj_chunks, const Seg* pmf_segs,
                     int n_pmf, int pmf_chunks, const Seg* pairs, int n_pairs, const Seg* sel_segs, int n_sel,
-                    int sel_chunks, int4* queue, int* count, int cap, int shade_grid, cudaStream_t s) {
+                    int sel_chunks, int4* queue, int* count, int cap, int shade_grid, cudaStream_t s, bool det) {
   if (n_pairs <= 0) return;
   if (proj_chunks > 0) k_b_edge_project<<<proj_chunks, 256, 0, s>>>(d_jobs, proj_segs, n_proj);
   if (pmf_chunks > 0) k_b_edge_pmf<<<pmf_chunks, 256, 0, s>>>(d_jobs, pmf_segs, n_pmf);
   k_b_edge_cdf<<<(n_pairs + 7) / 8, 256, 0, s>>>(d_jobs, pairs, n_pairs);
   DRGB_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
   if (sel_chunks > 0) k_b_edge_select<<<sel_chunks, 256, 0, s>>>(d_jobs, sel_segs, n_sel, queue, count, cap);
-  k_edge_shade_q<<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, queue, count, cap);
+  if (det) k_edge_shade_q<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, queue, count, cap);
+  else k_edge_shade_q<false><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, queue, count, cap);
   count_launch(5);
 }
 

@@ -397,6 +397,11 @@ void sync_dev(Job& J) {
   d.queue_count = J.queue_count.p;
   d.queue_cap = (int)J.queue.n;
   d.work = nullptr;
+  d.det = (J.det && J.rec_key.p) ? 1 : 0;
+  d.rec_item_cap = item_record_cap(J.mode, J.tile_w * J.tile_h * J.S);
+  d.rec_key = J.rec_key.p;
+  d.rec_val = J.rec_val.p;
+  d.rec_count = J.rec_count.p;
 }
 
 // ---------------------------------------------------------------------------

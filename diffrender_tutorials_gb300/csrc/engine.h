@@ -156,6 +156,11 @@ struct Job {
   DevBuf<float> grad;
   DevBuf<uint32_t> err;
   OptState opt;
+  // deterministic reduction (records, dense pairs, radix-sort scratch)
+  int det = 0;
+  DevBuf<uint32_t> rec_key, det_key[2], det_part, det_hist;
+  DevBuf<float4> rec_val;
+  DevBuf<int> rec_count, det_idx[2], det_n;
   // work items
   std::vector<int4> h_pixel_items;
   int n_tiles_x = 0, n_tiles_y = 0;
@@ -185,7 +190,7 @@ CamDev make_cam(const drgb_camera& c);
 // Pixel kernel flags
 enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8 };
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
-                   cudaStream_t s, int mode);
+                   cudaStream_t s, int mode, bool det = false);
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
 void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s);
 void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, int64_t n, uint32_t* prim,
@@ -193,6 +198,11 @@ void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, in
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s);
 void launch_opt_step(Job& J, cudaStream_t s);
 void launch_opt_record(Job& J, cudaStream_t s);
+
+// deterministic gradient reduction (detsum.cu)
+void det_buffers(Job& J, cudaStream_t s);
+void launch_det_clear(const Job& J, cudaStream_t s);
+void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s);
 
 // edge random table shared by every job with the same sample count
 const float* edge_random_table(int n, cudaStream_t s);

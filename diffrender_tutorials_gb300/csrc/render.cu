@@ -31,17 +31,23 @@ constexpr bool kPixelWarp = false;
 #endif
 
 // Warp-aggregated scatter of per-vertex colour gradients.  All 32 lanes
-// must call it; lanes without a contribution pass tri = -1.
+// must call it; lanes without a contribution pass tri = -1.  The peers of a
+// triangle are summed by its lowest lane in lane order; that lane then adds
+// the 9 sums with atomics, or, in deterministic mode, writes 3 records at
+// rec_base + rec_n (rec_n: records of this work item so far, warp-uniform).
+template <bool DET>
 __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
-                                                      const float c[9], float* wscr) {
+                                                      const float c[9], float* wscr, int64_t rec_base, int& rec_n) {
   const int lane = threadIdx.x & 31;
   const unsigned peers = __match_any_sync(0xffffffffu, tri);
   const int leader = __ffs(peers) - 1;
 #pragma unroll
   for (int i = 0; i < 9; i++) wscr[i * 32 + lane] = c[i];
   __syncwarp();
+  float s[9];
+  float* g = nullptr;
+  int a = 0, bb = 0, cc = 0;
   if (tri >= 0 && lane == leader) {
-    float s[9];
 #pragma unroll
     for (int i = 0; i < 9; i++) s[i] = 0.0f;
     unsigned m = peers;
@@ -55,39 +61,85 @@ __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, 
     const BlockDev bd = J.blocks[b];
     const MeshDev& md = J.meshes[bd.mesh];
     if (md.dslot >= 0) {
-      float* g = J.grad + md.g_base + md.color_off;
-      const int a = gA - bd.vert_off, bb = gB - bd.vert_off, cc = gC - bd.vert_off;
-      atomicAdd(g + 3 * a + 0, s[0]); atomicAdd(g + 3 * a + 1, s[1]); atomicAdd(g + 3 * a + 2, s[2]);
-      atomicAdd(g + 3 * bb + 0, s[3]); atomicAdd(g + 3 * bb + 1, s[4]); atomicAdd(g + 3 * bb + 2, s[5]);
-      atomicAdd(g + 3 * cc + 0, s[6]); atomicAdd(g + 3 * cc + 1, s[7]); atomicAdd(g + 3 * cc + 2, s[8]);
+      g = J.grad + md.g_base + md.color_off;
+      a = gA - bd.vert_off; bb = gB - bd.vert_off; cc = gC - bd.vert_off;
     }
+  }
+  if (DET && J.det) {
+    const unsigned writers = __ballot_sync(0xffffffffu, g != nullptr);
+    if (g) {
+      const int64_t slot = rec_base + rec_n + 3 * __popc(writers & ((1u << lane) - 1u));
+      const uint32_t k0 = (uint32_t)(g - J.grad);
+      J.rec_key[slot + 0] = k0 + 3 * a;
+      J.rec_val[slot + 0] = make_float4(s[0], s[1], s[2], 0.0f);
+      J.rec_key[slot + 1] = k0 + 3 * bb;
+      J.rec_val[slot + 1] = make_float4(s[3], s[4], s[5], 0.0f);
+      J.rec_key[slot + 2] = k0 + 3 * cc;
+      J.rec_val[slot + 2] = make_float4(s[6], s[7], s[8], 0.0f);
+    }
+    rec_n += 3 * __popc(writers);
+  } else if (g) {
+    atomicAdd(g + 3 * a + 0, s[0]); atomicAdd(g + 3 * a + 1, s[1]); atomicAdd(g + 3 * a + 2, s[2]);
+    atomicAdd(g + 3 * bb + 0, s[3]); atomicAdd(g + 3 * bb + 1, s[4]); atomicAdd(g + 3 * bb + 2, s[5]);
+    atomicAdd(g + 3 * cc + 0, s[6]); atomicAdd(g + 3 * cc + 1, s[7]); atomicAdd(g + 3 * cc + 2, s[8]);
   }
   __syncwarp();
 }
 
-// sample_bilinear_clamp_3f_grad (shade_common.cpp:23-46), atomics.
-__device__ __forceinline__ void texture_grad(f3 val, float tx, float ty, int w, int h, float* data) {
+// sample_bilinear_clamp_3f_grad (shade_common.cpp:23-46): the four taps
+// and their weights; data points at the texture's gradient block.
+__device__ __forceinline__ void texture_taps(f3 val, float tx, float ty, int w, int h, int idx[4], f3 v[4]) {
   const float px = tx * (float)w, py = ty * (float)h;
   const int ix = (int)px, iy = (int)py;
   const int x0 = clampi(ix, 0, w - 1), y0 = clampi(iy, 0, h - 1);
   const int x1 = clampi(ix + 1, 0, w - 1), y1 = clampi(iy + 1, 0, h - 1);
   const float dx = px - (float)x0, dy = py - (float)y0;
-  float* d00 = data + 3 * (y0 * w + x0);
-  float* d01 = data + 3 * (y1 * w + x0);
-  float* d10 = data + 3 * (y0 * w + x1);
-  float* d11 = data + 3 * (y1 * w + x1);
+  idx[0] = 3 * (y0 * w + x0);
+  idx[1] = 3 * (y1 * w + x0);
+  idx[2] = 3 * (y0 * w + x1);
+  idx[3] = 3 * (y1 * w + x1);
   const float w00 = (1 - dx) * (1 - dy), w01 = (1 - dx) * dy, w10 = dx * (1 - dy), w11 = dx * dy;
-  atomicAdd(d00 + 0, w00 * val.x); atomicAdd(d00 + 1, w00 * val.y); atomicAdd(d00 + 2, w00 * val.z);
-  atomicAdd(d01 + 0, w01 * val.x); atomicAdd(d01 + 1, w01 * val.y); atomicAdd(d01 + 2, w01 * val.z);
-  atomicAdd(d10 + 0, w10 * val.x); atomicAdd(d10 + 1, w10 * val.y); atomicAdd(d10 + 2, w10 * val.z);
-  atomicAdd(d11 + 0, w11 * val.x); atomicAdd(d11 + 1, w11 * val.y); atomicAdd(d11 + 2, w11 * val.z);
+  v[0] = val * w00;
+  v[1] = val * w01;
+  v[2] = val * w10;
+  v[3] = val * w11;
+}
+
+// All 32 lanes call it; lanes with g == nullptr contribute nothing.
+template <bool DET>
+__device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, float tx, float ty, int w, int h,
+                                             int64_t rec_base, int& rec_n) {
+  const int lane = threadIdx.x & 31;
+  int idx[4];
+  f3 v[4];
+  if (g) texture_taps(val, tx, ty, w, h, idx, v);
+  if (DET && J.det) {
+    const unsigned writers = __ballot_sync(0xffffffffu, g != nullptr);
+    if (g) {
+      const int64_t slot = rec_base + rec_n + 4 * __popc(writers & ((1u << lane) - 1u));
+      const uint32_t k0 = (uint32_t)(g - J.grad);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        J.rec_key[slot + k] = k0 + idx[k];
+        J.rec_val[slot + k] = make_float4(v[k].x, v[k].y, v[k].z, 0.0f);
+      }
+    }
+    rec_n += 4 * __popc(writers);
+  } else if (g) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      atomicAdd(g + idx[k] + 0, v[k].x);
+      atomicAdd(g + idx[k] + 1, v[k].y);
+      atomicAdd(g + idx[k] + 2, v[k].z);
+    }
+  }
 }
 
 // shade_grad<M> for one sample; every lane of the warp must call it.  MODE
 // as for shade().
-template <int MODE>
+template <int MODE, bool DET>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
-                                           uint32_t key, float* wscr) {
+                                           uint32_t key, float* wscr, int64_t rec_base, int& rec_n) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   const bool hit = cast_p<kPixelWarp>(J, cam, x, y, active, s);
@@ -124,14 +176,22 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
       tri = s.h.tri;
       gA = s.A; gB = s.B; gC = s.C;
     }
-    scatter_vertex_colors(J, tri, gA, gB, gC, c, wscr);
-  } else if (model_has_tex(mode) && hit) {
-    const BlockDev bd = J.blocks[s.block];
-    const MeshDev& md = J.meshes[bd.mesh];
-    if (md.dslot >= 0 && md.tex_off >= 0) {
-      const float2 tc = interp_tc(J, s);
-      texture_grad(val, tc.x, tc.y, md.tex_w, md.tex_h, J.grad + md.g_base + md.tex_off);
+    scatter_vertex_colors<DET>(J, tri, gA, gB, gC, c, wscr, rec_base, rec_n);
+  } else if (model_has_tex(mode)) {
+    float* g = nullptr;
+    float2 tc = make_float2(0.0f, 0.0f);
+    int tw = 0, th = 0;
+    if (hit) {
+      const BlockDev bd = J.blocks[s.block];
+      const MeshDev& md = J.meshes[bd.mesh];
+      if (md.dslot >= 0 && md.tex_off >= 0) {
+        tc = interp_tc(J, s);
+        g = J.grad + md.g_base + md.tex_off;
+        tw = md.tex_w;
+        th = md.tex_h;
+      }
     }
+    texture_grad<DET>(J, g, val, tc.x, tc.y, tw, th, rec_base, rec_n);
   }
 }
 
@@ -142,7 +202,9 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
 constexpr int PX_WARPS = PX_THREADS / 32;
 constexpr int PX_MAX_SAMPLES = 64;
 
-template <int MODE>
+// DET: the deterministic-mode variant (gradient records instead of atomics
+// for jobs that have record buffers).
+template <int MODE, bool DET>
 __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
                                                        int n_items, int* counter, const int flags) {
   __shared__ JobDev sJ_all[PX_WARPS];
@@ -260,6 +322,8 @@ __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict_
         }
       }
       __syncwarp();
+      const int64_t rec_base = (int64_t)(it - J.item_base) * J.rec_item_cap;
+      int rec_n = 0;
       for (int base = 0; base < NS; base += 32) {
         const int s = base + lane;
         const int p = s / S, k = s - p * S;
@@ -277,8 +341,9 @@ __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict_
           const int64_t pix = (int64_t)py * W + px;
           key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
         }
-        shade_grad<MODE>(J, C, act, sx, sy, val, key, wscr);
+        shade_grad<MODE, DET>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n);
       }
+      if (DET && J.det && lane == 0) J.rec_count[it - J.item_base] = rec_n;
     }
     __syncwarp();
   }
@@ -355,24 +420,33 @@ void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, in
 }
 
 // `mode` selects the kernel compiled for one shading model; 0 (a launch whose
-// jobs mix models) runs the generic kernel that switches per job.
+// jobs mix models) runs the generic kernel that switches per job.  `det`
+// selects the deterministic-mode variants.
+template <bool DET>
+static void launch_pixels_t(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags,
+                            int grid, cudaStream_t s, int mode) {
+  switch (mode) {
+    case SILHOUETTE: k_pixels<SILHOUETTE, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case VERTEX_COLOR: k_pixels<VERTEX_COLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT: k_pixels<LAMBERT, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT_POINT_VCOLOR:
+      k_pixels<LAMBERT_POINT_VCOLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
+      break;
+    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    default: k_pixels<0, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+  }
+}
+
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
-                   cudaStream_t s, int mode) {
+                   cudaStream_t s, int mode, bool det) {
   if (n_items <= 0) return;
   if ((flags & PX_LOSS) && !(flags & PX_FWD)) throw CudaError("loss needs the forward pass", DRGB_ERR_INVALID);
   DRGB_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int), s));
   if (grid <= 0 || grid > n_items) grid = n_items;
-  switch (mode) {
-    case SILHOUETTE: k_pixels<SILHOUETTE><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case VERTEX_COLOR: k_pixels<VERTEX_COLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case LAMBERT: k_pixels<LAMBERT><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case LAMBERT_POINT_VCOLOR:
-      k_pixels<LAMBERT_POINT_VCOLOR><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
-      break;
-    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    default: k_pixels<0><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-  }
+  // records are only written by the adjoint pass
+  if (det && (flags & PX_ADJ)) launch_pixels_t<true>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+  else launch_pixels_t<false>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
   count_launch();
 }
 

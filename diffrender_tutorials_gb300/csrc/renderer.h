@@ -116,6 +116,16 @@ struct drgb_renderer {
     J.queue.reserve(std::max<size_t>(1, (size_t)J.n_views * std::max(edge_samples, 1)));
     J.dev.edge_samples = edge_samples;
     J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
+    if (J.det) det_buffers(J, stream);
+  }
+
+  // Deterministic mode: clear the record counts before a gradient pass and
+  // reduce the records into the gradient after it.
+  void det_begin() {
+    if (job.det && job.rec_key.p) launch_det_clear(job, stream);
+  }
+  void det_end() {
+    if (job.det && job.rec_key.p) launch_det_reduce(job, sm_count, stream);
   }
 
   void push_dev() {
@@ -149,10 +159,13 @@ struct drgb_renderer {
     Job& J = job;
     const bool interior = J.mode != SILHOUETTE;
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
+    det_begin();
     int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
-    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream, J.mode);
+    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream, J.mode,
+                  J.det);
     launch_loss_finalize(d_job.p, 1, stream);
     if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
+    det_end();
   }
 };
 

@@ -13,6 +13,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libdrgb.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "drgb.h")
 
 DRGB_OK = 0
+# renderer / batch options (drgb_renderer_set_option, drgb_batch_set_option)
+OPT_TRACE_BRUTEFORCE, OPT_TILE_W, OPT_TILE_H, OPT_USE_GRAPH, OPT_DETERMINISTIC = 1, 2, 3, 4, 5
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
           -5: "kernel error flag", -6: "unsupported", -7: "no CUDA device"}
 
@@ -48,6 +50,24 @@ class OptParams(C.Structure):
                 ("base_lr", C.c_float), ("position_lr", C.c_float), ("textures_lr", C.c_float),
                 ("transforms_lr", C.c_float), ("flags", C.c_int32), ("n_dmesh_ids", C.c_int32),
                 ("dmesh_ids", C.c_int32 * 16)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_jobs", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+                ("start_worker", C.c_int32), ("deterministic", C.c_int32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("steps", C.c_int64), ("steps_done", C.c_int64),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("device_bytes", C.c_int64), ("final_loss", C.c_float)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int32), ("running", C.c_int32), ("done", C.c_int32), ("failed", C.c_int32),
+                ("bytes_in_use", C.c_int64), ("bytes_budget", C.c_int64), ("bytes_peak", C.c_int64),
+                ("batch_steps", C.c_int64), ("job_iterations", C.c_int64), ("busy_seconds", C.c_double),
+                ("now", C.c_double)]
 
 
 VP = C.c_void_p
@@ -92,6 +112,20 @@ _SIGS = {
     "drgb_batch_job_losses": (C.c_int, [VP, C.c_int32, C.c_int64, C.c_int64, VP, C.POINTER(C.c_int64)]),
     "drgb_batch_get_mesh": (C.c_int, [VP, C.c_int32, C.c_int, VP, VP, VP, VP]),
     "drgb_batch_job_device_bytes": (C.c_int64, [VP, C.c_int32]),
+    "drgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(VP)]),
+    "drgb_server_destroy": (C.c_int, [VP]),
+    "drgb_server_submit": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(ModelParams), C.POINTER(SceneDesc),
+                                     C.POINTER(Camera), VP, C.c_int, C.POINTER(OptParams), C.c_int64,
+                                     C.POINTER(C.c_int32)]),
+    "drgb_server_step": (C.c_int, [VP, C.POINTER(C.c_int32)]),
+    "drgb_server_wait": (C.c_int, [VP, C.c_int32, C.c_double]),
+    "drgb_server_job_info": (C.c_int, [VP, C.c_int32, C.POINTER(JobInfo)]),
+    "drgb_server_job_losses": (C.c_int, [VP, C.c_int32, C.c_int64, C.c_int64, VP]),
+    "drgb_server_get_mesh": (C.c_int, [VP, C.c_int32, C.c_int, VP, VP, VP, VP]),
+    "drgb_server_release": (C.c_int, [VP, C.c_int32]),
+    "drgb_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
+    "drgb_server_step_times": (C.c_int, [VP, C.c_int64, C.c_int64, VP, VP]),
+    "drgb_estimate_job_bytes": (C.c_int64, [C.c_int, C.POINTER(SceneDesc), C.POINTER(Camera), C.c_int]),
     "drgb_optimizer_profile": (C.c_int, [VP, C.c_int, VP]),
     "drgb_count_work": (C.c_int, [VP, VP]),
 }

@@ -57,7 +57,10 @@ enum {
   DRGB_OPT_TRACE_BRUTEFORCE = 1, /* 1: test every triangle in the reference's loop order instead of the LBVH */
   DRGB_OPT_TILE_W = 2,           /* pixel tile width of the fused forward/adjoint kernel */
   DRGB_OPT_TILE_H = 3,
-  DRGB_OPT_USE_GRAPH = 4         /* 1 (default): optimiser iterations replay a CUDA graph */
+  DRGB_OPT_USE_GRAPH = 4,        /* 1 (default): optimiser iterations replay a CUDA graph */
+  DRGB_OPT_DETERMINISTIC = 5     /* 1: gradients are summed in a fixed order (records sorted by gradient
+                                    index, then segmented sums) instead of by float atomics, so a job's
+                                    gradient is bit-identical run to run, alone or in a batch; default 0 */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -225,7 +228,8 @@ int drgb_batch_add_job(drgb_batch* b, int shading_model, int spp, const drgb_mod
                        const drgb_opt_params* p, int32_t* job_id);
 int drgb_batch_remove_job(drgb_batch* b, int32_t job_id);
 int drgb_batch_size(drgb_batch* b);
-int drgb_batch_set_option(drgb_batch* b, int option, int64_t value); /* DRGB_OPT_USE_GRAPH */
+/* DRGB_OPT_USE_GRAPH, or DRGB_OPT_DETERMINISTIC for every job, present and future */
+int drgb_batch_set_option(drgb_batch* b, int option, int64_t value);
 /* n_iters iterations of every job: enqueue only / enqueue and wait. */
 int drgb_batch_run_async(drgb_batch* b, int64_t n_iters);
 int drgb_batch_run(drgb_batch* b, int64_t n_iters);
@@ -236,6 +240,73 @@ int drgb_batch_get_mesh(drgb_batch* b, int32_t job_id, int mesh_id, float* verti
                         float* transforms);
 /* Device memory held by a job (for admission against a memory budget). */
 int64_t drgb_batch_job_device_bytes(drgb_batch* b, int32_t job_id);
+
+/* ---- serving (no reference counterpart; each job is one IOptimizer::Init +
+ * Run(n_steps), src/optimizer.h:52-61).  Jobs are submitted at any time and
+ * queue in arrival order; a job is admitted when a slot is free and its
+ * device memory fits the budget; every admitted job advances one iteration
+ * per batched step (continuous batching: jobs join and leave between steps,
+ * and new jobs are set up on their own streams while a step runs).  A
+ * finished job's final meshes and loss history are copied to host memory and
+ * its device memory is freed.  With start_worker = 1 a worker thread steps
+ * the batch whenever jobs are queued or resident; otherwise the caller calls
+ * drgb_server_step. ------------------------------------------------------- */
+typedef struct drgb_server drgb_server;
+
+typedef struct drgb_server_config {
+  int32_t device;
+  int32_t max_jobs;         /* resident jobs at most; <= 0: no limit */
+  int64_t hbm_budget_bytes; /* device memory of resident jobs at most */
+  int32_t start_worker;     /* 1: step from a worker thread */
+  int32_t deterministic;    /* 1: jobs use DRGB_OPT_DETERMINISTIC */
+} drgb_server_config;
+
+enum { DRGB_JOB_QUEUED = 0, DRGB_JOB_RUNNING = 1, DRGB_JOB_DONE = 2, DRGB_JOB_FAILED = 3 };
+
+typedef struct drgb_job_info {
+  int32_t state;        /* DRGB_JOB_* */
+  int32_t error;        /* error code of a failed job */
+  int64_t steps, steps_done;
+  double t_submit, t_admit, t_done; /* seconds on the server's clock; -1 until reached */
+  int64_t device_bytes; /* measured once admitted, estimated before */
+  float final_loss;
+} drgb_job_info;
+
+typedef struct drgb_server_stats {
+  int32_t queued, running, done, failed;
+  int64_t bytes_in_use, bytes_budget, bytes_peak;
+  int64_t batch_steps;    /* batched iterations run */
+  int64_t job_iterations; /* iterations summed over jobs */
+  double busy_seconds;    /* device time of the batched iterations (CUDA events) */
+  double now;             /* the server's clock */
+} drgb_server_stats;
+
+int drgb_server_create(const drgb_server_config* cfg, drgb_server** out);
+/* Stops the worker and frees every job. */
+int drgb_server_destroy(drgb_server* s);
+/* Queues a job; inputs are copied, so the caller may free them on return.
+ * DRGB_ERR_OOM when the job alone exceeds the budget. */
+int drgb_server_submit(drgb_server* s, int shading_model, int spp, const drgb_model_params* model_params,
+                       const drgb_scene_desc* scene, const drgb_camera* cams, const float* targets, int n_views,
+                       const drgb_opt_params* p, int64_t n_steps, int32_t* ticket);
+/* Without a worker: admit, run one batched iteration, retire finished jobs.
+ * *n_running (may be NULL) = jobs resident after the step. */
+int drgb_server_step(drgb_server* s, int32_t* n_running);
+/* Blocks until the job (ticket > 0) or every submitted job (ticket = 0) is
+ * done or failed; DRGB_ERR_STATE after timeout_s seconds (< 0: no limit). */
+int drgb_server_wait(drgb_server* s, int32_t ticket, double timeout_s);
+int drgb_server_job_info(drgb_server* s, int32_t ticket, drgb_job_info* out);
+int drgb_server_job_losses(drgb_server* s, int32_t ticket, int64_t first, int64_t n, float* out);
+int drgb_server_get_mesh(drgb_server* s, int32_t ticket, int mesh_id, float* vertices, float* colors,
+                         float* texture, float* transforms);
+/* Forgets a finished job's results. */
+int drgb_server_release(drgb_server* s, int32_t ticket);
+int drgb_server_get_stats(drgb_server* s, drgb_server_stats* out);
+/* Device time (ms) and resident job count of batched steps [first, first+n). */
+int drgb_server_step_times(drgb_server* s, int64_t first, int64_t n, float* ms, int32_t* jobs);
+/* Device bytes a job of this shape needs (an upper estimate used for admission). */
+int64_t drgb_estimate_job_bytes(int shading_model, const drgb_scene_desc* scene, const drgb_camera* cams,
+                                int n_views);
 
 /* ---- measurement (no reference counterpart: the reference prints wall-clock
  * ms/iter only, src/main.cpp:218-224, src/tests.cpp:136-203) -------------- */

@@ -1,0 +1,147 @@
+"""Deterministic gradient reduction (DRGB_OPT_DETERMINISTIC): records sorted
+by gradient index and summed in a fixed order instead of float atomics.
+
+The gradient must be bit-identical call to call, equal to the atomic path up
+to summation order, within the reference tolerances of the oracle, and the
+same bits for a job alone, in a batch and in the server."""
+import numpy as np
+import pytest
+
+import diffrender_tutorials_gb300 as D
+from diffrender_tutorials_gb300 import native as N
+from diffrender_tutorials_gb300.scene import Texture, TriangleMesh
+from fixtures import rel_l2
+from test_gpu_parity import O, assert_grad_close, ico_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def textured(seed=3):
+    m = D.make_icosphere(2, seed=seed)
+    P = m.vertices.astype(np.float64)
+    u = 0.5 + np.arctan2(P[:, 0], P[:, 2]) / (2 * np.pi)
+    v = np.arccos(np.clip(P[:, 1], -1, 1)) / np.pi
+    tex = np.random.default_rng(seed).uniform(0.1, 0.9, size=(16, 16, 3)).astype(np.float32)
+    return TriangleMesh(m.vertices, m.indices, tc=np.stack([u, v], 1).astype(np.float32), normals=m.normals,
+                        textures=[Texture(16, 16, 3, tex.reshape(-1))])
+
+
+def problems():
+    out = []
+    ts, isc, cams = ico_problem(64, 3)
+    out.append(("pointlight", 16, 4, ts, isc, cams))
+    true = D.make_cube(seed=1)
+    init = D.perturb_vertices(true, 0.1, seed=2)
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(true)
+    isc.add_mesh(init)
+    out.append(("vcolor", 2, 16, ts, isc, [D.CamInfo(origin=(0, 0, 3), width=96, height=96)]))
+    true = textured()
+    init = true.copy()
+    init.textures[0].data[:] = 0.5
+    init.vertices = D.perturb_vertices(true, 0.01, seed=9, radial=True).vertices
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(true)
+    isc.add_mesh(init)
+    out.append(("texture", 3, 4, ts, isc, [D.CamInfo(origin=(0.5, 0.8, 2.6), width=56, height=56)]))
+    return out
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_deterministic_gradient_bits(idx):
+    name, mode, spp, ts, isc, cams = problems()[idx]
+    W = cams[0].width
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL(mode), spp))
+    r.commit(ts)
+    tgt = r.render(ts, cams).reshape(-1)
+    r.commit(isc)
+    ref = D.DScene(r, [0])
+    l_atomic = r.d_render_and_compare(isc, cams, tgt, W * W, ref)
+    r.set_option(N.OPT_DETERMINISTIC, 1)
+    runs = []
+    for _ in range(3):
+        ds = D.DScene(r, [0])
+        loss = r.d_render_and_compare(isc, cams, tgt, W * W, ds)
+        runs.append((loss, ds.data.copy()))
+    for loss, g in runs[1:]:
+        assert loss == runs[0][0]
+        assert np.array_equal(g, runs[0][1])           # bit-identical call to call
+    assert runs[0][0] == l_atomic
+    assert np.abs(runs[0][1]).max() > 0
+    assert rel_l2(runs[0][1], ref.data) < 1e-5         # the atomic path, up to summation order
+    # and the oracle, within the reference tolerances
+    oloss, ods, _ = O.d_render_and_compare(isc, cams, mode, spp, tgt, W * W)
+    assert_grad_close(runs[0][1], ods, ds.layout)
+    # d_render accumulates: two calls give exactly twice one call
+    adj = 2.0 * (r.render(isc, cams).reshape(-1) - tgt)
+    one = D.DScene(r, [0])
+    r.d_render(isc, cams, adj, W * W, one)
+    two = D.DScene(r, [0])
+    r.d_render(isc, cams, adj, W * W, two)
+    r.d_render(isc, cams, adj, W * W, two)
+    assert np.array_equal(two.data, 2.0 * one.data)
+
+
+def opt_params(mode):
+    lr = 0.01 if mode == 2 else 0.005
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=lr, tex_lr=0.05)
+    p.base_lr = lr
+    return p
+
+
+def test_deterministic_plain_batch_and_server_agree_bit_for_bit():
+    iters = 6
+    setups, plain = [], []
+    for name, mode, spp, ts, isc, cams in problems():
+        st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+        r = D.MakeDifferentialRenderer(st)
+        r.commit(ts)
+        tgt = r.render(ts, cams)
+        r.set_option(N.OPT_DETERMINISTIC, 1)
+        opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, r, cams, tgt, opt_params(mode))
+        opt.Run(iters)
+        plain.append((np.array(opt.losses), opt.current_scene()))
+        setups.append((isc, cams, tgt, st, opt_params(mode)))
+    # batch: all three jobs in one fused launch sequence
+    b = D.BatchOptimizer()
+    b.set_option(N.OPT_DETERMINISTIC, 1)
+    ids = [b.add_job(*s) for s in setups]
+    b.run(iters)
+    # server: the jobs arrive together with two others and leave at different steps
+    srv = D.OptimizationServer(deterministic=True)
+    extra = [setups[1][:4] + (opt_params(2),), setups[0][:4] + (opt_params(16),)]
+    t_extra = [srv.submit(*extra[0], 3), srv.submit(*extra[1], 9)]
+    tickets = [srv.submit(*s, iters) for s in setups]
+    srv.wait(0, timeout=300)
+    assert srv.step_times()[1].max() == 5
+    for (losses, scene), jid, t in zip(plain, ids, tickets):
+        bs, ss = b.job_scene(jid), srv.result_scene(t)
+        assert np.array_equal(b.losses(jid), losses)
+        assert np.array_equal(srv.losses(t), losses)
+        for got in (bs, ss):
+            assert np.array_equal(got.meshes[0].vertices, scene.meshes[0].vertices)
+            if scene.meshes[0].colors is not None:
+                assert np.array_equal(got.meshes[0].colors, scene.meshes[0].colors)
+            if scene.meshes[0].textures:
+                assert np.array_equal(got.meshes[0].textures[0].data, scene.meshes[0].textures[0].data)
+    for t in t_extra:
+        assert srv.info(t)["state"] == "done"
+    srv.close()
+
+
+def test_noalloc_entry_refuses_deterministic_mode():
+    import torch
+    name, mode, spp, ts, isc, cams = problems()[1]
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL(mode), spp))
+    r.commit(isc)
+    r.set_option(N.OPT_DETERMINISTIC, 1)
+    W = cams[0].width
+    tg = torch.zeros(3 * W * W, device="cuda")
+    ds = D.DScene(r, [0])
+    g = torch.zeros(ds.data.size, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    ids = np.zeros(1, np.int32)
+    rc = N.load().drgb_d_render_and_compare_noalloc(r._h, D.api.make_cameras(cams), tg.data_ptr(), 1, W * W,
+                                                    ids.ctypes.data, 1, g.data_ptr(), loss.data_ptr())
+    assert rc == -6 and "deterministic" in N.last_error()
