@@ -252,6 +252,27 @@ def drgb_arm(args, w, ws, rank, local, pg):
     h2d = tg_pinned.nbytes + 168 * len(cams)
     d2h = ds.data.nbytes + 4
 
+    # the same iteration with the deterministic gradient reduction
+    from diffrender_tutorials_gb300 import native as N
+    r.set_option(N.OPT_DETERMINISTIC, 1)
+    for _ in range(args.warmup):
+        opt.run_async(1)
+    torch.cuda.synchronize()
+    det_ms = []
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            opt.run_async(1)
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    det_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    det_prof = opt.profile(2)
+    r.set_option(N.OPT_DETERMINISTIC, 0)
+    deterministic = {"value": args.steps / (sum(det_ms) / 1e3), "unit": "iters/s",
+                     "ms_per_step": sum(det_ms) / args.steps, "phases_ms": det_prof,
+                     "how": "DRGB_OPT_DETERMINISTIC: gradient records sorted by index, fixed-order sums"}
+
     # roofline of the dominant kernel (fused forward/adjoint pixel kernel)
     prof = opt.profile(3)
     work = opt.count_work()
@@ -295,6 +316,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
         "gpu_launches": int(launches),
         "phases_ms": prof,
+        "deterministic": deterministic,
         "work_per_iter": work,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                      "traffic": traffic, "kernel": "k_pixels (forward+loss+interior adjoint)",

@@ -141,23 +141,145 @@ __global__ void __launch_bounds__(DS_THREADS) k_ds_scatter(const uint32_t* kin, 
   }
 }
 
-__global__ void __launch_bounds__(DS_THREADS) k_ds_segments(const uint32_t* key, const int* idx, const int* n_ptr,
-                                                            const float4* val, float* grad) {
-  const int n = *n_ptr;
-  const int stride = gridDim.x * blockDim.x;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const uint32_t k = key[i];
-    if (i > 0 && key[i - 1] == k) continue;
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (int j = i; j < n && key[j] == k; j++) {
-      const float4 v = val[idx[j]];
-      sx += v.x;
-      sy += v.y;
-      sz += v.z;
+// ---- segmented sums in a fixed shape ---------------------------------------
+// The sorted records are cut into chunks of DS_SEG_CHUNK; a warp owns a
+// chunk and each lane a contiguous run of DS_SEG_LANE records.  A lane sums
+// its records sequentially: a run of one key that starts and ends inside the
+// lane's range is a whole segment (the keys are sorted) and goes straight to
+// the gradient; the lane's first and last runs are fragments.  Lane 0 merges
+// the 32 lanes' fragments in lane order the same way, leaving the chunk's
+// first and last runs as fragments in two slots per chunk; one warp finally
+// merges those in chunk order.  The association order of every sum depends
+// only on the record count and the sorted keys.
+constexpr int DS_SEG_LANE = 64;
+constexpr int DS_SEG_CHUNK = 32 * DS_SEG_LANE;
+
+__device__ __forceinline__ void frag_add(float* grad, uint32_t k, float x, float y, float z) {
+  grad[k + 0] += x;
+  grad[k + 1] += y;
+  grad[k + 2] += z;
+}
+
+// Sequential pass over items [b, e) of a sorted sequence given by get(i) ->
+// (key, value); keys equal to kNoKey are skipped.  Runs strictly inside the
+// range are written to grad; the first and last runs are returned (first ==
+// last when the range holds a single run: then last.key = kNoKey).
+template <class Get>
+__device__ __forceinline__ void seq_runs(Get get, int b, int e, float* grad, DetFrag& first, DetFrag& last) {
+  first.key = last.key = kNoKey;
+  uint32_t ck = kNoKey;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  bool have_first = false;
+  for (int i = b; i < e; i++) {
+    uint32_t k;
+    float4 v;
+    get(i, k, v);
+    if (k == kNoKey) continue;
+    if (k != ck) {
+      if (ck != kNoKey) {
+        if (!have_first) {
+          first = DetFrag{ck, sx, sy, sz};
+          have_first = true;
+        } else {
+          frag_add(grad, ck, sx, sy, sz);
+        }
+      }
+      ck = k;
+      sx = sy = sz = 0.0f;
     }
-    grad[k + 0] += sx;
-    grad[k + 1] += sy;
-    grad[k + 2] += sz;
+    sx += v.x;
+    sy += v.y;
+    sz += v.z;
+  }
+  if (ck != kNoKey) {
+    if (!have_first) first = DetFrag{ck, sx, sy, sz};
+    else last = DetFrag{ck, sx, sy, sz};
+  }
+}
+
+// Lane 0 merges the lanes' (first, last) fragments in lane order.  With
+// `whole` the sequence has no neighbours (its first and last runs are whole
+// segments); otherwise they are returned as the chunk's fragments.
+__device__ __forceinline__ void merge_lane_frags(const DetFrag* f, float* grad, bool whole, DetFrag& cf, DetFrag& cl) {
+  cf.key = cl.key = kNoKey;
+  uint32_t ck = kNoKey;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  bool have_first = false;
+  for (int j = 0; j < 64; j++) {
+    const DetFrag g = f[j];
+    if (g.key == kNoKey) continue;
+    if (g.key != ck) {
+      if (ck != kNoKey) {
+        if (!have_first && !whole) {
+          cf = DetFrag{ck, sx, sy, sz};
+          have_first = true;
+        } else {
+          frag_add(grad, ck, sx, sy, sz);
+          have_first = true;
+        }
+      }
+      ck = g.key;
+      sx = sy = sz = 0.0f;
+    }
+    sx += g.x;
+    sy += g.y;
+    sz += g.z;
+  }
+  if (ck != kNoKey) {
+    if (whole) frag_add(grad, ck, sx, sy, sz);
+    else if (!have_first) cf = DetFrag{ck, sx, sy, sz};
+    else cl = DetFrag{ck, sx, sy, sz};
+  }
+}
+
+__global__ void __launch_bounds__(DS_THREADS) k_ds_seg_chunks(const uint32_t* key, const int* idx, const int* n_ptr,
+                                                              const float4* val, float* grad, DetFrag* chunk_frags) {
+  __shared__ DetFrag sf[DS_THREADS / 32][64];
+  const int n = *n_ptr;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n_chunks = (n + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK;
+  const int warps = gridDim.x * (DS_THREADS / 32);
+  for (int c = blockIdx.x * (DS_THREADS / 32) + w; c < n_chunks; c += warps) {
+    const int b = min(n, c * DS_SEG_CHUNK + lane * DS_SEG_LANE), e = min(n, b + DS_SEG_LANE);
+    DetFrag f0, f1;
+    seq_runs([&](int i, uint32_t& k, float4& v) {
+      k = key[i];
+      v = val[idx[i]];
+    }, b, e, grad, f0, f1);
+    sf[w][2 * lane] = f0;
+    sf[w][2 * lane + 1] = f1;
+    __syncwarp();
+    if (lane == 0) {
+      DetFrag cf, cl;
+      merge_lane_frags(sf[w], grad, false, cf, cl);
+      chunk_frags[2 * c] = cf;
+      chunk_frags[2 * c + 1] = cl;
+    }
+    __syncwarp();
+  }
+}
+
+// One warp: the chunks' fragments in chunk order, lanes over contiguous
+// ranges of slots, then lane 0.
+__global__ void __launch_bounds__(32) k_ds_seg_final(const int* n_ptr, const DetFrag* chunk_frags, float* grad) {
+  __shared__ DetFrag sf[64];
+  const int n = *n_ptr;
+  const int lane = threadIdx.x;
+  const int slots = 2 * ((n + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK);
+  const int per = (slots + 31) / 32;
+  const int b = min(slots, lane * per), e = min(slots, b + per);
+  DetFrag f0, f1;
+  seq_runs([&](int i, uint32_t& k, float4& v) {
+    const DetFrag g = chunk_frags[i];
+    k = g.key;
+    v = make_float4(g.x, g.y, g.z, 0.0f);
+  }, b, e, grad, f0, f1);
+  sf[2 * lane] = f0;
+  sf[2 * lane + 1] = f1;
+  __syncwarp();
+  if (lane == 0) {
+    DetFrag cf, cl;
+    merge_lane_frags(sf, grad, true, cf, cl);
   }
 }
 
@@ -182,6 +304,7 @@ void det_buffers(Job& J, cudaStream_t s) {
   }
   J.det_part.reserve(std::max<int64_t>(1, (regions + DS_CHUNK - 1) / DS_CHUNK));
   J.det_hist.reserve(256 * DS_GRID);
+  J.det_frag.reserve(2 * ((std::max<int64_t>(1, cap) + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK));
   J.det_n.reserve(1);
   J.dev.det = 1;
   J.dev.rec_key = J.rec_key.p;
@@ -214,9 +337,10 @@ void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
     count_launch(2);
     cur ^= 1;
   }
-  k_ds_segments<<<std::max(1, sm_count) * 8, DS_THREADS, 0, s>>>(J.det_key[cur].p, J.det_idx[cur].p, J.det_n.p, J.rec_val.p,
-                                               J.grad.p);
-  count_launch();
+  k_ds_seg_chunks<<<std::max(1, sm_count) * 8, DS_THREADS, 0, s>>>(J.det_key[cur].p, J.det_idx[cur].p, J.det_n.p,
+                                                                    J.rec_val.p, J.grad.p, J.det_frag.p);
+  k_ds_seg_final<<<1, 32, 0, s>>>(J.det_n.p, J.det_frag.p, J.grad.p);
+  count_launch(2);
 }
 
 }  // namespace drgb

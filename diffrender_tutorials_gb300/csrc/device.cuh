@@ -155,6 +155,13 @@ __host__ __device__ inline int item_record_cap(int mode, int NS) {
   return passes * 32 * (model_has_tex(mode) ? 4 : 3);
 }
 
+// Partial sum of one gradient index in the deterministic reduction.
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+struct DetFrag {
+  uint32_t key;  // kNoKey: empty
+  float x, y, z;
+};
+
 // Record slots of the edge region of sample i of a view.
 constexpr int kEdgeRecords = 6;  // two vertex positions, four rows of the instance matrix
 __device__ __forceinline__ int64_t edge_region(const JobDev& J, int view, int i) {

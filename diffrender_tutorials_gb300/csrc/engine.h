@@ -161,6 +161,7 @@ struct Job {
   DevBuf<uint32_t> rec_key, det_key[2], det_part, det_hist;
   DevBuf<float4> rec_val;
   DevBuf<int> rec_count, det_idx[2], det_n;
+  DevBuf<DetFrag> det_frag;
   // work items
   std::vector<int4> h_pixel_items;
   int n_tiles_x = 0, n_tiles_y = 0;
