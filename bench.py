@@ -584,7 +584,7 @@ def main():
     ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device memory budget")
-    ap.add_argument("--slots", type=int, default=0, help="serving: resident jobs at most (0: no limit)")
+    ap.add_argument("--slots", type=int, default=8, help="serving: resident jobs at most (0: no limit)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)

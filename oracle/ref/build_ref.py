@@ -14,10 +14,12 @@ Test infrastructure only.  Recipe:
      own CMakeLists.txt:79-85,91) together with oracle/ref/ref_driver.cpp.
 
 The reference's CMake build, Embree (missing binary) and Mitsuba (not
-installed) are not used.  Only runs where the reference tree exists; the
-output is x86-specific and is not needed on other machines.
+installed) are not used.  Where the reference tree is absent, the patched copy under oracle/_ref/src
+(made earlier and shipped with the working tree) is compiled instead, so that
+the driver can be rebuilt on a machine of another architecture.
 """
 import os
+import platform
 import re
 import shutil
 import subprocess
@@ -27,6 +29,8 @@ REF_ROOT = os.environ.get("DRGB_REFERENCE_ROOT", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
+# objects and binaries per machine architecture (the source copy is shared)
+BIN = os.path.join(OUT, platform.machine())
 
 COMPILE = [
     "src/drender.cpp", "src/functions.cpp", "src/shade_simple.cpp", "src/shade_lambert.cpp",
@@ -62,34 +66,92 @@ def _copy_tree():
     return src_root
 
 
-def build(verbose=False):
-    if not os.path.isdir(REF_ROOT):
-        if verbose:
-            print("reference tree absent; skipping oracle/_ref build")
-        return None
-    os.makedirs(OUT, exist_ok=True)
-    exe = os.path.join(OUT, "ref_driver")
-    stamp_src = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "kvio.h"), __file__]
-    if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(s) for s in stamp_src):
-        return exe
-    src_root = _copy_tree()
+def _source_tree(verbose=False):
+    """The patched copy of the reference sources: made from the reference
+    tree where it exists, else the copy made earlier (a machine without the
+    reference tree receives oracle/_ref/src with the repository)."""
+    src_root = os.path.join(OUT, "src")
+    if os.path.isdir(REF_ROOT):
+        stamp = os.path.join(src_root, ".copied")
+        if not os.path.exists(stamp) or os.path.getmtime(stamp) < os.path.getmtime(__file__):
+            _copy_tree()
+            open(stamp, "w").close()
+        return src_root
+    if os.path.isdir(os.path.join(src_root, "src")):
+        return src_root
+    if verbose:
+        print("reference sources absent; skipping oracle/_ref build")
+    return None
+
+
+def _includes(src_root):
     incs = []
     for d in HEADER_DIRS + ["stub"]:
         incs += ["-I", os.path.join(src_root, d)]
-    incs += ["-I", HERE]
-    objs = []
-    procs = []
+    return incs + ["-I", HERE]
+
+
+FLAGS = ["g++", "-std=c++17", "-O3", "-fopenmp", "-DUSE_OMP", "-ffp-contract=off", "-w"]
+
+
+def _objects(src_root):
+    """The reference's translation units, compiled in parallel when stale."""
+    incs = _includes(src_root)
+    objs, procs = [], []
     for rel in COMPILE:
-        obj = os.path.join(OUT, rel.replace("/", "_") + ".o")
-        cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-DUSE_OMP", "-ffp-contract=off", "-w"] + incs + ["-c", os.path.join(src_root, rel), "-o", obj]
-        procs.append((subprocess.Popen(cmd), cmd))
+        src = os.path.join(src_root, rel)
+        obj = os.path.join(BIN, rel.replace("/", "_") + ".o")
         objs.append(obj)
+        if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src):
+            continue
+        cmd = FLAGS + incs + ["-c", src, "-o", obj]
+        procs.append((subprocess.Popen(cmd), cmd))
     for p, cmd in procs:
         if p.wait() != 0:
             raise RuntimeError("reference compile failed: " + " ".join(cmd))
-    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-DUSE_OMP", "-ffp-contract=off", "-w"] + incs + [
-        os.path.join(HERE, "ref_driver.cpp")] + objs + ["-o", exe]
-    subprocess.check_call(cmd)
+    return objs
+
+
+def _stale(exe, deps):
+    return not os.path.exists(exe) or any(os.path.getmtime(exe) < os.path.getmtime(d) for d in deps)
+
+
+def build(verbose=False):
+    """oracle/_ref/<arch>/ref_driver: the reference's CPU path behind the driver."""
+    src_root = _source_tree(verbose)
+    if src_root is None:
+        return None
+    os.makedirs(BIN, exist_ok=True)
+    exe = os.path.join(BIN, "ref_driver")
+    objs = _objects(src_root)
+    deps = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "kvio.h"), __file__] + objs
+    if _stale(exe, deps):
+        subprocess.check_call(FLAGS + _includes(src_root) + [os.path.join(HERE, "ref_driver.cpp")] + objs +
+                              ["-o", exe])
+    return exe
+
+
+def build_gpu_driver(verbose=False):
+    """oracle/_ref/<arch>/ref_driver_gpu: the same driver with the GPU renderer and
+    optimiser of diffrender_tutorials_gb300/cpp/gpu_drender.cpp behind the
+    reference's interfaces (backend 1 and 2), linked to libdrgb.so."""
+    src_root = _source_tree(verbose)
+    if src_root is None:
+        return None
+    sys.path.insert(0, os.path.dirname(ORACLE))
+    from diffrender_tutorials_gb300 import build as drgb_build
+    lib = drgb_build.build()
+    adapter = os.path.join(os.path.dirname(ORACLE), "diffrender_tutorials_gb300", "cpp")
+    include = os.path.join(os.path.dirname(ORACLE), "include")
+    os.makedirs(BIN, exist_ok=True)
+    exe = os.path.join(BIN, "ref_driver_gpu")
+    objs = _objects(src_root)
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(adapter, "gpu_drender.cpp")]
+    deps = srcs + [os.path.join(adapter, "gpu_drender.h"), os.path.join(HERE, "kvio.h"), __file__, lib] + objs
+    if _stale(exe, deps):
+        libdir = os.path.dirname(lib)
+        subprocess.check_call(FLAGS + ["-DDRGB_WITH_GPU", "-I", adapter, "-I", include] + _includes(src_root) + srcs +
+                              objs + ["-L", libdir, "-ldrgb", "-Wl,-rpath," + libdir, "-o", exe])
     return exe
 
 

@@ -23,6 +23,9 @@
 #include "qmc.h"
 #include "raytrace.h"
 #include "kvio.h"
+#ifdef DRGB_WITH_GPU
+#include "gpu_drender.h"  // the GPU IDiffRender / IOptimizer (diffrender_tutorials_gb300/cpp)
+#endif
 
 using namespace diff_render;
 
@@ -30,6 +33,16 @@ using namespace diff_render;
 // produce (src/drender_autodiff.cpp:97-107) is left at zero, exactly what a
 // build without the plugin computes.  No fixture uses restricted transforms.
 void dmat_dtransforms_jac(float const mat[7], float jac[7][12]) { (void)mat; (void)jac; }
+
+// backend 0: the reference's CPU renderer; 1: the GPU renderer behind the
+// same interface (the reference's own code drives it); 2 (optimiser task):
+// the GPU optimiser as well.
+static std::shared_ptr<IDiffRender> make_renderer(const kv::File& in, SHADING_MODEL mode, int spp) {
+#ifdef DRGB_WITH_GPU
+  if (in.i("backend", 0) >= 1) return MakeGpuDifferentialRenderer(DiffRenderSettings{mode, spp});
+#endif
+  return MakeDifferentialRenderer(DiffRenderSettings{mode, spp});
+}
 
 static std::string key(int m, const char* what) { return "m" + std::to_string(m) + "." + what; }
 
@@ -220,7 +233,7 @@ int main(int argc, char** argv) {
     Scene scene;
     build_scene(in, scene);
     auto cams = build_cams(in);
-    auto dr = MakeDifferentialRenderer(DiffRenderSettings{mode, spp});
+    auto dr = make_renderer(in, mode, spp);
     auto t0 = std::chrono::steady_clock::now();
     if (task == 2) {
       std::vector<Img> imgs(cams.size());
@@ -255,7 +268,7 @@ int main(int argc, char** argv) {
     auto cams = build_cams(in);
     std::vector<Img> tgt;
     images_in(in, "targets", cams, tgt);
-    auto dr = MakeDifferentialRenderer(DiffRenderSettings{mode, spp});
+    auto dr = make_renderer(in, mode, spp);
     OptimizerParameters p((OptimizerParameters::OPT_ALGORITHM)in.i("opt_alg", 4));
     p.position_lr = in.f("opt_pos_lr", p.position_lr);
     p.textures_lr = in.f("opt_tex_lr", p.textures_lr);
@@ -267,7 +280,10 @@ int main(int argc, char** argv) {
     p.verbose = false;
     p.differentiable_mesh_ids.clear();
     for (int32_t x : in.vec<int32_t>("dmesh_ids")) p.differentiable_mesh_ids.push_back(x);
-    std::unique_ptr<IOptimizer> opt(CreateSimpleOptimizer());
+    std::shared_ptr<IOptimizer> opt(CreateSimpleOptimizer());
+#ifdef DRGB_WITH_GPU
+    if (in.i("backend", 0) == 2) opt = CreateGpuOptimizer();
+#endif
     opt->Init(scene, dr, cams.data(), tgt.data(), (int)cams.size(), p);
     std::vector<Scene> dump;
     float err = 0.f;

@@ -12,9 +12,7 @@ are all that the tests read.
 """
 import math
 import os
-import subprocess
 import sys
-import tempfile
 
 import numpy as np
 
@@ -23,7 +21,9 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
 
 import build_ref  # noqa: E402
-import kvio  # noqa: E402
+import kvio  # noqa: E402,F401
+import refrun  # noqa: E402
+from refrun import cam_items, scene_items  # noqa: E402
 from diffrender_tutorials_gb300.scene import (Scene, TriangleMesh, Texture, make_cube, make_icosphere,  # noqa: E402
                                               perturb_vertices, identity4)
 
@@ -31,37 +31,8 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 SIL, VC, TEX, LAMBERT = 1, 2, 3, 4
 
 
-def scene_items(scene):
-    it = {"n_meshes": np.array([len(scene.meshes)], np.int32)}
-    for i, m in enumerate(scene.meshes):
-        p = f"m{i}."
-        it[p + "vertices"] = m.vertices.reshape(-1)
-        it[p + "indices"] = m.indices
-        for name in ("colors", "tc", "normals", "tangents"):
-            a = getattr(m, name)
-            if a is not None:
-                it[p + name] = a.reshape(-1)
-        if m.textures:
-            t = m.textures[0]
-            it[p + "tex"] = t.data
-            it[p + "tex_shape"] = np.array([t.w, t.h, t.channels], np.int32)
-        it[p + "transforms"] = scene.transforms_colmajor(i)
-    return it
-
-
-def cam_items(cams):
-    la = np.array([[*c.origin, *c.target, *c.up, c.width, c.height] for c in cams], np.float32).reshape(-1)
-    fov = np.array([c.fov_rad for c in cams], np.float32)
-    return {"cams_lookat": la, "cams_fov": fov}
-
-
 def run(items):
-    exe = build_ref.build()
-    with tempfile.TemporaryDirectory() as d:
-        fin, fout = os.path.join(d, "in.kv"), os.path.join(d, "out.kv")
-        kvio.save(fin, items)
-        subprocess.check_call([exe, fin, fout])
-        return kvio.load(fout)
+    return refrun.run(build_ref.build(), items)
 
 
 class Cam:

@@ -1,0 +1,134 @@
+"""The GPU renderer behind the reference's own C++ interfaces.
+
+oracle/_ref/ref_driver_gpu is the reference driver linked with the GPU
+IDiffRender / IOptimizer (diffrender_tutorials_gb300/cpp/gpu_drender.cpp):
+the same inputs run through the reference's CPU renderer (backend 0), the GPU
+renderer driven by the reference's own code -- including its OptSimple
+optimiser (backend 1) -- and the GPU optimiser (backend 2).  The driver is
+rebuilt from the patched reference sources (oracle/ref/build_ref.py) where
+they are present.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
+
+import build_ref  # noqa: E402
+import refrun  # noqa: E402
+
+import diffrender_tutorials_gb300 as D  # noqa: E402
+from diffrender_tutorials_gb300.scene import Texture, TriangleMesh  # noqa: E402
+from fixtures import rel_l2  # noqa: E402
+
+VC, TEX, LAMBERT = 2, 3, 4
+
+
+def driver():
+    exe = build_ref.build_gpu_driver()
+    if exe is None:
+        pytest.skip("reference sources absent (neither the reference tree nor oracle/_ref/src)")
+    return exe
+
+
+def textured_sphere(seed=3):
+    m = D.make_icosphere(2, seed=seed)
+    P = m.vertices.astype(np.float64)
+    u = 0.5 + np.arctan2(P[:, 0], P[:, 2]) / (2 * math.pi)
+    v = np.arccos(np.clip(P[:, 1], -1, 1)) / math.pi
+    tex = np.random.default_rng(seed).uniform(0.1, 0.9, size=(16, 16, 3)).astype(np.float32)
+    return TriangleMesh(m.vertices, m.indices, tc=np.stack([u, v], 1).astype(np.float32), normals=m.normals,
+                        textures=[Texture(16, 16, 3, tex.reshape(-1))])
+
+
+def problem(mode):
+    if mode == VC:
+        true = D.make_cube(seed=1)
+        init = D.perturb_vertices(true, 0.1, seed=2)
+        cams = [D.CamInfo(origin=(0, 0, 3), width=64, height=64)]
+    else:
+        true = textured_sphere()
+        init = true.copy()
+        init.textures[0].data[:] = 0.5
+        init.vertices = D.perturb_vertices(true, 0.01, seed=9, radial=True).vertices
+        cams = [D.CamInfo(origin=(0.5, 0.8, 2.6), width=48, height=48),
+                D.CamInfo(origin=(-2.6, 0.3, 0.8), width=48, height=48)]
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(true)
+    isc.add_mesh(init)
+    return ts, isc, cams
+
+
+def grads(out):
+    return np.concatenate([out[f"dmesh{k}"] for k in range(int(out["n_dmeshes"][0]))])
+
+
+def split(g, layout):
+    nv, ninst, p, c, t, tr, _, full = (int(x) for x in layout[:8])
+    pos = np.concatenate([g[p:p + 3 * nv], g[tr:tr + 12 * ninst]])
+    other = []
+    if c >= 0:
+        other.append(g[c:c + 3 * nv])
+    if t >= 0:
+        other.append(g[t:tr])
+    return pos, (np.concatenate(other) if other else np.zeros(0, np.float32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,spp", [(VC, 16), (TEX, 4), (LAMBERT, 4)])
+def test_gpu_renderer_behind_reference_interface(mode, spp):
+    exe = driver()
+    ts, isc, cams = problem(mode)
+    base = {"mode": np.array([mode], np.int32), "spp": np.array([spp], np.int32), **refrun.cam_items(cams)}
+    # render() of the true scene: the target
+    outs = {}
+    for be in (0, 1):
+        outs[be] = refrun.run(exe, {**base, **refrun.scene_items(ts), "task": np.array([2], np.int32),
+                                    "backend": np.array([be], np.int32)})
+    assert np.array_equal(outs[0]["images"], outs[1]["images"])          # bit-exact forward pass
+    tgt = outs[0]["images"]
+    items = {**base, **refrun.scene_items(isc), "task": np.array([4], np.int32), "targets": tgt,
+             "dmesh_ids": np.array([0], np.int32), "edge_samples": np.array([cams[0].width * cams[0].height], np.int32)}
+    cpu = refrun.run(exe, {**items, "backend": np.array([0], np.int32)})
+    gpu = refrun.run(exe, {**items, "backend": np.array([1], np.int32)})
+    assert np.array_equal(cpu["images"], gpu["images"])
+    assert float(gpu["loss"][0]) == pytest.approx(float(cpu["loss"][0]), rel=1e-6)
+    assert np.array_equal(cpu["dmesh0.layout"], gpu["dmesh0.layout"])
+    gp, gc = split(grads(gpu), gpu["dmesh0.layout"])
+    cp, cc = split(grads(cpu), cpu["dmesh0.layout"])
+    assert np.abs(cp).max() > 0 and np.abs(cc).max() > 0
+    assert rel_l2(gp, cp) <= 1e-2          # edge (boundary) term
+    assert rel_l2(gc, cc) <= 1e-3          # interior term
+
+
+@pytest.mark.gpu
+def test_reference_optimiser_and_gpu_optimiser_follow_the_cpu_trajectory():
+    exe = driver()
+    ts, isc, cams = problem(VC)
+    base = {"mode": np.array([VC], np.int32), "spp": np.array([16], np.int32), **refrun.cam_items(cams)}
+    tgt = refrun.run(exe, {**base, **refrun.scene_items(ts), "task": np.array([2], np.int32)})["images"]
+    items = {**base, **refrun.scene_items(isc), "task": np.array([5], np.int32), "targets": tgt,
+             "dmesh_ids": np.array([0], np.int32), "iters": np.array([8], np.int32),
+             "opt_alg": np.array([4], np.int32), "opt_pos_lr": np.array([0.01], np.float32),
+             "opt_base_lr": np.array([0.01], np.float32), "opt_flags": np.array([1 | 4], np.int32)}
+    runs = {be: refrun.run(exe, {**items, "backend": np.array([be], np.int32)}) for be in (0, 1, 2)}
+    for be in (1, 2):
+        assert int(runs[be]["n_iters"][0]) == 8
+        assert float(runs[be]["final_error"][0]) == pytest.approx(float(runs[0]["final_error"][0]), rel=1e-4)
+        for k in range(8):
+            for what in ("vertices", "colors"):
+                a, b = runs[0][f"it{k}.m0.{what}"], runs[be][f"it{k}.m0.{what}"]
+                assert np.abs(a - b).max() < 5e-5, (be, k, what)
+
+
+def test_adapter_builds_against_reference_headers():
+    """CPU check: the adapter compiles with the reference's headers and links
+    to libdrgb (the driver is not run without a GPU)."""
+    exe = build_ref.build_gpu_driver()
+    if exe is None:
+        pytest.skip("reference sources absent")
+    assert os.path.exists(exe)
