@@ -16,10 +16,11 @@ value: iterations/s with everything resident on the GPU (optimiser graph
 replays timed with CUDA events on the renderer stream; L2 flushed before
 every step).  e2e: the same metric through the public C-ABI call
 drgb_d_render_and_compare with host buffers (targets H2D, gradient + loss
-D2H inside the timed region).  The reference arm times the reference
-algorithm's CPU implementation (the oracle port; the reference itself cannot
-be built on the GPU host) on a bounded sample and extrapolates linearly in
-pixels x views.
+D2H inside the timed region).  The reference arm times the reference's own
+CPU implementation (its d_render_and_compare with the brute-force caster and
+OpenMP, rebuilt from the reference sources by oracle/ref/build_ref.py; the
+oracle port where they are absent) on a bounded sample and extrapolates
+linearly in pixels x views.
 """
 import argparse
 import json
@@ -137,23 +138,48 @@ def allmax(pg, x):
 
 
 def cpu_sample(w, reps=1):
-    """Oracle (CPU port of the reference algorithm) on a bounded sample:
-    returns (seconds per full-workload iteration, extrapolation factor, cores)."""
+    """The reference's own CPU path on a bounded sample of the workload:
+    returns (seconds per full-workload iteration, factor, threads, kind,
+    description).  The reference driver (oracle/ref/build_ref.py: brute-force
+    caster + OpenMP, with the point-light model of oracle/ref/ref_pointlight.h)
+    is built from the reference sources where they are available; otherwise
+    the oracle port of the same algorithm is timed."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
     import pyoracle as O
     import diffrender_tutorials_gb300 as D
     ts, isc, cams = make_problem(w)
     sres, sv = w["sample_res"], w["sample_views"]
     scams = [D.CamInfo(origin=c.origin, target=c.target, up=c.up, width=sres, height=sres) for c in cams[:sv]]
     cores = os.cpu_count() or 1
+    factor = (w["res"] * w["res"] * w["views"]) / (sres * sres * sv)
+    what = f"{sv} view(s) at {sres}x{sres} of the same scene, extrapolated x{factor:g}"
     O.set_threads(cores)
     tgt = O.render(ts, scams, w["mode"], w["spp"])
+    exe = None
+    try:
+        import build_ref
+        exe = build_ref.build()
+    except Exception:  # noqa: BLE001 - no compiler or sources: time the port
+        exe = None
+    if exe:
+        import refrun
+        items = {"task": np.array([4], np.int32), "mode": np.array([w["mode"]], np.int32),
+                 "spp": np.array([w["spp"]], np.int32), **refrun.cam_items(scams), **refrun.scene_items(isc),
+                 "targets": tgt, "dmesh_ids": np.array([0], np.int32),
+                 "edge_samples": np.array([sres * sres], np.int32)}
+        dt = 0.0
+        for _ in range(reps):
+            dt += float(refrun.run(exe, items)["seconds"][0])
+        dt /= reps
+        # the reference runs its loops on at most 14 OpenMP threads (MAXTHREADS, src/drender.h:12)
+        return dt * factor, factor, min(cores, 14), "reference", what + " (reference d_render_and_compare, " \
+            "brute-force caster, OpenMP)"
     t0 = time.perf_counter()
     for _ in range(reps):
         O.d_render_and_compare(isc, scams, w["mode"], w["spp"], tgt, sres * sres)
     dt = (time.perf_counter() - t0) / reps
-    factor = (w["res"] * w["res"] * w["views"]) / (sres * sres * sv)
-    return dt * factor, factor, cores, f"{sv} view(s) at {sres}x{sres} of the same scene, extrapolated x{factor:g}"
+    return dt * factor, factor, cores, "port", what + " (oracle: CPU port of the reference path)"
 
 
 def reference_arm(args, w, ws, rank, pg):
@@ -164,7 +190,7 @@ def reference_arm(args, w, ws, rank, pg):
         cpu_sample(w)
     times = []
     for _ in range(args.steps):
-        t, factor, cores, desc = cpu_sample(w)
+        t, factor, cores, kind, desc = cpu_sample(w)
         times.append(t)
     mean = sum(times) / len(times)
     val = 1.0 / mean
@@ -172,8 +198,7 @@ def reference_arm(args, w, ws, rank, pg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "parallelism": "replicas"},
-            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": cores, "kind": "port",
-                             "sample": desc + " (brute-force caster, 14-block reduction replay)"},
+            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc},
             "e2e": {"value": val, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -330,9 +355,8 @@ def drgb_arm(args, w, ws, rank, local, pg):
         "final_loss": losses[-1] if losses else None,
     }
     if ws == 1 and rank == 0 and not args.no_cpu_baseline:
-        t, factor, cores, desc = cpu_sample(w)
-        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "iters/s", "cores": cores, "kind": "port",
-                                "sample": desc + " (oracle: brute-force caster, CPU port of the reference path)"}
+        t, factor, cores, kind, desc = cpu_sample(w)
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

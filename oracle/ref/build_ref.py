@@ -100,9 +100,14 @@ def _objects(src_root):
     objs, procs = [], []
     for rel in COMPILE:
         src = os.path.join(src_root, rel)
+        if rel == "src/drender.cpp":
+            # compiled through drender_unit.cpp, which adds the point-light model
+            src = os.path.join(HERE, "drender_unit.cpp")
         obj = os.path.join(BIN, rel.replace("/", "_") + ".o")
         objs.append(obj)
-        if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src):
+        deps = [src, os.path.join(HERE, "ref_pointlight.h"), os.path.join(src_root, "src", "drender.cpp"),
+                os.path.join(src_root, "src", "drender.h")]
+        if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
             continue
         cmd = FLAGS + incs + ["-c", src, "-o", obj]
         procs.append((subprocess.Popen(cmd), cmd))

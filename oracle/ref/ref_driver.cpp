@@ -23,6 +23,7 @@
 #include "qmc.h"
 #include "raytrace.h"
 #include "kvio.h"
+#include "ref_pointlight.h"
 #ifdef DRGB_WITH_GPU
 #include "gpu_drender.h"  // the GPU IDiffRender / IOptimizer (diffrender_tutorials_gb300/cpp)
 #endif
@@ -37,11 +38,23 @@ void dmat_dtransforms_jac(float const mat[7], float jac[7][12]) { (void)mat; (vo
 // backend 0: the reference's CPU renderer; 1: the GPU renderer behind the
 // same interface (the reference's own code drives it); 2 (optimiser task):
 // the GPU optimiser as well.
+// Mode 16 (point light, vertex albedo) runs the reference's DiffRender<>
+// with the model of ref_pointlight.h (instantiated in drender_unit.cpp); its
+// gradients use the VERTEX_COLOR layout, which IDiffRender::mode reports so
+// that OptSimple allocates it.
+namespace diff_render {
+std::shared_ptr<IDiffRender> MakePointLightRenderer(const DiffRenderSettings& settings);
+}
 static std::shared_ptr<IDiffRender> make_renderer(const kv::File& in, SHADING_MODEL mode, int spp) {
 #ifdef DRGB_WITH_GPU
   if (in.i("backend", 0) >= 1) return MakeGpuDifferentialRenderer(DiffRenderSettings{mode, spp});
 #endif
+  if (mode == kPointLightVColor) return MakePointLightRenderer(DiffRenderSettings{mode, spp});
   return MakeDifferentialRenderer(DiffRenderSettings{mode, spp});
+}
+
+static SHADING_MODEL layout_mode(SHADING_MODEL m) {
+  return m == kPointLightVColor ? SHADING_MODEL::VERTEX_COLOR : m;
 }
 
 static std::string key(int m, const char* what) { return "m" + std::to_string(m) + "." + what; }
@@ -244,7 +257,7 @@ int main(int argc, char** argv) {
     } else {
       std::vector<int> ids;
       for (int32_t x : in.vec<int32_t>("dmesh_ids")) ids.push_back(x);
-      DScene ds(scene, mode, ids);
+      DScene ds(scene, layout_mode(mode), ids);
       const int edge_samples = in.i("edge_samples");
       if (task == 3) {
         std::vector<Img> adj;
