@@ -455,6 +455,134 @@ def batch_arm(args, ws, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def stress_problem(n_tris=200_000, res=1024, seed=0):
+    """Displaced sphere (8 seeded radial sinusoids, amplitude 0.05) with about
+    n_tris triangles, the 2-bounce diffuse path model, one view."""
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import workloads as WL
+    true = WL.sphere_with_triangles(n_tris, seed=seed)
+    init = D.perturb_vertices(true, 0.01, seed=seed + 2, radial=True)
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(true)
+    isc.add_mesh(init)
+    cams = [D.CamInfo(origin=(0.0, 0.4, 2.6), width=res, height=res)]
+    return ts, isc, cams
+
+
+def fd_check(r, isc, cams, tgt, grad_pos, coords, h=1e-3):
+    """Central finite differences of the loss at `coords` (flat vertex
+    coordinate indices of mesh 0) against the gradient's position block."""
+    import diffrender_tutorials_gb300 as D
+    fd = []
+    scratch = D.DScene(r, [0])
+    for c in coords:
+        vals = []
+        for sgn in (1.0, -1.0):
+            s = isc.copy()
+            v = s.meshes[0].vertices.reshape(-1)
+            v[c] = np.float32(v[c] + sgn * h)
+            r.commit(s)
+            vals.append(r.d_render_and_compare(s, cams, tgt, 0, scratch))
+        fd.append((vals[0] - vals[1]) / (2 * h))
+    r.commit(isc)
+    # the returned loss is the MSE / (views*W*H) while the adjoint 2(I-T), and
+    # so the gradient, belong to the sum of squared errors (src/drender.h:184-190)
+    n_pix = sum(int(c.width) * int(c.height) for c in cams)
+    fd = np.asarray(fd, np.float64) * n_pix
+    g = np.asarray(grad_pos[coords], np.float64)
+    rel = float(np.linalg.norm(g - fd) / max(np.linalg.norm(fd), 1e-30))
+    big = np.abs(fd) > 0.1 * np.abs(fd).max()
+    return {"coords": len(coords), "rel_l2": rel,
+            "sign_agreement": float(np.mean(np.sign(g[big]) == np.sign(fd[big]))) if big.any() else None,
+            "correlation": float(np.corrcoef(g, fd)[0, 1]) if np.std(g) > 0 and np.std(fd) > 0 else None,
+            "slope": float(np.dot(g, fd) / max(np.dot(fd, fd), 1e-30)),
+            "fd_norm": float(np.linalg.norm(fd)), "grad_norm": float(np.linalg.norm(g))}
+
+
+def stress_arm(args, ws, rank, local, pg):
+    """Differentiation stress: 200k-triangle displaced sphere, 2-bounce path
+    model, 1024x1024, 4 spp, 1,048,576 edge samples.  Re-traced vs stored
+    adjoint hits (bytes of the hit buffer), and the gradient against central
+    finite differences (h = 1e-3) on 64 seeded vertex coordinates."""
+    import torch
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import build as B
+    from diffrender_tutorials_gb300 import native as N
+    B.build()
+    torch.cuda.set_device(local)
+    ts, isc, cams = stress_problem(res=args.res)
+    S = D.SHADING_MODEL.PATH_DIFFUSE
+    spp = 4
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+    r.commit(ts)
+    tgt = r.render(ts, cams)
+    edge = args.res * args.res
+    n_tri = isc.meshes[0].face_count
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.001)
+    p.base_lr = 0.01
+    p.flags = D.OptimizerParameters._OPT_POS | D.OptimizerParameters._OPT_COL
+    results = {}
+    for label, hits in (("recompute", 0), ("stored_hits", 1)):
+        ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+        ro.set_option(N.OPT_ADJOINT_HITS, hits)
+        opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, ro, cams, tgt, p)
+        stream = torch.cuda.ExternalStream(ro.stream(), device=local)
+        for _ in range(args.warmup):
+            opt.run_async(1)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            with torch.cuda.stream(stream):
+                for e0, e1 in ev:
+                    e0.record(stream)
+                    opt.run_async(1)
+                    e1.record(stream)
+            torch.cuda.synchronize()
+        ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+        n_samples = args.res * args.res * spp
+        results[label] = {"value": args.steps / (sum(ms) / 1e3), "ms_per_step": sum(ms) / args.steps,
+                          "phases_ms": opt.profile(2), "clocks": clk.summary(),
+                          "hit_buffer_bytes_per_iter": (2 * 16 * n_samples) if hits else 0}
+        del opt, ro
+    # gradient at the initial mesh and the finite-difference check
+    r.commit(isc)
+    ds = D.DScene(r, [0])
+    r.d_render_and_compare(isc, cams, tgt, edge, ds)
+    gpos = ds.get_dmeshes()[0].pos().reshape(-1).copy()
+    rng = np.random.default_rng(args.seed)
+    nv = isc.meshes[0].vertex_count
+    coords = rng.choice(3 * nv, size=64, replace=False)
+    fd_random = fd_check(r, isc, cams, tgt, gpos, coords)
+    # 64 coordinates of silhouette vertices (normal nearly perpendicular to the view ray)
+    V = isc.meshes[0].vertices.astype(np.float64)
+    nrm = isc.meshes[0].normals.astype(np.float64)
+    view = V - np.asarray(cams[0].origin, np.float64)
+    cosang = np.abs(np.sum(view * nrm, 1)) / (np.linalg.norm(view, axis=1) * np.linalg.norm(nrm, axis=1))
+    sil = np.argsort(cosang)[:2000]
+    sv = rng.choice(sil, size=64, replace=False)
+    coords_sil = 3 * sv + rng.integers(0, 3, size=64)
+    fd_sil = fd_check(r, isc, cams, tgt, gpos, coords_sil)
+    rec = results["recompute"]
+    line = {
+        "metric": "fwd+adjoint iters/s", "value": rec["value"], "unit": "iters/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced sphere)",
+        "config": {"workload": f"stress_sphere{n_tri}_path2_{args.res}x{args.res}_4spp", "triangles": n_tri,
+                   "resolution": args.res, "spp": spp, "edge_samples": edge, "shading": "PATH_DIFFUSE (2 bounces)",
+                   "l2": "inputs larger than L2 (scene + LBVH ~40 MB, image buffers ~50 MB, edge queue 16 MB)",
+                   "parallelism": "replicas"},
+        "adjoint": results,
+        "fd_check": {"h": 1e-3, "random_coords": fd_random, "silhouette_coords": fd_sil,
+                     "note": "the method's position gradient is the edge (visibility) term only; the path "
+                             "model's smooth dependence of shading on positions is not differentiated, as in "
+                             "the reference (interior gradients cover the albedo only)"},
+        "clocks": rec["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def serve_setups(args, local):
     """The Poisson trace with its target images rendered from the true meshes."""
     import diffrender_tutorials_gb300 as D
@@ -603,7 +731,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="drgb", choices=["drgb", "reference"])
-    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve"])
+    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve", "stress"])
+    ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
     ap.add_argument("--seed", type=int, default=0)
@@ -613,6 +742,11 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)
     ws, rank, local, pg = dist_setup()
+    if args.workload == "stress":
+        stress_arm(args, ws, rank, local, pg)
+        if pg is not None:
+            pg.destroy_process_group()
+        return
     if args.workload in ("batch", "serve"):
         if args.jobs is None:
             args.jobs = 64 if args.workload == "batch" else 16

@@ -99,6 +99,16 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         break;
       }
       case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
+      case DRGB_OPT_ADJOINT_HITS: {
+        Job& J = r->job;
+        J.store_hits = value ? 1 : 0;
+        if (J.store_hits && J.opt.active) {
+          r->set_device();
+          r->hit_buffers();
+        }
+        if (r->d_job.p) r->push_dev();
+        break;
+      }
       case DRGB_OPT_DETERMINISTIC: {
         Job& J = r->job;
         J.det = value ? 1 : 0;
@@ -198,9 +208,7 @@ int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoin
     r->push_dev();
     launch_adj_convert(r->d_job.p, (int64_t)npix, r->stream);
     r->det_begin();
-    if (J.mode != SILHOUETTE)
-      launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_ADJ, r->px_grid(),
-                    r->stream, J.mode, J.det);
+    if (J.mode != SILHOUETTE) r->pixel_pass(PX_ADJ);
     if (edge_samples_in_total > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
     r->det_end();
     if (J.grad_total > 0)
@@ -434,8 +442,7 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
       DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), r->stream));
       r->det_begin();
       const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
-      launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
-                    r->stream, J.mode, J.det);
+      r->pixel_pass(flags);
       launch_loss_finalize(r->d_job.p, 1, r->stream);
       DRGB_CUDA(cudaEventRecord(ev[1], r->stream));
       if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);

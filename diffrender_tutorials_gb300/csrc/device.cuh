@@ -146,6 +146,8 @@ struct JobDev {
   uint32_t* rec_key;
   float4* rec_val;
   int* rec_count;            // records per region: work items, then (view, sample) edge regions
+  // stored adjoint hits (one float4 {t, u, v, triangle} per adjoint sample)
+  float4* hit_buf;
 };
 
 // Record slots a work item of NS samples may fill (deterministic mode):

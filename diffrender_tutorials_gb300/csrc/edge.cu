@@ -5,7 +5,8 @@
 //   project : VertexShader of every flattened vertex, per view
 //   pmf     : edge weights = 3-D length of the projected endpoints
 //   cdf     : the sampler's CDF, summed sequentially in edge order so that it
-//             is bit-identical to the reference's
+//             is bit-identical to the reference's (one block per view: the
+//             block stages chunks in shared memory, one thread runs the chain)
 //   select  : replayed random numbers -> edge (upper_bound) -> point ->
 //             off-image / small-adjoint rejection; survivors are appended to
 //             a queue with one atomic per warp (ballot compaction)
@@ -35,30 +36,56 @@ __device__ __forceinline__ void edge_pmf_body(const JobDev& J, int view, int e) 
   J.pmf[(int64_t)view * J.n_edges + e] = length(mk(b.x - a.x, b.y - a.y, b.z - a.z));
 }
 
-// One warp: cdf[k+1] = pmf[k] + cdf[k] in edge order, then both divided by
-// the total (drender.cpp:5-22).
-__device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view) {
-  const int lane = threadIdx.x & 31;
+// One block (CDF_THREADS): cdf[k+1] = pmf[k] + cdf[k] in edge order, then
+// both divided by the total (drender.cpp:5-22).  The running sum is one
+// dependent chain of float additions -- the reference's rounding sequence,
+// which the sampler's upper_bound must see bit for bit -- so one thread runs
+// it, over chunks that the whole block stages in shared memory; loads and
+// stores stay off the chain.
+constexpr int CDF_THREADS = 256;
+constexpr int CDF_CHUNK = 4096;
+__device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view, float* sbuf) {
+  const int tid = threadIdx.x;
   const int E = J.n_edges;
   float* pmf = J.pmf + (int64_t)view * E;
   float* cdf = J.cdf + (int64_t)view * (E + 1);
-  float run = 0.0f;
-  if (lane == 0) cdf[0] = 0.0f;
-  for (int base = 0; base < E; base += 32) {
-    const float v = (base + lane < E) ? pmf[base + lane] : 0.0f;
-    const int cnt = min(32, E - base);
-    float out = 0.0f;
-    for (int j = 0; j < cnt; j++) {
-      const float pj = __shfl_sync(0xffffffffu, v, j);
-      run = pj + run;
-      if (lane == j) out = run;
-    }
-    if (lane < cnt) cdf[base + lane + 1] = out;
+  __shared__ float s_run;
+  if (tid == 0) {
+    s_run = 0.0f;
+    cdf[0] = 0.0f;
   }
-  __syncwarp();
-  const float total = __shfl_sync(0xffffffffu, run, 0);
-  for (int k = lane; k < E; k += 32) pmf[k] = pmf[k] / total;
-  for (int k = lane; k <= E; k += 32) cdf[k] = cdf[k] / total;
+  for (int base = 0; base < E; base += CDF_CHUNK) {
+    const int n = min(CDF_CHUNK, E - base);
+    for (int j = tid; j < n; j += CDF_THREADS) sbuf[j] = pmf[base + j];
+    __syncthreads();
+    if (tid == 0) {
+      float run = s_run;
+      int j = 0;
+      for (; j + 8 <= n; j += 8) {
+        const float p0 = sbuf[j], p1 = sbuf[j + 1], p2 = sbuf[j + 2], p3 = sbuf[j + 3];
+        const float p4 = sbuf[j + 4], p5 = sbuf[j + 5], p6 = sbuf[j + 6], p7 = sbuf[j + 7];
+        run = p0 + run; sbuf[j] = run;
+        run = p1 + run; sbuf[j + 1] = run;
+        run = p2 + run; sbuf[j + 2] = run;
+        run = p3 + run; sbuf[j + 3] = run;
+        run = p4 + run; sbuf[j + 4] = run;
+        run = p5 + run; sbuf[j + 5] = run;
+        run = p6 + run; sbuf[j + 6] = run;
+        run = p7 + run; sbuf[j + 7] = run;
+      }
+      for (; j < n; j++) {
+        run = sbuf[j] + run;
+        sbuf[j] = run;
+      }
+      s_run = run;
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += CDF_THREADS) cdf[base + j + 1] = sbuf[j];
+    __syncthreads();
+  }
+  const float total = s_run;
+  for (int k = tid; k < E; k += CDF_THREADS) pmf[k] = pmf[k] / total;
+  for (int k = tid; k <= E; k += CDF_THREADS) cdf[k] = cdf[k] / total;
 }
 
 __device__ __forceinline__ int upper_bound_idx(const float* cdf, int n, float u) {
@@ -230,7 +257,10 @@ __global__ void k_edge_pmf(const JobDev* jobs, int job) {
   if (e < J.n_edges) edge_pmf_body(J, blockIdx.y, e);
 }
 
-__global__ void k_edge_cdf(const JobDev* jobs, int job) { edge_cdf_body(jobs[job], blockIdx.x); }
+__global__ void __launch_bounds__(CDF_THREADS) k_edge_cdf(const JobDev* jobs, int job) {
+  __shared__ float sbuf[CDF_CHUNK];
+  edge_cdf_body(jobs[job], blockIdx.x, sbuf);
+}
 
 __global__ void k_edge_select(const JobDev* jobs, int job) {
   const JobDev& J = jobs[job];
@@ -274,12 +304,12 @@ __global__ void k_b_edge_pmf(const JobDev* jobs, const Seg* segs, int nseg) {
   if (e < sg.count) edge_pmf_body(jobs[sg.job], sg.sub, e);
 }
 
-// one warp per (job, view) pair: segs[w].job / .sub
-__global__ void k_b_edge_cdf(const JobDev* jobs, const Seg* pairs, int n_pairs) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= n_pairs) return;
-  const Seg sg = pairs[w];
-  edge_cdf_body(jobs[sg.job], sg.sub);
+// one block per (job, view) pair: pairs[b].job / .sub
+__global__ void __launch_bounds__(CDF_THREADS) k_b_edge_cdf(const JobDev* jobs, const Seg* pairs, int n_pairs) {
+  __shared__ float sbuf[CDF_CHUNK];
+  if ((int)blockIdx.x >= n_pairs) return;
+  const Seg sg = pairs[blockIdx.x];
+  edge_cdf_body(jobs[sg.job], sg.sub, sbuf);
 }
 
 __global__ void k_b_edge_select(const JobDev* jobs, const Seg* segs, int nseg, int4* queue, int* count, int cap) {
@@ -297,7 +327,7 @@ void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, i
   if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
   k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
-  k_edge_cdf<<<n_views, 32, 0, s>>>(d_jobs, job);
+  k_edge_cdf<<<n_views, CDF_THREADS, 0, s>>>(d_jobs, job);
   DRGB_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int), s));
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   // the queue, its counter and capacity are read from the job on the device
@@ -320,7 +350,7 @@ void launch_b_edges(const JobDev* d_jobs, const Seg* proj_segs, int n_proj, int 
   if (n_pairs <= 0) return;
   if (proj_chunks > 0) k_b_edge_project<<<proj_chunks, 256, 0, s>>>(d_jobs, proj_segs, n_proj);
   if (pmf_chunks > 0) k_b_edge_pmf<<<pmf_chunks, 256, 0, s>>>(d_jobs, pmf_segs, n_pmf);
-  k_b_edge_cdf<<<(n_pairs + 7) / 8, 256, 0, s>>>(d_jobs, pairs, n_pairs);
+  k_b_edge_cdf<<<n_pairs, CDF_THREADS, 0, s>>>(d_jobs, pairs, n_pairs);
   DRGB_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
   if (sel_chunks > 0) k_b_edge_select<<<sel_chunks, 256, 0, s>>>(d_jobs, sel_segs, n_sel, queue, count, cap);
   if (det) k_edge_shade_q<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, queue, count, cap);

@@ -402,6 +402,7 @@ void sync_dev(Job& J) {
   d.rec_key = J.rec_key.p;
   d.rec_val = J.rec_val.p;
   d.rec_count = J.rec_count.p;
+  d.hit_buf = J.hit_buf.p;
 }
 
 // ---------------------------------------------------------------------------

@@ -158,6 +158,9 @@ struct Job {
   OptState opt;
   // deterministic reduction (records, dense pairs, radix-sort scratch)
   int det = 0;
+  // stored adjoint hits instead of re-tracing (one float4 per adjoint sample)
+  int store_hits = 0;
+  DevBuf<float4> hit_buf;
   DevBuf<uint32_t> rec_key, det_key[2], det_part, det_hist;
   DevBuf<float4> rec_val;
   DevBuf<int> rec_count, det_idx[2], det_n;
@@ -189,7 +192,9 @@ void camera_look_at(const float* o, const float* t, const float* u, float width,
 CamDev make_cam(const drgb_camera& c);
 
 // Pixel kernel flags
-enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8 };
+// PX_HIT_STORE: adjoint pass that only traces and stores the primary hits;
+// PX_HIT_LOAD: adjoint pass that reads them instead of tracing.
+enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8, PX_HIT_STORE = 16, PX_HIT_LOAD = 32 };
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
                    cudaStream_t s, int mode, bool det = false);
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);

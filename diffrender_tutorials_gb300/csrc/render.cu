@@ -137,12 +137,34 @@ __device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, 
 
 // shade_grad<M> for one sample; every lane of the warp must call it.  MODE
 // as for shade().
-template <int MODE, bool DET>
+// HITS: the sample's primary hit comes from the stored hit buffer (written by
+// a PX_HIT_STORE launch) instead of being traced again.
+template <int MODE, bool DET, bool HITS>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
-                                           uint32_t key, float* wscr, int64_t rec_base, int& rec_n) {
+                                           uint32_t key, float* wscr, int64_t rec_base, int& rec_n,
+                                           const float4* stored) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
-  const bool hit = cast_p<kPixelWarp>(J, cam, x, y, active, s);
+  bool hit;
+  if (HITS) {
+    camera_ray(cam, x, y, s.ro, s.rd);
+    const float4 hb = *stored;
+    s.h.t = hb.x;
+    s.h.u = hb.y;
+    s.h.v = hb.z;
+    s.h.tri = __float_as_int(hb.w);
+    hit = active && s.h.tri >= 0;
+    s.A = s.B = s.C = s.block = 0;
+    if (hit) {
+      const int4 tv = __ldg(J.tri_v + s.h.tri);
+      s.A = tv.x;
+      s.B = tv.y;
+      s.C = tv.z;
+      s.block = tv.w;
+    }
+  } else {
+    hit = cast_p<kPixelWarp>(J, cam, x, y, active, s);
+  }
   if (model_has_color(mode)) {
     float c[9];
     int tri = -1, gA = 0, gB = 0, gC = 0;
@@ -203,8 +225,10 @@ constexpr int PX_WARPS = PX_THREADS / 32;
 constexpr int PX_MAX_SAMPLES = 64;
 
 // DET: the deterministic-mode variant (gradient records instead of atomics
-// for jobs that have record buffers).
-template <int MODE, bool DET>
+// for jobs that have record buffers).  HITS: the adjoint's primary hits are
+// written to (PX_HIT_STORE) or read from (PX_HIT_LOAD) the job's hit buffer,
+// one float4 {t, u, v, triangle} per adjoint sample, instead of re-traced.
+template <int MODE, bool DET, bool HITS>
 __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
                                                        int n_items, int* counter, const int flags) {
   __shared__ JobDev sJ_all[PX_WARPS];
@@ -310,7 +334,8 @@ __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict_
       }
     }
     if (flags & PX_ADJ) {
-      if (!(flags & PX_LOSS)) {
+      const bool store_hits = HITS && (flags & PX_HIT_STORE);
+      if (!(flags & PX_LOSS) && !store_hits) {
         if (lane < P) {
           const int qx = x0 + lane % tw, qy = y0 + lane / tw;
           float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -333,17 +358,30 @@ __global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict_
         float sx = 0.0f, sy = 0.0f;
         uint32_t key = 0;
         if (s < NS && px < W && py < H) {
-          const float4 a = s_adj[p];
-          val = mk(a.x, a.y, a.z) / (float)S;
-          act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
+          if (store_hits) {
+            act = true;  // the adjoint is not known yet: every sample is traced
+          } else {
+            const float4 a = s_adj[p];
+            val = mk(a.x, a.y, a.z) / (float)S;
+            act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
+          }
           sx = (float)px + s_ham[2 * k];
           sy = (float)py + s_ham[2 * k + 1];
           const int64_t pix = (int64_t)py * W + px;
           key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
         }
-        shade_grad<MODE, DET>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n);
+        // one hit-buffer slot per adjoint sample of the item
+        const float4* hslot = HITS ? J.hit_buf + ((int64_t)(it - J.item_base) * NS + min(s, NS - 1)) : nullptr;
+        if (store_hits) {
+          Surf sf;
+          const bool h = cast_p<kPixelWarp>(J, C, sx, sy, act, sf);
+          if (s < NS)
+            const_cast<float4*>(hslot)[0] = make_float4(sf.h.t, sf.h.u, sf.h.v, __int_as_float(h ? sf.h.tri : -1));
+          continue;
+        }
+        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot);
       }
-      if (DET && J.det && lane == 0) J.rec_count[it - J.item_base] = rec_n;
+      if (DET && J.det && lane == 0 && !store_hits) J.rec_count[it - J.item_base] = rec_n;
     }
     __syncwarp();
   }
@@ -426,15 +464,30 @@ template <bool DET>
 static void launch_pixels_t(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags,
                             int grid, cudaStream_t s, int mode) {
   switch (mode) {
-    case SILHOUETTE: k_pixels<SILHOUETTE, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case VERTEX_COLOR: k_pixels<VERTEX_COLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    case LAMBERT: k_pixels<LAMBERT, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case SILHOUETTE: k_pixels<SILHOUETTE, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case VERTEX_COLOR: k_pixels<VERTEX_COLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT: k_pixels<LAMBERT, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
     case LAMBERT_POINT_VCOLOR:
-      k_pixels<LAMBERT_POINT_VCOLOR, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
+      k_pixels<LAMBERT_POINT_VCOLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
       break;
-    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
-    default: k_pixels<0, DET><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    default: k_pixels<0, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+  }
+}
+
+// Stored-hit variants: specialised for the vertex-colour, point-light and
+// path models, the generic kernel otherwise.
+template <bool DET>
+static void launch_pixels_hits(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags,
+                               int grid, cudaStream_t s, int mode) {
+  switch (mode) {
+    case VERTEX_COLOR: k_pixels<VERTEX_COLOR, DET, true><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case LAMBERT_POINT_VCOLOR:
+      k_pixels<LAMBERT_POINT_VCOLOR, DET, true><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
+      break;
+    case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE, DET, true><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    default: k_pixels<0, DET, true><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
   }
 }
 
@@ -445,8 +498,16 @@ void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* 
   DRGB_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int), s));
   if (grid <= 0 || grid > n_items) grid = n_items;
   // records are only written by the adjoint pass
-  if (det && (flags & PX_ADJ)) launch_pixels_t<true>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
-  else launch_pixels_t<false>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+  const bool rec = det && (flags & PX_ADJ) && !(flags & PX_HIT_STORE);
+  if (flags & (PX_HIT_STORE | PX_HIT_LOAD)) {
+    if (!(flags & PX_ADJ)) throw CudaError("stored hits belong to the adjoint pass", DRGB_ERR_INVALID);
+    if (rec) launch_pixels_hits<true>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+    else launch_pixels_hits<false>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+  } else if (rec) {
+    launch_pixels_t<true>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+  } else {
+    launch_pixels_t<false>(d_jobs, d_items, n_items, d_counter, flags, grid, s, mode);
+  }
   count_launch();
 }
 

@@ -117,6 +117,25 @@ struct drgb_renderer {
     J.dev.edge_samples = edge_samples;
     J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
     if (J.det) det_buffers(J, stream);
+    if (J.store_hits) hit_buffers();
+  }
+
+  // One float4 per adjoint sample of every work item (stored-hit mode).
+  void hit_buffers() {
+    Job& J = job;
+    const int64_t n = (int64_t)J.dev.item_count * J.tile_w * J.tile_h * J.S;
+    J.hit_buf.reserve(std::max<int64_t>(1, n));
+  }
+
+  // The pixel kernel; with stored hits, an adjoint pass is preceded by a
+  // launch that traces and stores the adjoint samples' primary hits.
+  void pixel_pass(int flags) {
+    Job& J = job;
+    const bool hits = J.store_hits && J.hit_buf.p && (flags & PX_ADJ);
+    const int n = (int)J.h_pixel_items.size();
+    if (hits) launch_pixels(d_job.p, d_items.p, n, d_counter.p, PX_ADJ | PX_HIT_STORE, px_grid(), stream, J.mode, J.det);
+    launch_pixels(d_job.p, d_items.p, n, d_counter.p, flags | (hits ? PX_HIT_LOAD : 0), px_grid(), stream, J.mode,
+                  J.det);
   }
 
   // Deterministic mode: clear the record counts before a gradient pass and
@@ -161,8 +180,7 @@ struct drgb_renderer {
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
     det_begin();
     int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
-    launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, px_grid(), stream, J.mode,
-                  J.det);
+    pixel_pass(flags);
     launch_loss_finalize(d_job.p, 1, stream);
     if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
     det_end();

@@ -58,9 +58,12 @@ enum {
   DRGB_OPT_TILE_W = 2,           /* pixel tile width of the fused forward/adjoint kernel */
   DRGB_OPT_TILE_H = 3,
   DRGB_OPT_USE_GRAPH = 4,        /* 1 (default): optimiser iterations replay a CUDA graph */
-  DRGB_OPT_DETERMINISTIC = 5     /* 1: gradients are summed in a fixed order (records sorted by gradient
+  DRGB_OPT_DETERMINISTIC = 5,    /* 1: gradients are summed in a fixed order (records sorted by gradient
                                     index, then segmented sums) instead of by float atomics, so a job's
                                     gradient is bit-identical run to run, alone or in a batch; default 0 */
+  DRGB_OPT_ADJOINT_HITS = 6      /* 1: the interior adjoint reads the primary hits of its samples from a buffer
+                                    written by a separate tracing pass (16 bytes per sample) instead of
+                                    re-tracing them; 0 (default): re-trace.  Single renderers only. */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
