@@ -489,7 +489,19 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   const f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
   const f3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   const float lo_t = tNear - fabsf(tNear) * 4e-6f - 1e-6f;
+#ifdef DRGB_SMEM_STACK
+  // the top DRGB_SMEM_STACK entries in shared memory (one column per thread,
+  // blocks of at most 256 threads), deeper ones in local memory
+  __shared__ int s_stack[DRGB_SMEM_STACK * 256];
+  int* const sst = s_stack + threadIdx.x;
+  int stack[kStackSize - DRGB_SMEM_STACK];
+#define DRGB_PUSH(v) (sp < DRGB_SMEM_STACK ? (sst[256 * sp] = (v)) : (stack[sp - DRGB_SMEM_STACK] = (v))), sp++
+#define DRGB_POP() (--sp, sp < DRGB_SMEM_STACK ? sst[256 * sp] : stack[sp - DRGB_SMEM_STACK])
+#else
   int stack[kStackSize];
+#define DRGB_PUSH(v) stack[sp++] = (v)
+#define DRGB_POP() stack[--sp]
+#endif
   int sp = 0;
   int node = J.root;
   int guard = 0;
@@ -512,7 +524,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
           add_work(J, n_box, n_tri);
           return best.tri >= 0;
         }
-        stack[sp++] = first0 ? c1 : c0;
+        DRGB_PUSH(first0 ? c1 : c0);
         node = first0 ? c0 : c1;
         continue;
       } else if (h0) {
@@ -542,7 +554,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
       }
     }
     if (sp == 0) break;
-    node = stack[--sp];
+    node = DRGB_POP();
     if (++guard > (1 << 24)) {
       atomicOr(J.err, ERR_TRAVERSAL_LIMIT);
       break;
@@ -551,6 +563,8 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   add_work(J, n_box, n_tri);
   return best.tri >= 0;
 }
+#undef DRGB_PUSH
+#undef DRGB_POP
 
 }  // namespace drgb
 

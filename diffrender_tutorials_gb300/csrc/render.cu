@@ -228,8 +228,19 @@ constexpr int PX_MAX_SAMPLES = 64;
 // for jobs that have record buffers).  HITS: the adjoint's primary hits are
 // written to (PX_HIT_STORE) or read from (PX_HIT_LOAD) the job's hit buffer,
 // one float4 {t, u, v, triangle} per adjoint sample, instead of re-traced.
+// Resident blocks per SM the register allocation must allow (the kernel is
+// latency bound: more warps hide more of it; values from timing on GB300).
+#ifndef DRGB_PX_MIN_BLOCKS
+#define DRGB_PX_MIN_BLOCKS 4
+#endif
+#ifndef DRGB_PX_MIN_BLOCKS_PATH
+#define DRGB_PX_MIN_BLOCKS_PATH 3
+#endif
+constexpr int px_min_blocks(int mode, bool det, bool hits) {
+  return (det || hits || mode == 0) ? 1 : mode == PATH_DIFFUSE ? DRGB_PX_MIN_BLOCKS_PATH : DRGB_PX_MIN_BLOCKS;
+}
 template <int MODE, bool DET, bool HITS>
-__global__ void __launch_bounds__(PX_THREADS) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
+__global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
                                                        int n_items, int* counter, const int flags) {
   __shared__ JobDev sJ_all[PX_WARPS];
   __shared__ CamDev sC_all[PX_WARPS];
