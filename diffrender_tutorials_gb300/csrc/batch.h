@@ -113,6 +113,7 @@ struct drgb_batch {
       A.perm = J.perm.p;
       A.tri = J.tri.p;
       A.nodes = J.nodes.p;
+      A.nodes4 = J.nodes4.p;
       A.leaf_parent = J.leaf_parent.p;
       A.node_parent = J.node_parent.p;
       A.counters = J.counters.p;

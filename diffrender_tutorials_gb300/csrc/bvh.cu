@@ -311,6 +311,54 @@ __global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const 
   leaf_refit_body(k, perm, n, tri_v, pos, block_tr, tri, nodes, leaf_parent, node_parent, counters);
 }
 
+// 4-wide node of binary internal node p (layout in JobDev::nodes4; used by
+// builds with -DDRGB_BVH4): slots
+// 0-1 hold child 0's two children when child 0 is internal, else child 0
+// itself and an unused slot; slots 2-3 the same for child 1.  The boxes are
+// copied from the refitted binary nodes, so they stay conservative.
+__device__ __forceinline__ void collapse4_body(const float4* nodes, int p, float4* nodes4) {
+  float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
+  int link[4];
+  const float4 q0 = __ldcg(nodes + 4 * p + 0), q1 = __ldcg(nodes + 4 * p + 1);
+  const float4 q2 = __ldcg(nodes + 4 * p + 2), q3 = __ldcg(nodes + 4 * p + 3);
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const int c = __float_as_int(side ? q3.y : q3.x);
+    const int s0 = 2 * side, s1 = 2 * side + 1;
+    if (c >= 0) {
+      const float4 a0 = __ldcg(nodes + 4 * c + 0), a1 = __ldcg(nodes + 4 * c + 1);
+      const float4 a2 = __ldcg(nodes + 4 * c + 2), a3 = __ldcg(nodes + 4 * c + 3);
+      lx[s0] = a0.x; hx[s0] = a0.y; ly[s0] = a0.z; hy[s0] = a0.w; lz[s0] = a2.x; hz[s0] = a2.y;
+      link[s0] = __float_as_int(a3.x);
+      lx[s1] = a1.x; hx[s1] = a1.y; ly[s1] = a1.z; hy[s1] = a1.w; lz[s1] = a2.z; hz[s1] = a2.w;
+      link[s1] = __float_as_int(a3.y);
+    } else {
+      const float4 b = side ? q1 : q0;
+      lx[s0] = b.x; hx[s0] = b.y; ly[s0] = b.z; hy[s0] = b.w;
+      lz[s0] = side ? q2.z : q2.x;
+      hz[s0] = side ? q2.w : q2.y;
+      link[s0] = c;
+      lx[s1] = hx[s1] = ly[s1] = hy[s1] = lz[s1] = hz[s1] = 0.0f;
+      link[s1] = kEmpty4;
+    }
+  }
+  float4* o = nodes4 + 8 * p;
+  o[0] = make_float4(lx[0], lx[1], lx[2], lx[3]);
+  o[1] = make_float4(hx[0], hx[1], hx[2], hx[3]);
+  o[2] = make_float4(ly[0], ly[1], ly[2], ly[3]);
+  o[3] = make_float4(hy[0], hy[1], hy[2], hy[3]);
+  o[4] = make_float4(lz[0], lz[1], lz[2], lz[3]);
+  o[5] = make_float4(hz[0], hz[1], hz[2], hz[3]);
+  o[6] = make_float4(__int_as_float(link[0]), __int_as_float(link[1]), __int_as_float(link[2]),
+                     __int_as_float(link[3]));
+  o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void k_collapse4(const float4* nodes, int n_internal, float4* nodes4) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n_internal) collapse4_body(nodes, p, nodes4);
+}
+
 // ---- batched forms: one launch over the scenes of many jobs --------------
 // The segment tables give, per job, the number of blocks / vertices /
 // internal nodes / triangles (Seg::count) and the first chunk of 256.
@@ -346,6 +394,15 @@ __global__ void k_b_refit(const JobAux* aux, const Seg* segs, int nseg) {
                   A.counters);
 }
 
+// segment table over the jobs' internal node counts
+__global__ void k_b_collapse4(const JobAux* aux, const Seg* segs, int nseg) {
+  const Seg sg = segs[find_seg(segs, nseg, blockIdx.x)];
+  const int p = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
+  if (p >= sg.count) return;
+  const JobAux& A = aux[sg.job];
+  collapse4_body(A.nodes, p, A.nodes4);
+}
+
 // Flatten + refit of every job of a batch (segment tables built by the host:
 // blocks, vertices, internal nodes and triangles per job).
 void launch_b_prepare(const JobAux* d_aux, const Seg* segs[4], const int nsegs[4], const int chunks[4],
@@ -354,6 +411,10 @@ void launch_b_prepare(const JobAux* d_aux, const Seg* segs[4], const int nsegs[4
   if (chunks[1] > 0) k_b_flatten<<<chunks[1], 256, 0, s>>>(d_aux, segs[1], nsegs[1]);
   if (chunks[2] > 0) k_b_zero_counters<<<chunks[2], 256, 0, s>>>(d_aux, segs[2], nsegs[2]);
   if (chunks[3] > 0) k_b_refit<<<chunks[3], 256, 0, s>>>(d_aux, segs[3], nsegs[3]);
+#ifdef DRGB_BVH4
+  if (chunks[2] > 0) k_b_collapse4<<<chunks[2], 256, 0, s>>>(d_aux, segs[2], nsegs[2]);
+  count_launch();
+#endif
   count_launch(4);
 }
 
@@ -386,6 +447,12 @@ void refit_bvh(Job& J, cudaStream_t s) {
   k_leaves_refit<<<(n + 127) / 128, 128, 0, s>>>(J.perm.p, n, J.tri_v.p, J.pos.p, J.block_tr.p, J.tri.p, J.nodes.p,
                                                  J.leaf_parent.p, J.node_parent.p, J.counters.p);
   count_launch();
+#ifdef DRGB_BVH4
+  if (n > 1) {
+    k_collapse4<<<(n - 1 + 127) / 128, 128, 0, s>>>(J.nodes.p, n - 1, J.nodes4.p);
+    count_launch();
+  }
+#endif
 }
 
 void build_bvh(Job& J, cudaStream_t s) {
@@ -394,6 +461,9 @@ void build_bvh(Job& J, cudaStream_t s) {
   J.perm.alloc(std::max(n, 1));
   J.leaf_parent.alloc(std::max(n, 1));
   J.nodes.alloc(4 * (size_t)std::max(n - 1, 1));
+#ifdef DRGB_BVH4
+  J.nodes4.alloc(8 * (size_t)std::max(n - 1, 1));
+#endif
   J.node_parent.alloc(std::max(n - 1, 1));
   J.counters.alloc(std::max(n - 1, 1));
   if (n == 0) {

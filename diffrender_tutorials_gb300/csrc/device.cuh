@@ -30,7 +30,8 @@ __host__ __device__ inline bool model_has_color(int m) {
 }
 __host__ __device__ inline bool model_has_tex(int m) { return m == TEXTURE_COLOR || m == LAMBERT; }
 
-constexpr int kStackSize = 64;
+constexpr int kStackSize = 96;
+constexpr int kEmpty4 = (int)0x80000000;  // unused slot of a 4-wide node
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 
 // Error flags raised by kernels (never trap): the host reads them after a call.
@@ -97,6 +98,14 @@ struct JobDev {
   // BVH: internal nodes (4 float4 each) and leaf triangles in leaf order
   const float4* nodes;
   const float4* tri;     // 3 float4 per leaf: (A, id bits), (e1), (e2)
+  // 4-wide view of the same hierarchy (builds with -DDRGB_BVH4, which
+  // traverse it instead of the binary nodes; measured slower on GB300 than
+  // the binary traversal), 8 float4 per binary internal node p:
+  // the boxes of p's children with every internal child replaced by its two
+  // children (slots 0-1 from child 0, 2-3 from child 1), stored as lo_x[4],
+  // hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4], links[4] (int bits: >= 0
+  // internal node, < 0 leaf ~k, kEmpty4 unused), one unused float4
+  const float4* nodes4;
   int root;              // >= 0 internal node, < 0 leaf ~k, INT_MIN if empty
   int trace_bruteforce;  // 1: test every triangle (reference loop order)
   // model
@@ -210,6 +219,7 @@ struct JobAux {
   const int* perm;
   float4* tri;
   float4* nodes;
+  float4* nodes4;
   const int* leaf_parent;
   const int* node_parent;
   int* counters;
@@ -507,6 +517,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   int guard = 0;
   while (true) {
     if (node >= 0) {
+#ifndef DRGB_BVH4
       const float4 n0 = __ldg(J.nodes + 4 * node + 0);
       const float4 n1 = __ldg(J.nodes + 4 * node + 1);
       const float4 n2 = __ldg(J.nodes + 4 * node + 2);
@@ -534,6 +545,43 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
         node = c1;
         continue;
       }
+#else
+      const float4* q = J.nodes4 + 8 * node;
+      const float4 LX = __ldg(q + 0), HX = __ldg(q + 1), LY = __ldg(q + 2), HY = __ldg(q + 3);
+      const float4 LZ = __ldg(q + 4), HZ = __ldg(q + 5), LK = __ldg(q + 6);
+      const float hi_t = cull_bound(best.t);
+      n_box += 4;
+      const float inf = __int_as_float(0x7f800000);
+      int c0 = __float_as_int(LK.x), c1 = __float_as_int(LK.y), c2 = __float_as_int(LK.z), c3 = __float_as_int(LK.w);
+      float t0 = c0 == kEmpty4 ? inf : slab(LX.x, HX.x, LY.x, HY.x, LZ.x, HZ.x, inv, oi, lo_t, hi_t);
+      float t1 = c1 == kEmpty4 ? inf : slab(LX.y, HX.y, LY.y, HY.y, LZ.y, HZ.y, inv, oi, lo_t, hi_t);
+      float t2 = c2 == kEmpty4 ? inf : slab(LX.z, HX.z, LY.z, HY.z, LZ.z, HZ.z, inv, oi, lo_t, hi_t);
+      float t3 = c3 == kEmpty4 ? inf : slab(LX.w, HX.w, LY.w, HY.w, LZ.w, HZ.w, inv, oi, lo_t, hi_t);
+      // nearest first: a 4-input sorting network on (t, link)
+#define DRGB_CSWAP(ta, ca, tb, cb)                 \
+  if (tb < ta) {                                  \
+    const float tt = ta; ta = tb; tb = tt;        \
+    const int cc = ca; ca = cb; cb = cc;          \
+  }
+      DRGB_CSWAP(t0, c0, t1, c1);
+      DRGB_CSWAP(t2, c2, t3, c3);
+      DRGB_CSWAP(t0, c0, t2, c2);
+      DRGB_CSWAP(t1, c1, t3, c3);
+      DRGB_CSWAP(t1, c1, t2, c2);
+#undef DRGB_CSWAP
+      if (t0 <= hi_t) {
+        if (sp + 3 > kStackSize) {
+          atomicOr(J.err, ERR_STACK_OVERFLOW);
+          add_work(J, n_box, n_tri);
+          return best.tri >= 0;
+        }
+        if (t3 <= hi_t) DRGB_PUSH(c3);
+        if (t2 <= hi_t) DRGB_PUSH(c2);
+        if (t1 <= hi_t) DRGB_PUSH(c1);
+        node = c0;
+        continue;
+      }
+#endif
     } else {
       const int k = ~node;
       const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);

@@ -363,6 +363,7 @@ void sync_dev(Job& J) {
   d.meshes = J.meshdev.p;
   d.tr_inv0 = J.tr_inv0.p;
   d.nodes = J.nodes.p;
+  d.nodes4 = J.nodes4.p;
   d.tri = J.tri.p;
   d.root = J.root;
   d.trace_bruteforce = J.trace_bruteforce;

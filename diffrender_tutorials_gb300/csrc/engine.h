@@ -124,6 +124,7 @@ struct Job {
   DevBuf<float> tr_inv0;   // inverse transforms of mesh 0 at the first commit
   // BVH
   DevBuf<float4> nodes, tri;
+  DevBuf<float4> nodes4;   // 4-wide view of the binary hierarchy, refreshed after each refit
   DevBuf<int> perm, leaf_parent, node_parent, counters;
   DevBuf<uint32_t> sort_keys[2], sort_hist;
   DevBuf<int> sort_vals[2];

@@ -224,6 +224,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.meshes = reinterpret_cast<const MeshDev*>(base + o_md);
     d.tr_inv0 = J.tr_inv0.p;
     d.nodes = J.nodes.p;
+    d.nodes4 = J.nodes4.p;
     d.tri = J.tri.p;
     d.root = J.root;
     d.trace_bruteforce = J.trace_bruteforce;
