@@ -231,6 +231,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
     p.flags = D.OptimizerParameters._OPT_POS | D.OptimizerParameters._OPT_COL
     opt = D.CreateSimpleOptimizer()
     opt.Init(isc, r, cams, targets, p)
+    tuned = opt.autotune(3)
     stream = torch.cuda.ExternalStream(r.stream(), device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -333,7 +334,8 @@ def drgb_arm(args, w, ws, rank, local, pg):
         "config": {"workload": w["name"], "triangles": n_tri, "vertices": n_v, "resolution": w["res"],
                    "views": w["views"], "spp": w["spp"], "edge_samples_per_view": edge_samples,
                    "shading": S.name, "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": "replicas", "step": "d_render_and_compare + Adam + LBVH refit (CUDA graph)"},
+                   "parallelism": "replicas", "step": "d_render_and_compare + Adam + LBVH refit (CUDA graph)",
+                   "autotuned": tuned},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -393,6 +395,7 @@ def batch_arm(args, ws, rank, local, pg):
     b = D.BatchOptimizer(device=local)
     for isc, cams, tgt, sp in setups:
         b.add_job(isc, cams, tgt, D.DiffRenderSettings(D.SHADING_MODEL(sp.mode), sp.spp), params())
+    tuned = b.autotune(2)
     b.run(args.warmup)
     bs = torch.cuda.ExternalStream(b.stream(), device=local)
     st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -419,6 +422,7 @@ def batch_arm(args, ws, rank, local, pg):
         r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL(sp.mode), sp.spp), device=local)
         o = D.CreateSimpleOptimizer()
         o.Init(isc, r, cams, tgt, params())
+        o.autotune(2)
         o.run_async(args.warmup)
         opts.append((r, o))
     torch.cuda.synchronize()
@@ -444,7 +448,8 @@ def batch_arm(args, ws, rank, local, pg):
                    "triangles_min": min(tris), "triangles_max": max(tris),
                    "resolutions": sorted({sp.cams[0].width for *_, sp in setups}),
                    "spp": sorted({sp.spp for *_, sp in setups}), "l2": "flushed (256 MiB write) before every step",
-                   "parallelism": "replicas"},
+                   "parallelism": "replicas", "autotuned": tuned,
+                   "plain_autotuned": "each job's tile and grids by drgb_optimizer_autotune"},
         "plain": {"value": plain, "unit": "job-iters/s", "ms_per_step": plain_ms / args.steps,
                   "how": "each job's own iteration graph, one job at a time"},
         "speedup_vs_plain": batched / plain,

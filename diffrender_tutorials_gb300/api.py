@@ -345,6 +345,15 @@ class IOptimizer:
         N.check(N.load().drgb_optimizer_profile(self._r._h, int(num_iters), _ptr(out)))
         return {k: float(v) for k, v in zip(("pixels", "edges", "optimizer", "refit", "total"), out)}
 
+    def autotune(self, trial_iters: int = 3) -> dict:
+        """Picks the work-item shape and the persistent grid sizes by timing
+        the gradient passes of the optimiser's views (the state is unchanged)."""
+        out = np.zeros(4, np.int32)
+        ms = C.c_float(0.0)
+        N.check(N.load().drgb_optimizer_autotune(self._r._h, int(trial_iters), _ptr(out), C.byref(ms)))
+        return {"tile": (int(out[0]), int(out[1])), "pixel_blocks_per_sm": int(out[2]),
+                "edge_blocks_per_sm": int(out[3]), "ms": float(ms.value)}
+
     def count_work(self):
         """Rays, box tests, triangle tests and shaded edge samples of one iteration."""
         out = np.zeros(4, np.uint64)
@@ -441,6 +450,14 @@ class BatchOptimizer:
         out = np.zeros(max(1, done.value), np.float32)
         N.check(N.load().drgb_batch_job_losses(self._h, int(job_id), 0, done.value, _ptr(out), C.byref(done)))
         return out[:done.value]
+
+    def autotune(self, trial_iters: int = 3) -> dict:
+        """Picks the grid sizes of the batch's shared launches by timing its
+        gradient passes (the jobs' state is unchanged)."""
+        out = np.zeros(2, np.int32)
+        ms = C.c_float(0.0)
+        N.check(N.load().drgb_batch_autotune(self._h, int(trial_iters), _ptr(out), C.byref(ms)))
+        return {"pixel_blocks_per_sm": int(out[0]), "edge_blocks_per_sm": int(out[1]), "ms": float(ms.value)}
 
     def device_bytes(self, job_id: int) -> int:
         return int(N.load().drgb_batch_job_device_bytes(self._h, int(job_id)))

@@ -259,6 +259,50 @@ int drgb_batch_get_mesh(drgb_batch* b, int32_t id, int mesh_id, float* vertices,
   return drgb_optimizer_get_mesh(r, mesh_id, vertices, colors, texture, transforms);
 }
 
+int drgb_batch_autotune(drgb_batch* b, int trial_iters, int32_t* chosen, float* best_ms) {
+  return guard([&] {
+    require(b != nullptr && trial_iters >= 1, "bad arguments");
+    require(!b->order.empty(), "empty batch", DRGB_ERR_STATE);
+    DRGB_CUDA(cudaSetDevice(b->device));
+    b->rebuild();
+    cudaEvent_t e0, e1;
+    DRGB_CUDA(cudaEventCreate(&e0));
+    DRGB_CUDA(cudaEventCreate(&e1));
+    auto trial = [&] {
+      b->enqueue_iteration(false);
+      DRGB_CUDA(cudaEventRecord(e0, b->stream));
+      for (int i = 0; i < trial_iters; i++) b->enqueue_iteration(false);
+      DRGB_CUDA(cudaEventRecord(e1, b->stream));
+      DRGB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      DRGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms / trial_iters;
+    };
+    float best = 1e30f;
+    for (int which = 0; which < 2; which++) {
+      int& knob = which == 0 ? b->px_blocks_per_sm : b->edge_blocks_per_sm;
+      int bk = knob;
+      for (int k : {2, 4, 8, 16}) {
+        knob = k;
+        const float ms = trial();
+        if (ms < best) {
+          best = ms;
+          bk = k;
+        }
+      }
+      knob = bk;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->graph_valid = false;
+    if (chosen) {
+      chosen[0] = b->px_blocks_per_sm;
+      chosen[1] = b->edge_blocks_per_sm;
+    }
+    if (best_ms) *best_ms = best;
+  });
+}
+
 int64_t drgb_batch_job_device_bytes(drgb_batch* b, int32_t id) {
   int64_t bytes = -1;
   guard([&] {

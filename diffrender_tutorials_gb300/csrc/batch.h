@@ -182,7 +182,10 @@ struct drgb_batch {
     graph_valid = false;
   }
 
-  void enqueue_iteration() {
+  int px_blocks_per_sm = 8, edge_blocks_per_sm = 8;  // shared persistent grids (autotuned)
+
+  // update = false: the gradient passes only (autotuning; state unchanged)
+  void enqueue_iteration(bool update = true) {
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
       DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
@@ -191,15 +194,17 @@ struct drgb_batch {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_clear(J, stream);
     }
-    launch_pixels(d_jobs.p, d_items.p, n_items, d_counter.p, PX_FWD | PX_LOSS | PX_ADJ, sm_count * 8, stream, mode,
-                  det_any);
+    launch_pixels(d_jobs.p, d_items.p, n_items, d_counter.p, PX_FWD | PX_LOSS | PX_ADJ, sm_count * px_blocks_per_sm,
+                  stream, mode, det_any);
     launch_loss_finalize(d_jobs.p, (int)order.size(), stream);
     launch_b_edges(d_jobs.p, seg_proj.p, n_proj, c_proj, seg_pmf.p, n_pmf, c_pmf, seg_pairs.p, n_pairs, seg_sel.p,
-                   n_sel, c_sel, queue.p, queue_count.p, (int)queue.n, sm_count * 8, stream, det_any);
+                   n_sel, c_sel, queue.p, queue_count.p, (int)queue.n, sm_count * edge_blocks_per_sm, stream,
+                   det_any);
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_reduce(J, sm_count, stream);
     }
+    if (!update) return;
     launch_b_opt(d_aux.p, (int)order.size(), seg_mom.p, n_mom, c_mom, seg_apply.p, n_apply, c_apply, stream);
     const Seg* sp[4] = {seg_btr.p, seg_flat.p, seg_cnt.p, seg_refit.p};
     launch_b_prepare(d_aux.p, sp, n_prep, c_prep, stream);

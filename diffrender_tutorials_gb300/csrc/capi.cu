@@ -99,6 +99,14 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         break;
       }
       case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
+      case DRGB_OPT_PIXEL_GRID:
+        require(value >= 1 && value <= 64, "pixel grid: 1..64 blocks per SM");
+        r->px_blocks_per_sm = (int)value;
+        break;
+      case DRGB_OPT_EDGE_GRID:
+        require(value >= 1 && value <= 64, "edge grid: 1..64 blocks per SM");
+        r->edge_blocks_per_sm = (int)value;
+        break;
       case DRGB_OPT_ADJOINT_HITS: {
         Job& J = r->job;
         J.store_hits = value ? 1 : 0;
@@ -466,6 +474,78 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
     J.opt.host_iter += n_iters;
     for (int k = 0; k < 5; k++) out_ms[k] = (float)(acc[k] / n_iters);
     r->check_flags();
+  });
+}
+
+// Mean device time (ms) of `iters` gradient passes (forward, loss, interior
+// adjoint, edges) of the optimiser's views, without the update: the
+// optimiser's state does not change.
+static float time_gradient_passes(drgb_renderer* r, int iters) {
+  cudaEvent_t e0, e1;
+  DRGB_CUDA(cudaEventCreate(&e0));
+  DRGB_CUDA(cudaEventCreate(&e1));
+  r->enqueue_iteration(false);  // warm-up
+  DRGB_CUDA(cudaEventRecord(e0, r->stream));
+  for (int i = 0; i < iters; i++) r->enqueue_iteration(false);
+  DRGB_CUDA(cudaEventRecord(e1, r->stream));
+  DRGB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  DRGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / iters;
+}
+
+int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, float* best_ms) {
+  return guard([&] {
+    check_renderer(r);
+    require(r->job.opt.active, "optimiser not initialised", DRGB_ERR_STATE);
+    require(trial_iters >= 1, "trial_iters must be >= 1");
+    r->set_device();
+    Job& J = r->job;
+    const int S = J.S;
+    // 1. work-item shape: 32 or 64 samples (one or two warp passes), at most 32 pixels
+    std::vector<std::pair<int, int>> tiles;
+    for (int n_samples : {32, 64}) {
+      const int P = std::max(1, std::min(32, n_samples / std::max(1, S)));
+      for (int th = 1; th * th <= P; th *= 2)
+        if (P % th == 0 && P / th >= th) tiles.emplace_back(P / th, th);
+    }
+    float best = 1e30f;
+    int bw = J.tile_w, bh = J.tile_h;
+    for (auto [tw, th] : tiles) {
+      r->apply_tile(tw, th);
+      const float ms = time_gradient_passes(r, trial_iters);
+      if (ms < best) {
+        best = ms;
+        bw = tw;
+        bh = th;
+      }
+    }
+    r->apply_tile(bw, bh);
+    // 2. persistent grid of the pixel kernel, 3. of the edge-shading kernel
+    for (int which = 0; which < 2; which++) {
+      int& knob = which == 0 ? r->px_blocks_per_sm : r->edge_blocks_per_sm;
+      int bk = knob;
+      for (int k : {2, 4, 8, 16}) {
+        knob = k;
+        const float ms = time_gradient_passes(r, trial_iters);
+        if (ms < best) {
+          best = ms;
+          bk = k;
+        }
+      }
+      knob = bk;
+    }
+    r->graph_valid = false;
+    r->check_flags();
+    if (chosen) {
+      chosen[0] = J.tile_w;
+      chosen[1] = J.tile_h;
+      chosen[2] = r->px_blocks_per_sm;
+      chosen[3] = r->edge_blocks_per_sm;
+    }
+    if (best_ms) *best_ms = best;
   });
 }
 

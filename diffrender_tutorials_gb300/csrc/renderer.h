@@ -64,8 +64,9 @@ struct drgb_renderer {
 
   void set_device() const { DRGB_CUDA(cudaSetDevice(device)); }
   void require_commit() const { require(job.committed, "no scene committed (call drgb_commit first)", DRGB_ERR_STATE); }
-  int px_grid() const { return sm_count * 8; }
-  int edge_grid() const { return sm_count * 8; }
+  int px_blocks_per_sm = 8, edge_blocks_per_sm = 8;  // persistent grids (autotuned or set by option)
+  int px_grid() const { return sm_count * px_blocks_per_sm; }
+  int edge_grid() const { return sm_count * edge_blocks_per_sm; }
 
   // Pixel work items for the current views: view-major, tiles row-major.
   void make_items() {
@@ -170,6 +171,17 @@ struct drgb_renderer {
       if (f & ERR_TRAVERSAL_LIMIT) m += " (traversal step limit)";
       throw CudaError(m, DRGB_ERR_KERNEL);
     }
+  }
+
+  // Work items of a new tile shape, with the buffers that depend on them.
+  void apply_tile(int tw, int th) {
+    job.tile_w = tw;
+    job.tile_h = th;
+    make_items();
+    if (job.det && job.rec_key.p) det_buffers(job, stream);
+    if (job.store_hits) hit_buffers();
+    push_dev();
+    graph_valid = false;
   }
 
   // Forward + loss + interior adjoint + edges of the current views; grad is

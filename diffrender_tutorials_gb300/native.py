@@ -15,6 +15,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "drgb.h")
 DRGB_OK = 0
 # renderer / batch options (drgb_renderer_set_option, drgb_batch_set_option)
 OPT_TRACE_BRUTEFORCE, OPT_TILE_W, OPT_TILE_H, OPT_USE_GRAPH, OPT_DETERMINISTIC, OPT_ADJOINT_HITS = 1, 2, 3, 4, 5, 6
+OPT_PIXEL_GRID, OPT_EDGE_GRID = 7, 8
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
           -5: "kernel error flag", -6: "unsupported", -7: "no CUDA device"}
 
@@ -128,6 +129,8 @@ _SIGS = {
     "drgb_estimate_job_bytes": (C.c_int64, [C.c_int, C.POINTER(SceneDesc), C.POINTER(Camera), C.c_int]),
     "drgb_optimizer_profile": (C.c_int, [VP, C.c_int, VP]),
     "drgb_count_work": (C.c_int, [VP, VP]),
+    "drgb_optimizer_autotune": (C.c_int, [VP, C.c_int, VP, C.POINTER(C.c_float)]),
+    "drgb_batch_autotune": (C.c_int, [VP, C.c_int, VP, C.POINTER(C.c_float)]),
 }
 
 _lib = None

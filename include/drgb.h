@@ -61,9 +61,11 @@ enum {
   DRGB_OPT_DETERMINISTIC = 5,    /* 1: gradients are summed in a fixed order (records sorted by gradient
                                     index, then segmented sums) instead of by float atomics, so a job's
                                     gradient is bit-identical run to run, alone or in a batch; default 0 */
-  DRGB_OPT_ADJOINT_HITS = 6      /* 1: the interior adjoint reads the primary hits of its samples from a buffer
+  DRGB_OPT_ADJOINT_HITS = 6,     /* 1: the interior adjoint reads the primary hits of its samples from a buffer
                                     written by a separate tracing pass (16 bytes per sample) instead of
                                     re-tracing them; 0 (default): re-trace.  Single renderers only. */
+  DRGB_OPT_PIXEL_GRID = 7,       /* blocks per SM of the persistent pixel kernel (default 8) */
+  DRGB_OPT_EDGE_GRID = 8         /* blocks per SM of the persistent edge-shading kernel (default 8) */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -322,6 +324,17 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms);
  * instrumented replay: counts[0] rays traced, [1] ray/box tests,
  * [2] ray/triangle tests, [3] edge samples shaded. */
 int drgb_count_work(drgb_renderer* r, uint64_t* counts);
+
+/* ---- autotuning (no reference counterpart) ------------------------------
+ * Times the gradient passes of the optimiser's views (no update: the
+ * optimiser's state does not change) for candidate work-item shapes (32 or
+ * 64 samples per item) and persistent grid sizes (2, 4, 8, 16 blocks per SM
+ * for the pixel and the edge-shading kernels), by coordinate descent, and
+ * keeps the fastest.  chosen (may be NULL) receives tile_w, tile_h, pixel
+ * blocks per SM, edge blocks per SM; best_ms the mean time of the passes. */
+int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, float* best_ms);
+/* The same for a batch: the grid sizes of its shared launches (2 ints). */
+int drgb_batch_autotune(drgb_batch* b, int trial_iters, int32_t* chosen, float* best_ms);
 
 #ifdef __cplusplus
 }
