@@ -33,6 +33,8 @@ class SHADING_MODEL(enum.IntEnum):
     VERTEX_COLOR = 2
     TEXTURE_COLOR = 3
     LAMBERT = 4
+    PHONG = 5
+    GGX = 6
     LAMBERT_POINT_VCOLOR = 16  # point light + per-vertex albedo (no reference counterpart)
     PATH_DIFFUSE = 17          # fixed-depth diffuse path tracer (no reference counterpart)
 

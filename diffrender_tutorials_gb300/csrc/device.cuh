@@ -21,6 +21,8 @@ enum Model : int {
   VERTEX_COLOR = 2,
   TEXTURE_COLOR = 3,
   LAMBERT = 4,
+  PHONG = 5,
+  GGX = 6,
   LAMBERT_POINT_VCOLOR = 16,
   PATH_DIFFUSE = 17,
 };
@@ -28,7 +30,9 @@ enum Model : int {
 __host__ __device__ inline bool model_has_color(int m) {
   return m == VERTEX_COLOR || m == LAMBERT_POINT_VCOLOR || m == PATH_DIFFUSE;
 }
-__host__ __device__ inline bool model_has_tex(int m) { return m == TEXTURE_COLOR || m == LAMBERT; }
+__host__ __device__ inline bool model_has_tex(int m) {
+  return m == TEXTURE_COLOR || m == LAMBERT || m == PHONG || m == GGX;
+}
 
 constexpr int kStackSize = 96;
 constexpr int kEmpty4 = (int)0x80000000;  // unused slot of a 4-wide node

@@ -479,6 +479,8 @@ static void launch_pixels_t(const JobDev* d_jobs, const int4* d_items, int n_ite
     case VERTEX_COLOR: k_pixels<VERTEX_COLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
     case TEXTURE_COLOR: k_pixels<TEXTURE_COLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
     case LAMBERT: k_pixels<LAMBERT, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case PHONG: k_pixels<PHONG, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case GGX: k_pixels<GGX, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
     case LAMBERT_POINT_VCOLOR:
       k_pixels<LAMBERT_POINT_VCOLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
       break;

@@ -295,6 +295,44 @@ __device__ inline f3 path_diffuse_p(const JobDev& J, const Surf& first, uint32_t
 // compiles a single model (no code, hence no registers, for the others);
 // MODE == 0 switches on the job's model at run time.  Inactive lanes return
 // the background.
+// Lit term of shade<PHONG> (shade_lambert.cpp:45-77): Kd*max(0,n.-L) +
+// Ks*pow(max(0,n.r),32).  The reference's unqualified pow(float, int)
+// resolves to pow(double, double), so the sum is formed in double and
+// rounded to float where it multiplies the light colour.
+__device__ __forceinline__ float phong_term(f3 n, f3 light_dir) {
+  const float ndl = ref_max(0.0f, dot(n, light_dir * -1.0f));
+  const f3 refl = light_dir - n * (2.0f * dot(n, light_dir));
+  const double spec = pow((double)ref_max(0.0f, dot(n, refl)), 32.0);
+  return (float)((double)(1.0f * ndl) + (double)1.0f * spec);
+}
+
+// LightingFuncGGX (shade_lambert.cpp:90-124) with the reference's float /
+// double promotions: the D denominator and the Fresnel term are evaluated in
+// double (double literals and pow) and stored to float.
+__device__ __forceinline__ float ggx_specular(f3 N, f3 V, f3 L, float roughness, float F0) {
+  const float alpha = roughness * roughness;
+  const f3 H = normalize(V + L);
+  const float dotNL = ref_max(0.0f, ref_min(1.0f, dot(N, L)));
+  const float dotNV = ref_max(0.0f, ref_min(1.0f, dot(N, V)));
+  const float dotNH = ref_max(0.0f, ref_min(1.0f, dot(N, H)));
+  const float dotLH = ref_max(0.0f, ref_min(1.0f, dot(L, H)));
+  const float alphaSqr = alpha * alpha;
+  const float pi = 3.14159f;
+  const float denom = (float)((double)(dotNH * dotNH) * ((double)alphaSqr - 1.0) + 1.0);
+  const float D = alphaSqr / (pi * denom * denom);
+  const float dotLH5 = (float)pow((double)(1.0f - dotLH), 5.0);
+  const float F = (float)((double)F0 + (1.0 - (double)F0) * (double)dotLH5);
+  const float k = alpha / 2.0f;
+  const float vis = (1.0f / (dotNL * (1.0f - k) + k)) * (1.0f / (dotNV * (1.0f - k) + k));
+  return dotNL * D * F * vis;
+}
+
+// Lit term of shade<GGX> (shade_lambert.cpp:128-161): max(0,n.-L) + GGX.
+__device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
+  const float ggx = ggx_specular(n, ray_dir * -1.0f, light_dir * -1.0f, 0.2f, 0.8f);
+  return ref_max(0.0f, dot(n, light_dir * -1.0f)) + ggx;
+}
+
 template <int MODE, bool WARP>
 __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active) {
   const int mode = MODE ? MODE : J.mode;
@@ -332,6 +370,30 @@ __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float 
       if (!hit) return mk(0.0f, 0.0f, 0.0f);
       const f3 lit = (mk(1.0f, 0.5f, 0.2f) * (occ ? 0.0f : 1.0f)) * ndl;
       return (lit + mk(1.0f, 1.0f, 1.0f) * 0.1f) * diffuse;
+    }
+    case PHONG:
+    case GGX: {
+      // shade<PHONG> / shade<GGX>: light direction, colour (1,0.5,0.2),
+      // ambient Ka*(1,1,1), shadow ray toward the light, times the texture
+      const bool phong = mode == PHONG;
+      const f3 light_dir = phong ? normalize(mk(0.0f, -0.25f, -1.0f)) : normalize(mk(0.15f, 0.0f, -1.0f));
+      const f3 to_light = light_dir * -1.0f;
+      f3 diffuse = mk(0.0f, 0.0f, 0.0f), surf_pos = mk(0.0f, 0.0f, 0.0f);
+      float term = 0.0f;
+      if (hit) {
+        const MeshDev& m = J.meshes[J.blocks[s.block].mesh];
+        const float2 tc = interp_tc(J, s);
+        const f3 n = interp(ld3(J.nrm, s.A), ld3(J.nrm, s.B), ld3(J.nrm, s.C), u, v);
+        diffuse = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+        surf_pos = s.ro + s.rd * (s.h.t - 1e-5f);
+        term = phong ? phong_term(n, light_dir) : ggx_term(n, s.rd, light_dir);
+      }
+      // (colour * vis) * 0 is 0 for either visibility: trace only when lit
+      Hit sh;
+      const bool occ = trace_p<true, WARP>(J, surf_pos, to_light, 0.0f, 1e9f, hit && term != 0.0f, sh);
+      if (!hit) return mk(0.0f, 0.0f, 0.0f);
+      const f3 lit = (mk(1.0f, 0.5f, 0.2f) * (occ ? 0.0f : 1.0f)) * term;
+      return (lit + mk(1.0f, 1.0f, 1.0f) * (phong ? 0.1f : 0.01f)) * diffuse;
     }
     case LAMBERT_POINT_VCOLOR: {
       const float k = lpv_factor_p<WARP>(J, s, hit);

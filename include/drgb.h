@@ -43,6 +43,8 @@ enum {
   DRGB_VERTEX_COLOR = 2,
   DRGB_TEXTURE_COLOR = 3,
   DRGB_LAMBERT = 4,
+  DRGB_PHONG = 5,                 /* shade_lambert.cpp:45-84 */
+  DRGB_GGX = 6,                   /* shade_lambert.cpp:86-168 */
   DRGB_LAMBERT_POINT_VCOLOR = 16, /* point light, per-vertex albedo, ambient; no reference counterpart */
   DRGB_PATH_DIFFUSE = 17          /* fixed-depth diffuse path tracer with counter RNG; no reference counterpart */
 };

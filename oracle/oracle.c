@@ -625,6 +625,53 @@ static f3 shade(const ctx_t* c, f2 sp) {
       f3 lit = scl3(scl3(light_color, sh), ndl);
       return mul3(add3(lit, ambient), diffuse);
     }
+    case ORC_PHONG:   /* shade_lambert.cpp:45-77 */
+    case ORC_GGX: {   /* shade_lambert.cpp:128-161 */
+      const int phong = c->mode == ORC_PHONG;
+      const f3 light_dir = phong ? norm3(v3(0.0f, -0.25f, -1.0f)) : norm3(v3(0.15f, 0.0f, -1.0f));
+      const f3 light_color = v3(1.0f, 0.5f, 0.2f);
+      const float Ka = phong ? 0.1f : 0.01f;
+      const float BIAS = 1e-5f;
+      const orc_mesh* m = s->meshes + sf.h.geom;
+      f2 tc = interp2(s->tc[sf.A], s->tc[sf.B], s->tc[sf.C], u, v);
+      f3 n = interp3(s->nrm[sf.A], s->nrm[sf.B], s->nrm[sf.C], u, v);
+      f3 diffuse = sample_bilinear(tc, m->tex_w, m->tex_h, m->texture);
+      f3 surf_pos = add3(sf.ro, scl3(sf.rd, sf.h.t - BIAS));
+      const f3 to_light = scl3(light_dir, -1.0f);
+      float term;
+      if (phong) {
+        /* Kd*max(0,n.-L) + Ks*pow(max(0,n.r),32); the reference's pow(float,int)
+         * is pow(double,double), so the sum is a double */
+        const float ndl = maxf_ref(0.0f, dot3(n, to_light));
+        const f3 refl = sub3(light_dir, scl3(n, 2.0f * dot3(n, light_dir)));
+        const double spec = pow((double)maxf_ref(0.0f, dot3(n, refl)), 32.0);
+        term = (float)((double)(1.0f * ndl) + (double)1.0f * spec);
+      } else {
+        /* LightingFuncGGX(n, -view, -light, 0.2, 0.8), shade_lambert.cpp:90-124 */
+        const f3 N = n, V = scl3(sf.rd, -1.0f), L = to_light;
+        const float roughness = 0.2f, F0 = 0.8f;
+        const float alpha = roughness * roughness;
+        const f3 H = norm3(add3(V, L));
+        const float dotNL = maxf_ref(0.0f, minf_ref(1.0f, dot3(N, L)));
+        const float dotNV = maxf_ref(0.0f, minf_ref(1.0f, dot3(N, V)));
+        const float dotNH = maxf_ref(0.0f, minf_ref(1.0f, dot3(N, H)));
+        const float dotLH = maxf_ref(0.0f, minf_ref(1.0f, dot3(L, H)));
+        const float alphaSqr = alpha * alpha;
+        const float pi = 3.14159f;
+        const float denom = (float)((double)(dotNH * dotNH) * ((double)alphaSqr - 1.0) + 1.0);
+        const float D = alphaSqr / (pi * denom * denom);
+        const float dotLH5 = (float)pow((double)(1.0f - dotLH), 5.0);
+        const float F = (float)((double)F0 + (1.0 - (double)F0) * (double)dotLH5);
+        const float k = alpha / 2.0f;
+        const float vis = (1.0f / (dotNL * (1.0f - k) + k)) * (1.0f / (dotNV * (1.0f - k) + k));
+        const float ggx = dotNL * D * F * vis;
+        term = maxf_ref(0.0f, dot3(n, to_light)) + ggx;
+      }
+      /* (colour * vis) * 0 is 0 for either visibility: trace only when lit */
+      const float sh = (term != 0.0f && nearest_hit(s, surf_pos, to_light, 0.0f, 1e9f).prim != 0xFFFFFFFFu) ? 0.0f : 1.0f;
+      const f3 lit = scl3(scl3(light_color, sh), term);
+      return mul3(add3(lit, scl3(v3(1, 1, 1), Ka)), diffuse);
+    }
     case ORC_LAMBERT_POINT_VCOLOR: {
       const f3 alb = interp3(s->col[sf.A], s->col[sf.B], s->col[sf.C], u, v);
       return scl3(alb, lpv_factor(c, &sf));
@@ -646,7 +693,9 @@ typedef struct {
 } dlayout_t;
 
 static int mode_has_color(int mode) { return mode == ORC_VERTEX_COLOR || mode == ORC_LAMBERT_POINT_VCOLOR || mode == ORC_PATH_DIFFUSE; }
-static int mode_has_tex(int mode) { return mode == ORC_TEXTURE_COLOR || mode == ORC_LAMBERT; }
+static int mode_has_tex(int mode) {
+  return mode == ORC_TEXTURE_COLOR || mode == ORC_LAMBERT || mode == ORC_PHONG || mode == ORC_GGX;
+}
 
 static dlayout_t make_layout(const orc_mesh* m, int mode) {
   dlayout_t L;
@@ -806,7 +855,7 @@ static void shade_grad(const ctx_t* c, const dmap_t* dm, f2 sp, f3 val, float* g
     col[3 * A + 0] += ca.x; col[3 * A + 1] += ca.y; col[3 * A + 2] += ca.z;
     col[3 * B + 0] += cb.x; col[3 * B + 1] += cb.y; col[3 * B + 2] += cb.z;
     col[3 * C + 0] += cc.x; col[3 * C + 1] += cc.y; col[3 * C + 2] += cc.z;
-  } else if (c->mode == ORC_TEXTURE_COLOR || c->mode == ORC_LAMBERT) {
+  } else if (mode_has_tex(c->mode)) { /* PHONG, GGX: shade_lambert.cpp:80-84, 163-168 */
     if (L->tex_off < 0) return;
     const f2 tc = interp2(s->tc[sf.A], s->tc[sf.B], s->tc[sf.C], u, v);
     sample_bilinear_grad(val, tc, m->tex_w, m->tex_h, g + L->tex_off);

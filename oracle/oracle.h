@@ -30,6 +30,8 @@ enum {
   ORC_VERTEX_COLOR = 2,
   ORC_TEXTURE_COLOR = 3,
   ORC_LAMBERT = 4,
+  ORC_PHONG = 5,
+  ORC_GGX = 6,
   ORC_LAMBERT_POINT_VCOLOR = 16, /* point light + per-vertex albedo */
   ORC_PATH_DIFFUSE = 17          /* fixed-depth diffuse path tracer, counter RNG */
 };

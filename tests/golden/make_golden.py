@@ -28,7 +28,7 @@ from diffrender_tutorials_gb300.scene import (Scene, TriangleMesh, Texture, make
                                               perturb_vertices, identity4)
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-SIL, VC, TEX, LAMBERT = 1, 2, 3, 4
+SIL, VC, TEX, LAMBERT, PHONG, GGX = 1, 2, 3, 4, 5, 6
 
 
 def run(items):
@@ -120,7 +120,7 @@ def main():
         save(f"render_cube_m{mode}_spp{spp}", **items, **prefixed("out.", out))
     ts = Scene()
     ts.add_mesh(textured_sphere())
-    for mode in (TEX, LAMBERT):
+    for mode in (TEX, LAMBERT, PHONG, GGX):
         items = {"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),
                  **scene_items(ts), **cam_items([Cam((0.5, 0.8, 2.6), 48, 48)])}
         out = run(items)
@@ -152,7 +152,7 @@ def main():
     out = run(items)
     save("drender_cube_2views", **items, **prefixed("out.", out))
 
-    # textured sphere: texture derivatives (TEXTURE_COLOR) and Lambert
+    # textured sphere: texture derivatives (TEXTURE_COLOR, Lambert, Phong, GGX)
     tsph = textured_sphere()
     isph = tsph.copy()
     isph.textures[0].data[:] = 0.5
@@ -161,7 +161,7 @@ def main():
     tsc.add_mesh(tsph)
     isc.add_mesh(isph)
     cams = [Cam((0.5, 0.8, 2.6), 40, 40)]
-    for mode in (TEX, LAMBERT):
+    for mode in (TEX, LAMBERT, PHONG, GGX):
         tg = run({"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),
                   **scene_items(tsc), **cam_items(cams)})["images"]
         items = {"task": np.array([4], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([4], np.int32),

@@ -79,7 +79,8 @@ def test_hits_bit_exact_vs_reference(name, bruteforce):
 
 @pytest.mark.parametrize("name,mode,spp", [("render_cube_m2_spp16", 2, 16), ("render_cube_m1_spp9", 1, 9),
                                            ("render_cube_m2_spp8", 2, 8), ("render_sphere_m3", 3, 4),
-                                           ("render_sphere_m4", 4, 4)])
+                                           ("render_sphere_m4", 4, 4), ("render_sphere_m5", 5, 4),
+                                           ("render_sphere_m6", 6, 4)])
 def test_render_bit_exact_vs_reference(name, mode, spp):
     d = load(name)
     sc = scene_from(d)
@@ -90,7 +91,7 @@ def test_render_bit_exact_vs_reference(name, mode, spp):
 
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
-                                       ("drc_sphere_m4", 4)])
+                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6)])
 def test_d_render_and_compare_vs_reference(name, mode):
     d = load(name)
     sc = scene_from(d)

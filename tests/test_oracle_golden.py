@@ -64,7 +64,8 @@ def test_hits_bit_exact(name):
 
 @pytest.mark.parametrize("name,mode,spp", [("render_cube_m2_spp16", 2, 16), ("render_cube_m1_spp9", 1, 9),
                                            ("render_cube_m2_spp8", 2, 8), ("render_sphere_m3", 3, 4),
-                                           ("render_sphere_m4", 4, 4)])
+                                           ("render_sphere_m4", 4, 4), ("render_sphere_m5", 5, 4),
+                                           ("render_sphere_m6", 6, 4)])
 def test_render_bit_exact(name, mode, spp):
     d = load(name)
     img = O.render(scene_from(d), cams_from(d), mode, spp)
@@ -73,7 +74,7 @@ def test_render_bit_exact(name, mode, spp):
 
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
-                                       ("drc_sphere_m4", 4)])
+                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6)])
 def test_d_render_and_compare(name, mode):
     d = load(name)
     loss, ds, imgs = O.d_render_and_compare(scene_from(d), cams_from(d), mode, int(d["spp"][0]), d["targets"],
