@@ -215,15 +215,20 @@ def read_traffic():
     return None
 
 
+BVH_BUILDERS = {"lbvh": 0, "sah": 1}
+
+
 def drgb_arm(args, w, ws, rank, local, pg):
     import torch
     import diffrender_tutorials_gb300 as D
     from diffrender_tutorials_gb300 import build as B
+    from diffrender_tutorials_gb300 import native as N
     B.build()
     torch.cuda.set_device(local)
     ts, isc, cams = make_problem(w)
     S = D.SHADING_MODEL(w["mode"])
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
+    r.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
     r.commit(ts)
     targets = r.render(ts, cams)
     p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.01)
@@ -260,6 +265,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
 
     # e2e: the public C-ABI call with host buffers (pinned), one call per step
     r2 = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
+    r2.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
     r2.commit(isc)
     tg_pinned = torch.empty(targets.size, dtype=torch.float32, pin_memory=True).numpy()
     tg_pinned[:] = targets.reshape(-1)
@@ -334,7 +340,8 @@ def drgb_arm(args, w, ws, rank, local, pg):
         "config": {"workload": w["name"], "triangles": n_tri, "vertices": n_v, "resolution": w["res"],
                    "views": w["views"], "spp": w["spp"], "edge_samples_per_view": edge_samples,
                    "shading": S.name, "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": "replicas", "step": "d_render_and_compare + Adam + LBVH refit (CUDA graph)",
+                   "parallelism": "replicas", "step": "d_render_and_compare + Adam + BVH refit (CUDA graph)",
+                   "bvh": args.bvh,
                    "autotuned": tuned},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "clocks": clocks,
@@ -519,6 +526,7 @@ def stress_arm(args, ws, rank, local, pg):
     S = D.SHADING_MODEL.PATH_DIFFUSE
     spp = 4
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+    r.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
     r.commit(ts)
     tgt = r.render(ts, cams)
     edge = args.res * args.res
@@ -530,6 +538,7 @@ def stress_arm(args, ws, rank, local, pg):
     for label, hits in (("recompute", 0), ("stored_hits", 1)):
         ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
         ro.set_option(N.OPT_ADJOINT_HITS, hits)
+        ro.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
         opt = D.CreateSimpleOptimizer()
         opt.Init(isc, ro, cams, tgt, p)
         stream = torch.cuda.ExternalStream(ro.stream(), device=local)
@@ -738,6 +747,7 @@ def main():
     ap.add_argument("--impl", default="drgb", choices=["drgb", "reference"])
     ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve", "stress"])
     ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
+    ap.add_argument("--bvh", default="sah", choices=sorted(BVH_BUILDERS), help="hierarchy builder")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
     ap.add_argument("--seed", type=int, default=0)

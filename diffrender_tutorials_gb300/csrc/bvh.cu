@@ -16,6 +16,7 @@
 // not.  Boxes are padded so that the traversal never culls a triangle the
 // brute-force test would accept.
 #include <algorithm>
+#include <cstring>
 #include <climits>
 
 #include "engine.h"
@@ -455,8 +456,148 @@ void refit_bvh(Job& J, cudaStream_t s) {
 #endif
 }
 
+// Binned SAH build of the hierarchy's topology on the host (16 bins per
+// axis over the triangle centroids, one triangle per leaf); the boxes are
+// filled by the device refit, exactly as for the LBVH.  Outputs the child
+// links of every internal node (root 0), the leaf permutation and the
+// parent arrays.
+static void sah_topology(const std::vector<float4>& pos, const std::vector<int4>& tri_v, int n,
+                         std::vector<float4>& links, std::vector<int>& perm, std::vector<int>& leaf_parent,
+                         std::vector<int>& node_parent) {
+  struct Item {
+    float lo[3], hi[3], c[3];
+  };
+  std::vector<Item> items((size_t)n);
+  for (int t = 0; t < n; t++) {
+    const int4 tv = tri_v[t];
+    const float4 a = pos[tv.x], b = pos[tv.y], c = pos[tv.z];
+    Item& it = items[t];
+    const float xa[3] = {a.x, a.y, a.z}, xb[3] = {b.x, b.y, b.z}, xc[3] = {c.x, c.y, c.z};
+    for (int k = 0; k < 3; k++) {
+      it.lo[k] = std::min(xa[k], std::min(xb[k], xc[k]));
+      it.hi[k] = std::max(xa[k], std::max(xb[k], xc[k]));
+      it.c[k] = 0.5f * (it.lo[k] + it.hi[k]);
+    }
+  }
+  std::vector<int> idx((size_t)n);
+  for (int t = 0; t < n; t++) idx[t] = t;
+  links.assign((size_t)std::max(n - 1, 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  perm.assign((size_t)n, 0);
+  leaf_parent.assign((size_t)n, -1);
+  node_parent.assign((size_t)std::max(n - 1, 1), -1);
+  constexpr int NB = 16;
+  struct Task {
+    int b, e, node;
+  };
+  std::vector<Task> stack{{0, n, 0}};
+  int next_node = 1, next_leaf = 0;
+  auto area = [](const float* lo, const float* hi) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx * dy + dy * dz + dz * dx;
+  };
+  while (!stack.empty()) {
+    const Task t = stack.back();
+    stack.pop_back();
+    float cmin[3] = {1e30f, 1e30f, 1e30f}, cmax[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = t.b; i < t.e; i++)
+      for (int k = 0; k < 3; k++) {
+        cmin[k] = std::min(cmin[k], items[idx[i]].c[k]);
+        cmax[k] = std::max(cmax[k], items[idx[i]].c[k]);
+      }
+    int best_axis = -1, best_split = 0;
+    float best_cost = 1e38f;
+    for (int ax = 0; ax < 3; ax++) {
+      const float ext = cmax[ax] - cmin[ax];
+      if (!(ext > 0.0f)) continue;
+      int cnt[NB] = {0};
+      float blo[NB][3], bhi[NB][3];
+      for (int q = 0; q < NB; q++)
+        for (int k = 0; k < 3; k++) {
+          blo[q][k] = 1e30f;
+          bhi[q][k] = -1e30f;
+        }
+      for (int i = t.b; i < t.e; i++) {
+        const Item& it = items[idx[i]];
+        const int q = std::min(NB - 1, (int)((it.c[ax] - cmin[ax]) / ext * NB));
+        cnt[q]++;
+        for (int k = 0; k < 3; k++) {
+          blo[q][k] = std::min(blo[q][k], it.lo[k]);
+          bhi[q][k] = std::max(bhi[q][k], it.hi[k]);
+        }
+      }
+      float rlo[NB][3], rhi[NB][3];
+      int rcnt[NB];
+      float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+      int c = 0;
+      for (int q = NB - 1; q >= 0; q--) {
+        c += cnt[q];
+        for (int k = 0; k < 3; k++) {
+          lo[k] = std::min(lo[k], blo[q][k]);
+          hi[k] = std::max(hi[k], bhi[q][k]);
+          rlo[q][k] = lo[k];
+          rhi[q][k] = hi[k];
+        }
+        rcnt[q] = c;
+      }
+      for (int k = 0; k < 3; k++) {
+        lo[k] = 1e30f;
+        hi[k] = -1e30f;
+      }
+      c = 0;
+      for (int q = 0; q < NB - 1; q++) {
+        c += cnt[q];
+        for (int k = 0; k < 3; k++) {
+          lo[k] = std::min(lo[k], blo[q][k]);
+          hi[k] = std::max(hi[k], bhi[q][k]);
+        }
+        if (c == 0 || rcnt[q + 1] == 0) continue;
+        const float cost = c * area(lo, hi) + rcnt[q + 1] * area(rlo[q + 1], rhi[q + 1]);
+        if (cost < best_cost) {
+          best_cost = cost;
+          best_axis = ax;
+          best_split = q;
+        }
+      }
+    }
+    int mid = (t.b + t.e) / 2;
+    if (best_axis >= 0) {
+      const float ext = cmax[best_axis] - cmin[best_axis];
+      auto it = std::partition(idx.begin() + t.b, idx.begin() + t.e, [&](int tri) {
+        return std::min(NB - 1, (int)((items[tri].c[best_axis] - cmin[best_axis]) / ext * NB)) <= best_split;
+      });
+      mid = (int)(it - idx.begin());
+      if (mid == t.b || mid == t.e) mid = (t.b + t.e) / 2;
+    }
+    int child[2];
+    const int rb[2] = {t.b, mid}, re[2] = {mid, t.e};
+    for (int side = 0; side < 2; side++) {
+      if (re[side] - rb[side] == 1) {
+        const int slot = next_leaf++;
+        perm[slot] = idx[rb[side]];
+        leaf_parent[slot] = t.node;
+        child[side] = ~slot;
+      } else {
+        const int id = next_node++;
+        node_parent[id] = t.node;
+        child[side] = id;
+        stack.push_back(Task{rb[side], re[side], id});
+      }
+    }
+    float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    std::memcpy(&l.x, &child[0], sizeof(int));
+    std::memcpy(&l.y, &child[1], sizeof(int));
+    links[t.node] = l;
+  }
+}
+
 void build_bvh(Job& J, cudaStream_t s) {
   const int n = J.n_tris;
+  // same triangles, same builder: keep the topology, the refit renews the boxes
+  const bool same_tris = J.topo_tri_v.size() == J.h_tri_v.size() &&
+                         (J.h_tri_v.empty() || std::memcmp(J.topo_tri_v.data(), J.h_tri_v.data(),
+                                                           sizeof(int4) * J.h_tri_v.size()) == 0);
+  if (J.topo_builder == J.bvh_builder && same_tris && J.nodes.p && J.perm.p) return;
+  J.topo_builder = -1;
   J.tri.alloc(3 * (size_t)std::max(n, 1));
   J.perm.alloc(std::max(n, 1));
   J.leaf_parent.alloc(std::max(n, 1));
@@ -479,6 +620,24 @@ void build_bvh(Job& J, cudaStream_t s) {
     return;
   }
   J.root = 0;
+  if (J.bvh_builder == 1) {
+    std::vector<float4> pos((size_t)J.n_vertices);
+    DRGB_CUDA(cudaMemcpyAsync(pos.data(), J.pos.p, sizeof(float4) * pos.size(), cudaMemcpyDeviceToHost, s));
+    DRGB_CUDA(cudaStreamSynchronize(s));
+    std::vector<float4> links;
+    std::vector<int> perm, leaf_parent, node_parent;
+    sah_topology(pos, J.h_tri_v, n, links, perm, leaf_parent, node_parent);
+    std::vector<float4> nodes(4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (int i = 0; i < n - 1; i++) nodes[4 * (size_t)i + 3] = links[i];
+    DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.perm.p, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.leaf_parent.p, leaf_parent.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, node_parent.data(), sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaStreamSynchronize(s));
+    J.topo_tri_v = J.h_tri_v;
+    J.topo_builder = 1;
+    return;
+  }
   for (int b = 0; b < 2; b++) {
     J.sort_keys[b].alloc(n);
     J.sort_vals[b].alloc(n);
@@ -503,6 +662,8 @@ void build_bvh(Job& J, cudaStream_t s) {
   DRGB_CUDA(cudaMemsetAsync(J.nodes.p, 0, sizeof(float4) * 4 * (n - 1), s));
   k_karras<<<(n - 1 + 255) / 256, 256, 0, s>>>(J.sort_keys[cur].p, n, J.nodes.p, J.leaf_parent.p, J.node_parent.p);
   count_launch();
+  J.topo_tri_v = J.h_tri_v;
+  J.topo_builder = 0;
 }
 
 }  // namespace drgb

@@ -100,6 +100,10 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         break;
       }
       case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
+      case DRGB_OPT_BVH_BUILDER:
+        require(value == 0 || value == 1, "hierarchy builder: 0 (LBVH) or 1 (binned SAH)");
+        r->job.bvh_builder = (int)value;  // used from the next commit on
+        break;
       case DRGB_OPT_PIXEL_GRID:
         require(value >= 1 && value <= 64, "pixel grid: 1..64 blocks per SM");
         r->px_blocks_per_sm = (int)value;

@@ -171,6 +171,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   J.blocks.upload(J.h_blocks.data(), J.h_blocks.size(), s);
   J.vblock.upload(vblock.data(), vblock.size(), s);
   J.tri_v.upload(tri_v.data(), tri_v.size(), s);
+  J.h_tri_v.swap(tri_v);  // kept for the hierarchy builders and their topology cache
   std::vector<MeshSrc> src(nm);
   std::vector<const float*> trs(nm);
   for (int m = 0; m < nm; m++) {

@@ -130,6 +130,12 @@ struct Job {
   DevBuf<int> sort_vals[2];
   DevBuf<float> bounds;
   int root = 0;
+  // hierarchy builder (0: LBVH from Morton codes on the device, 1 (default):
+  // binned SAH on the host, measured faster to traverse) and the topology cache: a commit of the same triangles with
+  // the same builder keeps the topology and only refits the boxes
+  int bvh_builder = 1;
+  std::vector<int4> h_tri_v, topo_tri_v;
+  int topo_builder = -1;
   // edges (topology; one list per differentiable-mesh set)
   DevBuf<int4> edges;   // v0, v1, vn0, vn1
   DevBuf<int2> edge_mi; // mesh, instance

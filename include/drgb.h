@@ -67,7 +67,10 @@ enum {
                                     written by a separate tracing pass (16 bytes per sample) instead of
                                     re-tracing them; 0 (default): re-trace.  Single renderers only. */
   DRGB_OPT_PIXEL_GRID = 7,       /* blocks per SM of the persistent pixel kernel (default 8) */
-  DRGB_OPT_EDGE_GRID = 8         /* blocks per SM of the persistent edge-shading kernel (default 8) */
+  DRGB_OPT_EDGE_GRID = 8,        /* blocks per SM of the persistent edge-shading kernel (default 8) */
+  DRGB_OPT_BVH_BUILDER = 9       /* hierarchy topology from the next commit on: 0 LBVH from Morton codes on
+                                    the device, 1 (default) binned SAH on the host; boxes are refitted on the
+                                    device either way, and a commit of the same triangles keeps the topology */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory

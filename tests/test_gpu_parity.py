@@ -206,7 +206,8 @@ def test_icosphere_point_light_vs_oracle():
     assert_grad_close(ds.data, ods, ds.layout)
 
 
-def test_bvh_equals_bruteforce_on_large_mesh():
+@pytest.mark.parametrize("builder", [0, 1])  # LBVH, binned SAH
+def test_bvh_equals_bruteforce_on_large_mesh(builder):
     true = D.displace_radially(D.make_uv_sphere(120, 240, seed=4), seed=5)
     sc = D.Scene()
     sc.add_mesh(true)
@@ -214,6 +215,7 @@ def test_bvh_equals_bruteforce_on_large_mesh():
     rng = np.random.default_rng(9)
     xy = rng.uniform(0, 512, size=(400000, 2)).astype(np.float32)
     a, b = make(2, 1), make(2, 1, bruteforce=True)
+    a.set_option(N.OPT_BVH_BUILDER, builder)
     a.commit(sc)
     b.commit(sc)
     ha, hb = a.cast_rays(cam, xy), b.cast_rays(cam, xy)
@@ -234,14 +236,14 @@ def test_bvh_equals_bruteforce_on_large_mesh():
         p = hb["prim"][i]
         assert p != 0xFFFFFFFF
         A, B, C = V[F[p]]
-        N = np.cross(B - A, C - A)
+        nrm = np.cross(B - A, C - A)
         # the brute-force hit is nearer than the LBVH's, its determinant was
         # clamped (|d.(e1 x e2)| < 1e-6), and it sits at the clamped distance
         # |(o-A).N|/1e-6 (o = the camera position; float32 cancellation in
         # (o-A).N allows a few per cent)
         assert hb["t"][i] < ha["t"][i] or ha["prim"][i] == 0xFFFFFFFF
         o = np.array(cam.origin, np.float64)
-        tc = abs(np.dot(A - o, N)) / 1e-6
+        tc = abs(np.dot(A - o, nrm)) / 1e-6
         assert abs(tc - hb["t"][i]) <= 5e-2 * max(tc, 1e-3), (i, tc, hb["t"][i])
 
 

@@ -91,8 +91,9 @@ def test_server_job_alone_and_in_mix_atomic_mode():
     a, alone, plain, mixed = run_alone_plain_and_mix(False)
     assert alone[0][0] == mixed[0][0] == plain[0][0]
     assert alone[0].size == mixed[0].size == plain[0].size == 12
-    np.testing.assert_allclose(mixed[0], alone[0], rtol=2e-2)
-    np.testing.assert_allclose(plain[0], alone[0], rtol=2e-2)
+    for other in (mixed[0], plain[0]):
+        np.testing.assert_allclose(other[:3], alone[0][:3], rtol=5e-3)
+        np.testing.assert_allclose(other, alone[0], rtol=0.1)
 
 
 def test_server_budget_and_slots():
