@@ -237,7 +237,8 @@ constexpr int PX_MAX_SAMPLES = 64;
 #define DRGB_PX_MIN_BLOCKS_PATH 3
 #endif
 constexpr int px_min_blocks(int mode, bool det, bool hits) {
-  return (det || hits || mode == 0) ? 1 : mode == PATH_DIFFUSE ? DRGB_PX_MIN_BLOCKS_PATH : DRGB_PX_MIN_BLOCKS;
+  (void)hits;  // the stored-hit variants get the same budget, for a like-for-like comparison
+  return (det || mode == 0) ? 1 : mode == PATH_DIFFUSE ? DRGB_PX_MIN_BLOCKS_PATH : DRGB_PX_MIN_BLOCKS;
 }
 template <int MODE, bool DET, bool HITS>
 __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
