@@ -9,3 +9,4 @@ from .scene import (CamInfo, Scene, Texture, TriangleMesh, displace_radially, ma
 from .api import (SHADING_MODEL, CreateSimpleOptimizer, DiffRenderSettings, DMesh, DScene, IDiffRender,  # noqa: F401
                   IOptimizer, MakeDifferentialRenderer, ModelParams, OptimizerParameters, kernel_launches,
                   BatchOptimizer, OptimizationServer, estimate_job_bytes)
+from . import io  # noqa: F401,E402  (mesh and image files)

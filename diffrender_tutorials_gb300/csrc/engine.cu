@@ -192,11 +192,16 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   // inverse transforms of mesh 0 (Scene::get_transform_inv(0), kept from the
   // first commit: prepare_for_render appends, scene_utils.cpp:118-129)
   if (nm > 0) {
-    std::vector<float> tr(16 * (size_t)J.meshes[0].n_inst), inv(tr.size());
+    // The edge term indexes this table by the instance of any mesh; instances
+    // beyond mesh 0's (an out-of-range read in the reference) get the
+    // identity, so that every index stays inside the table.
+    int max_inst = 1;
+    for (int m = 0; m < nm; m++) max_inst = std::max(max_inst, J.meshes[m].n_inst);
+    std::vector<float> tr(16 * (size_t)max_inst, 0.0f), inv(tr.size(), 0.0f);
     const drgb_mesh_desc& d = scene->meshes[0];
-    for (int j = 0; j < J.meshes[0].n_inst; j++) {
-      if (d.transforms) std::memcpy(&tr[16 * j], d.transforms + 16 * j, 16 * sizeof(float));
-      else { std::fill(&tr[16 * j], &tr[16 * j] + 16, 0.0f); tr[16 * j] = tr[16 * j + 5] = tr[16 * j + 10] = tr[16 * j + 15] = 1.0f; }
+    for (int j = 0; j < max_inst; j++) {
+      if (d.transforms && j < J.meshes[0].n_inst) std::memcpy(&tr[16 * j], d.transforms + 16 * j, 16 * sizeof(float));
+      else tr[16 * j] = tr[16 * j + 5] = tr[16 * j + 10] = tr[16 * j + 15] = 1.0f;
       mat_inverse44(&tr[16 * j], &inv[16 * j]);
     }
     J.tr_inv0.upload(inv.data(), inv.size(), s);

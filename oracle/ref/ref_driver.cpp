@@ -12,6 +12,7 @@
 //   CreateSimpleOptimizer / Run       src/optimizer.h:52-61, src/optimizer_simple.cpp:272-309
 //   CamInfo                           common_src/camera.h:6-44
 //   qmc::planeHammersley, prng::*     common_src/qmc.cpp:227-268
+//   mesh_utils::LoadMeshFromVSGF      common_src/cmesh.cpp:139-170
 #include <chrono>
 #include <cstdio>
 #include <memory>
@@ -21,6 +22,7 @@
 #include "drender.h"
 #include "optimizer.h"
 #include "qmc.h"
+#include "cmesh.h"
 #include "raytrace.h"
 #include "kvio.h"
 #include "ref_pointlight.h"
@@ -321,6 +323,18 @@ int main(int argc, char** argv) {
     std::vector<float> h(2 * n);
     qmc::planeHammersley(h.data(), n);
     out.put_f32("ham", h);
+  } else if (task == 8) {  // a VSGF mesh through the reference's loader (common_src/cmesh.cpp:139-170)
+    std::string path;
+    for (int32_t ch : in.vec<int32_t>("path")) path.push_back((char)ch);
+    mesh_utils::SimpleMesh m = mesh_utils::LoadMeshFromVSGF(path.c_str());
+    auto flat = [](const void* p, size_t n) {
+      const float* f = static_cast<const float*>(p);
+      return std::vector<float>(f, f + n);
+    };
+    out.put_f32("pos4", flat(m.vPos4f.data(), 4 * m.vPos4f.size()));
+    out.put_f32("norm4", flat(m.vNorm4f.data(), 4 * m.vNorm4f.size()));
+    out.put_f32("tc2", flat(m.vTexCoord2f.data(), 2 * m.vTexCoord2f.size()));
+    out.put_u32("indices", std::vector<uint32_t>(m.indices.begin(), m.indices.end()));
   } else {
     std::fprintf(stderr, "unknown task %d\n", task);
     return 2;

@@ -143,6 +143,27 @@ def main():
         out = run(items)
         save(f"drc_cube_m{mode}", **items, **prefixed("out.", out))
 
+    # instancing: two instances of the cube (Scene::add_mesh with two
+    # matrices, BASE_TRANSFORM); gradients of positions and of both 4x3
+    # transform blocks
+    iscene2 = Scene()
+    t0, t1 = identity4(), identity4()
+    t0[0, 3], t0[1, 3] = -0.7, 0.1
+    c, s_ = np.cos(0.4), np.sin(0.4)
+    t1[:3, :3] = np.array([[c, 0, s_], [0, 1, 0], [-s_, 0, c]]) * 0.8
+    t1[0, 3], t1[2, 3] = 0.8, -0.3
+    iscene2.add_mesh(init_cube, [t0, t1])
+    tscene2 = Scene()
+    tscene2.add_mesh(true_cube, [t0, t1])
+    cams_i = [Cam((0, 0.5, 3.2), 64, 64)]
+    tgt_i = run({"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+                 **scene_items(tscene2), **cam_items(cams_i)})["images"]
+    items = {"task": np.array([4], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+             **scene_items(iscene2), **cam_items(cams_i), "targets": tgt_i, "edge_samples": np.array([64 * 64], np.int32),
+             "dmesh_ids": np.array([0], np.int32)}
+    out = run(items)
+    save("drc_cube_instanced", **items, **prefixed("out.", out))
+
     # two views, d_render with a given adjoint (accumulation over views)
     cams2 = [Cam((0, 0, 3), 48, 48), Cam((2.2, 1.0, 1.8), 48, 48)]
     adj = np.random.default_rng(13).normal(0, 0.5, size=2 * 48 * 48 * 3).astype(np.float32)

@@ -91,7 +91,8 @@ def test_render_bit_exact_vs_reference(name, mode, spp):
 
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
-                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6)])
+                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6),
+                                       ("drc_cube_instanced", 2)])
 def test_d_render_and_compare_vs_reference(name, mode):
     d = load(name)
     sc = scene_from(d)

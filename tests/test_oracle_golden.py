@@ -74,7 +74,8 @@ def test_render_bit_exact(name, mode, spp):
 
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
-                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6)])
+                                       ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6),
+                                       ("drc_cube_instanced", 2)])
 def test_d_render_and_compare(name, mode):
     d = load(name)
     loss, ds, imgs = O.d_render_and_compare(scene_from(d), cams_from(d), mode, int(d["spp"][0]), d["targets"],
