@@ -271,10 +271,10 @@ __global__ void k_edge_select(const JobDev* jobs, int job) {
   queue_append(J.queue, J.queue_count, J.queue_cap, keep, make_int4(view, i, edge_id, job));
 }
 
-// Three resident blocks per SM (85 registers): faster on GB300 than two
-// without spills, for the point-light and path models alike.
+// Four resident blocks per SM (64 registers, with spills): faster on GB300
+// than two or three, for the point-light and path models alike.
 #ifndef DRGB_EDGE_MIN_BLOCKS
-#define DRGB_EDGE_MIN_BLOCKS 3
+#define DRGB_EDGE_MIN_BLOCKS 4
 #endif
 // Persistent over the queue, in whole warps (the reductions need every lane).
 template <bool DET>

@@ -234,7 +234,7 @@ constexpr int PX_MAX_SAMPLES = 64;
 #define DRGB_PX_MIN_BLOCKS 4
 #endif
 #ifndef DRGB_PX_MIN_BLOCKS_PATH
-#define DRGB_PX_MIN_BLOCKS_PATH 3
+#define DRGB_PX_MIN_BLOCKS_PATH 4
 #endif
 constexpr int px_min_blocks(int mode, bool det, bool hits) {
   (void)hits;  // the stored-hit variants get the same budget, for a like-for-like comparison
