@@ -9,7 +9,8 @@
 namespace drgb {
 void launch_b_edges(const JobDev* d_jobs, const Seg* proj_segs, int n_proj, int proj_chunks, const Seg* pmf_segs,
                     int n_pmf, int pmf_chunks, const Seg* pairs, int n_pairs, const Seg* sel_segs, int n_sel,
-                    int sel_chunks, int4* queue, int* count, int cap, int shade_grid, cudaStream_t s, bool det);
+                    int sel_chunks, int4* queue, int* count, int cap, int shade_grid, cudaStream_t s, bool det,
+                    const QueueSort* qs);
 void launch_b_opt(const JobAux* d_aux, int n_jobs, const Seg* d_moment_segs, int n_moment_segs, int moment_chunks,
                   const Seg* d_apply_segs, int n_apply_segs, int apply_chunks, cudaStream_t s);
 void launch_b_prepare(const JobAux* d_aux, const Seg* segs[4], const int nsegs[4], const int chunks[4],
@@ -40,6 +41,9 @@ struct drgb_batch {
   DevBuf<Seg> seg_proj, seg_pmf, seg_pairs, seg_sel, seg_mom, seg_apply, seg_btr, seg_flat, seg_cnt, seg_refit;
   DevBuf<int4> queue;
   DevBuf<int> queue_count;
+  DevBuf<uint32_t> qkey[2], qhist;  // shading order of the queue, sorted by (job, view, edge)
+  DevBuf<int> qidx[2], qn;
+  int qbits = 1;
   int n_items = 0, mode = 0;
   int n_proj = 0, c_proj = 0, n_pmf = 0, c_pmf = 0, n_pairs = 0, n_sel = 0, c_sel = 0;
   int n_mom = 0, c_mom = 0, n_apply = 0, c_apply = 0;
@@ -77,10 +81,13 @@ struct drgb_batch {
     std::vector<Seg> proj, pmf, pairs, sel, mom, apply, btr, flat, cnt, refit;
     int modes = -1;
     queue_cap = 0;
+    uint64_t key_base = 0;
     for (int j = 0; j < n; j++) {
       drgb_renderer* r = jobs.at(order[j]).get();
       Job& J = r->job;
       JobDev d = J.dev;
+      d.edge_key_base = (uint32_t)key_base;
+      key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
       d.item_base = (int)items.size();
       d.item_count = (int)J.h_pixel_items.size();
       for (int4 it : J.h_pixel_items) items.push_back(make_int4(j, it.y, it.z, it.w));
@@ -177,6 +184,14 @@ struct drgb_batch {
     d_counter.alloc(1);
     queue.reserve(std::max(1, queue_cap));
     queue_count.alloc(1);
+    for (int b = 0; b < 2; b++) {
+      qkey[b].reserve(queue.n);
+      qidx[b].reserve(queue.n);
+    }
+    qhist.reserve(256 * (size_t)kSortGrid);
+    qn.reserve(1);
+    qbits = 1;
+    while (qbits < 32 && (1ull << qbits) < std::max<uint64_t>(1, key_base)) qbits++;
     DRGB_CUDA(cudaStreamSynchronize(stream));
     dirty = false;
     graph_valid = false;
@@ -186,6 +201,7 @@ struct drgb_batch {
 
   // update = false: the gradient passes only (autotuning; state unchanged)
   void enqueue_iteration(bool update = true) {
+    const QueueSort qsort{{qkey[0].p, qkey[1].p}, {qidx[0].p, qidx[1].p}, qhist.p, qn.p, qbits};
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
       DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
@@ -199,7 +215,7 @@ struct drgb_batch {
     launch_loss_finalize(d_jobs.p, (int)order.size(), stream);
     launch_b_edges(d_jobs.p, seg_proj.p, n_proj, c_proj, seg_pmf.p, n_pmf, c_pmf, seg_pairs.p, n_pairs, seg_sel.p,
                    n_sel, c_sel, queue.p, queue_count.p, (int)queue.n, sm_count * edge_blocks_per_sm, stream,
-                   det_any);
+                   det_any, &qsort);
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_reduce(J, sm_count, stream);

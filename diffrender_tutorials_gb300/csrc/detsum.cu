@@ -283,6 +283,22 @@ __global__ void __launch_bounds__(32) k_ds_seg_final(const int* n_ptr, const Det
   }
 }
 
+// Stable radix sort of (key, value) pairs whose count is on the device, keys
+// below 2^bits; the pairs are in keys[0]/vals[0] and end in the buffer whose
+// index is returned.
+int sort_pairs_device(uint32_t* keys[2], int* vals[2], const int* n_ptr, int bits, uint32_t* hist, cudaStream_t s) {
+  const int passes = std::max(1, (bits + 7) / 8);
+  int cur = 0;
+  for (int p = 0; p < passes; p++) {
+    k_ds_hist<<<DS_GRID, DS_THREADS, 0, s>>>(keys[cur], n_ptr, 8 * p, hist);
+    launch_rs_scan(hist, 256 * DS_GRID, s);
+    k_ds_scatter<<<DS_GRID, DS_THREADS, 0, s>>>(keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n_ptr, 8 * p, hist);
+    count_launch(2);
+    cur ^= 1;
+  }
+  return cur;
+}
+
 int64_t det_regions(const Job& J) { return (int64_t)J.dev.item_count + (int64_t)J.n_views * J.dev.edge_samples; }
 
 // Buffers of the deterministic mode for the current views, work items and

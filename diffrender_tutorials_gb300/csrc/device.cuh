@@ -148,6 +148,7 @@ struct JobDev {
   int queue_cap;
   int edge_samples;
   const float* rnd;         // 2 * edge_samples replayed random numbers
+  uint32_t edge_key_base;   // first queue-sort key of this job in a batch
   // optional work counters (rays, box tests, triangle tests); null normally
   unsigned long long* work;
   // deterministic reduction: gradient contributions become records

@@ -156,6 +156,9 @@ struct Job {
   DevBuf<float> pmf, cdf;  // per view
   DevBuf<int4> queue;      // surviving edge samples
   DevBuf<int> queue_count;
+  // the queue's shading order sorted by (view, edge) for coherent rays
+  DevBuf<uint32_t> qkey[2], qhist;
+  DevBuf<int> qidx[2], qn;
   // gradients
   std::vector<DLayout> dlay;
   std::vector<int> dmesh_ids;
@@ -216,6 +219,16 @@ void launch_opt_record(Job& J, cudaStream_t s);
 void det_buffers(Job& J, cudaStream_t s);
 void launch_det_clear(const Job& J, cudaStream_t s);
 void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s);
+int sort_pairs_device(uint32_t* keys[2], int* vals[2], const int* n_ptr, int bits, uint32_t* hist, cudaStream_t s);
+// Buffers of a batch's edge-queue sort (all null: shade in queue order).
+struct QueueSort {
+  uint32_t* keys[2];
+  int* vals[2];
+  uint32_t* hist;
+  int* n;
+  int bits;
+};
+constexpr int kSortGrid = 512;  // blocks of sort_pairs_device (its histogram has 256 * kSortGrid entries)
 
 // edge random table shared by every job with the same sample count
 const float* edge_random_table(int n, cudaStream_t s);

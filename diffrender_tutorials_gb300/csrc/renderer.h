@@ -115,6 +115,14 @@ struct drgb_renderer {
     J.pmf.reserve(std::max<size_t>(1, (size_t)J.n_views * J.n_edges));
     J.cdf.reserve(std::max<size_t>(1, (size_t)J.n_views * (J.n_edges + 1)));
     J.queue.reserve(std::max<size_t>(1, (size_t)J.n_views * std::max(edge_samples, 1)));
+#ifndef DRGB_EDGE_NO_SORT
+    for (int b = 0; b < 2; b++) {
+      J.qkey[b].reserve(J.queue.n);
+      J.qidx[b].reserve(J.queue.n);
+    }
+    J.qhist.reserve(256 * (size_t)kSortGrid);
+    J.qn.reserve(1);
+#endif
     J.dev.edge_samples = edge_samples;
     J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
     if (J.det) det_buffers(J, stream);

@@ -186,8 +186,15 @@ __device__ __forceinline__ float2 interp_tc(const JobDev& J, const Surf& s) {
 // Lighting factor of the point-light vertex-albedo model:
 // vis * I * max(0, n.l) / d^2 + ambient, with the reference Lambert's bias.
 // With n.l <= 0 the lit term is 0 whatever the visibility: no shadow ray.
+// One out-of-line copy for the forward and adjoint passes (+2 % on GB300;
+// -DDRGB_LPV_INLINE inlines it).
+#ifdef DRGB_LPV_INLINE
+#define DRGB_LPV_ATTR __forceinline__
+#else
+#define DRGB_LPV_ATTR __noinline__
+#endif
 template <bool WARP>
-__device__ __forceinline__ float lpv_factor_p(const JobDev& J, const Surf& s, bool hit) {
+__device__ DRGB_LPV_ATTR float lpv_factor_p(const JobDev& J, const Surf& s, bool hit) {
   f3 p = mk(0.0f, 0.0f, 0.0f), l = mk(0.0f, 0.0f, 1.0f);
   float d2 = 1.0f, dist = 0.0f, ndl = 0.0f;
   if (hit) {
@@ -413,5 +420,18 @@ template <int MODE = 0>
 __device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
   return shade_p<MODE, false>(J, cam, x, y, key, true);
 }
+
+// The generic shader as one out-of-line function (callers that shade
+// several points keep a single copy of every model's code).
+#ifdef DRGB_EDGE_SHADE_NOINLINE
+static __device__ __noinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
+  return shade_p<0, false>(J, cam, x, y, key, true);
+}
+#else
+static __device__ __forceinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y,
+                                                   uint32_t key) {
+  return shade_p<0, false>(J, cam, x, y, key, true);
+}
+#endif
 
 }  // namespace drgb
