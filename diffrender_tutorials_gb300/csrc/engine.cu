@@ -171,6 +171,10 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   J.blocks.upload(J.h_blocks.data(), J.h_blocks.size(), s);
   J.vblock.upload(vblock.data(), vblock.size(), s);
   J.tri_v.upload(tri_v.data(), tri_v.size(), s);
+  // the same triangles (global vertex ids and blocks) keep the edge list
+  const bool same_topology = tri_v.size() == J.h_tri_v.size() &&
+                             (tri_v.empty() || std::memcmp(tri_v.data(), J.h_tri_v.data(),
+                                                           sizeof(int4) * tri_v.size()) == 0);
   J.h_tri_v.swap(tri_v);  // kept for the hierarchy builders and their topology cache
   std::vector<MeshSrc> src(nm);
   std::vector<const float*> trs(nm);
@@ -206,8 +210,10 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     }
     J.tr_inv0.upload(inv.data(), inv.size(), s);
   }
-  J.edge_ids_key.clear();
-  J.n_edges = 0;
+  if (!same_topology) {
+    J.edge_ids_key.clear();
+    J.n_edges = 0;
+  }
   J.committed = true;
 }
 

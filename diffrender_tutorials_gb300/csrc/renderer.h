@@ -3,6 +3,7 @@
 #pragma once
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <memory>
 #include <string>
 
@@ -84,18 +85,30 @@ struct drgb_renderer {
     J.dev.item_count = (int)items.size();
   }
 
+  // Views of the last call: repeated calls with the same cameras and tile
+  // shape keep the device cameras and work items.
+  std::vector<drgb_camera> last_cams;
+  int last_tw = 0, last_th = 0;
+
   void views(const drgb_camera* cams, int n, bool same_size) {
     require(cams != nullptr && n > 0, "need at least one camera");
     if (same_size)
       for (int i = 1; i < n; i++)
         require((int)cams[i].width == (int)cams[0].width && (int)cams[i].height == (int)cams[0].height,
                 "gradient calls need all views of the same size");
+    if ((int)last_cams.size() == n && last_tw == job.tile_w && last_th == job.tile_h && d_items.p &&
+        std::memcmp(last_cams.data(), cams, sizeof(drgb_camera) * (size_t)n) == 0)
+      return;
+    last_cams.clear();
     setup_views(job, cams, n);
     job.cams.upload(job.h_cams.data(), job.h_cams.size(), stream);
     std::vector<int64_t> off(n + 1, 0);
     for (int i = 0; i < n; i++) off[i + 1] = off[i] + (int64_t)cams[i].width * (int64_t)cams[i].height;
     job.img_off.upload(off.data(), off.size(), stream);
     make_items();
+    last_cams.assign(cams, cams + n);
+    last_tw = job.tile_w;
+    last_th = job.tile_h;
   }
 
   int64_t n_pixels() const {
