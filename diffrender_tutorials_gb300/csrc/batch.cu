@@ -26,7 +26,7 @@ int64_t job_device_bytes(const Job& J) {
   b += J.pos.bytes() + J.orig.bytes() + J.col.bytes() + J.nrm.bytes() + J.tc.bytes() + J.tri_v.bytes() +
        J.blocks.bytes() + J.meshdev.bytes() + J.block_tr.bytes() + J.vblock.bytes() + J.src_tab.bytes() +
        J.tr_tab.bytes() + J.tr_inv0.bytes();
-  b += J.nodes.bytes() + J.nodes4.bytes() + J.tri.bytes() + J.perm.bytes() + J.leaf_parent.bytes() + J.node_parent.bytes() +
+  b += J.nodes.bytes() + J.nodes4.bytes() + J.tri.bytes() + J.perm.bytes() + J.leaf_of.bytes() + J.leaf_parent.bytes() + J.node_parent.bytes() +
        J.counters.bytes();
   for (int k = 0; k < 2; k++) b += J.sort_keys[k].bytes() + J.sort_vals[k].bytes();
   b += J.sort_hist.bytes() + J.bounds.bytes() + J.edges.bytes() + J.edge_mi.bytes() + J.cams.bytes() + J.ham.bytes();

@@ -590,6 +590,14 @@ static void sah_topology(const std::vector<float4>& pos, const std::vector<int4>
   }
 }
 
+// triangle -> leaf slot, for traversals seeded with a candidate triangle
+__global__ void k_leaf_of(const int* perm, int n, int* leaf_of) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) leaf_of[perm[k]] = k;
+}
+
+static void build_topology(Job& J, cudaStream_t s);
+
 void build_bvh(Job& J, cudaStream_t s) {
   const int n = J.n_tris;
   // same triangles, same builder: keep the topology, the refit renews the boxes
@@ -597,6 +605,18 @@ void build_bvh(Job& J, cudaStream_t s) {
                          (J.h_tri_v.empty() || std::memcmp(J.topo_tri_v.data(), J.h_tri_v.data(),
                                                            sizeof(int4) * J.h_tri_v.size()) == 0);
   if (J.topo_builder == J.bvh_builder && same_tris && J.nodes.p && J.perm.p) return;
+  build_topology(J, s);
+#ifdef DRGB_SEED_HITS
+  J.leaf_of.alloc(std::max(n, 1));
+  if (n > 0) {
+    k_leaf_of<<<(n + 255) / 256, 256, 0, s>>>(J.perm.p, n, J.leaf_of.p);
+    count_launch();
+  }
+#endif
+}
+
+static void build_topology(Job& J, cudaStream_t s) {
+  const int n = J.n_tris;
   J.topo_builder = -1;
   J.tri.alloc(3 * (size_t)std::max(n, 1));
   J.perm.alloc(std::max(n, 1));

@@ -111,6 +111,7 @@ struct JobDev {
   // internal node, < 0 leaf ~k, kEmpty4 unused), one unused float4
   const float4* nodes4;
   int root;              // >= 0 internal node, < 0 leaf ~k, INT_MIN if empty
+  const int* leaf_of;    // flattened triangle -> its leaf slot in `tri`
   int trace_bruteforce;  // 1: test every triangle (reference loop order)
   // model
   int mode;
@@ -478,16 +479,18 @@ __device__ __forceinline__ void add_work(const JobDev& J, unsigned boxes, unsign
 // instruction-fetch stalls (+10 % on the point-light workload on GB300;
 // -DDRGB_TRACE_SPLIT builds one copy per kind).
 static __device__ DRGB_TRACE_ATTR bool trace_impl(const JobDev& J, f3 o, f3 d, float tNear, float tFar,
-                                                  Hit& best, const bool ANY);
+                                                  Hit& best, const bool ANY, const int seed);
 template <bool ANY>
-__device__ __forceinline__ bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best) {
-  return trace_impl(J, o, d, tNear, tFar, best, ANY);
+__device__ __forceinline__ bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best,
+                                      int seed = -1) {
+  return trace_impl(J, o, d, tNear, tFar, best, ANY, seed);
 }
 static __device__ DRGB_TRACE_ATTR bool trace_impl(const JobDev& J, f3 o, f3 d, float tNear, float tFar,
-                                                  Hit& best, const bool ANY) {
+                                                  Hit& best, const bool ANY, const int seed) {
 #else
 template <bool ANY>
-__device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best) {
+__device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, float tFar, Hit& best,
+                                      int seed = -1) {
 #endif
   best.t = tFar;
   best.tri = -1;
@@ -515,6 +518,21 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
     }
     add_work(J, 0, J.n_tris);
     return best.tri >= 0;
+  }
+  // seed: a triangle likely to be the nearest hit (the hit of a nearby ray),
+  // tested first so that the traversal culls with its distance from the
+  // start.  A valid candidate cannot change the result (the same test and
+  // tie rule decide, and the culling keeps a slack).
+  if (!ANY && seed >= 0 && J.leaf_of) {
+    const int k = __ldg(J.leaf_of + seed);
+    const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+    float t, u, v;
+    if (mt_test(o, d, f4to3(a), f4to3(e1), f4to3(e2), tNear, t, u, v) && t < best.t) {
+      best.t = t;
+      best.u = u;
+      best.v = v;
+      best.tri = __float_as_int(a.w);
+    }
   }
   const f3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
   const f3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);

@@ -377,6 +377,7 @@ void sync_dev(Job& J) {
   d.nodes = J.nodes.p;
   d.nodes4 = J.nodes4.p;
   d.tri = J.tri.p;
+  d.leaf_of = J.leaf_of.p;
   d.root = J.root;
   d.trace_bruteforce = J.trace_bruteforce;
   d.mode = J.mode;

@@ -126,6 +126,7 @@ struct Job {
   DevBuf<float4> nodes, tri;
   DevBuf<float4> nodes4;   // 4-wide view of the binary hierarchy, refreshed after each refit
   DevBuf<int> perm, leaf_parent, node_parent, counters;
+  DevBuf<int> leaf_of;  // triangle -> leaf slot (inverse of perm)
   DevBuf<uint32_t> sort_keys[2], sort_hist;
   DevBuf<int> sort_vals[2];
   DevBuf<float> bounds;

@@ -226,6 +226,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.nodes = J.nodes.p;
     d.nodes4 = J.nodes4.p;
     d.tri = J.tri.p;
+    d.leaf_of = J.leaf_of.p;
     d.root = J.root;
     d.trace_bruteforce = J.trace_bruteforce;
     d.mode = J.mode;

@@ -142,7 +142,7 @@ __device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, 
 template <int MODE, bool DET, bool HITS>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
                                            uint32_t key, float* wscr, int64_t rec_base, int& rec_n,
-                                           const float4* stored) {
+                                           const float4* stored, int seed) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   bool hit;
@@ -163,7 +163,7 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
       s.block = tv.w;
     }
   } else {
-    hit = cast_p<kPixelWarp>(J, cam, x, y, active, s);
+    hit = cast_p<kPixelWarp>(J, cam, x, y, active, s, seed);
   }
   if (model_has_color(mode)) {
     float c[9];
@@ -249,6 +249,9 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   __shared__ float4 s_adj_all[PX_WARPS][32];
   __shared__ float s_ham_all[PX_WARPS][2 * 64];
   __shared__ float wscr_all[PX_WARPS][9 * 32];
+#ifdef DRGB_SEED_HITS
+  __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
+#endif
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
@@ -256,6 +259,9 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   float4* s_adj = s_adj_all[warp];
   float* s_ham = s_ham_all[warp];
   float* wscr = wscr_all[warp];
+#ifdef DRGB_SEED_HITS
+  int* s_hit = s_hit_all[warp];
+#endif
   int cur_job = -1, cur_view = -1;
   for (;;) {
     int it = 0;
@@ -304,7 +310,13 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
           fy = (float)py + yoff;
         }
         // every lane calls it (required by the warp-coherent policy)
+#ifdef DRGB_SEED_HITS
+        int ht = -1;
+        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, &ht);
+        if (s < NS) s_hit[s] = act ? ht : -1;
+#else
         const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act);
+#endif
         if (act) c = sc / (float)S;
         if (s < NS) {
           s_col[3 * s + 0] = c.x;
@@ -391,7 +403,18 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
             const_cast<float4*>(hslot)[0] = make_float4(sf.h.t, sf.h.u, sf.h.v, __int_as_float(h ? sf.h.tri : -1));
           continue;
         }
-        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot);
+        // -DDRGB_SEED_HITS: test first the forward hit of the grid sample whose
+        // cell holds this point (bit-identical results; 3 % slower on GB300
+        // for the point-light sphere, so off)
+        int seed = -1;
+#ifdef DRGB_SEED_HITS
+        if ((flags & PX_FWD) && act) {
+          const int gx = min(sq - 1, (int)(s_ham[2 * k] * (float)sq));
+          const int gy = min(sq - 1, (int)(s_ham[2 * k + 1] * (float)sq));
+          seed = s_hit[p * S + gy * sq + gx];
+        }
+#endif
+        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed);
       }
       if (DET && J.det && lane == 0 && !store_hits) J.rec_count[it - J.item_base] = rec_n;
     }

@@ -115,7 +115,8 @@ __device__ DRGB_TRACE_ATTR bool trace_warp(const JobDev& J, f3 o, f3 d, float tN
 
 // Traversal under a policy; inactive lanes report a miss.
 template <bool ANY, bool WARP>
-__device__ __forceinline__ bool trace_p(const JobDev& J, f3 o, f3 d, float tNear, float tFar, bool active, Hit& h) {
+__device__ __forceinline__ bool trace_p(const JobDev& J, f3 o, f3 d, float tNear, float tFar, bool active, Hit& h,
+                                        int seed = -1) {
   if (WARP) return trace_warp<ANY>(J, o, d, tNear, tFar, active, h);
   if (!active) {
     h.t = tFar;
@@ -123,7 +124,7 @@ __device__ __forceinline__ bool trace_p(const JobDev& J, f3 o, f3 d, float tNear
     h.u = h.v = 0.0f;
     return false;
   }
-  return trace<ANY>(J, o, d, tNear, tFar, h);
+  return trace<ANY>(J, o, d, tNear, tFar, h, seed);
 }
 
 // Surface record of a camera ray (SurfaceInfo, raytrace.h:21-29, plus ids).
@@ -136,9 +137,10 @@ struct Surf {
 };
 
 template <bool WARP>
-__device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float x, float y, bool active, Surf& s) {
+__device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float x, float y, bool active, Surf& s,
+                                       int seed = -1) {
   camera_ray(cam, x, y, s.ro, s.rd);
-  const bool hit = trace_p<false, WARP>(J, s.ro, s.rd, 0.0f, 1e9f, active, s.h);
+  const bool hit = trace_p<false, WARP>(J, s.ro, s.rd, 0.0f, 1e9f, active, s.h, seed);
   s.A = s.B = s.C = 0;
   s.block = 0;
   if (hit) {
@@ -340,11 +342,14 @@ __device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
   return ref_max(0.0f, dot(n, light_dir * -1.0f)) + ggx;
 }
 
+// hit_tri (may be null) receives the camera ray's triangle, -1 on a miss.
 template <int MODE, bool WARP>
-__device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active) {
+__device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active,
+                             int* hit_tri = nullptr) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   const bool hit = cast_p<WARP>(J, cam, x, y, active, s);
+  if (hit_tri) *hit_tri = hit ? s.h.tri : -1;
   const float u = s.h.u, v = s.h.v;
   switch (mode) {
     case SILHOUETTE:
