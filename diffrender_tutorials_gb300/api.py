@@ -24,7 +24,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import native as N
-from .scene import CamInfo, Scene
+from .scene import CamInfo, Scene, TransformR
 
 
 class SHADING_MODEL(enum.IntEnum):
@@ -68,13 +68,38 @@ class _SceneHandle:
         self.meshes = (N.MeshDesc * max(1, n))()
         for i, m in enumerate(scene.meshes):
             tr = scene.transforms_colmajor(i)
-            self.keep.append(tr)
+            rp = scene.restricted_params(i)
+            self.keep += [tr, rp]
             tex = m.textures[0] if m.textures else None
             self.meshes[i] = N.MeshDesc(m.vertex_count, m.indices.size, _ptr(m.vertices), _ptr(m.colors), _ptr(m.tc),
                                         _ptr(m.normals), _ptr(m.tangents), _ptr(m.indices), len(scene.transforms[i]),
                                         _ptr(tr), tex.w if tex else 0, tex.h if tex else 0,
-                                        tex.channels if tex else 0, _ptr(tex.data) if tex else None)
+                                        tex.channels if tex else 0, _ptr(tex.data) if tex else None, _ptr(rp))
         self.desc = N.SceneDesc(n, C.cast(self.meshes, C.POINTER(N.MeshDesc)))
+
+
+def _read_scene(template: Scene, get_mesh, get_restricted) -> Scene:
+    """A copy of template with the optimised parameters read back through
+    get_mesh(i, vertices, colors, texture, transforms) and, for restricted
+    meshes, get_restricted(i, params)."""
+    s = template.copy()
+    for i, m in enumerate(s.meshes):
+        v = np.zeros_like(m.vertices)
+        col = np.zeros_like(m.colors) if m.colors is not None else None
+        tex = np.zeros_like(m.textures[0].data) if m.textures else None
+        tr = np.zeros(16 * len(s.transforms[i]), np.float32)
+        N.check(get_mesh(i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
+        m.vertices = v
+        if col is not None:
+            m.colors = col
+        if tex is not None:
+            m.textures[0].data = tex
+        s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
+        if s.restricted[i] is not None:
+            p = np.zeros(7 * len(s.restricted[i]), np.float32)
+            N.check(get_restricted(i, _ptr(p)))
+            s.restricted[i] = [TransformR.from_params(q) for q in p.reshape(-1, 7)]
+    return s
 
 
 def make_camera(cam: CamInfo) -> N.Camera:
@@ -108,6 +133,7 @@ class DMesh:
         self.data = data
         self.vertices, self.instances = int(layout[0]), int(layout[1])
         self._pos, self._col, self._tex, self._tr = (int(layout[2]), int(layout[3]), int(layout[4]), int(layout[5]))
+        self._rt = int(layout[6])
         self.mesh_id = int(layout[8])
 
     def pos(self):
@@ -119,10 +145,18 @@ class DMesh:
     def tex(self):
         if self._tex < 0:
             return None
-        return self.data[self._tex:self._tr]
+        return self.data[self._tex:self._tr if self._tr >= 0 else self._rt]
 
     def transform_mat(self):
+        if self._tr < 0:
+            return None
         return self.data[self._tr:self._tr + 12 * self.instances].reshape(-1, 12)
+
+    def restricted_transform(self):
+        """7 values per instance of a restricted mesh (dmesh.h:132), else None."""
+        if self._rt < 0:
+            return None
+        return self.data[self._rt:self._rt + 7 * self.instances].reshape(-1, 7)
 
     def full_data(self):
         return self.data
@@ -363,20 +397,9 @@ class IOptimizer:
         return {k: int(v) for k, v in zip(("rays", "box_tests", "tri_tests", "edge_samples"), out)}
 
     def current_scene(self) -> Scene:
-        s = self._scene.copy()
-        for i, m in enumerate(s.meshes):
-            v = np.zeros_like(m.vertices)
-            col = np.zeros_like(m.colors) if m.colors is not None else None
-            tex = np.zeros_like(m.textures[0].data) if m.textures else None
-            tr = np.zeros(16 * len(s.transforms[i]), np.float32)
-            N.check(N.load().drgb_optimizer_get_mesh(self._r._h, i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
-            m.vertices = v
-            if col is not None:
-                m.colors = col
-            if tex is not None:
-                m.textures[0].data = tex
-            s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
-        return s
+        L, h = N.load(), self._r._h
+        return _read_scene(self._scene, lambda i, *a: L.drgb_optimizer_get_mesh(h, i, *a),
+                           lambda i, p: L.drgb_optimizer_get_restricted(h, i, p))
 
 
 def CreateSimpleOptimizer() -> IOptimizer:
@@ -465,20 +488,9 @@ class BatchOptimizer:
         return int(N.load().drgb_batch_job_device_bytes(self._h, int(job_id)))
 
     def job_scene(self, job_id: int) -> Scene:
-        s = self._scenes[job_id].copy()
-        for i, m in enumerate(s.meshes):
-            v = np.zeros_like(m.vertices)
-            col = np.zeros_like(m.colors) if m.colors is not None else None
-            tex = np.zeros_like(m.textures[0].data) if m.textures else None
-            tr = np.zeros(16 * len(s.transforms[i]), np.float32)
-            N.check(N.load().drgb_batch_get_mesh(self._h, int(job_id), i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
-            m.vertices = v
-            if col is not None:
-                m.colors = col
-            if tex is not None:
-                m.textures[0].data = tex
-            s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
-        return s
+        L, h, j = N.load(), self._h, int(job_id)
+        return _read_scene(self._scenes[job_id], lambda i, *a: L.drgb_batch_get_mesh(h, j, i, *a),
+                           lambda i, p: L.drgb_batch_get_restricted(h, j, i, p))
 
 
 JOB_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
@@ -547,20 +559,9 @@ class OptimizationServer:
         return out[:n]
 
     def result_scene(self, ticket: int) -> Scene:
-        s = self._scenes[ticket].copy()
-        for i, m in enumerate(s.meshes):
-            v = np.zeros_like(m.vertices)
-            col = np.zeros_like(m.colors) if m.colors is not None else None
-            tex = np.zeros_like(m.textures[0].data) if m.textures else None
-            tr = np.zeros(16 * len(s.transforms[i]), np.float32)
-            N.check(N.load().drgb_server_get_mesh(self._h, int(ticket), i, _ptr(v), _ptr(col), _ptr(tex), _ptr(tr)))
-            m.vertices = v
-            if col is not None:
-                m.colors = col
-            if tex is not None:
-                m.textures[0].data = tex
-            s.transforms[i] = [t.T.copy() for t in tr.reshape(-1, 4, 4)]
-        return s
+        L, h, t = N.load(), self._h, int(ticket)
+        return _read_scene(self._scenes[ticket], lambda i, *a: L.drgb_server_get_mesh(h, t, i, *a),
+                           lambda i, p: L.drgb_server_get_restricted(h, t, i, p))
 
     def release(self, ticket: int):
         N.check(N.load().drgb_server_release(self._h, int(ticket)))

@@ -37,13 +37,13 @@ bool ok(int rc, const char* where) {
 // drgb_scene_desc over a Scene's arrays (kept alive by this object).
 struct SceneView {
   std::vector<drgb_mesh_desc> meshes;
-  std::vector<std::vector<float4x4>> mats;  // restricted transforms as matrices
+  std::vector<std::vector<float>> rparams;  // TransformR parameters, 7 per instance
   drgb_scene_desc desc{};
 
   explicit SceneView(const Scene& s) {
     const auto& ms = s.get_meshes();
     meshes.resize(ms.size());
-    mats.resize(ms.size());
+    rparams.resize(ms.size());
     for (size_t i = 0; i < ms.size(); i++) {
       const TriangleMesh& m = ms[i];
       drgb_mesh_desc& d = meshes[i];
@@ -56,13 +56,19 @@ struct SceneView {
       d.normals = m.normals.empty() ? nullptr : reinterpret_cast<const float*>(m.normals.data());
       d.tangents = m.tangents.empty() ? nullptr : reinterpret_cast<const float*>(m.tangents.data());
       d.indices = m.indices.data();
-      const std::vector<float4x4>* tr = &s.get_transform((unsigned)i);
       if (s.get_instancing_type((unsigned)i) == Scene::RESTRICTED_TRANSFORM) {
-        for (const TransformR& r : s.get_restricted_transform((unsigned)i)) mats[i].push_back(r.to_mat());
-        tr = &mats[i];
+        for (const TransformR& r : s.get_restricted_transform((unsigned)i)) {
+          const float p[7] = {r.translate.x, r.translate.y, r.translate.z, r.rotate.x, r.rotate.y, r.rotate.z,
+                              r.scale};
+          rparams[i].insert(rparams[i].end(), p, p + 7);
+        }
+        d.n_instances = (int32_t)(rparams[i].size() / 7);
+        d.restricted = rparams[i].empty() ? nullptr : rparams[i].data();
+      } else {
+        const std::vector<float4x4>& tr = s.get_transform((unsigned)i);
+        d.n_instances = (int32_t)tr.size();
+        d.transforms = tr.empty() ? nullptr : reinterpret_cast<const float*>(tr.data());
       }
-      d.n_instances = (int32_t)tr->size();
-      d.transforms = tr->empty() ? nullptr : reinterpret_cast<const float*>(tr->data());
       if (!m.textures.empty()) {
         const CPUTexture& t = m.textures[0];
         d.tex_w = t.w;
@@ -108,15 +114,14 @@ void scatter(const std::vector<float>& v, DScene& ds) {
   }
 }
 
-// The gradient vector drgb fills must have the DScene's size (meshes with
-// restricted transforms have another layout in the reference).
+// The gradient vector drgb fills must have the DScene's size.
 bool layout_matches(drgb_renderer* r, const std::vector<int32_t>& ids, DScene& ds, const char* where) {
   int64_t total = 0;
   std::vector<int32_t> lay(9 * ids.size() + 9);
   if (!ok(drgb_dscene_layout(r, ids.data(), (int)ids.size(), lay.data(), &total), where)) return false;
   if (total != (int64_t)ds.full_size()) {
     t_code = DRGB_ERR_UNSUPPORTED;
-    t_msg = "gradient layout differs from the DScene (restricted transforms are not supported)";
+    t_msg = "gradient layout differs from the DScene";
     std::printf("[%s]: error, %s\n", where, t_msg.c_str());
     return false;
   }
@@ -307,6 +312,17 @@ class GpuOptimizer : public IOptimizer {
                                  own_tr ? reinterpret_cast<float*>(tr.data()) : nullptr),
          "GpuOptimizer::Run");
       if (own_tr) scene_.get_transform_modify((unsigned)i) = tr;
+      if (scene_.get_instancing_type((unsigned)i) == Scene::RESTRICTED_TRANSFORM) {
+        auto& rts = scene_.get_restricted_transform_modify((unsigned)i);
+        std::vector<float> p(7 * rts.size());
+        if (p.empty() || !ok(drgb_optimizer_get_restricted(r_, (int)i, p.data()), "GpuOptimizer::Run")) continue;
+        for (size_t j = 0; j < rts.size(); j++) {
+          const float* q = &p[7 * j];
+          rts[j].translate = float3(q[0], q[1], q[2]);
+          rts[j].rotate = float3(q[3], q[4], q[5]);
+          rts[j].scale = q[6];
+        }
+      }
     }
   }
 

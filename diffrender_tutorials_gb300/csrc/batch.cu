@@ -259,6 +259,18 @@ int drgb_batch_get_mesh(drgb_batch* b, int32_t id, int mesh_id, float* vertices,
   return drgb_optimizer_get_mesh(r, mesh_id, vertices, colors, texture, transforms);
 }
 
+int drgb_batch_get_restricted(drgb_batch* b, int32_t id, int mesh_id, float* params) {
+  drgb_renderer* r = nullptr;
+  int rc = guard([&] {
+    require(b != nullptr, "null batch");
+    r = batch_job(b, id);
+    DRGB_CUDA(cudaSetDevice(b->device));
+    DRGB_CUDA(cudaStreamSynchronize(b->stream));
+  });
+  if (rc != DRGB_OK) return rc;
+  return drgb_optimizer_get_restricted(r, mesh_id, params);
+}
+
 int drgb_batch_autotune(drgb_batch* b, int trial_iters, int32_t* chosen, float* best_ms) {
   return guard([&] {
     require(b != nullptr && trial_iters >= 1, "bad arguments");

@@ -142,8 +142,7 @@ struct drgb_batch {
       for (int k = 0; k < A.n_dmesh; k++) {
         const DLayout& L = J.dlay[k];
         MeshState& M = J.meshes[L.mesh_id];
-        A.dm[k] = OptMesh{L.base, L.full, L.pos_off, L.color_off, L.tex_off, L.tr_off, L.vertices, L.instances,
-                          M.vertices.p, M.has_colors ? M.colors.p : nullptr, M.texture.p, M.transforms.p};
+        A.dm[k] = opt_mesh(L, M);
         apply.push_back(Seg{j, k, 0, L.full});
       }
       mom.push_back(Seg{j, 0, 0, J.opt.params.alg >= DRGB_GD_ADAGRAD ? (int)J.grad_total : 0});
@@ -204,7 +203,7 @@ struct drgb_batch {
     const QueueSort qsort{{qkey[0].p, qkey[1].p}, {qidx[0].p, qidx[1].p}, qhist.p, qn.p, qbits};
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
-      DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
+      DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, J.grad_bytes(), stream));
     }
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
@@ -219,9 +218,11 @@ struct drgb_batch {
     for (int32_t id : order) {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_reduce(J, sm_count, stream);
+      launch_restricted_grad(J, stream);
     }
     if (!update) return;
     launch_b_opt(d_aux.p, (int)order.size(), seg_mom.p, n_mom, c_mom, seg_apply.p, n_apply, c_apply, stream);
+    for (int32_t id : order) launch_restricted_mats(jobs.at(id)->job, stream);
     const Seg* sp[4] = {seg_btr.p, seg_flat.p, seg_cnt.p, seg_refit.p};
     launch_b_prepare(d_aux.p, sp, n_prep, c_prep, stream);
   }

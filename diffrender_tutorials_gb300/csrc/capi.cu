@@ -196,7 +196,8 @@ int drgb_dscene_layout(drgb_renderer* r, const int32_t* ids, int n_ids, int32_t*
       for (size_t k = 0; k < L.size(); k++) {
         int32_t* o = layout + 9 * k;
         o[0] = L[k].vertices; o[1] = L[k].instances; o[2] = L[k].pos_off; o[3] = L[k].color_off;
-        o[4] = L[k].tex_off; o[5] = L[k].tr_off; o[6] = -1; o[7] = L[k].full; o[8] = L[k].mesh_id;
+        o[4] = L[k].tex_off; o[5] = L[k].rt_off >= 0 ? -1 : L[k].tr_off; o[6] = L[k].rt_off; o[7] = L[k].full;
+        o[8] = L[k].mesh_id;
       }
     if (total) *total = t;
   });
@@ -218,12 +219,15 @@ int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoin
     DRGB_CUDA(cudaMemcpyAsync(J.adj_in.p, adjoints, sizeof(float) * 3 * npix, cudaMemcpyHostToDevice, r->stream));
     if (J.grad_total > 0)
       DRGB_CUDA(cudaMemcpyAsync(J.grad.p, dscene, sizeof(float) * J.grad_total, cudaMemcpyHostToDevice, r->stream));
+    if (J.grad_alloc > J.grad_total)
+      DRGB_CUDA(cudaMemsetAsync(J.grad.p + J.grad_total, 0, sizeof(float) * (J.grad_alloc - J.grad_total), r->stream));
     r->push_dev();
     launch_adj_convert(r->d_job.p, (int64_t)npix, r->stream);
     r->det_begin();
     if (J.mode != SILHOUETTE) r->pixel_pass(PX_ADJ);
     if (edge_samples_in_total > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
     r->det_end();
+    launch_restricted_grad(J, r->stream);
     if (J.grad_total > 0)
       DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, cudaMemcpyDeviceToHost, r->stream));
     r->check_flags();
@@ -452,7 +456,7 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
     double acc[5] = {0, 0, 0, 0, 0};
     for (int it = 0; it < n_iters; it++) {
       DRGB_CUDA(cudaEventRecord(ev[0], r->stream));
-      DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), r->stream));
+      DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, J.grad_bytes(), r->stream));
       r->det_begin();
       const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
       r->pixel_pass(flags);
@@ -460,6 +464,7 @@ int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms) {
       DRGB_CUDA(cudaEventRecord(ev[1], r->stream));
       if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
       r->det_end();  // deterministic mode: the record reduction is timed with the edge phase
+      launch_restricted_grad(J, r->stream);
       DRGB_CUDA(cudaEventRecord(ev[2], r->stream));
       launch_opt_record(J, r->stream);
       launch_opt_step(J, r->stream);
@@ -571,7 +576,7 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
     const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
     // gradients of this replay are discarded: save and restore the buffer
     DevBuf<float> save;
-    save.alloc(std::max<int64_t>(1, J.grad_total));
+    save.alloc(std::max<int64_t>(1, J.grad_alloc));
     DRGB_CUDA(cudaMemcpyAsync(save.p, J.grad.p, save.bytes(), cudaMemcpyDeviceToDevice, r->stream));
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, save.bytes(), r->stream));
     launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
@@ -608,6 +613,20 @@ int drgb_optimizer_get_mesh(drgb_renderer* r, int mesh_id, float* vertices, floa
       DRGB_CUDA(cudaMemcpyAsync(texture, M.texture.p, M.texture.bytes(), cudaMemcpyDeviceToHost, r->stream));
     if (transforms)
       DRGB_CUDA(cudaMemcpyAsync(transforms, M.transforms.p, M.transforms.bytes(), cudaMemcpyDeviceToHost, r->stream));
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+int drgb_optimizer_get_restricted(drgb_renderer* r, int mesh_id, float* params) {
+  return guard([&] {
+    check_renderer(r);
+    r->require_commit();
+    require(mesh_id >= 0 && mesh_id < (int)r->job.meshes.size(), "mesh id out of range");
+    const MeshState& M = r->job.meshes[mesh_id];
+    require(M.restricted, "not a restricted-transform mesh");
+    require(params != nullptr, "null output");
+    r->set_device();
+    DRGB_CUDA(cudaMemcpyAsync(params, M.rparams.p, M.rparams.bytes(), cudaMemcpyDeviceToHost, r->stream));
     DRGB_CUDA(cudaStreamSynchronize(r->stream));
   });
 }

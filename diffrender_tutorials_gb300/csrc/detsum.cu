@@ -334,7 +334,7 @@ void launch_det_clear(const Job& J, cudaStream_t s) {
 
 void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
   const int64_t regions = det_regions(J);
-  if (regions <= 0 || J.grad_total <= 0) return;
+  if (regions <= 0 || J.grad_alloc <= 0) return;
   const int nb = (int)((regions + DS_CHUNK - 1) / DS_CHUNK);
   k_ds_count_sums<<<nb, DS_THREADS, 0, s>>>(J.rec_count.p, regions, J.det_part.p);
   launch_rs_scan(J.det_part.p, nb, s);
@@ -342,7 +342,7 @@ void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
                                          J.dev.rec_item_cap, J.det_key[0].p, J.det_idx[0].p, J.det_n.p);
   count_launch(2);
   int bits = 1;
-  while (bits < 32 && ((int64_t)1 << bits) < J.grad_total) bits++;
+  while (bits < 32 && ((int64_t)1 << bits) < J.grad_alloc) bits++;
   const int passes = (bits + 7) / 8;
   int cur = 0;
   for (int p = 0; p < passes; p++) {

@@ -206,6 +206,7 @@ struct OptMesh {
   float* colors;
   float* texture;
   float* transforms;
+  float* rparams;  // restricted mesh: 7 parameters per instance at tr_off (else null)
 };
 
 constexpr int kBatchMaxDMeshes = 4;

@@ -82,6 +82,31 @@ CamDev make_cam(const drgb_camera& c) {
   return d;
 }
 
+// TransformR::to_mat (common_src/scene.h:99-104): translate4x4(t) *
+// rotate4x4Z(rz) * rotate4x4Y(ry) * rotate4x4X(rx) * scale4x4(s), the
+// products left to right in LiteMath's order (LiteMath.h:1474-1549).
+void restricted_to_mat(const float* p, float* out) {
+  auto ident = [](float* m) {
+    std::fill(m, m + 16, 0.0f);
+    m[0] = m[5] = m[10] = m[15] = 1.0f;
+  };
+  float T[16], Rz[16], Ry[16], Rx[16], S[16], a[16], b[16];
+  ident(T);
+  T[12] = p[0]; T[13] = p[1]; T[14] = p[2];
+  ident(Rz);
+  Rz[0] = std::cos(p[5]); Rz[1] = std::sin(p[5]); Rz[4] = -std::sin(p[5]); Rz[5] = std::cos(p[5]);
+  ident(Ry);
+  Ry[0] = std::cos(p[4]); Ry[2] = -std::sin(p[4]); Ry[8] = std::sin(p[4]); Ry[10] = std::cos(p[4]);
+  ident(Rx);
+  Rx[5] = std::cos(p[3]); Rx[6] = std::sin(p[3]); Rx[9] = -std::sin(p[3]); Rx[10] = std::cos(p[3]);
+  ident(S);
+  S[0] = S[5] = S[10] = p[6];
+  mat_mul(T, Rz, a);
+  mat_mul(a, Ry, b);
+  mat_mul(b, Rx, a);
+  mat_mul(a, S, out);
+}
+
 // qmc::planeHammersley (common_src/qmc.cpp:227-243)
 static void hammersley(int n, float* out) {
   for (int k = 0; k < n; k++) {
@@ -114,7 +139,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
         (d.n_indices > 0 && !d.indices))
       throw CudaError("mesh " + std::to_string(m) + ": bad vertex/index arrays", DRGB_ERR_INVALID);
     const int ninst = d.n_instances <= 0 ? 1 : d.n_instances;
-    if (d.n_instances > 1 && !d.transforms)
+    if (d.n_instances > 1 && !d.transforms && !d.restricted)
       throw CudaError("mesh " + std::to_string(m) + ": several instances need transforms", DRGB_ERR_INVALID);
     for (int i = 0; i < d.n_indices; i++)
       if (d.indices[i] >= (uint32_t)d.n_vertices)
@@ -134,11 +159,17 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     M.h_indices.assign(d.indices, d.indices + d.n_indices);
     M.indices.upload(d.indices, d.n_indices, s);
     std::vector<float> tr(16 * (size_t)ninst, 0.0f);
-    if (d.transforms) {
+    M.restricted = d.restricted != nullptr;
+    if (M.restricted) {
+      for (int j = 0; j < ninst; j++) restricted_to_mat(d.restricted + 7 * j, &tr[16 * j]);
+      M.rparams.upload(d.restricted, 7 * (size_t)ninst, s);
+    } else if (d.transforms) {
       std::memcpy(tr.data(), d.transforms, sizeof(float) * 16 * ninst);
     } else {
       for (int j = 0; j < ninst; j++) tr[16 * j + 0] = tr[16 * j + 5] = tr[16 * j + 10] = tr[16 * j + 15] = 1.0f;
     }
+    if (!M.restricted) M.rparams.reset();
+    M.h_transforms = tr;
     M.transforms.upload(tr.data(), tr.size(), s);
     if (d.texture && d.tex_w > 0 && d.tex_h > 0) {
       if (d.tex_channels != 3) throw CudaError("textures must have 3 channels", DRGB_ERR_INVALID);
@@ -202,9 +233,9 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     int max_inst = 1;
     for (int m = 0; m < nm; m++) max_inst = std::max(max_inst, J.meshes[m].n_inst);
     std::vector<float> tr(16 * (size_t)max_inst, 0.0f), inv(tr.size(), 0.0f);
-    const drgb_mesh_desc& d = scene->meshes[0];
+    const MeshState& M0 = J.meshes[0];
     for (int j = 0; j < max_inst; j++) {
-      if (d.transforms && j < J.meshes[0].n_inst) std::memcpy(&tr[16 * j], d.transforms + 16 * j, 16 * sizeof(float));
+      if (j < M0.n_inst) std::memcpy(&tr[16 * j], &M0.h_transforms[16 * j], 16 * sizeof(float));
       else tr[16 * j] = tr[16 * j + 5] = tr[16 * j + 10] = tr[16 * j + 15] = 1.0f;
       mat_inverse44(&tr[16 * j], &inv[16 * j]);
     }
@@ -230,7 +261,8 @@ void setup_views(Job& J, const drgb_camera* cams, int n_views) {
   J.H = (int)cams[0].height;
 }
 
-int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out) {
+int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out,
+                       int64_t* alloc_total) {
   if (n_ids < 0 || n_ids > 16 || (n_ids > 0 && !ids)) throw CudaError("bad differentiable mesh ids", DRGB_ERR_INVALID);
   out.clear();
   int64_t off = 0;
@@ -249,13 +281,26 @@ int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<
     o += 3 * M.nv;
     if (model_has_color(J.mode)) { L.color_off = o; o += 3 * M.nv; }
     if (model_has_tex(J.mode) && M.texture.p) { L.tex_off = o; o += M.tex_w * M.tex_h * M.tex_c; }
-    L.tr_off = o;
-    o += 12 * M.n_inst;
+    if (M.restricted) {
+      L.rt_off = o;
+      o += 7 * M.n_inst;
+    } else {
+      L.tr_off = o;
+      o += 12 * M.n_inst;
+    }
     L.full = o;
     L.base = off;
     off += o;
     out.push_back(L);
   }
+  // scratch matrix blocks of the restricted meshes, after the public vector
+  int64_t scratch = off;
+  for (DLayout& L : out)
+    if (L.rt_off >= 0) {
+      L.tr_off = (int)(scratch - L.base);
+      scratch += 12 * (int64_t)L.instances;
+    }
+  if (alloc_total) *alloc_total = scratch;
   return off;
 }
 
@@ -308,9 +353,9 @@ void build_edges(Job& J) {
 }
 
 void set_dscene(Job& J, const int32_t* ids, int n_ids) {
-  J.grad_total = compute_layout(J, ids, n_ids, J.dlay);
+  J.grad_total = compute_layout(J, ids, n_ids, J.dlay, &J.grad_alloc);
   J.dmesh_ids.assign(ids, ids + n_ids);
-  J.grad.reserve(std::max<int64_t>(1, J.grad_total));
+  J.grad.reserve(std::max<int64_t>(1, J.grad_alloc));
   std::vector<MeshDev> md(J.meshes.size());
   for (size_t m = 0; m < J.meshes.size(); m++) {
     const MeshState& M = J.meshes[m];

@@ -6,6 +6,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -74,6 +75,11 @@ struct DLayout {
   int mesh_id = -1;
   int vertices = 0, instances = 0;
   int pos_off = 0, color_off = -1, tex_off = -1, tr_off = 0;
+  // Restricted mesh: its 7 parameters per instance at rt_off (public part),
+  // while tr_off points past the public vector, at a scratch block of 12
+  // matrix entries per instance that the edge pass accumulates into and
+  // launch_restricted_grad() folds through the Jacobian of to_mat.
+  int rt_off = -1;
   int full = 0;
   int64_t base = 0;  // offset in the concatenated vector
 };
@@ -83,7 +89,9 @@ void count_launch(int n = 1);
 
 struct MeshState {
   int nv = 0, ni = 0, n_inst = 1;
-  DevBuf<float> vertices, colors, tc, normals, tangents, transforms, texture;
+  bool restricted = false;  // TransformR instances: rparams drive transforms
+  DevBuf<float> vertices, colors, tc, normals, tangents, transforms, texture, rparams;
+  std::vector<float> h_transforms;  // instance matrices as committed (column major)
   DevBuf<uint32_t> indices;
   int tex_w = 0, tex_h = 0, tex_c = 0;
   bool has_colors = false, has_tc = false, has_normals = false, has_tangents = false;
@@ -163,7 +171,9 @@ struct Job {
   // gradients
   std::vector<DLayout> dlay;
   std::vector<int> dmesh_ids;
-  int64_t grad_total = 0;
+  int64_t grad_total = 0;  // public gradient vector (DScene)
+  int64_t grad_alloc = 0;  // + scratch matrix blocks of restricted meshes
+  size_t grad_bytes() const { return sizeof(float) * (size_t)std::max<int64_t>(1, grad_alloc); }
   DevBuf<float> grad;
   DevBuf<uint32_t> err;
   OptState opt;
@@ -194,7 +204,17 @@ void setup_views(Job& J, const drgb_camera* cams, int n_views);
 void sync_dev(Job& J);
 void set_dscene(Job& J, const int32_t* ids, int n_ids);
 void build_edges(Job& J);
-int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out);
+int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out,
+                       int64_t* alloc_total = nullptr);
+// TransformR::to_mat on the host (column-major, LiteMath's rounding).
+void restricted_to_mat(const float* params7, float* out16);
+// Restricted meshes: fold the scratch matrix gradient into the 7 parameters
+// (after the gradient passes); rebuild the matrices from the parameters
+// (after an optimiser step that changed them).
+void launch_restricted_grad(Job& J, cudaStream_t s);
+void launch_restricted_mats(Job& J, cudaStream_t s);
+// The optimiser's view of one differentiable mesh.
+OptMesh opt_mesh(const DLayout& L, MeshState& M);
 
 void init_job_model(Job& J, int mode, int spp);
 void choose_tile(int S, int& tw, int& th);

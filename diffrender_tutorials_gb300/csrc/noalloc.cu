@@ -163,6 +163,9 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
         for (int x = 0; x < W; x += J.tile_w) items.push_back(make_int4(0, v, x, y));
     std::vector<DLayout> lay;
     const int64_t grad_total = compute_layout(J, ids, n_ids, lay);
+    for (const DLayout& L : lay)
+      require(L.rt_off < 0, "restricted-transform meshes need drgb_d_render_and_compare_device (the Jacobian step "
+                            "works on a scratch block the caller's gradient vector has no room for)");
     std::vector<MeshDev> md(J.meshes.size());
     for (size_t m = 0; m < J.meshes.size(); m++) {
       const MeshState& M = J.meshes[m];

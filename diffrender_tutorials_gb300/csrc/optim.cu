@@ -64,8 +64,11 @@ __device__ __forceinline__ void opt_apply_body(float* grad, const float* G, cons
   } else if (seg == 2) {
     if ((flags & DRGB_OPT_TEX) && mode != SILHOUETTE && mode != VERTEX_COLOR && M.texture)
       M.texture[j - M.tex_off] -= v;
-  } else {
-    if (flags & DRGB_OPT_TFM) {
+  } else if (flags & DRGB_OPT_TFM) {
+    if (M.rparams) {
+      // translate, rotate, scale -= step (optimizer_simple.cpp:138-160)
+      M.rparams[j - M.tr_off] -= v;
+    } else {
       const int l = j - M.tr_off, inst = l / 12, r = (l % 12) / 4, c = l % 4;
       M.transforms[16 * inst + 4 * c + r] -= v;
     }
@@ -144,8 +147,7 @@ void launch_opt_step(Job& J, cudaStream_t s) {
   for (int k = 0; k < o.n; k++) {
     const DLayout& L = J.dlay[k];
     MeshState& M = J.meshes[L.mesh_id];
-    o.m[k] = OptMesh{L.base, L.full, L.pos_off, L.color_off, L.tex_off, L.tr_off, L.vertices, L.instances,
-                     M.vertices.p, M.has_colors ? M.colors.p : nullptr, M.texture.p, M.transforms.p};
+    o.m[k] = opt_mesh(L, M);
     max_full = std::max(max_full, L.full);
   }
   if (J.opt.params.alg >= DRGB_GD_ADAGRAD) {
@@ -157,6 +159,113 @@ void launch_opt_step(Job& J, cudaStream_t s) {
   k_opt_apply<<<g, 256, 0, s>>>(J.grad.p, J.opt.G.p, J.opt.lr.p, o);
   k_opt_decay<<<1, 1, 0, s>>>(J.opt.lr.p, 4 * o.n, J.opt.iter.p, std::max(1, o.decay_period), o.decay_mult);
   count_launch(2);
+  launch_restricted_mats(J, s);
+}
+
+OptMesh opt_mesh(const DLayout& L, MeshState& M) {
+  const bool rt = L.rt_off >= 0;
+  return OptMesh{L.base, L.full, L.pos_off, L.color_off, L.tex_off, rt ? L.rt_off : L.tr_off, L.vertices,
+                 L.instances, M.vertices.p, M.has_colors ? M.colors.p : nullptr, M.texture.p, M.transforms.p,
+                 rt ? M.rparams.p : nullptr};
+}
+
+// ---- restricted transforms (TransformR, scene.h:91-116) -------------------
+// Row-major 3x4 product with translation, `mul` of drender_autodiff.cpp:22-43.
+__device__ void mul34(const float* a, const float* b, float* out) {
+  float r[12];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) r[4 * i + j] = a[4 * i + 0] * b[j] + a[4 * i + 1] * b[4 + j] + a[4 * i + 2] * b[8 + j];
+    r[4 * i + 3] = a[4 * i + 0] * b[3] + a[4 * i + 1] * b[7] + a[4 * i + 2] * b[11] + a[4 * i + 3];
+  }
+#pragma unroll
+  for (int i = 0; i < 12; i++) out[i] = r[i];
+}
+
+// Row q of d(to_mat)/d(params) over the row-major 3x4 entries.  The matrix is
+// Rz (Ry (Rx S)) plus the translation column (dmat_dtransforms_jac_f,
+// drender_autodiff.cpp:78-95); the derivative by an angle or by the scale
+// replaces that factor by its derivative, by a translation it is a unit entry.
+// The reference takes these rows from Enzyme's forward mode (:97-107).
+__device__ void restricted_jacobian_row(const float* x, int q, float* row) {
+  const float sx = sinf(x[3]), cx = cosf(x[3]), sy = sinf(x[4]), cy = cosf(x[4]), sz = sinf(x[5]), cz = cosf(x[5]);
+  const float S[12] = {x[6], 0, 0, 0, 0, x[6], 0, 0, 0, 0, x[6], 0};
+  const float dS[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  const float Rx[12] = {1, 0, 0, 0, 0, cx, -sx, 0, 0, sx, cx, 0};
+  const float Ry[12] = {cy, 0, sy, 0, 0, 1, 0, 0, -sy, 0, cy, 0};
+  const float Rz[12] = {cz, -sz, 0, 0, sz, cz, 0, 0, 0, 0, 1, 0};
+  const float dRx[12] = {0, 0, 0, 0, 0, -sx, -cx, 0, 0, cx, -sx, 0};
+  const float dRy[12] = {-sy, 0, cy, 0, 0, 0, 0, 0, -cy, 0, -sy, 0};
+  const float dRz[12] = {-sz, -cz, 0, 0, cz, -sz, 0, 0, 0, 0, 0, 0};
+  float a[12], b[12];
+  if (q < 3) {
+    for (int l = 0; l < 12; l++) row[l] = 0.0f;
+    row[4 * q + 3] = 1.0f;
+    return;
+  }
+  mul34(q == 3 ? dRx : Rx, q == 6 ? dS : S, a);
+  mul34(q == 4 ? dRy : Ry, a, b);
+  mul34(q == 5 ? dRz : Rz, b, row);
+}
+
+// grad[rt + 7j + q] += sum_l jac[q][l] * grad[tr12 + 12j + l], l in order
+// (drender.h:398-421).
+__global__ void k_restricted_grad(float* grad, int64_t rt, int64_t tr12, const float* rparams, int n_inst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 7 * n_inst) return;
+  const int j = i / 7, q = i % 7;
+  float x[7], row[12];
+  for (int k = 0; k < 7; k++) x[k] = rparams[7 * j + k];
+  restricted_jacobian_row(x, q, row);
+  float acc = grad[rt + i];
+  for (int l = 0; l < 12; l++) acc += row[l] * grad[tr12 + 12 * j + l];
+  grad[rt + i] = acc;
+}
+
+// TransformR::to_mat on the device (column major), LiteMath's product order.
+__device__ void mat_mul44(const float* a, const float* b, float* out) {
+  float t[16];
+  for (int c = 0; c < 4; c++)
+    for (int r = 0; r < 4; r++)
+      t[4 * c + r] = b[4 * c + 0] * a[r] + b[4 * c + 1] * a[4 + r] + b[4 * c + 2] * a[8 + r] + b[4 * c + 3] * a[12 + r];
+  for (int i = 0; i < 16; i++) out[i] = t[i];
+}
+
+__global__ void k_restricted_mats(const float* rparams, int n_inst, float* transforms) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_inst) return;
+  const float* p = rparams + 7 * j;
+  float T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, p[0], p[1], p[2], 1};
+  float Rz[16] = {cosf(p[5]), sinf(p[5]), 0, 0, -sinf(p[5]), cosf(p[5]), 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  float Ry[16] = {cosf(p[4]), 0, -sinf(p[4]), 0, 0, 1, 0, 0, sinf(p[4]), 0, cosf(p[4]), 0, 0, 0, 0, 1};
+  float Rx[16] = {1, 0, 0, 0, 0, cosf(p[3]), sinf(p[3]), 0, 0, -sinf(p[3]), cosf(p[3]), 0, 0, 0, 0, 1};
+  float S[16] = {p[6], 0, 0, 0, 0, p[6], 0, 0, 0, 0, p[6], 0, 0, 0, 0, 1};
+  float a[16], b[16];
+  mat_mul44(T, Rz, a);
+  mat_mul44(a, Ry, b);
+  mat_mul44(b, Rx, a);
+  mat_mul44(a, S, transforms + 16 * j);
+}
+
+void launch_restricted_grad(Job& J, cudaStream_t s) {
+  for (const DLayout& L : J.dlay) {
+    if (L.rt_off < 0) continue;
+    const int n = 7 * L.instances;
+    k_restricted_grad<<<(n + 127) / 128, 128, 0, s>>>(J.grad.p, L.base + L.rt_off, L.base + L.tr_off,
+                                                      J.meshes[L.mesh_id].rparams.p, L.instances);
+    count_launch();
+  }
+}
+
+void launch_restricted_mats(Job& J, cudaStream_t s) {
+  if (!(J.opt.params.flags & DRGB_OPT_TFM)) return;
+  for (const DLayout& L : J.dlay) {
+    if (L.rt_off < 0) continue;
+    MeshState& M = J.meshes[L.mesh_id];
+    k_restricted_mats<<<(L.instances + 127) / 128, 128, 0, s>>>(M.rparams.p, L.instances, M.transforms.p);
+    count_launch();
+  }
 }
 
 void launch_opt_record(Job& J, cudaStream_t s) {

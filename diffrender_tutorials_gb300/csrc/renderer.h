@@ -210,13 +210,14 @@ struct drgb_renderer {
   void enqueue_iteration(bool want_images) {
     Job& J = job;
     const bool interior = J.mode != SILHOUETTE;
-    DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, sizeof(float) * std::max<int64_t>(1, J.grad_total), stream));
+    DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, J.grad_bytes(), stream));
     det_begin();
     int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
     pixel_pass(flags);
     launch_loss_finalize(d_job.p, 1, stream);
     if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
     det_end();
+    launch_restricted_grad(J, stream);
   }
 };
 

@@ -32,7 +32,7 @@ using Clock = std::chrono::steady_clock;
 
 // Host copy of a scene description and its arrays.
 struct HostScene {
-  std::vector<std::vector<float>> v, col, tc, nrm, tan, tr, tex;
+  std::vector<std::vector<float>> v, col, tc, nrm, tan, tr, tex, rt;
   std::vector<std::vector<uint32_t>> idx;
   std::vector<drgb_mesh_desc> meshes;
   drgb_scene_desc desc{};
@@ -45,6 +45,7 @@ struct HostScene {
   explicit HostScene(const drgb_scene_desc& s) {
     const int n = s.n_meshes;
     v.resize(n); col.resize(n); tc.resize(n); nrm.resize(n); tan.resize(n); tr.resize(n); tex.resize(n);
+    rt.resize(n);
     idx.resize(n);
     meshes.resize(n);
     for (int i = 0; i < n; i++) {
@@ -58,6 +59,7 @@ struct HostScene {
       idx[i] = take(m.indices, (size_t)std::max(0, m.n_indices));
       tr[i] = take(m.transforms, 16 * (size_t)std::max(0, m.n_instances));
       tex[i] = take(m.texture, (size_t)std::max(0, m.tex_w) * std::max(0, m.tex_h) * std::max(0, m.tex_channels));
+      rt[i] = take(m.restricted, 7 * (size_t)std::max(1, m.n_instances));
       drgb_mesh_desc d = m;
       d.vertices = v[i].empty() ? nullptr : v[i].data();
       d.colors = col[i].empty() ? nullptr : col[i].data();
@@ -67,6 +69,7 @@ struct HostScene {
       d.indices = idx[i].empty() ? nullptr : idx[i].data();
       d.transforms = tr[i].empty() ? nullptr : tr[i].data();
       d.texture = tex[i].empty() ? nullptr : tex[i].data();
+      d.restricted = rt[i].empty() ? nullptr : rt[i].data();
       meshes[i] = d;
     }
     desc.n_meshes = n;
@@ -88,7 +91,7 @@ struct Ticket {
   int32_t batch_id = 0;
   // results
   std::vector<float> losses;
-  std::vector<std::vector<float>> out_v, out_col, out_tex, out_tr;
+  std::vector<std::vector<float>> out_v, out_col, out_tex, out_tr, out_rt;
 };
 
 int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_views) {
@@ -201,7 +204,7 @@ struct drgb_server {
     t.losses.resize((size_t)n);
     if (n) DRGB_CUDA(cudaMemcpy(t.losses.data(), J.opt.losses.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
     const int nm = (int)J.meshes.size();
-    t.out_v.resize(nm); t.out_col.resize(nm); t.out_tex.resize(nm); t.out_tr.resize(nm);
+    t.out_v.resize(nm); t.out_col.resize(nm); t.out_tex.resize(nm); t.out_tr.resize(nm); t.out_rt.resize(nm);
     for (int m = 0; m < nm; m++) {
       const MeshState& M = J.meshes[m];
       t.out_v[m].resize(3 * (size_t)M.nv);
@@ -212,6 +215,11 @@ struct drgb_server {
                                              t.out_tex[m].empty() ? nullptr : t.out_tex[m].data(),
                                              t.out_tr[m].empty() ? nullptr : t.out_tr[m].data());
       if (rc != DRGB_OK) throw CudaError(t_err_message(), rc);
+      if (M.restricted) {
+        t.out_rt[m].resize(M.rparams.n);
+        const int rc2 = drgb_optimizer_get_restricted(r, m, t.out_rt[m].data());
+        if (rc2 != DRGB_OK) throw CudaError(t_err_message(), rc2);
+      }
     }
     batch_detach(batch, t.batch_id);
     std::lock_guard<std::mutex> lk(mu);
@@ -474,6 +482,18 @@ int drgb_server_get_mesh(drgb_server* s, int32_t ticket, int mesh_id, float* ver
     if (colors) std::copy(t.out_col[mesh_id].begin(), t.out_col[mesh_id].end(), colors);
     if (texture) std::copy(t.out_tex[mesh_id].begin(), t.out_tex[mesh_id].end(), texture);
     if (transforms) std::copy(t.out_tr[mesh_id].begin(), t.out_tr[mesh_id].end(), transforms);
+  });
+}
+
+int drgb_server_get_restricted(drgb_server* s, int32_t ticket, int mesh_id, float* params) {
+  return guard([&] {
+    require(s != nullptr && params != nullptr, "null server or output");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const Ticket& t = find_ticket(s, ticket);
+    require(t.info.state == DRGB_JOB_DONE, "job not finished", DRGB_ERR_STATE);
+    require(mesh_id >= 0 && mesh_id < (int)t.out_rt.size(), "mesh id out of range");
+    require(!t.out_rt[mesh_id].empty(), "not a restricted-transform mesh");
+    std::copy(t.out_rt[mesh_id].begin(), t.out_rt[mesh_id].end(), params);
   });
 }
 

@@ -34,7 +34,8 @@ class MeshDesc(C.Structure):
     _fields_ = [("n_vertices", C.c_int32), ("n_indices", C.c_int32), ("vertices", C.c_void_p),
                 ("colors", C.c_void_p), ("tc", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p),
                 ("indices", C.c_void_p), ("n_instances", C.c_int32), ("transforms", C.c_void_p),
-                ("tex_w", C.c_int32), ("tex_h", C.c_int32), ("tex_channels", C.c_int32), ("texture", C.c_void_p)]
+                ("tex_w", C.c_int32), ("tex_h", C.c_int32), ("tex_channels", C.c_int32), ("texture", C.c_void_p),
+                ("restricted", C.c_void_p)]
 
 
 class SceneDesc(C.Structure):
@@ -99,6 +100,7 @@ _SIGS = {
     "drgb_optimizer_run": (C.c_int, [VP, C.c_int64, VP, VP]),
     "drgb_optimizer_run_async": (C.c_int, [VP, C.c_int64]),
     "drgb_optimizer_get_mesh": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+    "drgb_optimizer_get_restricted": (C.c_int, [VP, C.c_int, VP]),
     "drgb_batch_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
     "drgb_batch_destroy": (C.c_int, [VP]),
     "drgb_batch_stream": (VP, [VP]),
@@ -112,6 +114,7 @@ _SIGS = {
     "drgb_batch_sync": (C.c_int, [VP]),
     "drgb_batch_job_losses": (C.c_int, [VP, C.c_int32, C.c_int64, C.c_int64, VP, C.POINTER(C.c_int64)]),
     "drgb_batch_get_mesh": (C.c_int, [VP, C.c_int32, C.c_int, VP, VP, VP, VP]),
+    "drgb_batch_get_restricted": (C.c_int, [VP, C.c_int32, C.c_int, VP]),
     "drgb_batch_job_device_bytes": (C.c_int64, [VP, C.c_int32]),
     "drgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(VP)]),
     "drgb_server_destroy": (C.c_int, [VP]),
@@ -123,6 +126,7 @@ _SIGS = {
     "drgb_server_job_info": (C.c_int, [VP, C.c_int32, C.POINTER(JobInfo)]),
     "drgb_server_job_losses": (C.c_int, [VP, C.c_int32, C.c_int64, C.c_int64, VP]),
     "drgb_server_get_mesh": (C.c_int, [VP, C.c_int32, C.c_int, VP, VP, VP, VP]),
+    "drgb_server_get_restricted": (C.c_int, [VP, C.c_int32, C.c_int, VP]),
     "drgb_server_release": (C.c_int, [VP, C.c_int32]),
     "drgb_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
     "drgb_server_step_times": (C.c_int, [VP, C.c_int64, C.c_int64, VP, VP]),

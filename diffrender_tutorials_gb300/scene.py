@@ -89,26 +89,92 @@ def identity4() -> np.ndarray:
     return np.eye(4, dtype=np.float32)
 
 
+def _mul44(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """float32 a @ b summed left to right over k (LiteMath.h:1536-1549)."""
+    out = np.zeros((4, 4), np.float32)
+    for r in range(4):
+        for c in range(4):
+            acc = np.float32(b[0, c] * a[r, 0])
+            for k in range(1, 4):
+                acc = np.float32(acc + np.float32(b[k, c] * a[r, k]))
+            out[r, c] = acc
+    return out
+
+
+@dataclass
+class TransformR:
+    """TransformR (common_src/scene.h:91-116): translation, rotation angles
+    about x, y and z (radians) and a uniform scale.  A mesh added with a list
+    of these is a RESTRICTED_TRANSFORM mesh: its instance matrices are
+    ``to_mat()`` and its gradient holds these 7 parameters per instance."""
+    translate: tuple = (0.0, 0.0, 0.0)
+    rotate: tuple = (0.0, 0.0, 0.0)
+    scale: float = 1.0
+
+    def params(self) -> np.ndarray:
+        return np.asarray([*self.translate, *self.rotate, self.scale], np.float32)
+
+    @staticmethod
+    def from_params(p) -> "TransformR":
+        p = [float(x) for x in np.asarray(p, np.float32).reshape(7)]
+        return TransformR(tuple(p[0:3]), tuple(p[3:6]), p[6])
+
+    def to_mat(self) -> np.ndarray:
+        """translate * rotZ * rotY * rotX * scale (scene.h:99-104), M[row, col]."""
+        p = self.params()
+        f = np.float32
+        T = identity4()
+        T[:3, 3] = p[:3]
+        c, s = f(math.cos(p[5])), f(math.sin(p[5]))
+        Rz = identity4()
+        Rz[0, 0], Rz[0, 1], Rz[1, 0], Rz[1, 1] = c, -s, s, c
+        c, s = f(math.cos(p[4])), f(math.sin(p[4]))
+        Ry = identity4()
+        Ry[0, 0], Ry[0, 2], Ry[2, 0], Ry[2, 2] = c, s, -s, c
+        c, s = f(math.cos(p[3])), f(math.sin(p[3]))
+        Rx = identity4()
+        Rx[1, 1], Rx[1, 2], Rx[2, 1], Rx[2, 2] = c, -s, s, c
+        S = np.diag([p[6], p[6], p[6], f(1)]).astype(np.float32)
+        return _mul44(_mul44(_mul44(_mul44(T, Rz), Ry), Rx), S)
+
+
 class Scene:
     """Scene (common_src/scene.h:121-247): meshes, each with instance transforms.
 
     Transforms are 4x4 matrices given in the usual row/column sense
     (``M[row, col]``); they are passed to the native side in the reference's
-    column-major memory order.
+    column-major memory order.  A mesh added with ``TransformR`` instances is
+    a RESTRICTED_TRANSFORM mesh (scene.h:140-148): ``restricted[i]`` holds
+    them and ``transforms[i]`` their matrices.
     """
 
     def __init__(self):
         self.meshes: List[TriangleMesh] = []
         self.transforms: List[List[np.ndarray]] = []
+        self.restricted: List[Optional[List[TransformR]]] = []
         self.names: List[str] = []
 
     def add_mesh(self, mesh: TriangleMesh, transforms=None, name: str = "") -> int:
         if transforms is None:
             transforms = [identity4()]
+        transforms = list(transforms)
         self.meshes.append(mesh)
-        self.transforms.append([np.asarray(t, dtype=np.float32).reshape(4, 4) for t in transforms])
+        if transforms and all(isinstance(t, TransformR) for t in transforms):
+            self.restricted.append(list(transforms))
+            self.transforms.append([t.to_mat() for t in transforms])
+        else:
+            self.restricted.append(None)
+            self.transforms.append([np.asarray(t, dtype=np.float32).reshape(4, 4) for t in transforms])
         self.names.append(name)
         return len(self.meshes) - 1
+
+    def get_restricted_transform(self, i: int) -> Optional[List[TransformR]]:
+        return self.restricted[i]
+
+    def restricted_params(self, i: int) -> Optional[np.ndarray]:
+        """7 floats per instance of a restricted mesh, else None."""
+        r = self.restricted[i]
+        return None if r is None else np.ascontiguousarray(np.concatenate([t.params() for t in r]))
 
     def get_mesh(self, i: int) -> TriangleMesh:
         return self.meshes[i]
@@ -119,8 +185,8 @@ class Scene:
 
     def copy(self) -> "Scene":
         s = Scene()
-        for m, t, n in zip(self.meshes, self.transforms, self.names):
-            s.add_mesh(m.copy(), [x.copy() for x in t], n)
+        for m, t, r, n in zip(self.meshes, self.transforms, self.restricted, self.names):
+            s.add_mesh(m.copy(), list(r) if r is not None else [x.copy() for x in t], n)
         return s
 
 

@@ -101,6 +101,12 @@ typedef struct drgb_mesh_desc {
   const float* transforms; /* 16*n_instances, column major; NULL = one identity instance */
   int32_t tex_w, tex_h, tex_channels; /* first texture; 0 when absent */
   const float* texture;    /* tex_w*tex_h*tex_channels or NULL */
+  /* Non-NULL: a RESTRICTED_TRANSFORM mesh (Scene::add_mesh with TransformR,
+   * common_src/scene.h:91-116,140-148), 7 floats per instance
+   * {translate x,y,z; rotate x,y,z (radians); scale}.  The instance matrices
+   * are TransformR::to_mat of these (`transforms` is ignored) and the
+   * gradient holds 7 values per instance in place of the 12 matrix entries. */
+  const float* restricted;
 } drgb_mesh_desc;
 
 typedef struct drgb_scene_desc {
@@ -159,7 +165,8 @@ int drgb_render(drgb_renderer* r, const drgb_camera* cams, int n_views, float* i
 /* Layout of the gradient vector of DScene(scene, mode, dmesh_ids)
  * (src/dmesh.h:35-85, 155-222): 9 ints per differentiable mesh
  * [vertices, instances, pos_off, color_off, tex_off, transform_off,
- *  restricted_off(-1), full_size, mesh_id]; *total = sum of full sizes. */
+ *  restricted_off, full_size, mesh_id]; *total = sum of full sizes.  A
+ * restricted mesh has transform_off -1, any other mesh restricted_off -1. */
 int drgb_dscene_layout(drgb_renderer* r, const int32_t* dmesh_ids, int n_ids, int32_t* layout, int64_t* total);
 
 /* IDiffRender::d_render (src/drender.h:144-167): accumulates (+=) into the
@@ -218,6 +225,10 @@ int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters);
 /* Current optimised parameters of one mesh (host arrays, may be NULL). */
 int drgb_optimizer_get_mesh(drgb_renderer* r, int mesh_id, float* vertices, float* colors, float* texture,
                             float* transforms);
+/* Current TransformR parameters of a restricted mesh (7 per instance,
+ * Scene::get_restricted_transform, scene.h:191); DRGB_ERR_INVALID for any
+ * other mesh. */
+int drgb_optimizer_get_restricted(drgb_renderer* r, int mesh_id, float* params);
 
 /* ---- batched optimisation (no reference counterpart: the reference runs one
  * OptSimple at a time, src/tests.cpp:125-204).  A batch advances many
@@ -248,6 +259,7 @@ int drgb_batch_sync(drgb_batch* b);
 int drgb_batch_job_losses(drgb_batch* b, int32_t job_id, int64_t first, int64_t n, float* out, int64_t* iters_done);
 int drgb_batch_get_mesh(drgb_batch* b, int32_t job_id, int mesh_id, float* vertices, float* colors, float* texture,
                         float* transforms);
+int drgb_batch_get_restricted(drgb_batch* b, int32_t job_id, int mesh_id, float* params);
 /* Device memory held by a job (for admission against a memory budget). */
 int64_t drgb_batch_job_device_bytes(drgb_batch* b, int32_t job_id);
 
@@ -309,6 +321,7 @@ int drgb_server_job_info(drgb_server* s, int32_t ticket, drgb_job_info* out);
 int drgb_server_job_losses(drgb_server* s, int32_t ticket, int64_t first, int64_t n, float* out);
 int drgb_server_get_mesh(drgb_server* s, int32_t ticket, int mesh_id, float* vertices, float* colors,
                          float* texture, float* transforms);
+int drgb_server_get_restricted(drgb_server* s, int32_t ticket, int mesh_id, float* params);
 /* Forgets a finished job's results. */
 int drgb_server_release(drgb_server* s, int32_t ticket);
 int drgb_server_get_stats(drgb_server* s, drgb_server_stats* out);

@@ -161,6 +161,65 @@ static void mat_identity(float* m) {
 }
 
 /* ---------------------------------------------------------------------------
+ * Restricted transforms (TransformR, scene.h:91-116).
+ * ------------------------------------------------------------------------- */
+/* to_mat: translate4x4(t) * rotate4x4Z(rz) * rotate4x4Y(ry) * rotate4x4X(rx)
+ * * scale4x4(s), products left to right (LiteMath.h:1474-1549). */
+void orc_restricted_to_mat(const float* p, float* out) {
+  float T[16], Rz[16], Ry[16], Rx[16], S[16], a[16], b[16];
+  mat_identity(T);
+  M(T, 0, 3) = p[0]; M(T, 1, 3) = p[1]; M(T, 2, 3) = p[2];
+  mat_identity(Rz);
+  M(Rz, 0, 0) = cosf(p[5]); M(Rz, 1, 0) = sinf(p[5]); M(Rz, 0, 1) = -sinf(p[5]); M(Rz, 1, 1) = cosf(p[5]);
+  mat_identity(Ry);
+  M(Ry, 0, 0) = cosf(p[4]); M(Ry, 2, 0) = -sinf(p[4]); M(Ry, 0, 2) = sinf(p[4]); M(Ry, 2, 2) = cosf(p[4]);
+  mat_identity(Rx);
+  M(Rx, 1, 1) = cosf(p[3]); M(Rx, 2, 1) = sinf(p[3]); M(Rx, 1, 2) = -sinf(p[3]); M(Rx, 2, 2) = cosf(p[3]);
+  mat_identity(S);
+  M(S, 0, 0) = p[6]; M(S, 1, 1) = p[6]; M(S, 2, 2) = p[6];
+  mat_mul(T, Rz, a);
+  mat_mul(a, Ry, b);
+  mat_mul(b, Rx, a);
+  mat_mul(a, S, out);
+}
+
+/* Row-major 3x4 product with translation, `mul` of drender_autodiff.cpp:22-43. */
+static void mul34(const float* a, const float* b, float* out) {
+  float r[12];
+  for (int i = 0; i < 3; i++) {
+    for (int j = 0; j < 3; j++) r[4 * i + j] = a[4 * i + 0] * b[j] + a[4 * i + 1] * b[4 + j] + a[4 * i + 2] * b[8 + j];
+    r[4 * i + 3] = a[4 * i + 0] * b[3] + a[4 * i + 1] * b[7] + a[4 * i + 2] * b[11] + a[4 * i + 3];
+  }
+  memcpy(out, r, sizeof(r));
+}
+
+/* dmat_dtransforms_jac_f (drender_autodiff.cpp:78-95) builds
+ * out = Rz (Ry (Rx S)) + translation; its derivative for each parameter is
+ * the same chain with one factor replaced by that factor's derivative
+ * (d/dr of {cos r, sin r} = {-sin r, cos r}), the translation entries have
+ * derivative 1.  Row k of jac is d out / d params[k]. */
+void orc_restricted_jacobian(const float* x, float* jac) {
+  const float sx = sinf(x[3]), cx = cosf(x[3]), sy = sinf(x[4]), cy = cosf(x[4]), sz = sinf(x[5]), cz = cosf(x[5]);
+  const float S[12] = {x[6], 0, 0, 0, 0, x[6], 0, 0, 0, 0, x[6], 0};
+  const float dS[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  const float Rx[12] = {1, 0, 0, 0, 0, cx, -sx, 0, 0, sx, cx, 0};
+  const float Ry[12] = {cy, 0, sy, 0, 0, 1, 0, 0, -sy, 0, cy, 0};
+  const float Rz[12] = {cz, -sz, 0, 0, sz, cz, 0, 0, 0, 0, 1, 0};
+  const float dRx[12] = {0, 0, 0, 0, 0, -sx, -cx, 0, 0, cx, -sx, 0};
+  const float dRy[12] = {-sy, 0, cy, 0, 0, 0, 0, 0, -cy, 0, -sy, 0};
+  const float dRz[12] = {-sz, -cz, 0, 0, cz, -sz, 0, 0, 0, 0, 0, 0};
+  float a[12], b[12];
+  memset(jac, 0, 84 * sizeof(float));
+  jac[0 * 12 + 3] = 1.0f;
+  jac[1 * 12 + 7] = 1.0f;
+  jac[2 * 12 + 11] = 1.0f;
+  mul34(dRx, S, a); mul34(Ry, a, b); mul34(Rz, b, jac + 3 * 12);
+  mul34(Rx, S, a); mul34(dRy, a, b); mul34(Rz, b, jac + 4 * 12);
+  mul34(Rx, S, a); mul34(Ry, a, b); mul34(dRz, b, jac + 5 * 12);
+  mul34(Rx, dS, a); mul34(Ry, a, b); mul34(Rz, b, jac + 6 * 12);
+}
+
+/* ---------------------------------------------------------------------------
  * Camera: CamInfo (common_src/camera.h:9-44), lookAt / perspectiveMatrix
  * (LiteMath.h:1679-1729), BruteForce3D::SetCamera (raytrace3d_bf.cpp:93-100).
  * ------------------------------------------------------------------------- */
@@ -239,6 +298,10 @@ typedef struct {
 } prep_t;
 
 static const float* mesh_tr(const orc_mesh* m, int j, float* tmp) {
+  if (m->restricted) {
+    orc_restricted_to_mat(m->restricted + 7 * j, tmp);
+    return tmp;
+  }
   if (m->transforms) return m->transforms + 16 * j;
   mat_identity(tmp);
   return tmp;
@@ -689,7 +752,7 @@ static f3 shade(const ctx_t* c, f2 sp) {
  * Gradient layout (DMesh, dmesh.h:35-85).
  * ------------------------------------------------------------------------- */
 typedef struct {
-  int vertices, instances, pos_off, color_off, tex_off, tr_off, full;
+  int vertices, instances, pos_off, color_off, tex_off, tr_off, rt_off, full;
 } dlayout_t;
 
 static int mode_has_color(int mode) { return mode == ORC_VERTEX_COLOR || mode == ORC_LAMBERT_POINT_VCOLOR || mode == ORC_PATH_DIFFUSE; }
@@ -708,7 +771,10 @@ static dlayout_t make_layout(const orc_mesh* m, int mode) {
   if (mode_has_color(mode)) { L.color_off = off; off += 3 * m->n_vertices; }
   L.tex_off = -1;
   if (mode_has_tex(mode) && m->texture) { L.tex_off = off; off += tex; }
-  L.tr_off = off; off += 12 * m->n_instances;
+  /* transform matrices, or the restricted parameters (dmesh.h:42-50,76-84) */
+  L.tr_off = L.rt_off = -1;
+  if (m->restricted) { L.rt_off = off; off += 7 * m->n_instances; }
+  else { L.tr_off = off; off += 12 * m->n_instances; }
   L.full = off;
   return L;
 }
@@ -721,7 +787,7 @@ int orc_dscene_layout(const orc_mesh* meshes, int n_meshes, int mode, const int3
     dlayout_t L = make_layout(meshes + ids[k], mode);
     int32_t* o = layout + 9 * k;
     o[0] = L.vertices; o[1] = L.instances; o[2] = L.pos_off; o[3] = L.color_off; o[4] = L.tex_off;
-    o[5] = L.tr_off; o[6] = -1; o[7] = L.full; o[8] = ids[k];
+    o[5] = L.tr_off; o[6] = L.rt_off; o[7] = L.full; o[8] = ids[k];
     t += L.full;
   }
   if (total) *total = t;
@@ -1134,9 +1200,26 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
       const float* P = dpos + (int64_t)th * (pos_total + 1) + pos_base[k];
       for (int j = 0; j < 3 * L->vertices; j++) g[L->pos_off + j] += P[j];
     }
-    for (int th = 0; th < REF_THREADS; th++) {
-      const float* T = dtr + (int64_t)th * (tr_total + 1) + tr_base[k];
-      for (int j = 0; j < 12 * L->instances; j++) g[L->tr_off + j] += T[j];
+    if (L->tr_off >= 0) {
+      for (int th = 0; th < REF_THREADS; th++) {
+        const float* T = dtr + (int64_t)th * (tr_total + 1) + tr_base[k];
+        for (int j = 0; j < 12 * L->instances; j++) g[L->tr_off + j] += T[j];
+      }
+    } else {
+      /* restricted: the matrix gradient through the Jacobian of to_mat (drender.h:398-421) */
+      float* mat = (float*)calloc(12 * (size_t)L->instances, sizeof(float));
+      for (int th = 0; th < REF_THREADS; th++) {
+        const float* T = dtr + (int64_t)th * (tr_total + 1) + tr_base[k];
+        for (int j = 0; j < 12 * L->instances; j++) mat[j] += T[j];
+      }
+      const float* rp = s->meshes[dm->ids[k]].restricted;
+      for (int j = 0; j < L->instances; j++) {
+        float jac[84];
+        orc_restricted_jacobian(rp + 7 * j, jac);
+        for (int q = 0; q < 7; q++)
+          for (int l = 0; l < 12; l++) g[L->rt_off + 7 * j + q] += jac[12 * q + l] * mat[12 * j + l];
+      }
+      free(mat);
     }
   }
   free(dpos); free(dtr); free(pmf); free(cdf); free(E); free(p2);
@@ -1292,7 +1375,8 @@ void orc_opt_params_default(int alg, orc_opt_params* p) {
 
 int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, const orc_model_params* mp,
                  const float* cams, int n_views, const float* targets, const orc_opt_params* P, int iters,
-                 float* final_error, float* losses, float* traj_v, float* traj_c, float* traj_t, float* traj_tr) {
+                 float* final_error, float* losses, float* traj_v, float* traj_c, float* traj_t, float* traj_tr,
+                 float* traj_rt) {
   orc_model_params dmp;
   if (!mp) { orc_default_model_params(&dmp); mp = &dmp; }
   /* private copy of the scene (OptSimple::m_scene) */
@@ -1301,6 +1385,7 @@ int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, con
   float** cbuf = (float**)calloc(n_meshes, sizeof(float*));
   float** tbuf = (float**)calloc(n_meshes, sizeof(float*));
   float** trbuf = (float**)calloc(n_meshes, sizeof(float*));
+  float** rbuf = (float**)calloc(n_meshes, sizeof(float*));
   for (int i = 0; i < n_meshes; i++) {
     ms[i] = meshes_in[i];
     vbuf[i] = (float*)malloc(sizeof(float) * 3 * ms[i].n_vertices);
@@ -1317,10 +1402,15 @@ int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, con
       memcpy(tbuf[i], meshes_in[i].texture, sizeof(float) * nt);
       ms[i].texture = tbuf[i];
     }
+    if (meshes_in[i].restricted) {
+      rbuf[i] = (float*)malloc(sizeof(float) * 7 * ms[i].n_instances);
+      memcpy(rbuf[i], meshes_in[i].restricted, sizeof(float) * 7 * ms[i].n_instances);
+      ms[i].restricted = rbuf[i];
+    }
     trbuf[i] = (float*)malloc(sizeof(float) * 16 * ms[i].n_instances);
     for (int j = 0; j < ms[i].n_instances; j++) {
-      if (meshes_in[i].transforms) memcpy(trbuf[i] + 16 * j, meshes_in[i].transforms + 16 * j, 16 * sizeof(float));
-      else mat_identity(trbuf[i] + 16 * j);
+      float tmp[16];
+      memcpy(trbuf[i] + 16 * j, mesh_tr(ms + i, j, tmp), 16 * sizeof(float));
     }
     ms[i].transforms = trbuf[i];
   }
@@ -1337,14 +1427,14 @@ int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, con
     lr_off[k][n] = 0; lr_val[k][n++] = P->position_lr;
     if (dm.lay[k].color_off >= 0) { lr_off[k][n] = dm.lay[k].color_off; lr_val[k][n++] = P->base_lr; }
     if (dm.lay[k].tex_off >= 0) { lr_off[k][n] = dm.lay[k].tex_off; lr_val[k][n++] = P->textures_lr; }
-    lr_off[k][n] = dm.lay[k].tr_off; lr_val[k][n++] = P->transforms_lr;
+    lr_off[k][n] = dm.lay[k].tr_off >= 0 ? dm.lay[k].tr_off : dm.lay[k].rt_off; lr_val[k][n++] = P->transforms_lr;
     lr_n[k] = n;
   }
   /* the inverse of mesh 0's transforms is taken once, at the first prepare
    * (Scene::prepare_for_render appends to transforms_inv, scene_utils.cpp:118-129) */
   float* tr_inv0 = (float*)malloc(sizeof(float) * 16 * ms[0].n_instances);
   for (int j = 0; j < ms[0].n_instances; j++) mat_inverse(ms[0].transforms + 16 * j, tr_inv0 + 16 * j);
-  int64_t off_v = 0, off_c = 0, off_t = 0, off_tr = 0;
+  int64_t off_v = 0, off_c = 0, off_t = 0, off_tr = 0, off_rt = 0;
   float err = 0.0f;
   for (int it = 0; it < iters; it++) {
     prep_t s;
@@ -1387,10 +1477,15 @@ int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, con
       const dlayout_t* L = dm.lay + k;
       if (P->flags & 1)
         for (int v = 0; v < 3 * m->n_vertices; v++) vbuf[mid][v] -= g[L->pos_off + v];
-      if (P->flags & 2)
+      if ((P->flags & 2) && L->tr_off >= 0)
         for (int j = 0; j < m->n_instances; j++)
           for (int r = 0; r < 3; r++)
             for (int c2 = 0; c2 < 4; c2++) M(trbuf[mid] + 16 * j, r, c2) -= g[L->tr_off + 12 * j + 4 * r + c2];
+      if ((P->flags & 2) && L->rt_off >= 0) {
+        /* translate, rotate, scale -= step; the matrices follow at the next prepare */
+        for (int j = 0; j < 7 * m->n_instances; j++) rbuf[mid][j] -= g[L->rt_off + j];
+        for (int j = 0; j < m->n_instances; j++) orc_restricted_to_mat(rbuf[mid] + 7 * j, trbuf[mid] + 16 * j);
+      }
       if (L->color_off >= 0 && (P->flags & 4) && cbuf[mid])
         for (int v = 0; v < 3 * m->n_vertices; v++) cbuf[mid][v] -= g[L->color_off + v];
       if (mode != ORC_SILHOUETTE && mode != ORC_VERTEX_COLOR && (P->flags & 8) && L->tex_off >= 0 && tbuf[mid]) {
@@ -1412,11 +1507,12 @@ int orc_optimize(const orc_mesh* meshes_in, int n_meshes, int mode, int spp, con
         off_t += nt;
       }
       if (traj_tr) { memcpy(traj_tr + off_tr, trbuf[i], sizeof(float) * 16 * ms[i].n_instances); off_tr += 16 * ms[i].n_instances; }
+      if (traj_rt && rbuf[i]) { memcpy(traj_rt + off_rt, rbuf[i], sizeof(float) * 7 * ms[i].n_instances); off_rt += 7 * ms[i].n_instances; }
     }
   }
   if (final_error) *final_error = err;
-  for (int i = 0; i < n_meshes; i++) { free(vbuf[i]); free(cbuf[i]); free(tbuf[i]); free(trbuf[i]); }
-  free(vbuf); free(cbuf); free(tbuf); free(trbuf); free(ms);
+  for (int i = 0; i < n_meshes; i++) { free(vbuf[i]); free(cbuf[i]); free(tbuf[i]); free(trbuf[i]); free(rbuf[i]); }
+  free(vbuf); free(cbuf); free(tbuf); free(trbuf); free(rbuf); free(ms);
   free(grad); free(G); free(mv); free(tr_inv0);
   return 0;
 }

@@ -50,6 +50,10 @@ typedef struct orc_mesh {
   const float* transforms; /* 16 floats per instance, column-major; NULL = identity */
   int32_t tex_w, tex_h, tex_channels;
   const float* texture; /* may be NULL */
+  /* RESTRICTED_TRANSFORM mesh (scene.h:91-116,140-148): 7 floats per
+   * instance {translate xyz, rotate xyz (radians), scale}; the matrices are
+   * TransformR::to_mat of these and `transforms` is ignored.  NULL otherwise. */
+  const float* restricted;
 } orc_mesh;
 
 /* Camera: 82 floats = world_view[16] proj[16] wvp[16] proj_inv[16] wv_inv[16] width height. */
@@ -82,7 +86,8 @@ int orc_render(const orc_mesh* meshes, int n_meshes, int mode, int spp, const or
 
 /* Size/layout of the DMesh gradient block of each differentiable mesh
  * (dmesh.h:35-85): per mesh 9 ints [vertices, instances, pos_off, color_off,
- * tex_off, transform_off, restricted_off(-1), full_size, mesh_id]. */
+ * tex_off, transform_off, restricted_off, full_size, mesh_id]; a restricted
+ * mesh has transform_off -1, every other mesh restricted_off -1. */
 int orc_dscene_layout(const orc_mesh* meshes, int n_meshes, int mode, const int32_t* dmesh_ids, int n_ids,
                       int32_t* layout, int64_t* total);
 
@@ -112,11 +117,20 @@ void orc_opt_params_default(int alg, orc_opt_params* p);
 /* OptSimple::Run (optimizer_simple.cpp:272-309).  Meshes are copied; the
  * optimised vertices/colors/textures/transforms of every iteration are
  * written to the optional trajectory arrays (per iteration, per mesh,
- * concatenated), and the loss of every iteration to losses. */
+ * concatenated; transforms are the matrices the next iteration renders
+ * with), the restricted parameters (7 per instance of each restricted mesh)
+ * to traj_restricted, and the loss of every iteration to losses. */
 int orc_optimize(const orc_mesh* meshes, int n_meshes, int mode, int spp, const orc_model_params* mp, const float* cams,
                  int n_views, const float* targets, const orc_opt_params* p, int iters, float* final_error,
                  float* losses, float* traj_vertices, float* traj_colors, float* traj_textures,
-                 float* traj_transforms);
+                 float* traj_transforms, float* traj_restricted);
+
+/* TransformR::to_mat (scene.h:99-104): column-major 4x4 of 7 parameters. */
+void orc_restricted_to_mat(const float* params7, float* out16);
+/* d(to_mat)/d(params), jac[7][12] over the row-major 3x4 part: what the
+ * Enzyme forward pass of drender_autodiff.cpp:78-107 computes, derived
+ * analytically (the plugin is not part of this build). */
+void orc_restricted_jacobian(const float* params7, float* jac84);
 
 /* Random streams of the edge sampler (qmc.cpp:250-268, drender.h:306-331). */
 void orc_prng(int seed, int count, float* out);

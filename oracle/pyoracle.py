@@ -37,7 +37,8 @@ class OrcMesh(C.Structure):
     _fields_ = [("n_vertices", C.c_int32), ("n_indices", C.c_int32), ("vertices", C.c_void_p),
                 ("colors", C.c_void_p), ("tc", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p),
                 ("indices", C.c_void_p), ("n_instances", C.c_int32), ("transforms", C.c_void_p),
-                ("tex_w", C.c_int32), ("tex_h", C.c_int32), ("tex_channels", C.c_int32), ("texture", C.c_void_p)]
+                ("tex_w", C.c_int32), ("tex_h", C.c_int32), ("tex_channels", C.c_int32), ("texture", C.c_void_p),
+                ("restricted", C.c_void_p)]
 
 
 class OrcModelParams(C.Structure):
@@ -79,12 +80,13 @@ class _Scene:
         self.arr = (OrcMesh * max(1, len(scene.meshes)))()
         for i, m in enumerate(scene.meshes):
             tr = scene.transforms_colmajor(i)
-            self.keep.append(tr)
+            rp = scene.restricted_params(i)
+            self.keep += [tr, rp]
             tex = m.textures[0] if m.textures else None
             self.arr[i] = OrcMesh(m.vertex_count, m.indices.size, _addr(m.vertices), _addr(m.colors), _addr(m.tc),
                                   _addr(m.normals), _addr(m.tangents), _addr(m.indices), len(scene.transforms[i]),
                                   _addr(tr), tex.w if tex else 0, tex.h if tex else 0, tex.channels if tex else 0,
-                                  _addr(tex.data) if tex else None)
+                                  _addr(tex.data) if tex else None, _addr(rp))
         self.n = len(scene.meshes)
 
 
@@ -211,6 +213,8 @@ def optimize(scene, cams, mode, spp, targets, params, iters, mp=None):
     nc = sum(3 * m.vertex_count for m in scene.meshes if m.colors is not None)
     nt = sum(m.textures[0].data.size for m in scene.meshes if m.textures)
     ntr = sum(16 * len(t) for t in scene.transforms)
+    nrt = sum(7 * len(r) for r in scene.restricted if r is not None)
+    trt = np.zeros(iters * max(nrt, 1), dtype=np.float32)
     tv = np.zeros(iters * nv, dtype=np.float32)
     tcol = np.zeros(iters * max(nc, 1), dtype=np.float32)
     ttex = np.zeros(iters * max(nt, 1), dtype=np.float32)
@@ -220,13 +224,30 @@ def optimize(scene, cams, mode, spp, targets, params, iters, mp=None):
     mp = mp or model_params()
     r = lib().orc_optimize(sc.arr, sc.n, mode, spp, C.byref(mp), _ptr(cb), len(cams), _ptr(tg), C.byref(params),
                            iters, C.byref(fe), _ptr(losses), _ptr(tv), _ptr(tcol) if nc else None,
-                           _ptr(ttex) if nt else None, _ptr(ttr))
+                           _ptr(ttex) if nt else None, _ptr(ttr), _ptr(trt) if nrt else None)
     if r != 0:
         raise RuntimeError("orc_optimize failed")
     return {"final_error": float(fe.value), "losses": losses, "vertices": tv.reshape(iters, -1),
             "colors": tcol[:iters * nc].reshape(iters, -1) if nc else None,
             "textures": ttex[:iters * nt].reshape(iters, -1) if nt else None,
-            "transforms": ttr.reshape(iters, -1)}
+            "transforms": ttr.reshape(iters, -1),
+            "restricted": trt[:iters * nrt].reshape(iters, -1) if nrt else None}
+
+
+def restricted_to_mat(params):
+    """Column-major 4x4 of TransformR parameters (translate xyz, rotate xyz, scale)."""
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(7))
+    out = np.zeros(16, dtype=np.float32)
+    lib().orc_restricted_to_mat(_ptr(p), _ptr(out))
+    return out
+
+
+def restricted_jacobian(params):
+    """jac[7][12]: derivative of the row-major 3x4 of to_mat by each parameter."""
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(7))
+    out = np.zeros(84, dtype=np.float32)
+    lib().orc_restricted_jacobian(_ptr(p), _ptr(out))
+    return out.reshape(7, 12)
 
 
 def prng(seed, count):

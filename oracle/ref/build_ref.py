@@ -8,10 +8,13 @@ Test infrastructure only.  Recipe:
      common_src/scene.h:105-115 wraps float3 members in an anonymous union,
      a clang extension that g++ rejects ("member with constructor not allowed
      in anonymous aggregate").  The union becomes plain members; the aliased
-     ``M[7]`` view is only read by the Enzyme restricted-transform Jacobian,
-     which is stubbed to zero because the Enzyme plugin is absent;
+     ``M[7]`` view (read only by the restricted-transform Jacobian) becomes a
+     mutable array that ``to_mat()`` -- called by every prepare_for_render
+     before a gradient pass -- fills with the same 7 values;
   3. compile with g++ -O3 -fopenmp -DUSE_OMP (the flags of the reference's
-     own CMakeLists.txt:79-85,91) together with oracle/ref/ref_driver.cpp.
+     own CMakeLists.txt:79-85,91) together with oracle/ref/ref_driver.cpp and
+     the oracle's C file, whose analytic TransformR Jacobian stands in for the
+     absent Enzyme plugin (src/drender_autodiff.cpp:97-107).
 
 The reference's CMake build, Embree (missing binary) and Mitsuba (not
 installed) are not used.  Where the reference tree is absent, the patched copy under oracle/_ref/src
@@ -59,9 +62,14 @@ def _copy_tree():
     scene_h = os.path.join(src_root, "common_src", "scene.h")
     text = open(scene_h).read()
     pat = re.compile(r"union\s*\{\s*struct\s*\{\s*float3 translate;\s*float3 rotate;\s*float scale;\s*\};\s*float M\[7\];\s*\};")
-    new, n = pat.subn("float3 translate; float3 rotate; float scale; float M[7];", text)
+    new, n = pat.subn("float3 translate; float3 rotate; float scale; mutable float M[7];", text)
     if n != 1:
         raise RuntimeError("TransformR union not found in scene.h; the reference layout changed")
+    fill = ("M[0] = translate.x; M[1] = translate.y; M[2] = translate.z; "
+            "M[3] = rotate.x; M[4] = rotate.y; M[5] = rotate.z; M[6] = scale;")
+    new, n = re.subn(r"(float4x4 to_mat\(\) const\s*\{)", lambda m: m.group(1) + " " + fill, new)
+    if n != 1:
+        raise RuntimeError("TransformR::to_mat not found in scene.h; the reference layout changed")
     open(scene_h, "w").write(new)
     return src_root
 
@@ -88,7 +96,7 @@ def _includes(src_root):
     incs = []
     for d in HEADER_DIRS + ["stub"]:
         incs += ["-I", os.path.join(src_root, d)]
-    return incs + ["-I", HERE]
+    return incs + ["-I", HERE, "-I", ORACLE]
 
 
 FLAGS = ["g++", "-std=c++17", "-O3", "-fopenmp", "-DUSE_OMP", "-ffp-contract=off", "-w"]
@@ -121,6 +129,16 @@ def _stale(exe, deps):
     return not os.path.exists(exe) or any(os.path.getmtime(exe) < os.path.getmtime(d) for d in deps)
 
 
+def _oracle_object():
+    """oracle.c compiled for the driver (its TransformR Jacobian)."""
+    src, hdr = os.path.join(ORACLE, "oracle.c"), os.path.join(ORACLE, "oracle.h")
+    obj = os.path.join(BIN, "oracle.o")
+    if _stale(obj, [src, hdr, __file__]):
+        subprocess.check_call(["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-w", "-c",
+                               src, "-o", obj])
+    return obj
+
+
 def build(verbose=False):
     """oracle/_ref/<arch>/ref_driver: the reference's CPU path behind the driver."""
     src_root = _source_tree(verbose)
@@ -128,7 +146,7 @@ def build(verbose=False):
         return None
     os.makedirs(BIN, exist_ok=True)
     exe = os.path.join(BIN, "ref_driver")
-    objs = _objects(src_root)
+    objs = _objects(src_root) + [_oracle_object()]
     deps = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "kvio.h"), __file__] + objs
     if _stale(exe, deps):
         subprocess.check_call(FLAGS + _includes(src_root) + [os.path.join(HERE, "ref_driver.cpp")] + objs +
@@ -150,7 +168,7 @@ def build_gpu_driver(verbose=False):
     include = os.path.join(os.path.dirname(ORACLE), "include")
     os.makedirs(BIN, exist_ok=True)
     exe = os.path.join(BIN, "ref_driver_gpu")
-    objs = _objects(src_root)
+    objs = _objects(src_root) + [_oracle_object()]
     srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(adapter, "gpu_drender.cpp")]
     deps = srcs + [os.path.join(adapter, "gpu_drender.h"), os.path.join(HERE, "kvio.h"), __file__, lib] + objs
     if _stale(exe, deps):

@@ -26,16 +26,22 @@
 #include "raytrace.h"
 #include "kvio.h"
 #include "ref_pointlight.h"
+#include "oracle.h"
 #ifdef DRGB_WITH_GPU
 #include "gpu_drender.h"  // the GPU IDiffRender / IOptimizer (diffrender_tutorials_gb300/cpp)
 #endif
 
 using namespace diff_render;
 
-// The Enzyme plugin is absent; the restricted-transform Jacobian it would
-// produce (src/drender_autodiff.cpp:97-107) is left at zero, exactly what a
-// build without the plugin computes.  No fixture uses restricted transforms.
-void dmat_dtransforms_jac(float const mat[7], float jac[7][12]) { (void)mat; (void)jac; }
+// The Enzyme plugin is absent, so the restricted-transform Jacobian it
+// would produce (src/drender_autodiff.cpp:97-107, the forward derivative of
+// dmat_dtransforms_jac_f, :78-95) comes from the oracle's analytic form of
+// the same derivative (oracle.c, orc_restricted_jacobian; pinned against
+// central differences of to_mat by the tests).  Everything around it -- the
+// chain rule over the 12 matrix gradients, the layout, the optimiser update
+// -- is the reference's own code.  `mat` is TransformR::M, which to_mat()
+// fills in the patched scene.h (build_ref.py).
+void dmat_dtransforms_jac(float const mat[7], float jac[7][12]) { orc_restricted_jacobian(mat, &jac[0][0]); }
 
 // backend 0: the reference's CPU renderer; 1: the GPU renderer behind the
 // same interface (the reference's own code drives it); 2 (optimiser task):
@@ -92,6 +98,16 @@ static void build_scene(const kv::File& in, Scene& scene) {
       t.channels = shape[2];
       t.m_data = in.vec<float>(key(m, "tex"));
       mesh.textures.push_back(t);
+    }
+    if (in.has(key(m, "restricted"))) {  // Scene::add_mesh with TransformR (scene.h:140-148)
+      auto rp = in.vec<float>(key(m, "restricted"));
+      std::vector<TransformR> rts;
+      for (size_t k = 0; k < rp.size() / 7; k++) {
+        const float* q = rp.data() + 7 * k;
+        rts.push_back(TransformR(float3(q[0], q[1], q[2]), float3(q[3], q[4], q[5]), q[6]));
+      }
+      scene.add_mesh(mesh, rts);
+      continue;
     }
     std::vector<float4x4> trs;
     if (in.has(key(m, "transforms"))) {
@@ -197,6 +213,14 @@ static void scene_out(kv::File& out, const std::string& prefix, const Scene& s) 
     std::vector<float> t;
     for (auto& M : s.get_transform(m)) { auto mv = mat_to_vec(M); t.insert(t.end(), mv.begin(), mv.end()); }
     out.put_f32(b + "transforms", t);
+    if (s.get_instancing_type(m) == Scene::RESTRICTED_TRANSFORM) {
+      std::vector<float> r;
+      for (auto& R : s.get_restricted_transform(m)) {
+        const float q[7] = {R.translate.x, R.translate.y, R.translate.z, R.rotate.x, R.rotate.y, R.rotate.z, R.scale};
+        r.insert(r.end(), q, q + 7);
+      }
+      out.put_f32(b + "restricted", r);
+    }
   }
 }
 

@@ -32,6 +32,9 @@ def scene_items(scene):
             it[p + "tex"] = t.data
             it[p + "tex_shape"] = np.array([t.w, t.h, t.channels], np.int32)
         it[p + "transforms"] = scene.transforms_colmajor(i)
+        rp = scene.restricted_params(i) if hasattr(scene, "restricted_params") else None
+        if rp is not None:
+            it[p + "restricted"] = rp
     return it
 
 

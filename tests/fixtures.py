@@ -10,7 +10,7 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-from diffrender_tutorials_gb300.scene import CamInfo, Scene, Texture, TriangleMesh  # noqa: E402
+from diffrender_tutorials_gb300.scene import CamInfo, Scene, Texture, TransformR, TriangleMesh  # noqa: E402
 
 
 def load(name):
@@ -28,6 +28,9 @@ def scene_from(d):
             tex = [Texture(w, h, c, d[p + "tex"])]
         m = TriangleMesh(get("vertices"), get("indices"), colors=get("colors"), tc=get("tc"), normals=get("normals"),
                          tangents=get("tangents"), textures=tex)
+        if p + "restricted" in d:
+            s.add_mesh(m, [TransformR.from_params(q) for q in d[p + "restricted"].reshape(-1, 7)])
+            continue
         tr = d[p + "transforms"].reshape(-1, 4, 4)
         s.add_mesh(m, [t.T.copy() for t in tr])  # stored column-major
     return s

@@ -24,8 +24,8 @@ import build_ref  # noqa: E402
 import kvio  # noqa: E402,F401
 import refrun  # noqa: E402
 from refrun import cam_items, scene_items  # noqa: E402
-from diffrender_tutorials_gb300.scene import (Scene, TriangleMesh, Texture, make_cube, make_icosphere,  # noqa: E402
-                                              perturb_vertices, identity4)
+from diffrender_tutorials_gb300.scene import (Scene, TriangleMesh, Texture, TransformR, make_cube,  # noqa: E402
+                                              make_icosphere, perturb_vertices, identity4)
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 SIL, VC, TEX, LAMBERT, PHONG, GGX = 1, 2, 3, 4, 5, 6
@@ -50,6 +50,15 @@ def textured_sphere(sub=2, tex_size=16, seed=3):
     tex = rng.uniform(0.1, 0.9, size=(tex_size, tex_size, 3)).astype(np.float32)
     return TriangleMesh(m.vertices, m.indices, tc=np.stack([u, v], 1).astype(np.float32), normals=m.normals,
                         textures=[Texture(tex_size, tex_size, 3, tex.reshape(-1))])
+
+
+def pyramid(seed=4):
+    """Square pyramid, 5 vertices / 6 triangles, random vertex colours."""
+    v = np.array([[-0.5, -0.5, -0.5], [0.5, -0.5, -0.5], [0.5, -0.5, 0.5], [-0.5, -0.5, 0.5], [0.0, 0.5, 0.0]],
+                 np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3, 0, 4, 1, 1, 4, 2, 2, 4, 3, 3, 4, 0], np.uint32)
+    col = np.random.default_rng(seed).uniform(0.2, 0.9, size=(5, 3)).astype(np.float32)
+    return TriangleMesh(v, idx, colors=col)
 
 
 def save(name, **arrays):
@@ -163,6 +172,39 @@ def main():
              "dmesh_ids": np.array([0], np.int32)}
     out = run(items)
     save("drc_cube_instanced", **items, **prefixed("out.", out))
+
+    # restricted transforms (TransformR: translation, rotation, scale per
+    # instance; TEST 2.11 of src/tests.cpp:350-361): forward render through
+    # to_mat, gradients of the 7 parameters per instance, and a trajectory
+    pyr = pyramid()
+    r_true = [TransformR((-0.6, 0.0, 0.0), (0.0, 0.0, 0.0), 1.0), TransformR((0.6, 0.1, -0.2), (0.3, 0.0, 0.0), 0.8)]
+    r_init = [TransformR((-0.55, 0.05, 0.0), (0.0, 0.2, 0.2), 1.05),
+              TransformR((0.65, 0.05, -0.2), (0.25, -0.1, 0.15), 0.85)]
+    tsr, isr = Scene(), Scene()
+    tsr.add_mesh(pyr, r_true)
+    isr.add_mesh(pyr, r_init)
+    cams_r = [Cam((0.3, 0.9, 2.8), 64, 64)]
+    items = {"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+             **scene_items(isr), **cam_items(cams_r)}
+    save("render_pyramid_restricted", **items, **prefixed("out.", run(items)))
+    # (the brute-force caster applies instance matrices twice, raytrace3d_bf.cpp:116-125,
+    # so a silhouette model sees no edge of a rotated instance; VC and the point light do)
+    for mode in (VC, 16):
+        tg = run({"task": np.array([2], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([16], np.int32),
+                  **scene_items(tsr), **cam_items(cams_r)})["images"]
+        items = {"task": np.array([4], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([16], np.int32),
+                 **scene_items(isr), **cam_items(cams_r), "targets": tg, "edge_samples": np.array([64 * 64], np.int32),
+                 "dmesh_ids": np.array([0], np.int32)}
+        save(f"drc_pyramid_restricted_m{mode}", **items, **prefixed("out.", run(items)))
+    cams_o = [Cam((0.3, 0.9, 2.8), 48, 48)]
+    tg = run({"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+              **scene_items(tsr), **cam_items(cams_o)})["images"]
+    items = {"task": np.array([5], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([16], np.int32),
+             **scene_items(isr), **cam_items(cams_o), "targets": tg, "iters": np.array([5], np.int32),
+             "opt_alg": np.array([4], np.int32), "opt_pos_lr": np.array([0.0], np.float32),
+             "opt_tfm_lr": np.array([0.05], np.float32), "opt_flags": np.array([2], np.int32),
+             "dmesh_ids": np.array([0], np.int32)}
+    save("optimize_pyramid_restricted", **items, **prefixed("out.", run(items)))
 
     # two views, d_render with a given adjoint (accumulation over views)
     cams2 = [Cam((0, 0, 3), 48, 48), Cam((2.2, 1.0, 1.8), 48, 48)]

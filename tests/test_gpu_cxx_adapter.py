@@ -23,7 +23,7 @@ import refrun  # noqa: E402
 
 import diffrender_tutorials_gb300 as D  # noqa: E402
 from diffrender_tutorials_gb300.scene import Texture, TriangleMesh  # noqa: E402
-from fixtures import rel_l2  # noqa: E402
+from fixtures import load, rel_l2  # noqa: E402
 
 VC, TEX, LAMBERT = 2, 3, 4
 
@@ -123,6 +123,24 @@ def test_reference_optimiser_and_gpu_optimiser_follow_the_cpu_trajectory():
             for what in ("vertices", "colors"):
                 a, b = runs[0][f"it{k}.m0.{what}"], runs[be][f"it{k}.m0.{what}"]
                 assert np.abs(a - b).max() < 5e-5, (be, k, what)
+
+
+@pytest.mark.gpu
+def test_restricted_transforms_behind_reference_interface():
+    """TransformR meshes through the adapter: the reference's OptSimple over
+    the GPU renderer (backend 1) and the GPU optimiser (backend 2) follow the
+    reference's own trajectory of the 7 parameters per instance."""
+    exe = driver()
+    d = load("optimize_pyramid_restricted")
+    items = {k: v for k, v in d.items() if not k.startswith("out.")}
+    iters = int(d["iters"][0])
+    for be in (1, 2):
+        out = refrun.run(exe, {**items, "backend": np.array([be], np.int32)})
+        assert int(out["n_iters"][0]) == iters
+        for k in range(iters):
+            got, ref = out[f"it{k}.m0.restricted"], d[f"out.it{k}.m0.restricted"]
+            assert np.abs(got - ref).max() < 5e-5, (be, k)
+        assert float(out["final_error"][0]) == pytest.approx(float(d["out.final_error"][0]), rel=1e-4)
 
 
 def test_adapter_builds_against_reference_headers():

@@ -38,14 +38,17 @@ def split_grad(vec, layout):
     pos, col = [], []
     off = 0
     for row in layout:
-        nv, ninst, p, c, t, tr, _, full = (int(x) for x in row[:8])
+        nv, ninst, p, c, t, tr, rt, full = (int(x) for x in row[:8])
         blk = vec[off:off + full]
         pos.append(blk[p:p + 3 * nv])
-        pos.append(blk[tr:tr + 12 * ninst])
+        if tr >= 0:
+            pos.append(blk[tr:tr + 12 * ninst])
+        if rt >= 0:  # restricted transform parameters, also from the edge term
+            pos.append(blk[rt:rt + 7 * ninst])
         if c >= 0:
             col.append(blk[c:c + 3 * nv])
         if t >= 0:
-            col.append(blk[t:tr])
+            col.append(blk[t:tr if tr >= 0 else rt])
         off += full
     cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0, np.float32)  # noqa: E731
     return cat(pos), cat(col)

@@ -6,6 +6,8 @@ images, gradients and an optimiser trajectory must equal the reference's
 output (bit-exact where the arithmetic is the same, tolerances noted where
 the reference's own reduction order is nondeterministic).
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -65,7 +67,7 @@ def test_hits_bit_exact(name):
 @pytest.mark.parametrize("name,mode,spp", [("render_cube_m2_spp16", 2, 16), ("render_cube_m1_spp9", 1, 9),
                                            ("render_cube_m2_spp8", 2, 8), ("render_sphere_m3", 3, 4),
                                            ("render_sphere_m4", 4, 4), ("render_sphere_m5", 5, 4),
-                                           ("render_sphere_m6", 6, 4)])
+                                           ("render_sphere_m6", 6, 4), ("render_pyramid_restricted", 2, 16)])
 def test_render_bit_exact(name, mode, spp):
     d = load(name)
     img = O.render(scene_from(d), cams_from(d), mode, spp)
@@ -75,7 +77,8 @@ def test_render_bit_exact(name, mode, spp):
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
                                        ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6),
-                                       ("drc_cube_instanced", 2)])
+                                       ("drc_cube_instanced", 2), ("drc_pyramid_restricted_m2", 2),
+                                       ("drc_pyramid_restricted_m16", 16)])
 def test_d_render_and_compare(name, mode):
     d = load(name)
     loss, ds, imgs = O.d_render_and_compare(scene_from(d), cams_from(d), mode, int(d["spp"][0]), d["targets"],
@@ -109,3 +112,45 @@ def test_optimizer_trajectory():
         assert np.array_equal(r["vertices"][k], d[f"out.it{k}.m0.vertices"]), k
         assert np.array_equal(r["colors"][k], d[f"out.it{k}.m0.colors"]), k
     assert r["final_error"] == pytest.approx(float(d["out.final_error"][0]), rel=1e-6)
+
+
+def test_optimizer_trajectory_restricted_transforms():
+    """TEST 2.11 shape: only the TransformR parameters move (flags = transforms)."""
+    d = load("optimize_pyramid_restricted")
+    p = O.opt_params(4, position_lr=float(d["opt_pos_lr"][0]), transforms_lr=float(d["opt_tfm_lr"][0]),
+                     flags=int(d["opt_flags"][0]), dmesh_ids=[0])
+    iters = int(d["iters"][0])
+    sc = scene_from(d)
+    r = O.optimize(sc, cams_from(d), 2, int(d["spp"][0]), d["targets"], p, iters)
+    for k in range(iters):
+        assert np.array_equal(r["restricted"][k], d[f"out.it{k}.m0.restricted"]), k
+        assert np.array_equal(r["vertices"][k], sc.meshes[0].vertices.reshape(-1)), k
+    assert not np.array_equal(r["restricted"][-1], sc.restricted_params(0))
+    assert r["final_error"] == pytest.approx(float(d["out.final_error"][0]), rel=1e-6)
+
+
+def _to_mat64(p):
+    """TransformR::to_mat in float64 (translate * rotZ * rotY * rotX * scale)."""
+    tx, ty, tz, rx, ry, rz, s = (float(x) for x in p)
+    c, n = math.cos, math.sin
+    Rx = np.array([[1, 0, 0], [0, c(rx), -n(rx)], [0, n(rx), c(rx)]])
+    Ry = np.array([[c(ry), 0, n(ry)], [0, 1, 0], [-n(ry), 0, c(ry)]])
+    Rz = np.array([[c(rz), -n(rz), 0], [n(rz), c(rz), 0], [0, 0, 1]])
+    M = np.zeros((3, 4))
+    M[:, :3] = Rz @ Ry @ Rx * s
+    M[:, 3] = (tx, ty, tz)
+    return M.reshape(-1)  # row-major 3x4, the layout of the 12 transform gradients
+
+
+def test_restricted_transform_jacobian_vs_central_differences():
+    rng = np.random.default_rng(4)
+    for _ in range(20):
+        p = np.concatenate([rng.uniform(-1, 1, 3), rng.uniform(-math.pi, math.pi, 3), rng.uniform(0.3, 2, 1)])
+        jac = O.restricted_jacobian(p.astype(np.float32)).astype(np.float64)
+        p32 = p.astype(np.float32).astype(np.float64)
+        h = 1e-6
+        fd = np.stack([(_to_mat64(p32 + h * e) - _to_mat64(p32 - h * e)) / (2 * h) for e in np.eye(7)])
+        assert np.abs(jac - fd).max() < 2e-6, np.abs(jac - fd).max()
+        m = O.restricted_to_mat(p32.astype(np.float32)).reshape(4, 4).T  # column-major storage
+        assert np.abs(m[:3].reshape(-1) - _to_mat64(p32)).max() < 1e-6
+        assert np.array_equal(m[3], [0, 0, 0, 1])

@@ -94,3 +94,26 @@ def test_noalloc_rejects_oversized_calls():
                                                C.c_void_p(l.data_ptr()))
     assert rc == -1
     assert "scratch" in N.last_error()
+
+
+def test_noalloc_refuses_restricted_transform_meshes():
+    """Their Jacobian step needs a scratch block beyond the caller's gradient vector."""
+    torch = pytest.importorskip("torch")
+    lib = N.load()
+    s = D.Scene()
+    s.add_mesh(D.make_cube(seed=1), [D.TransformR((0.1, 0.0, 0.0), (0.0, 0.3, 0.0), 1.0)])
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL.VERTEX_COLOR, 4))
+    r.commit(s)
+    ds = D.DScene(r, [0])
+    cams = [D.CamInfo(origin=(0, 0, 3), width=32, height=32)]
+    dev = torch.device("cuda:0")
+    d_t = torch.zeros(32 * 32 * 3, dtype=torch.float32, device=dev)
+    g = torch.zeros(ds.data.size, dtype=torch.float32, device=dev)
+    l = torch.zeros(1, dtype=torch.float32, device=dev)
+    ids = np.array([0], np.int32)
+    torch.cuda.synchronize()
+    rc = lib.drgb_d_render_and_compare_noalloc(r._h, make_cameras(cams), C.c_void_p(d_t.data_ptr()), 1, 32 * 32,
+                                               C.c_void_p(ids.ctypes.data), 1, C.c_void_p(g.data_ptr()),
+                                               C.c_void_p(l.data_ptr()))
+    assert rc == -1
+    assert "restricted" in N.last_error()
