@@ -31,7 +31,7 @@ int64_t job_device_bytes(const Job& J) {
   for (int k = 0; k < 2; k++) b += J.sort_keys[k].bytes() + J.sort_vals[k].bytes();
   b += J.sort_hist.bytes() + J.bounds.bytes() + J.edges.bytes() + J.edge_mi.bytes() + J.cams.bytes() + J.ham.bytes();
   b += J.images.bytes() + J.targets.bytes() + J.adj_in.bytes() + J.img_off.bytes() + J.adj.bytes() +
-       J.loss_part.bytes() + J.loss_out.bytes() + J.proj.bytes() + J.pmf.bytes() + J.cdf.bytes() + J.queue.bytes() +
+       J.loss_part.bytes() + J.loss_blk.bytes() + J.loss_out.bytes() + J.proj.bytes() + J.pmf.bytes() + J.cdf.bytes() + J.queue.bytes() +
        J.queue_count.bytes() + J.grad.bytes() + J.err.bytes();
   b += J.opt.m.bytes() + J.opt.G.bytes() + J.opt.lr.bytes() + J.opt.iter.bytes() + J.opt.losses.bytes();
   return b;

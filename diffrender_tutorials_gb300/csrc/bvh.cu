@@ -151,26 +151,66 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* keys, in
   hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of m counts by one block.
+// Exclusive prefix sum of hist[0, m) in place (one block): tiles of 16,384
+// counters, 16 consecutive ones per thread (four 16-byte loads, so a warp
+// reads 2 KB contiguously), a warp-shuffle scan of the thread sums, and a
+// carry from tile to tile.  hist must be 16-byte aligned (a buffer start).
 __global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* hist, int m) {
-  __shared__ uint32_t part[1024];
-  const int per = (m + 1023) / 1024;
-  const int b = threadIdx.x * per, e = min(m, b + per);
-  uint32_t s = 0;
-  for (int i = b; i < e; i++) s += hist[i];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+  __shared__ uint32_t wsum[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t carry = 0;
+  for (int base = 0; base < m; base += 1024 * 16) {
+    const int i0 = base + tid * 16;
+    uint32_t v[16];
+    if (i0 + 16 <= m) {
+      const uint4* p = reinterpret_cast<const uint4*>(hist + i0);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint4 x = p[q];
+        v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; k++) v[k] = i0 + k < m ? hist[i0 + k] : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const uint32_t x = v[k];
+      v[k] = sum;
+      sum += x;
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += y;
+    }
+    if (lane == 31) wsum[warp] = inc;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if (warp == 0) {
+      uint32_t w = wsum[lane];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+        if (lane >= off) w += y;
+      }
+      wsum[lane] = w;
+    }
     __syncthreads();
-  }
-  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-  for (int i = b; i < e; i++) {
-    const uint32_t v = hist[i];
-    hist[i] = run;
-    run += v;
+    const uint32_t before = carry + (warp ? wsum[warp - 1] : 0u) + (inc - sum);
+    if (i0 + 16 <= m) {
+      uint4* p = reinterpret_cast<uint4*>(hist + i0);
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        p[q] = make_uint4(v[4 * q] + before, v[4 * q + 1] + before, v[4 * q + 2] + before, v[4 * q + 3] + before);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        if (i0 + k < m) hist[i0 + k] = v[k] + before;
+    }
+    carry += wsum[31];
+    __syncthreads();  // wsum is rewritten by the next tile
   }
 }
 

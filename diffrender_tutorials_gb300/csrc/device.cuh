@@ -57,6 +57,10 @@ struct CamDev {
 };
 
 // A (mesh, instance) pair: where its vertices start in the flattened arrays.
+// Blocks per job of the loss reduction (a power of two: the completion
+// ticket counts modulo this and wraps around cleanly).
+constexpr int kLossBlocks = 64;
+
 struct BlockDev {
   int vert_off;   // first flattened vertex
   int tri_off;    // first flattened triangle
@@ -134,6 +138,8 @@ struct JobDev {
   float4* adj;              // adjoint image, W*H per view
   const float* adj_in;      // caller-supplied adjoint images (d_render), 3 floats per pixel
   double* loss_part;        // one partial sum per pixel item of this job
+  double* loss_blk;         // kLossBlocks chunk sums per view
+  unsigned* loss_ticket;    // blocks of the loss reduction done (modulo kLossBlocks)
   float* loss_out;          // final loss of the last call
   int tile_w, tile_h;
   int item_base, item_count;  // pixel items of this job in the launch's item list

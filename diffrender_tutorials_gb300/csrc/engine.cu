@@ -443,6 +443,8 @@ void sync_dev(Job& J) {
   d.adj = J.adj.p;
   d.adj_in = J.adj_in.p;
   d.loss_part = J.loss_part.p;
+  d.loss_blk = J.loss_blk.p;
+  d.loss_ticket = J.loss_ticket.p;
   d.loss_out = J.loss_out.p;
   d.tile_w = J.tile_w;
   d.tile_h = J.tile_h;

@@ -160,6 +160,8 @@ struct Job {
   DevBuf<int64_t> img_off;
   DevBuf<float4> adj;
   DevBuf<double> loss_part;
+  DevBuf<double> loss_blk;        // chunk sums of the loss reduction
+  DevBuf<unsigned> loss_ticket;   // its completion ticket (zeroed once)
   DevBuf<float> loss_out;  // 1 float: last loss
   DevBuf<float4> proj;     // per view per vertex projected position
   DevBuf<float> pmf, cdf;  // per view

@@ -422,34 +422,51 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   }
 }
 
-// Loss of each job (one block per job): per view, the double sum of its
-// items' partials -> float; float sum over views in view order; divided by
-// views*W*H (drender.h:184-190).  Each thread sums a contiguous run of items
-// and the 256 run sums are added in run order, so the result does not
-// depend on scheduling.
+// LossAndDiffLoss (utils.cpp:15-27) summed as d_render_and_compare does
+// (drender.h:183-189): a double sum per view, cast to float, views added in
+// order, divided by views*W*H.  The per-item double partials of a view are
+// summed by kLossBlocks blocks over fixed contiguous chunks, each in a fixed
+// tree order; the block of a job that finishes last (completion ticket) adds
+// the chunk sums of each view in chunk order.  The association is fixed, so
+// the loss does not depend on scheduling; FP64 work is spread over
+// kLossBlocks SMs (GB300's FP64 rate is 1/32 of FP32).
 constexpr int LOSS_THREADS = 256;
 __global__ void __launch_bounds__(LOSS_THREADS) k_loss_finalize(const JobDev* jobs, int n_jobs) {
-  __shared__ double part[LOSS_THREADS];
-  const int j = blockIdx.x;
+  __shared__ double red[LOSS_THREADS];
+  __shared__ bool last;
+  const int j = blockIdx.y;
   if (j >= n_jobs) return;
   const JobDev& J = jobs[j];
-  const int per_view = J.item_count / J.n_views;
-  const int chunk = (per_view + LOSS_THREADS - 1) / LOSS_THREADS;
-  float mse = 0.0f;
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const int per_view = J.n_views > 0 ? J.item_count / J.n_views : 0;
+  const int cs = (per_view + kLossBlocks - 1) / kLossBlocks;
+  const int lo = b * cs, hi = min(per_view, lo + cs);
   for (int v = 0; v < J.n_views; v++) {
-    const int b = threadIdx.x * chunk, e = min(per_view, b + chunk);
     double acc = 0.0;
-    for (int i = b; i < e; i++) acc += J.loss_part[v * per_view + i];
-    part[threadIdx.x] = acc;
+    for (int i = lo + tid; i < hi; i += LOSS_THREADS) acc += J.loss_part[(int64_t)v * per_view + i];
+    red[tid] = acc;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int t = 0; t < LOSS_THREADS; t++) s += part[t];
-      mse += (float)s;
+    for (int h = LOSS_THREADS / 2; h > 0; h >>= 1) {
+      if (tid < h) red[tid] += red[tid + h];
+      __syncthreads();
     }
+    if (tid == 0) J.loss_blk[v * kLossBlocks + b] = red[0];
     __syncthreads();
   }
-  if (threadIdx.x == 0) J.loss_out[0] = mse / (float)(J.n_views * J.W * J.H);
+  if (tid == 0) {
+    __threadfence();
+    last = (atomicAdd(J.loss_ticket, 1u) % kLossBlocks) == kLossBlocks - 1;
+  }
+  __syncthreads();
+  if (!last || tid != 0) return;
+  __threadfence();
+  float mse = 0.0f;
+  for (int v = 0; v < J.n_views; v++) {
+    double sum = 0.0;
+    for (int k = 0; k < kLossBlocks; k++) sum += __ldcg(J.loss_blk + v * kLossBlocks + k);
+    mse += (float)sum;
+  }
+  J.loss_out[0] = mse / (float)(J.n_views * J.W * J.H);
 }
 
 // Caller-supplied adjoint images (3 floats per pixel) -> float4 adjoint.
@@ -549,7 +566,7 @@ void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* 
 }
 
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s) {
-  k_loss_finalize<<<n_jobs, LOSS_THREADS, 0, s>>>(d_jobs, n_jobs);
+  k_loss_finalize<<<dim3(kLossBlocks, n_jobs), LOSS_THREADS, 0, s>>>(d_jobs, n_jobs);
   count_launch();
 }
 

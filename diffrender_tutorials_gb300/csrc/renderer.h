@@ -81,6 +81,11 @@ struct drgb_renderer {
     J.h_pixel_items = items;
     d_items.upload(items.data(), items.size(), stream);
     J.loss_part.reserve(std::max<size_t>(1, items.size()));
+    J.loss_blk.reserve((size_t)std::max(1, J.n_views) * kLossBlocks);
+    if (!J.loss_ticket.p) {
+      J.loss_ticket.alloc(1);
+      DRGB_CUDA(cudaMemsetAsync(J.loss_ticket.p, 0, sizeof(unsigned), stream));
+    }
     J.dev.item_base = 0;
     J.dev.item_count = (int)items.size();
   }
