@@ -7,6 +7,7 @@
 // brute-force caster.  Where rounding does not have to match (BVH slab
 // tests), fused multiply-adds are requested explicitly with __fmaf_rn.
 #pragma once
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
