@@ -182,7 +182,7 @@ struct drgb_batch {
     d_items.upload(items.data(), items.size(), stream);
     d_counter.alloc(1);
     queue.reserve(std::max(1, queue_cap));
-    queue_count.alloc(1);
+    queue_count.alloc(2);  // [0] queue entries, [1] shading counter
     for (int b = 0; b < 2; b++) {
       qkey[b].reserve(queue.n);
       qidx[b].reserve(queue.n);

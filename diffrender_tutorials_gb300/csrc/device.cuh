@@ -439,6 +439,27 @@ struct Hit {
   int tri;  // flattened triangle index, -1 = miss
 };
 
+// Three-input min / max (one instruction on sm_100 and later); exact, so the
+// grouping does not change any result.
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(DRGB_NO_MINMAX3)
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fminf(fminf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(DRGB_NO_MINMAX3)
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fmaxf(fmaxf(a, b), c);
+#endif
+}
+
 // Ray/box slab test with precomputed inverse direction; returns the entry
 // distance (or +inf when the box is missed within [lo_t, hi_t]).
 __device__ __forceinline__ float slab(float lx, float hx, float ly, float hy, float lz, float hz, f3 inv, f3 oi,
@@ -446,8 +467,8 @@ __device__ __forceinline__ float slab(float lx, float hx, float ly, float hy, fl
   const float tx0 = __fmaf_rn(lx, inv.x, -oi.x), tx1 = __fmaf_rn(hx, inv.x, -oi.x);
   const float ty0 = __fmaf_rn(ly, inv.y, -oi.y), ty1 = __fmaf_rn(hy, inv.y, -oi.y);
   const float tz0 = __fmaf_rn(lz, inv.z, -oi.z), tz1 = __fmaf_rn(hz, inv.z, -oi.z);
-  const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), lo_t));
-  const float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), hi_t));
+  const float tmin = fmax3f(fminf(tx0, tx1), fminf(ty0, ty1), fmaxf(fminf(tz0, tz1), lo_t));
+  const float tmax = fmin3f(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), hi_t));
   return tmin <= tmax ? tmin : __int_as_float(0x7f800000);
 }
 

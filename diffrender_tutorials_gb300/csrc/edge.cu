@@ -277,15 +277,35 @@ __global__ void k_edge_select(const JobDev* jobs, int job) {
 #ifndef DRGB_EDGE_MIN_BLOCKS
 #define DRGB_EDGE_MIN_BLOCKS 4
 #endif
-// Persistent over the queue, in whole warps (the reductions need every lane);
+// Persistent over the queue, in whole warps (the reductions need every lane):
+// each warp takes the next 32 entries from a counter (count[1], zeroed with
+// the queue count), so warps that drew cheap samples take more and the launch
+// ends without a tail of idle SMs; -DDRGB_EDGE_STATIC strides statically.
 // `order` (may be null) is the shading order of the entries.
 template <bool DET>
-__global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_q(const JobDev* jobs, const int4* queue, const int* count,
-                                                      int cap, const int* order) {
-  const int n = min(*count, cap);
+__device__ __forceinline__ void edge_shade_loop(const JobDev* jobs, const int4* queue, int n, int* work,
+                                                const int* order) {
+#ifdef DRGB_EDGE_STATIC
+  (void)work;
   const int stride = gridDim.x * blockDim.x;
   for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
     edge_shade_warp<DET>(jobs, queue, n, q0, order);
+#else
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int q0 = 0;
+    if (lane == 0) q0 = atomicAdd(work, 32);
+    q0 = __shfl_sync(0xffffffffu, q0, 0);
+    if (q0 >= n) break;
+    edge_shade_warp<DET>(jobs, queue, n, q0, order);
+  }
+#endif
+}
+
+template <bool DET>
+__global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_q(const JobDev* jobs, const int4* queue, int* count,
+                                                      int cap, const int* order) {
+  edge_shade_loop<DET>(jobs, queue, min(count[0], cap), count + 1, order);
 }
 
 // Sort keys of a batch queue: each job's (view, edge) range starts at the
@@ -308,10 +328,7 @@ template <bool DET>
 __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(const JobDev* jobs, int job,
                                                                               const int* order) {
   const JobDev& J = jobs[job];
-  const int n = min(*J.queue_count, J.queue_cap);
-  const int stride = gridDim.x * blockDim.x;
-  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
-    edge_shade_warp<DET>(jobs, J.queue, n, q0, order);
+  edge_shade_loop<DET>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
 }
 
 // Sort keys of the queue entries: (view, edge), so that neighbouring lanes
@@ -385,7 +402,7 @@ void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, i
   k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   k_edge_cdf<<<n_views, CDF_THREADS, 0, s>>>(d_jobs, job);
-  DRGB_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int), s));
+  DRGB_CUDA(cudaMemsetAsync(queue_count, 0, 2 * sizeof(int), s));  // queue count, shading counter
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   // the queue, its counter and capacity are read from the job on the device
   const int* order = Jq ? sort_queue(d_jobs, job, *Jq, shade_grid, s) : nullptr;
@@ -410,7 +427,7 @@ void launch_b_edges(const JobDev* d_jobs, const Seg* proj_segs, int n_proj, int 
   if (proj_chunks > 0) k_b_edge_project<<<proj_chunks, 256, 0, s>>>(d_jobs, proj_segs, n_proj);
   if (pmf_chunks > 0) k_b_edge_pmf<<<pmf_chunks, 256, 0, s>>>(d_jobs, pmf_segs, n_pmf);
   k_b_edge_cdf<<<n_pairs, CDF_THREADS, 0, s>>>(d_jobs, pairs, n_pairs);
-  DRGB_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
+  DRGB_CUDA(cudaMemsetAsync(count, 0, 2 * sizeof(int), s));  // queue count, shading counter
   if (sel_chunks > 0) k_b_edge_select<<<sel_chunks, 256, 0, s>>>(d_jobs, sel_segs, n_sel, queue, count, cap);
   const int* order = nullptr;
 #ifndef DRGB_EDGE_NO_SORT

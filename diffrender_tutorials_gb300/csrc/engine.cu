@@ -531,7 +531,7 @@ void init_job_model(Job& J, int mode, int spp) {
   J.err.alloc(1);
   DRGB_CUDA(cudaMemset(J.err.p, 0, sizeof(uint32_t)));
   J.loss_out.alloc(1);
-  J.queue_count.alloc(1);
+  J.queue_count.alloc(2);  // [0] queue entries, [1] shading counter
 }
 
 }  // namespace drgb

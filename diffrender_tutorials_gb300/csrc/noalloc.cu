@@ -204,7 +204,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     const size_t o_emi = c.take<int2>(std::max(1, E));
     const size_t o_rnd = c.take<float>(std::max<size_t>(1, rnd.size()));
     const size_t o_lblk = c.take<double>((size_t)n_views * kLossBlocks);
-    const size_t o_cnt = c.take<int>(3);
+    const size_t o_cnt = c.take<int>(4);
     if (c.used > kScratchBytes)
       throw CudaError("drgb_d_render_and_compare_noalloc: this call needs " + std::to_string(c.used) +
                           " bytes of scratch; the fixed array holds " + std::to_string(kScratchBytes) +
@@ -264,9 +264,10 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.pmf = reinterpret_cast<float*>(base + o_pmf);
     d.cdf = reinterpret_cast<float*>(base + o_cdf);
     d.queue = reinterpret_cast<int4*>(base + o_queue);
-    int* counters = reinterpret_cast<int*>(base + o_cnt);  // [0] sample queue, [1] work queue, [2] loss ticket
+    // [0] edge-sample queue, [1] its shading counter, [2] pixel work queue, [3] loss ticket
+    int* counters = reinterpret_cast<int*>(base + o_cnt);
     d.queue_count = counters;
-    d.loss_ticket = reinterpret_cast<unsigned*>(counters + 2);
+    d.loss_ticket = reinterpret_cast<unsigned*>(counters + 3);
     d.queue_cap = n_views * std::max(1, edge_samples);
     d.edge_samples = edge_samples;
     d.rnd = reinterpret_cast<const float*>(base + o_rnd);
@@ -287,10 +288,10 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     put(o_emi, emi.data(), sizeof(int2) * emi.size());
     if (edge_samples > 0) put(o_rnd, rnd.data(), sizeof(float) * rnd.size());
     if (grad_total > 0) DRGB_CUDA(cudaMemsetAsync(d_dscene, 0, sizeof(float) * grad_total, s));
-    DRGB_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(int), s));
+    DRGB_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int), s));
     const JobDev* d_job = reinterpret_cast<const JobDev*>(base + o_job);
     const int flags = PX_FWD | PX_LOSS | (J.mode != SILHOUETTE ? PX_ADJ : 0);
-    launch_pixels(d_job, reinterpret_cast<const int4*>(base + o_items), (int)items.size(), counters + 1, flags,
+    launch_pixels(d_job, reinterpret_cast<const int4*>(base + o_items), (int)items.size(), counters + 2, flags,
                   r->px_grid(), s, J.mode);
     launch_loss_finalize(d_job, 1, s);
     if (edge_samples > 0)
