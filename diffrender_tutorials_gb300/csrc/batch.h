@@ -44,7 +44,11 @@ struct drgb_batch {
   DevBuf<uint32_t> qkey[2], qhist;  // shading order of the queue, sorted by (job, view, edge)
   DevBuf<int> qidx[2], qn;
   int qbits = 1;
-  int n_items = 0, mode = 0;
+  int n_items = 0;
+  struct ModeGroup {
+    int mode, begin, count;  // contiguous pixel items of one shading model
+  };
+  std::vector<ModeGroup> mode_groups;
   int n_proj = 0, c_proj = 0, n_pmf = 0, c_pmf = 0, n_pairs = 0, n_sel = 0, c_sel = 0;
   int n_mom = 0, c_mom = 0, n_apply = 0, c_apply = 0;
   int n_prep[4] = {0, 0, 0, 0}, c_prep[4] = {0, 0, 0, 0};
@@ -79,7 +83,11 @@ struct drgb_batch {
     std::vector<JobAux> aux(n);
     std::vector<int4> items;
     std::vector<Seg> proj, pmf, pairs, sel, mom, apply, btr, flat, cnt, refit;
-    int modes = -1;
+    // jobs grouped by shading model: each group's pixel items run in the
+    // kernel specialised for that model (item_base is relative to the group)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return jobs.at(a)->job.mode < jobs.at(b)->job.mode; });
+    mode_groups.clear();
     queue_cap = 0;
     uint64_t key_base = 0;
     for (int j = 0; j < n; j++) {
@@ -88,11 +96,13 @@ struct drgb_batch {
       JobDev d = J.dev;
       d.edge_key_base = (uint32_t)key_base;
       key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
-      d.item_base = (int)items.size();
+      if (mode_groups.empty() || mode_groups.back().mode != J.mode)
+        mode_groups.push_back(ModeGroup{J.mode, (int)items.size(), 0});
+      d.item_base = (int)items.size() - mode_groups.back().begin;
       d.item_count = (int)J.h_pixel_items.size();
       for (int4 it : J.h_pixel_items) items.push_back(make_int4(j, it.y, it.z, it.w));
+      mode_groups.back().count += d.item_count;
       h_jobs[j] = d;
-      modes = (modes == -1 || modes == J.mode) ? J.mode : 0;
       for (int v = 0; v < J.n_views; v++) {
         proj.push_back(Seg{j, v, 0, J.n_vertices});
         pmf.push_back(Seg{j, v, 0, J.n_edges});
@@ -151,7 +161,6 @@ struct drgb_batch {
       cnt.push_back(Seg{j, 0, 0, std::max(0, J.n_tris - 1)});
       refit.push_back(Seg{j, 0, 0, J.n_tris});
     }
-    mode = modes < 0 ? 0 : modes;
     n_items = (int)items.size();
     det_any = false;
     for (int32_t id : order) det_any = det_any || jobs.at(id)->job.det;
@@ -180,7 +189,7 @@ struct drgb_batch {
     d_jobs.upload(h_jobs.data(), h_jobs.size(), stream);
     d_aux.upload(aux.data(), aux.size(), stream);
     d_items.upload(items.data(), items.size(), stream);
-    d_counter.alloc(1);
+    d_counter.alloc(std::max<size_t>(1, mode_groups.size()));
     queue.reserve(std::max(1, queue_cap));
     queue_count.alloc(2);  // [0] queue entries, [1] shading counter
     for (int b = 0; b < 2; b++) {
@@ -209,8 +218,9 @@ struct drgb_batch {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_clear(J, stream);
     }
-    launch_pixels(d_jobs.p, d_items.p, n_items, d_counter.p, PX_FWD | PX_LOSS | PX_ADJ, sm_count * px_blocks_per_sm,
-                  stream, mode, det_any);
+    for (size_t g = 0; g < mode_groups.size(); g++)
+      launch_pixels(d_jobs.p, d_items.p + mode_groups[g].begin, mode_groups[g].count, d_counter.p + g,
+                    PX_FWD | PX_LOSS | PX_ADJ, sm_count * px_blocks_per_sm, stream, mode_groups[g].mode, det_any);
     launch_loss_finalize(d_jobs.p, (int)order.size(), stream);
     launch_b_edges(d_jobs.p, seg_proj.p, n_proj, c_proj, seg_pmf.p, n_pmf, c_pmf, seg_pairs.p, n_pairs, seg_sel.p,
                    n_sel, c_sel, queue.p, queue_count.p, (int)queue.n, sm_count * edge_blocks_per_sm, stream,
