@@ -40,49 +40,84 @@ __device__ __forceinline__ void edge_pmf_body(const JobDev& J, int view, int e) 
 // both divided by the total (drender.cpp:5-22).  The running sum is one
 // dependent chain of float additions -- the reference's rounding sequence,
 // which the sampler's upper_bound must see bit for bit -- so one thread runs
-// it, over chunks that the whole block stages in shared memory; loads and
-// stores stay off the chain.
+// it, chunk by chunk in shared memory.  Three chunk buffers keep the memory
+// traffic off the chain: while thread 0 sums chunk c, warps 1-7 write chunk
+// c-1 out and stage chunk c+1.
 constexpr int CDF_THREADS = 256;
-constexpr int CDF_CHUNK = 4096;
+constexpr int CDF_CHUNK = 2048;
+constexpr int CDF_SMEM = 3 * CDF_CHUNK;  // floats of 16-byte aligned shared memory the caller provides
 __device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view, float* sbuf) {
   const int tid = threadIdx.x;
   const int E = J.n_edges;
   float* pmf = J.pmf + (int64_t)view * E;
   float* cdf = J.cdf + (int64_t)view * (E + 1);
   __shared__ float s_run;
+  const int n_chunks = (E + CDF_CHUNK - 1) / CDF_CHUNK;
   if (tid == 0) {
     s_run = 0.0f;
     cdf[0] = 0.0f;
   }
-  for (int base = 0; base < E; base += CDF_CHUNK) {
-    const int n = min(CDF_CHUNK, E - base);
-    for (int j = tid; j < n; j += CDF_THREADS) sbuf[j] = pmf[base + j];
-    __syncthreads();
+  for (int j = tid; j < min(CDF_CHUNK, E); j += CDF_THREADS) sbuf[j] = pmf[j];
+  __syncthreads();
+  for (int c = 0; c < n_chunks; c++) {
     if (tid == 0) {
+      // 8 values per step in two 16-byte loads, the next 8 loaded while the
+      // current ones are added, so only the additions are on the chain
+      float* buf = sbuf + (c % 3) * CDF_CHUNK;
+      float4* b4 = reinterpret_cast<float4*>(buf);
+      const int n = min(CDF_CHUNK, E - c * CDF_CHUNK);
+      const int n8 = n & ~7;
       float run = s_run;
-      int j = 0;
-      for (; j + 8 <= n; j += 8) {
-        const float p0 = sbuf[j], p1 = sbuf[j + 1], p2 = sbuf[j + 2], p3 = sbuf[j + 3];
-        const float p4 = sbuf[j + 4], p5 = sbuf[j + 5], p6 = sbuf[j + 6], p7 = sbuf[j + 7];
-        run = p0 + run; sbuf[j] = run;
-        run = p1 + run; sbuf[j + 1] = run;
-        run = p2 + run; sbuf[j + 2] = run;
-        run = p3 + run; sbuf[j + 3] = run;
-        run = p4 + run; sbuf[j + 4] = run;
-        run = p5 + run; sbuf[j + 5] = run;
-        run = p6 + run; sbuf[j + 6] = run;
-        run = p7 + run; sbuf[j + 7] = run;
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+      if (n8 > 0) {
+        a = b4[0];
+        b = b4[1];
       }
-      for (; j < n; j++) {
-        run = sbuf[j] + run;
-        sbuf[j] = run;
+      for (int j = 0; j < n8; j += 8) {
+        float4 na = a, nb = b;
+        if (j + 8 < n8) {
+          na = b4[(j >> 2) + 2];
+          nb = b4[(j >> 2) + 3];
+        }
+        float4 ra, rb;
+        run = a.x + run; ra.x = run;
+        run = a.y + run; ra.y = run;
+        run = a.z + run; ra.z = run;
+        run = a.w + run; ra.w = run;
+        run = b.x + run; rb.x = run;
+        run = b.y + run; rb.y = run;
+        run = b.z + run; rb.z = run;
+        run = b.w + run; rb.w = run;
+        b4[j >> 2] = ra;
+        b4[(j >> 2) + 1] = rb;
+        a = na;
+        b = nb;
+      }
+      for (int j = n8; j < n; j++) {
+        run = buf[j] + run;
+        buf[j] = run;
       }
       s_run = run;
+    } else if (tid >= 32) {
+      const int t = tid - 32, T = CDF_THREADS - 32;
+      if (c >= 1) {  // chunk c-1 is complete (and full: only the last chunk is short)
+        const float* done = sbuf + ((c - 1) % 3) * CDF_CHUNK;
+        for (int j = t; j < CDF_CHUNK; j += T) cdf[(c - 1) * CDF_CHUNK + j + 1] = done[j];
+      }
+      if (c + 1 < n_chunks) {
+        float* next = sbuf + ((c + 1) % 3) * CDF_CHUNK;
+        const int n1 = min(CDF_CHUNK, E - (c + 1) * CDF_CHUNK);
+        for (int j = t; j < n1; j += T) next[j] = pmf[(c + 1) * CDF_CHUNK + j];
+      }
     }
     __syncthreads();
-    for (int j = tid; j < n; j += CDF_THREADS) cdf[base + j + 1] = sbuf[j];
-    __syncthreads();
   }
+  if (n_chunks > 0) {
+    const int c = n_chunks - 1;
+    const float* done = sbuf + (c % 3) * CDF_CHUNK;
+    for (int j = tid; j < E - c * CDF_CHUNK; j += CDF_THREADS) cdf[c * CDF_CHUNK + j + 1] = done[j];
+  }
+  __syncthreads();
   const float total = s_run;
   for (int k = tid; k < E; k += CDF_THREADS) pmf[k] = pmf[k] / total;
   for (int k = tid; k <= E; k += CDF_THREADS) cdf[k] = cdf[k] / total;
@@ -259,7 +294,7 @@ __global__ void k_edge_pmf(const JobDev* jobs, int job) {
 }
 
 __global__ void __launch_bounds__(CDF_THREADS) k_edge_cdf(const JobDev* jobs, int job) {
-  __shared__ float sbuf[CDF_CHUNK];
+  __shared__ __align__(16) float sbuf[CDF_SMEM];
   edge_cdf_body(jobs[job], blockIdx.x, sbuf);
 }
 
@@ -359,7 +394,7 @@ __global__ void k_b_edge_pmf(const JobDev* jobs, const Seg* segs, int nseg) {
 
 // one block per (job, view) pair: pairs[b].job / .sub
 __global__ void __launch_bounds__(CDF_THREADS) k_b_edge_cdf(const JobDev* jobs, const Seg* pairs, int n_pairs) {
-  __shared__ float sbuf[CDF_CHUNK];
+  __shared__ __align__(16) float sbuf[CDF_SMEM];
   if ((int)blockIdx.x >= n_pairs) return;
   const Seg sg = pairs[blockIdx.x];
   edge_cdf_body(jobs[sg.job], sg.sub, sbuf);
