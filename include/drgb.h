@@ -32,7 +32,7 @@ enum {
   DRGB_ERR_OOM = -3,          /* device allocation failed */
   DRGB_ERR_STATE = -4,        /* call out of order (e.g. render before commit) */
   DRGB_ERR_KERNEL = -5,       /* a kernel raised an error flag (traversal stack/limit) */
-  DRGB_ERR_UNSUPPORTED = -6,  /* feature not available in this build */
+  DRGB_ERR_UNSUPPORTED = -6,  /* feature not available in this library */
   DRGB_ERR_NO_DEVICE = -7     /* no CUDA device */
 };
 

@@ -129,7 +129,7 @@ int orc_optimize(const orc_mesh* meshes, int n_meshes, int mode, int spp, const 
 void orc_restricted_to_mat(const float* params7, float* out16);
 /* d(to_mat)/d(params), jac[7][12] over the row-major 3x4 part: what the
  * Enzyme forward pass of drender_autodiff.cpp:78-107 computes, derived
- * analytically (the plugin is not part of this build). */
+ * analytically (the plugin is not available to compile with). */
 void orc_restricted_jacobian(const float* params7, float* jac84);
 
 /* Random streams of the edge sampler (qmc.cpp:250-268, drender.h:306-331). */

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through the C ABI) against the reference's own
 outputs (golden fixtures) and against the CPU oracle.
 
-Tolerances (spec bar):
+Tolerances:
   * per-sample hit ids, t, u, v: bit-exact (ties resolve to the lowest
     flattened triangle, which is the triangle the brute-force loop keeps);
   * images: bit-exact (max abs 0 <= 1e-4);
