@@ -71,6 +71,7 @@ std::unique_ptr<drgb_renderer> batch_prepare_job(int device, int shading_model, 
 int32_t batch_attach(drgb_batch* b, std::unique_ptr<drgb_renderer> r) {
   require(r && r->device == b->device, "job prepared for another device");
   const int32_t id = b->next_id++;
+  if (b->bvh_rebuild >= 0) r->bvh_rebuild = b->bvh_rebuild;
   b->jobs[id] = std::move(r);
   b->order.push_back(id);
   b->dirty = true;
@@ -144,6 +145,10 @@ int drgb_batch_set_option(drgb_batch* b, int option, int64_t value) {
     require(b != nullptr, "null batch");
     if (option == DRGB_OPT_USE_GRAPH) {
       b->use_graph = value ? 1 : 0;
+    } else if (option == DRGB_OPT_BVH_REBUILD) {
+      require(value >= 0 && value <= (1 << 30), "hierarchy rebuild period: 0 (never) or iterations");
+      b->bvh_rebuild = (int)value;
+      for (auto& kv : b->jobs) kv.second->bvh_rebuild = b->bvh_rebuild;
     } else if (option == DRGB_OPT_DETERMINISTIC) {
       DRGB_CUDA(cudaSetDevice(b->device));
       DRGB_CUDA(cudaStreamSynchronize(b->stream));
@@ -160,26 +165,9 @@ int drgb_batch_set_option(drgb_batch* b, int option, int64_t value) {
   });
 }
 
-int drgb_batch_run_async(drgb_batch* b, int64_t n_iters) {
-  return guard([&] {
-    require(b != nullptr && n_iters >= 0, "bad arguments");
-    if (b->order.empty() || n_iters == 0) return;
-    DRGB_CUDA(cudaSetDevice(b->device));
-    // loss histories must hold the new iterations
-    for (int32_t id : b->order) {
-      Job& J = b->jobs.at(id)->job;
-      if ((int64_t)J.opt.losses.n < J.opt.host_iter + n_iters) {
-        size_t cap = std::max<size_t>(1024, J.opt.losses.n);
-        while ((int64_t)cap < J.opt.host_iter + n_iters) cap *= 2;
-        DevBuf<float> nb;
-        nb.alloc(cap);
-        DRGB_CUDA(cudaMemcpyAsync(nb.p, J.opt.losses.p, J.opt.losses.bytes(), cudaMemcpyDeviceToDevice, b->stream));
-        DRGB_CUDA(cudaStreamSynchronize(b->stream));
-        J.opt.losses = std::move(nb);
-        b->dirty = true;
-      }
-    }
-    b->rebuild();
+// n batched steps: graph replays, or the launches themselves.
+static void batch_enqueue_steps(drgb_batch* b, int64_t n_iters) {
+  {
     if (b->use_graph) {
       if (!b->graph_valid) {
         if (b->graph) {
@@ -207,9 +195,50 @@ int drgb_batch_run_async(drgb_batch* b, int64_t n_iters) {
     } else {
       for (int64_t i = 0; i < n_iters; i++) b->enqueue_iteration();
     }
-    for (int32_t id : b->order) b->jobs.at(id)->job.opt.host_iter += n_iters;
+  }
+}
+
+int drgb_batch_run_async(drgb_batch* b, int64_t n_iters) {
+  return guard([&] {
+    require(b != nullptr && n_iters >= 0, "bad arguments");
+    if (b->order.empty() || n_iters == 0) return;
+    DRGB_CUDA(cudaSetDevice(b->device));
+    // loss histories must hold the new iterations
+    for (int32_t id : b->order) {
+      Job& J = b->jobs.at(id)->job;
+      if ((int64_t)J.opt.losses.n < J.opt.host_iter + n_iters) {
+        size_t cap = std::max<size_t>(1024, J.opt.losses.n);
+        while ((int64_t)cap < J.opt.host_iter + n_iters) cap *= 2;
+        DevBuf<float> nb;
+        nb.alloc(cap);
+        DRGB_CUDA(cudaMemcpyAsync(nb.p, J.opt.losses.p, J.opt.losses.bytes(), cudaMemcpyDeviceToDevice, b->stream));
+        DRGB_CUDA(cudaStreamSynchronize(b->stream));
+        J.opt.losses = std::move(nb);
+        b->dirty = true;
+      }
+    }
+    b->rebuild();
+    // steps up to the next job's hierarchy rebuild, which then overlaps the
+    // following steps (the job's device pointers stay the same, so the graph
+    // stays valid)
+    while (n_iters > 0) {
+      for (int32_t id : b->order) rebuild_bvh_poll(b->jobs.at(id)->job, b->stream);
+      int64_t n = n_iters;
+      for (int32_t id : b->order) {
+        const drgb_renderer& r = *b->jobs.at(id);
+        if (r.bvh_rebuild > 0) n = std::min<int64_t>(n, r.bvh_rebuild - r.job.opt.host_iter % r.bvh_rebuild);
+      }
+      batch_enqueue_steps(b, n);
+      n_iters -= n;
+      for (int32_t id : b->order) {
+        drgb_renderer& r = *b->jobs.at(id);
+        r.job.opt.host_iter += n;
+        if (r.bvh_rebuild > 0 && r.job.opt.host_iter % r.bvh_rebuild == 0) rebuild_bvh_begin(r.job, b->stream);
+      }
+    }
   });
 }
+
 
 int drgb_batch_sync(drgb_batch* b) {
   return guard([&] {

@@ -16,8 +16,10 @@
 // not.  Boxes are padded so that the traversal never culls a triangle the
 // brute-force test would accept.
 #include <algorithm>
-#include <cstring>
+#include <chrono>
 #include <climits>
+#include <cstring>
+#include <future>
 
 #include "engine.h"
 
@@ -481,6 +483,75 @@ void commit_scene(Job& J, cudaStream_t s) {
   refit_bvh(J, s);
 }
 
+// A new topology from the flattened positions of the last prepare_scene (the
+// optimiser's current vertices); same sizes, so every device pointer and a
+// captured iteration graph stay valid.
+void rebuild_bvh(Job& J, cudaStream_t s) {
+  J.topo_builder = -1;  // defeats the same-triangles cache
+  build_bvh(J, s);
+  refit_bvh(J, s);
+}
+
+static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int n, std::vector<float4>& links,
+                         std::vector<int>& perm, std::vector<int>& leaf_parent, std::vector<int>& node_parent);
+
+void rebuild_bvh_begin(Job& J, cudaStream_t s) {
+  const int n = J.n_tris;
+  if (J.bvh_builder != 1 || n <= 1) {  // a device build blocks nothing
+    rebuild_bvh(J, s);
+    return;
+  }
+  if (!J.topo_async) J.topo_async.reset(new TopoRebuild());
+  TopoRebuild& T = *J.topo_async;
+  if (T.stage != 0) return;  // the previous one is still on its way
+  if (!T.ev) DRGB_CUDA(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
+  T.pos.reserve((size_t)J.n_vertices);
+  DRGB_CUDA(cudaMemcpyAsync(T.pos.p, J.pos.p, sizeof(float4) * J.n_vertices, cudaMemcpyDeviceToHost, s));
+  DRGB_CUDA(cudaEventRecord(T.ev, s));
+  T.stage = 1;
+}
+
+void rebuild_bvh_poll(Job& J, cudaStream_t s) {
+  if (!J.topo_async) return;
+  TopoRebuild& T = *J.topo_async;
+  if (T.stage == 1) {
+    const cudaError_t q = cudaEventQuery(T.ev);
+    if (q == cudaErrorNotReady) return;
+    DRGB_CUDA(q);
+    const int n = J.n_tris;
+    T.nodes.reserve(4 * (size_t)(n - 1));
+    T.perm.reserve(n);
+    T.leaf_parent.reserve(n);
+    T.node_parent.reserve(n - 1);
+    TopoRebuild* t = &T;
+    const std::vector<int4>* tri_v = &J.h_tri_v;
+    T.task = std::async(std::launch::async, [t, tri_v, n] {
+      std::vector<float4> links;
+      std::vector<int> perm, leaf_parent, node_parent;
+      sah_topology(t->pos.p, *tri_v, n, links, perm, leaf_parent, node_parent);
+      std::fill(t->nodes.p, t->nodes.p + 4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+      for (int i = 0; i < n - 1; i++) t->nodes.p[4 * (size_t)i + 3] = links[i];
+      std::memcpy(t->perm.p, perm.data(), sizeof(int) * n);
+      std::memcpy(t->leaf_parent.p, leaf_parent.data(), sizeof(int) * n);
+      std::memcpy(t->node_parent.p, node_parent.data(), sizeof(int) * (n - 1));
+    });
+    T.stage = 2;
+    return;
+  }
+  if (T.stage == 2 && T.task.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+    T.task.get();
+    const int n = J.n_tris;
+    DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, T.nodes.p, sizeof(float4) * 4 * (n - 1), cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.perm.p, T.perm.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.leaf_parent.p, T.leaf_parent.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, T.node_parent.p, sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
+    refit_bvh(J, s);
+    J.topo_tri_v = J.h_tri_v;
+    J.topo_builder = 1;
+    T.stage = 0;
+  }
+}
+
 void refit_bvh(Job& J, cudaStream_t s) {
   const int n = J.n_tris;
   if (n == 0) return;
@@ -501,7 +572,7 @@ void refit_bvh(Job& J, cudaStream_t s) {
 // filled by the device refit, exactly as for the LBVH.  Outputs the child
 // links of every internal node (root 0), the leaf permutation and the
 // parent arrays.
-static void sah_topology(const std::vector<float4>& pos, const std::vector<int4>& tri_v, int n,
+static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int n,
                          std::vector<float4>& links, std::vector<int>& perm, std::vector<int>& leaf_parent,
                          std::vector<int>& node_parent) {
   struct Item {
@@ -686,7 +757,7 @@ static void build_topology(Job& J, cudaStream_t s) {
     DRGB_CUDA(cudaStreamSynchronize(s));
     std::vector<float4> links;
     std::vector<int> perm, leaf_parent, node_parent;
-    sah_topology(pos, J.h_tri_v, n, links, perm, leaf_parent, node_parent);
+    sah_topology(pos.data(), J.h_tri_v, n, links, perm, leaf_parent, node_parent);
     std::vector<float4> nodes(4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (int i = 0; i < n - 1; i++) nodes[4 * (size_t)i + 3] = links[i];
     DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice, s));

@@ -104,6 +104,10 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         require(value == 0 || value == 1, "hierarchy builder: 0 (LBVH) or 1 (binned SAH)");
         r->job.bvh_builder = (int)value;  // used from the next commit on
         break;
+      case DRGB_OPT_BVH_REBUILD:
+        require(value >= 0 && value <= (1 << 30), "hierarchy rebuild period: 0 (never) or iterations");
+        r->bvh_rebuild = (int)value;
+        break;
       case DRGB_OPT_PIXEL_GRID:
         require(value >= 1 && value <= 64, "pixel grid: 1..64 blocks per SM");
         r->px_blocks_per_sm = (int)value;
@@ -376,25 +380,9 @@ static void enqueue_opt_iteration(drgb_renderer* r) {
   prepare_scene(J, r->stream);
 }
 
-int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters) {
-  return guard([&] {
-    check_renderer(r);
-    require(r->job.opt.active, "optimiser not initialised", DRGB_ERR_STATE);
-    require(n_iters >= 0, "negative iteration count");
-    r->set_device();
-    Job& J = r->job;
-    OptState& O = J.opt;
-    const int64_t need = O.host_iter + n_iters;
-    if ((int64_t)O.losses.n < need) {
-      size_t cap = O.losses.n;
-      while ((int64_t)cap < need) cap *= 2;
-      DevBuf<float> nb;
-      nb.alloc(cap);
-      DRGB_CUDA(cudaMemcpyAsync(nb.p, O.losses.p, sizeof(float) * O.losses.n, cudaMemcpyDeviceToDevice, r->stream));
-      DRGB_CUDA(cudaStreamSynchronize(r->stream));
-      O.losses = std::move(nb);
-      r->graph_valid = false;
-    }
+// n optimiser iterations: graph replays, or the launches themselves.
+static void enqueue_opt_iterations(drgb_renderer* r, int64_t n_iters) {
+  {
     if (r->use_graph) {
       if (!r->graph_valid) {
         if (r->graph) {
@@ -424,9 +412,43 @@ int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters) {
     } else {
       for (int64_t i = 0; i < n_iters; i++) enqueue_opt_iteration(r);
     }
-    O.host_iter += n_iters;
+  }
+}
+
+int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters) {
+  return guard([&] {
+    check_renderer(r);
+    require(r->job.opt.active, "optimiser not initialised", DRGB_ERR_STATE);
+    require(n_iters >= 0, "negative iteration count");
+    r->set_device();
+    Job& J = r->job;
+    OptState& O = J.opt;
+    const int64_t need = O.host_iter + n_iters;
+    if ((int64_t)O.losses.n < need) {
+      size_t cap = O.losses.n;
+      while ((int64_t)cap < need) cap *= 2;
+      DevBuf<float> nb;
+      nb.alloc(cap);
+      DRGB_CUDA(cudaMemcpyAsync(nb.p, O.losses.p, sizeof(float) * O.losses.n, cudaMemcpyDeviceToDevice, r->stream));
+      DRGB_CUDA(cudaStreamSynchronize(r->stream));
+      O.losses = std::move(nb);
+      r->graph_valid = false;
+    }
+    // iterations up to the next hierarchy rebuild, then the rebuild (host
+    // SAH build from the current vertices; the device pointers stay the same,
+    // so the captured graph stays valid)
+    const int64_t period = r->bvh_rebuild;
+    while (n_iters > 0) {
+      int64_t n = n_iters;
+      if (period > 0) n = std::min<int64_t>(n, period - O.host_iter % period);
+      enqueue_opt_iterations(r, n);
+      O.host_iter += n;
+      n_iters -= n;
+      if (period > 0 && O.host_iter % period == 0) rebuild_bvh(J, r->stream);
+    }
   });
 }
+
 
 int drgb_optimizer_run(drgb_renderer* r, int64_t n_iters, float* final_error, float* losses) {
   const int64_t start = r ? r->job.opt.host_iter : 0;

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <future>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -68,6 +69,43 @@ struct DevBuf {
     if (count) DRGB_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
   }
   size_t bytes() const { return n * sizeof(T); }
+};
+
+// Page-locked host buffer: copies to and from it run asynchronously.
+template <class T>
+struct HostBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+  ~HostBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void reserve(size_t count) {
+    if (count <= n && p) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    DRGB_CUDA(cudaMallocHost((void**)&p, std::max<size_t>(1, count) * sizeof(T)));
+    n = count;
+  }
+};
+
+// A hierarchy rebuild that overlaps the device's work (batched jobs): the
+// flattened positions are copied out behind the enqueued steps, a host
+// thread builds the SAH topology, and the new topology is copied in and
+// refitted in stream order a few steps later.
+struct TopoRebuild {
+  int stage = 0;  // 0 idle, 1 positions in flight, 2 topology being built
+  cudaEvent_t ev = nullptr;
+  HostBuf<float4> pos, nodes;
+  HostBuf<int> perm, leaf_parent, node_parent;
+  std::future<void> task;
+  ~TopoRebuild() {
+    if (task.valid()) task.wait();
+    if (ev) cudaEventDestroy(ev);
+  }
 };
 
 // Gradient layout of one differentiable mesh (DMesh, dmesh.h:35-85).
@@ -145,6 +183,7 @@ struct Job {
   int bvh_builder = 1;
   std::vector<int4> h_tri_v, topo_tri_v;
   int topo_builder = -1;
+  std::unique_ptr<TopoRebuild> topo_async;  // overlapped rebuild in progress (batches)
   // edges (topology; one list per differentiable-mesh set)
   DevBuf<int4> edges;   // v0, v1, vn0, vn1
   DevBuf<int2> edge_mi; // mesh, instance
@@ -200,6 +239,9 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s);
 void flatten_scene(Job& J, cudaStream_t s);            // instance transforms -> flattened arrays
 void prepare_scene(Job& J, cudaStream_t s);            // flatten + traced triangles + refit
 void commit_scene(Job& J, cudaStream_t s);             // flatten + LBVH build + refit
+void rebuild_bvh(Job& J, cudaStream_t s);              // new topology from the current vertices + refit
+void rebuild_bvh_begin(Job& J, cudaStream_t s);        // the same, overlapped with later steps...
+void rebuild_bvh_poll(Job& J, cudaStream_t s);         // ...advanced between steps, never blocking
 void build_bvh(Job& J, cudaStream_t s);                // topology (Morton, sort, Karras)
 void refit_bvh(Job& J, cudaStream_t s);
 void setup_views(Job& J, const drgb_camera* cams, int n_views);

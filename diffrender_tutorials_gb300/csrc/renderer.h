@@ -66,6 +66,7 @@ struct drgb_renderer {
   void set_device() const { DRGB_CUDA(cudaSetDevice(device)); }
   void require_commit() const { require(job.committed, "no scene committed (call drgb_commit first)", DRGB_ERR_STATE); }
   int px_blocks_per_sm = 8, edge_blocks_per_sm = 8;  // persistent grids (autotuned or set by option)
+  int bvh_rebuild = 100;  // optimiser iterations between hierarchy rebuilds (0: refit only)
   int px_grid() const { return sm_count * px_blocks_per_sm; }
   int edge_grid() const { return sm_count * edge_blocks_per_sm; }
 

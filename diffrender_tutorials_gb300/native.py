@@ -15,7 +15,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "drgb.h")
 DRGB_OK = 0
 # renderer / batch options (drgb_renderer_set_option, drgb_batch_set_option)
 OPT_TRACE_BRUTEFORCE, OPT_TILE_W, OPT_TILE_H, OPT_USE_GRAPH, OPT_DETERMINISTIC, OPT_ADJOINT_HITS = 1, 2, 3, 4, 5, 6
-OPT_PIXEL_GRID, OPT_EDGE_GRID, OPT_BVH_BUILDER = 7, 8, 9
+OPT_PIXEL_GRID, OPT_EDGE_GRID, OPT_BVH_BUILDER, OPT_BVH_REBUILD = 7, 8, 9, 10
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
           -5: "kernel error flag", -6: "unsupported", -7: "no CUDA device"}
 

@@ -68,9 +68,14 @@ enum {
                                     re-tracing them; 0 (default): re-trace.  Single renderers only. */
   DRGB_OPT_PIXEL_GRID = 7,       /* blocks per SM of the persistent pixel kernel (default 8) */
   DRGB_OPT_EDGE_GRID = 8,        /* blocks per SM of the persistent edge-shading kernel (default 8) */
-  DRGB_OPT_BVH_BUILDER = 9       /* hierarchy topology from the next commit on: 0 LBVH from Morton codes on
+  DRGB_OPT_BVH_BUILDER = 9,      /* hierarchy topology from the next commit on: 0 LBVH from Morton codes on
                                     the device, 1 (default) binned SAH on the host; boxes are refitted on the
                                     device either way, and a commit of the same triangles keeps the topology */
+  DRGB_OPT_BVH_REBUILD = 10      /* optimiser (and batch, for every job): rebuild the hierarchy topology from
+                                    the current vertices every N iterations (default 100; 0: refit only).
+                                    Refitted boxes of moving vertices overlap more and more (icosphere
+                                    workload: 55 box tests per ray after 500 steps against 47 with
+                                    rebuilds); the hit set does not depend on the topology. */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -249,7 +254,7 @@ int drgb_batch_add_job(drgb_batch* b, int shading_model, int spp, const drgb_mod
                        const drgb_opt_params* p, int32_t* job_id);
 int drgb_batch_remove_job(drgb_batch* b, int32_t job_id);
 int drgb_batch_size(drgb_batch* b);
-/* DRGB_OPT_USE_GRAPH, or DRGB_OPT_DETERMINISTIC for every job, present and future */
+/* DRGB_OPT_USE_GRAPH, or DRGB_OPT_DETERMINISTIC / DRGB_OPT_BVH_REBUILD for every job, present and future */
 int drgb_batch_set_option(drgb_batch* b, int option, int64_t value);
 /* n_iters iterations of every job: enqueue only / enqueue and wait. */
 int drgb_batch_run_async(drgb_batch* b, int64_t n_iters);

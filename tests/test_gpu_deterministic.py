@@ -130,6 +130,35 @@ def test_deterministic_plain_batch_and_server_agree_bit_for_bit():
     srv.close()
 
 
+def test_hierarchy_rebuilds_leave_the_trajectory_unchanged():
+    """DRGB_OPT_BVH_REBUILD: a new topology every 2 iterations (plain and
+    batched) gives the same bits as refitting one topology throughout."""
+    iters = 6
+    name, mode, spp, ts, isc, cams = problems()[0]
+    st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+    r0 = D.MakeDifferentialRenderer(st)
+    r0.commit(ts)
+    tgt = r0.render(ts, cams)
+    runs = []
+    for period in (0, 2):
+        r = D.MakeDifferentialRenderer(st)
+        r.set_option(N.OPT_DETERMINISTIC, 1)
+        r.set_option(N.OPT_BVH_REBUILD, period)
+        opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, r, cams, tgt, opt_params(mode))
+        opt.Run(iters)
+        runs.append((np.array(opt.losses), opt.current_scene().meshes[0].vertices))
+        b = D.BatchOptimizer()
+        b.set_option(N.OPT_DETERMINISTIC, 1)
+        b.set_option(N.OPT_BVH_REBUILD, period)
+        jid = b.add_job(isc, cams, tgt, st, opt_params(mode))
+        b.run(iters)
+        runs.append((b.losses(jid), b.job_scene(jid).meshes[0].vertices))
+    for losses, verts in runs[1:]:
+        assert np.array_equal(losses, runs[0][0])
+        assert np.array_equal(verts, runs[0][1])
+
+
 def test_noalloc_entry_refuses_deterministic_mode():
     import torch
     name, mode, spp, ts, isc, cams = problems()[1]
