@@ -61,39 +61,35 @@ __device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view, float* 
   __syncthreads();
   for (int c = 0; c < n_chunks; c++) {
     if (tid == 0) {
-      // 8 values per step in two 16-byte loads, the next 8 loaded while the
-      // current ones are added, so only the additions are on the chain
+      // 16 values per step in four 16-byte loads; the next 16 are loaded
+      // while the current ones are added (the 16 dependent additions outlast
+      // a shared-memory load), so only the additions are on the chain
       float* buf = sbuf + (c % 3) * CDF_CHUNK;
       float4* b4 = reinterpret_cast<float4*>(buf);
       const int n = min(CDF_CHUNK, E - c * CDF_CHUNK);
-      const int n8 = n & ~7;
+      const int n16 = n & ~15;
       float run = s_run;
-      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-      if (n8 > 0) {
-        a = b4[0];
-        b = b4[1];
-      }
-      for (int j = 0; j < n8; j += 8) {
-        float4 na = a, nb = b;
-        if (j + 8 < n8) {
-          na = b4[(j >> 2) + 2];
-          nb = b4[(j >> 2) + 3];
+      float4 q[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) q[k] = n16 > 0 ? b4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int j = 0; j < n16; j += 16) {
+        float4 nq[4];
+        const bool more = j + 16 < n16;
+#pragma unroll
+        for (int k = 0; k < 4; k++) nq[k] = more ? b4[(j >> 2) + 4 + k] : q[k];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          float4 r;
+          run = q[k].x + run; r.x = run;
+          run = q[k].y + run; r.y = run;
+          run = q[k].z + run; r.z = run;
+          run = q[k].w + run; r.w = run;
+          b4[(j >> 2) + k] = r;
         }
-        float4 ra, rb;
-        run = a.x + run; ra.x = run;
-        run = a.y + run; ra.y = run;
-        run = a.z + run; ra.z = run;
-        run = a.w + run; ra.w = run;
-        run = b.x + run; rb.x = run;
-        run = b.y + run; rb.y = run;
-        run = b.z + run; rb.z = run;
-        run = b.w + run; rb.w = run;
-        b4[j >> 2] = ra;
-        b4[(j >> 2) + 1] = rb;
-        a = na;
-        b = nb;
+#pragma unroll
+        for (int k = 0; k < 4; k++) q[k] = nq[k];
       }
-      for (int j = n8; j < n; j++) {
+      for (int j = n16; j < n; j++) {
         run = buf[j] + run;
         buf[j] = run;
       }
