@@ -95,6 +95,7 @@ struct drgb_batch {
       drgb_renderer* r = jobs.at(order[j]).get();
       Job& J = r->job;
       JobDev d = J.dev;
+      d.top_n = 0;  // batched kernels stage no job's top levels
       d.edge_key_base = (uint32_t)key_base;
       key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
       if (mode_groups.empty() || mode_groups.back().mode != J.mode)

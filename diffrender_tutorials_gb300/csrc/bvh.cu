@@ -699,6 +699,47 @@ static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int 
     std::memcpy(&l.y, &child[1], sizeof(int));
     links[t.node] = l;
   }
+  // The top levels of the hierarchy take node ids 0..K-1 in breadth-first
+  // order (the range kernels stage in shared memory); every other node keeps
+  // its depth-first order after them, so that a subtree stays contiguous.
+#ifdef DRGB_NO_RENUMBER
+  return;
+#endif
+  if (n < 2) return;
+  const int K = std::min(n - 1, kTopNodes);
+  std::vector<int> order;
+  order.reserve((size_t)(n - 1));
+  order.push_back(0);
+  for (size_t i = 0; i < order.size() && (int)order.size() < K; i++) {
+    int c[2];
+    std::memcpy(&c[0], &links[order[i]].x, sizeof(int));
+    std::memcpy(&c[1], &links[order[i]].y, sizeof(int));
+    for (int side = 0; side < 2 && (int)order.size() < K; side++)
+      if (c[side] >= 0) order.push_back(c[side]);
+  }
+  std::vector<char> top((size_t)(n - 1), 0);
+  for (int v : order) top[v] = 1;
+  for (int v = 0; v < n - 1; v++)
+    if (!top[v]) order.push_back(v);
+  std::vector<int> new_id((size_t)(n - 1));
+  for (int i = 0; i < n - 1; i++) new_id[order[i]] = i;
+  std::vector<float4> nl((size_t)(n - 1));
+  std::vector<int> np((size_t)(n - 1));
+  for (int old = 0; old < n - 1; old++) {
+    int c[2];
+    std::memcpy(&c[0], &links[old].x, sizeof(int));
+    std::memcpy(&c[1], &links[old].y, sizeof(int));
+    for (int side = 0; side < 2; side++)
+      if (c[side] >= 0) c[side] = new_id[c[side]];
+    float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    std::memcpy(&l.x, &c[0], sizeof(int));
+    std::memcpy(&l.y, &c[1], sizeof(int));
+    nl[new_id[old]] = l;
+    np[new_id[old]] = node_parent[old] >= 0 ? new_id[node_parent[old]] : -1;
+  }
+  links.swap(nl);
+  node_parent.swap(np);
+  for (int k = 0; k < n; k++) leaf_parent[k] = new_id[leaf_parent[k]];
 }
 
 // triangle -> leaf slot, for traversals seeded with a candidate triangle

@@ -116,6 +116,8 @@ struct JobDev {
   // internal node, < 0 leaf ~k, kEmpty4 unused), one unused float4
   const float4* nodes4;
   int root;              // >= 0 internal node, < 0 leaf ~k, INT_MIN if empty
+  int top_n;             // internal nodes 0..top_n-1 (the top levels, breadth-first numbering)
+                         // are read from the block's shared copy; 0: none staged
   const int* leaf_of;    // flattened triangle -> its leaf slot in `tri`
   int trace_bruteforce;  // 1: test every triangle (reference loop order)
   // model
@@ -482,6 +484,19 @@ __device__ __forceinline__ float safe_inv(float d) {
 // brute-force test would accept is skipped (boxes are also padded).
 __device__ __forceinline__ float cull_bound(float t) { return t + fabsf(t) * 4e-6f + 1e-6f; }
 
+// The top levels of the hierarchy in shared memory: kernels that trace for
+// a single job copy the first top_n internal nodes there once per block
+// (stage_top_nodes) before their first traversal; every other kernel traces
+// with top_n = 0.  127 nodes = the top 7 levels of a breadth-first numbered
+// binary hierarchy, 8 KB.
+constexpr int kTopNodes = 127;
+static __shared__ float4 g_top_nodes[4 * kTopNodes];
+
+__device__ __forceinline__ void stage_top_nodes(const JobDev& J) {
+  for (int i = threadIdx.x; i < 4 * J.top_n; i += blockDim.x) g_top_nodes[i] = __ldg(J.nodes + i);
+  __syncthreads();
+}
+
 // Nearest hit (ANY=false) or any hit (ANY=true) in [tNear, tFar).  Equal
 // distances resolve to the lowest flattened triangle index, which is the
 // triangle the reference's in-order brute-force loop keeps.
@@ -585,10 +600,18 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   while (true) {
     if (node >= 0) {
 #ifndef DRGB_BVH4
-      const float4 n0 = __ldg(J.nodes + 4 * node + 0);
-      const float4 n1 = __ldg(J.nodes + 4 * node + 1);
-      const float4 n2 = __ldg(J.nodes + 4 * node + 2);
-      const float4 n3 = __ldg(J.nodes + 4 * node + 3);
+      float4 n0, n1, n2, n3;
+      if (node < J.top_n) {
+        n0 = g_top_nodes[4 * node + 0];
+        n1 = g_top_nodes[4 * node + 1];
+        n2 = g_top_nodes[4 * node + 2];
+        n3 = g_top_nodes[4 * node + 3];
+      } else {
+        n0 = __ldg(J.nodes + 4 * node + 0);
+        n1 = __ldg(J.nodes + 4 * node + 1);
+        n2 = __ldg(J.nodes + 4 * node + 2);
+        n3 = __ldg(J.nodes + 4 * node + 3);
+      }
       const float hi_t = cull_bound(best.t);
       n_box += 2;
       const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, inv, oi, lo_t, hi_t);

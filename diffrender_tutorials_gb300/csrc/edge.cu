@@ -359,6 +359,7 @@ template <bool DET>
 __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(const JobDev* jobs, int job,
                                                                               const int* order) {
   const JobDev& J = jobs[job];
+  stage_top_nodes(J);
   edge_shade_loop<DET>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
 }
 

@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
 #ifdef DRGB_SEED_HITS
   __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
 #endif
+  stage_top_nodes(jobs[0]);  // a single job's top levels (none for a batch)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
@@ -487,6 +488,7 @@ void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s) {
 __global__ void k_cast(const JobDev* jobs, const CamDev* cam, const float* xy, int64_t n, uint32_t* prim,
                        uint32_t* inst, uint32_t* geom, float* t, float* u, float* v) {
   const JobDev& J = jobs[0];
+  stage_top_nodes(J);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   Surf s;
