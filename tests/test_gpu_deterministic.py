@@ -159,6 +159,35 @@ def test_hierarchy_rebuilds_leave_the_trajectory_unchanged():
         assert np.array_equal(verts, runs[0][1])
 
 
+def test_overlapped_rebuilds_with_jobs_leaving_mid_pipeline():
+    """Rebuild every step in a batch (the overlapped pipeline is always in
+    flight) while jobs are removed and added between steps: the remaining
+    job's bits match a run without rebuilds."""
+    probs = problems()
+    setups = []
+    for name, mode, spp, ts, isc, cams in probs[:2]:
+        st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+        r = D.MakeDifferentialRenderer(st)
+        r.commit(ts)
+        setups.append((isc, cams, r.render(ts, cams), st, opt_params(mode)))
+    out = []
+    for period in (0, 1):
+        b = D.BatchOptimizer()
+        b.set_option(N.OPT_DETERMINISTIC, 1)
+        b.set_option(N.OPT_BVH_REBUILD, period)
+        keep = b.add_job(*setups[0])
+        gone = b.add_job(*setups[1])
+        b.run(2)
+        b.remove_job(gone)
+        b.run(1)
+        late = b.add_job(*setups[1])
+        b.run(3)
+        out.append((b.losses(keep), b.job_scene(keep).meshes[0].vertices, b.losses(late)))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 def test_noalloc_entry_refuses_deterministic_mode():
     import torch
     name, mode, spp, ts, isc, cams = problems()[1]
