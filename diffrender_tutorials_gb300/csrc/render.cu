@@ -31,10 +31,67 @@ constexpr bool kPixelWarp = false;
 #endif
 
 // Warp-aggregated scatter of per-vertex colour gradients.  All 32 lanes
-// must call it; lanes without a contribution pass tri = -1.  The peers of a
-// triangle are summed by its lowest lane in lane order; that lane then adds
-// the 9 sums with atomics, or, in deterministic mode, writes 3 records at
-// rec_base + rec_n (rec_n: records of this work item so far, warp-uniform).
+// must call it; lanes without a contribution pass tri = -1.  The lanes that
+// hit one triangle form a group; for each group (in order of its lowest
+// lane) lanes 0-8 each sum one of the 9 values over the group's lanes in
+// lane order, then add it with one atomic each (or, in deterministic mode,
+// lane 0 writes the group's 3 records at rec_base + rec_n; rec_n: records of
+// this work item so far, warp-uniform).
+#ifndef DRGB_SCATTER_LEADER
+template <bool DET>
+__device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
+                                                      const float c[9], float* wscr, int64_t rec_base, int& rec_n) {
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(0xffffffffu, tri);
+#pragma unroll
+  for (int i = 0; i < 9; i++) wscr[i * 32 + lane] = c[i];
+  __syncwarp();
+  unsigned leaders = __ballot_sync(0xffffffffu, tri >= 0 && lane == __ffs(peers) - 1);
+  while (leaders) {
+    const int ld = __ffs(leaders) - 1;
+    leaders &= leaders - 1;
+    const unsigned group = __shfl_sync(0xffffffffu, peers, ld);
+    const int t = __shfl_sync(0xffffffffu, tri, ld);
+    const int vA = __shfl_sync(0xffffffffu, gA, ld), vB = __shfl_sync(0xffffffffu, gB, ld);
+    const int vC = __shfl_sync(0xffffffffu, gC, ld);
+    float sum = 0.0f;
+    if (lane < 9) {
+      unsigned m = group;
+      while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        sum += wscr[lane * 32 + l];
+      }
+    }
+    const int b = __ldg(J.tri_v + t).w;
+    const BlockDev bd = J.blocks[b];
+    const MeshDev& md = J.meshes[bd.mesh];
+    if (md.dslot < 0) continue;  // warp-uniform: the group's mesh
+    float* g = J.grad + md.g_base + md.color_off;
+    const int vert = (lane < 3 ? vA : lane < 6 ? vB : vC) - bd.vert_off;
+    if (DET && J.det) {
+      float v[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) v[i] = __shfl_sync(0xffffffffu, sum, i);
+      if (lane == 0) {
+        const int64_t slot = rec_base + rec_n;
+        const uint32_t k0 = (uint32_t)(g - J.grad);
+        J.rec_key[slot + 0] = k0 + 3 * (vA - bd.vert_off);
+        J.rec_val[slot + 0] = make_float4(v[0], v[1], v[2], 0.0f);
+        J.rec_key[slot + 1] = k0 + 3 * (vB - bd.vert_off);
+        J.rec_val[slot + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+        J.rec_key[slot + 2] = k0 + 3 * (vC - bd.vert_off);
+        J.rec_val[slot + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+      }
+      rec_n += 3;
+    } else if (lane < 9) {
+      atomicAdd(g + 3 * vert + lane % 3, sum);
+    }
+  }
+  __syncwarp();
+}
+#else
+// -DDRGB_SCATTER_LEADER: the group's lowest lane sums all 9 values alone.
 template <bool DET>
 __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
                                                       const float c[9], float* wscr, int64_t rec_base, int& rec_n) {
@@ -85,6 +142,7 @@ __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, 
   }
   __syncwarp();
 }
+#endif
 
 // sample_bilinear_clamp_3f_grad (shade_common.cpp:23-46): the four taps
 // and their weights; data points at the texture's gradient block.
