@@ -597,6 +597,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
   int sp = 0;
   int node = J.root;
   int guard = 0;
+  float hi_t = cull_bound(best.t);  // renewed when best.t shrinks
   while (true) {
     if (node >= 0) {
 #ifndef DRGB_BVH4
@@ -612,7 +613,9 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
         n2 = __ldg(J.nodes + 4 * node + 2);
         n3 = __ldg(J.nodes + 4 * node + 3);
       }
-      const float hi_t = cull_bound(best.t);
+#ifdef DRGB_CULL_PER_VISIT
+      hi_t = cull_bound(best.t);
+#endif
       n_box += 2;
       const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, inv, oi, lo_t, hi_t);
       const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, inv, oi, lo_t, hi_t);
@@ -639,7 +642,6 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
       const float4* q = J.nodes4 + 8 * node;
       const float4 LX = __ldg(q + 0), HX = __ldg(q + 1), LY = __ldg(q + 2), HY = __ldg(q + 3);
       const float4 LZ = __ldg(q + 4), HZ = __ldg(q + 5), LK = __ldg(q + 6);
-      const float hi_t = cull_bound(best.t);
       n_box += 4;
       const float inf = __int_as_float(0x7f800000);
       int c0 = __float_as_int(LK.x), c1 = __float_as_int(LK.y), c2 = __float_as_int(LK.z), c3 = __float_as_int(LK.w);
@@ -688,6 +690,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
             add_work(J, n_box, n_tri);
             return true;
           }
+          hi_t = cull_bound(best.t);
         }
       }
     }
