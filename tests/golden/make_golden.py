@@ -206,6 +206,37 @@ def main():
              "dmesh_ids": np.array([0], np.int32)}
     save("optimize_pyramid_restricted", **items, **prefixed("out.", run(items)))
 
+    # two meshes, a cube and a tetrahedron (one instance each), both
+    # differentiable (DScene with two DMesh blocks; the optimiser's "Adam"
+    # indexes its second-moment accumulator mesh-locally,
+    # optimizer_simple.cpp:224), and the cube alone differentiable with the
+    # tetrahedron as a static occluder
+    tet = TriangleMesh(np.array([[0, 0, 0], [0.6, 0, 0], [0, 0.6, 0], [0, 0, 0.6]], np.float32) +
+                       np.array([0.9, -0.1, 0.6], np.float32),
+                       np.array([0, 2, 1, 0, 1, 3, 0, 3, 2, 1, 2, 3], np.uint32),
+                       colors=np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0]], np.float32))
+    tet_init = perturb_vertices(tet, 0.05, seed=31)
+    tet_init.colors = np.clip(tet.colors + np.random.default_rng(32).normal(0, 0.1, (4, 3)), 0, 1).astype(np.float32)
+    tsm, ism = Scene(), Scene()
+    tsm.add_mesh(true_cube)
+    tsm.add_mesh(tet)
+    ism.add_mesh(init_cube)
+    ism.add_mesh(tet_init)
+    cams_m = [Cam((0.4, 0.7, 3.0), 64, 64)]
+    tgt_m = run({"task": np.array([2], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+                 **scene_items(tsm), **cam_items(cams_m)})["images"]
+    for name, ids in (("drc_two_meshes", [0, 1]), ("drc_static_occluders", [0])):
+        items = {"task": np.array([4], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+                 **scene_items(ism), **cam_items(cams_m), "targets": tgt_m,
+                 "edge_samples": np.array([64 * 64], np.int32), "dmesh_ids": np.array(ids, np.int32)}
+        save(name, **items, **prefixed("out.", run(items)))
+    items = {"task": np.array([5], np.int32), "mode": np.array([VC], np.int32), "spp": np.array([4], np.int32),
+             **scene_items(ism), **cam_items(cams_m), "targets": tgt_m, "iters": np.array([5], np.int32),
+             "opt_alg": np.array([4], np.int32), "opt_pos_lr": np.array([0.01], np.float32),
+             "opt_base_lr": np.array([0.01], np.float32), "opt_flags": np.array([1 | 4], np.int32),
+             "dmesh_ids": np.array([0, 1], np.int32)}
+    save("optimize_two_meshes", **items, **prefixed("out.", run(items)))
+
     # two views, d_render with a given adjoint (accumulation over views)
     cams2 = [Cam((0, 0, 3), 48, 48), Cam((2.2, 1.0, 1.8), 48, 48)]
     adj = np.random.default_rng(13).normal(0, 0.5, size=2 * 48 * 48 * 3).astype(np.float32)

@@ -95,7 +95,8 @@ def test_render_bit_exact_vs_reference(name, mode, spp):
 
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
                                        ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6),
-                                       ("drc_cube_instanced", 2)])
+                                       ("drc_cube_instanced", 2), ("drc_two_meshes", 2),
+                                       ("drc_static_occluders", 2)])
 def test_d_render_and_compare_vs_reference(name, mode):
     d = load(name)
     sc = scene_from(d)
@@ -149,6 +150,37 @@ def test_optimizer_trajectory_vs_reference(deterministic):
         assert np.abs(cur.vertices.reshape(-1) - d[f"out.it{k}.m0.vertices"]).max() < 5e-5, k
         assert np.abs(cur.colors.reshape(-1) - d[f"out.it{k}.m0.colors"]).max() < 5e-5, k
     assert opt.losses[-1] == pytest.approx(float(d["out.final_error"][0]), rel=1e-4)
+
+
+def test_optimizer_trajectory_two_meshes_vs_reference():
+    """Two differentiable meshes, the second stepped with the first mesh's
+    second-moment accumulator (the reference's mesh-local index).  The first
+    step must match.  After it, the per-component normalised steps turn
+    summation-order noise in near-zero gradient components into full
+    learning-rate steps of either sign, so the second step of the first mesh
+    is compared component-wise for most components; the second mesh divides
+    by the first mesh's (unrelated, often near-zero) accumulator entries and
+    is compared at the first step only."""
+    d = load("optimize_two_meshes")
+    sc = scene_from(d)
+    r = make(2, int(d["spp"][0]))
+    r.set_option(N.OPT_DETERMINISTIC, 1)
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=float(d["opt_pos_lr"][0]), diff_mesh_ids=(0, 1))
+    p.base_lr = float(d["opt_base_lr"][0])
+    p.flags = int(d["opt_flags"][0])
+    opt = D.CreateSimpleOptimizer()
+    opt.Init(sc, r, cams_from(d), d["targets"], p)
+    for k in range(2):
+        opt.Run(1)
+        cur = opt.current_scene()
+        for m in range(2 if k == 0 else 1):
+            for what, got in (("vertices", cur.meshes[m].vertices), ("colors", cur.meshes[m].colors)):
+                ref = d[f"out.it{k}.m{m}.{what}"]
+                close = np.abs(got.reshape(-1) - ref) <= 1e-4 * max(1.0, float(np.abs(ref).max()))
+                if k == 0:
+                    assert close.all(), (k, m, what)
+                else:
+                    assert close.mean() >= 0.75, (k, m, what, close.mean())
 
 
 # ---------------------------------------------------------------------------

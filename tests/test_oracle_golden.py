@@ -78,7 +78,8 @@ def test_render_bit_exact(name, mode, spp):
 @pytest.mark.parametrize("name,mode", [("drc_cube_m2", 2), ("drc_cube_m1", 1), ("drc_sphere_m3", 3),
                                        ("drc_sphere_m4", 4), ("drc_sphere_m5", 5), ("drc_sphere_m6", 6),
                                        ("drc_cube_instanced", 2), ("drc_pyramid_restricted_m2", 2),
-                                       ("drc_pyramid_restricted_m16", 16)])
+                                       ("drc_pyramid_restricted_m16", 16), ("drc_two_meshes", 2),
+                                       ("drc_static_occluders", 2)])
 def test_d_render_and_compare(name, mode):
     d = load(name)
     loss, ds, imgs = O.d_render_and_compare(scene_from(d), cams_from(d), mode, int(d["spp"][0]), d["targets"],
@@ -111,6 +112,26 @@ def test_optimizer_trajectory():
     for k in range(iters):
         assert np.array_equal(r["vertices"][k], d[f"out.it{k}.m0.vertices"]), k
         assert np.array_equal(r["colors"][k], d[f"out.it{k}.m0.colors"]), k
+    assert r["final_error"] == pytest.approx(float(d["out.final_error"][0]), rel=1e-6)
+
+
+def test_optimizer_trajectory_two_meshes():
+    """Two differentiable meshes: the reference's "Adam" divides every mesh's
+    moment by the second-moment accumulator indexed mesh-locally
+    (optimizer_simple.cpp:224), so the second mesh steps with the first
+    mesh's accumulator."""
+    d = load("optimize_two_meshes")
+    p = O.opt_params(4, position_lr=float(d["opt_pos_lr"][0]), base_lr=float(d["opt_base_lr"][0]),
+                     flags=int(d["opt_flags"][0]), dmesh_ids=[0, 1])
+    iters = int(d["iters"][0])
+    sc = scene_from(d)
+    r = O.optimize(sc, cams_from(d), 2, int(d["spp"][0]), d["targets"], p, iters)
+    n0v, n0c = 3 * sc.meshes[0].vertex_count, 3 * sc.meshes[0].vertex_count
+    for k in range(iters):
+        assert np.array_equal(r["vertices"][k][:n0v], d[f"out.it{k}.m0.vertices"]), k
+        assert np.array_equal(r["vertices"][k][n0v:], d[f"out.it{k}.m1.vertices"]), k
+        assert np.array_equal(r["colors"][k][:n0c], d[f"out.it{k}.m0.colors"]), k
+        assert np.array_equal(r["colors"][k][n0c:], d[f"out.it{k}.m1.colors"]), k
     assert r["final_error"] == pytest.approx(float(d["out.final_error"][0]), rel=1e-6)
 
 
