@@ -428,6 +428,28 @@ static const int* sort_queue(const JobDev* d_jobs, int job, const Job& J, int gr
 }
 
 // Jq (may be null): the job whose queue-sort buffers order the shading.
+// The part of the edge pass that needs only the vertices: projection, pmf
+// and CDF of every view (may run beside the pixel pass).
+void launch_edges_prep(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, cudaStream_t s) {
+  if (n_edges <= 0 || n_views <= 0) return;
+  k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  k_edge_cdf<<<n_views, CDF_THREADS, 0, s>>>(d_jobs, job);
+  count_launch(3);
+}
+
+// The rest, which reads the adjoint image: selection, ordering, shading.
+void launch_edges_rest(const JobDev* d_jobs, int job, int n_edges, int n_views, int edge_samples, int* queue_count,
+                       int shade_grid, cudaStream_t s, bool det, const Job* Jq) {
+  if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
+  DRGB_CUDA(cudaMemsetAsync(queue_count, 0, 2 * sizeof(int), s));  // queue count, shading counter
+  k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
+  const int* order = Jq ? sort_queue(d_jobs, job, *Jq, shade_grid, s) : nullptr;
+  if (det) k_edge_shade_job<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
+  else k_edge_shade_job<false><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
+  count_launch(2);
+}
+
 void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
                       int* queue_count, int shade_grid, cudaStream_t s, bool det, const Job* Jq) {
   if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;

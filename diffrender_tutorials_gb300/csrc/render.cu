@@ -625,6 +625,24 @@ void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* 
   count_launch();
 }
 
+int pixel_blocks_resident(int mode) {
+  int n = 0;
+  const void* f = nullptr;
+  switch (mode) {
+    case SILHOUETTE: f = (const void*)k_pixels<SILHOUETTE, false, false>; break;
+    case VERTEX_COLOR: f = (const void*)k_pixels<VERTEX_COLOR, false, false>; break;
+    case TEXTURE_COLOR: f = (const void*)k_pixels<TEXTURE_COLOR, false, false>; break;
+    case LAMBERT: f = (const void*)k_pixels<LAMBERT, false, false>; break;
+    case PHONG: f = (const void*)k_pixels<PHONG, false, false>; break;
+    case GGX: f = (const void*)k_pixels<GGX, false, false>; break;
+    case LAMBERT_POINT_VCOLOR: f = (const void*)k_pixels<LAMBERT_POINT_VCOLOR, false, false>; break;
+    case PATH_DIFFUSE: f = (const void*)k_pixels<PATH_DIFFUSE, false, false>; break;
+    default: f = (const void*)k_pixels<0, false, false>; break;
+  }
+  DRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, PX_THREADS, 0));
+  return std::max(1, n);
+}
+
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s) {
   k_loss_finalize<<<dim3(kLossBlocks, n_jobs), LOSS_THREADS, 0, s>>>(d_jobs, n_jobs);
   count_launch();

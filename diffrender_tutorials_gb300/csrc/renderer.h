@@ -58,8 +58,18 @@ struct drgb_renderer {
   int64_t graph_kernels = 0;
   bool graph_valid = false;
 
+  // Side branch of an iteration: the edge pass's projection, pmf and CDF run
+  // beside the pixel kernel when the mesh has many edges (the CDF is one
+  // sequential chain per view).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int px_resident = 0;  // pixel blocks per SM of the current model (0: not queried)
+
   ~drgb_renderer() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -211,17 +221,48 @@ struct drgb_renderer {
     graph_valid = false;
   }
 
+  // Meshes with at least this many edges run the CDF beside the pixel pass.
+  static constexpr int kSideCdfEdges = 50000;
+  bool side_cdf() const {
+#ifdef DRGB_NO_SIDE_CDF
+    return false;
+#endif
+    return job.dev.edge_samples > 0 && job.n_edges >= kSideCdfEdges && !job.det && !job.store_hits;
+  }
+
   // Forward + loss + interior adjoint + edges of the current views; grad is
-  // cleared first.  Everything is enqueued on the stream.
+  // cleared first.  Everything is enqueued on the stream (and, for meshes
+  // with many edges, on the side stream that joins it before the edge
+  // samples are drawn).
   void enqueue_iteration(bool want_images) {
     Job& J = job;
     const bool interior = J.mode != SILHOUETTE;
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, J.grad_bytes(), stream));
     det_begin();
     int flags = PX_FWD | PX_LOSS | (interior ? PX_ADJ : 0) | (want_images ? PX_IMG : 0);
-    pixel_pass(flags);
-    launch_loss_finalize(d_job.p, 1, stream);
-    if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
+    if (side_cdf()) {
+      if (!side) {
+        DRGB_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        DRGB_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        DRGB_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+      }
+      if (!px_resident) px_resident = pixel_blocks_resident(J.mode);
+      DRGB_CUDA(cudaEventRecord(ev_fork, stream));
+      DRGB_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+      launch_edges_prep(d_job.p, 0, J.n_edges, J.n_views, J.n_vertices, side);
+      DRGB_CUDA(cudaEventRecord(ev_join, side));
+      // one SM slot per CDF block stays free of the persistent pixel kernel
+      const int grid = std::max(1, std::min(px_grid(), sm_count * px_resident - J.n_views));
+      launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, grid, stream, J.mode, J.det);
+      launch_loss_finalize(d_job.p, 1, stream);
+      DRGB_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+      launch_edges_rest(d_job.p, 0, J.n_edges, J.n_views, J.dev.edge_samples, J.queue_count.p, edge_grid(), stream,
+                        false, &J);
+    } else {
+      pixel_pass(flags);
+      launch_loss_finalize(d_job.p, 1, stream);
+      if (J.dev.edge_samples > 0) launch_edges(d_job.p, 0, J, edge_grid(), stream);
+    }
     det_end();
     launch_restricted_grad(J, stream);
   }
