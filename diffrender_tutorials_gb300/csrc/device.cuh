@@ -484,18 +484,26 @@ __device__ __forceinline__ float safe_inv(float d) {
 // brute-force test would accept is skipped (boxes are also padded).
 __device__ __forceinline__ float cull_bound(float t) { return t + fabsf(t) * 4e-6f + 1e-6f; }
 
-// The top levels of the hierarchy in shared memory: kernels that trace for
-// a single job copy the first top_n internal nodes there once per block
-// (stage_top_nodes) before their first traversal; every other kernel traces
-// with top_n = 0.  127 nodes = the top 7 levels of a breadth-first numbered
-// binary hierarchy, 8 KB.
+// -DDRGB_TOP_SMEM: the top levels of the hierarchy in shared memory.  Kernels
+// that trace for a single job copy the first top_n internal nodes there once
+// per block (stage_top_nodes) before their first traversal; every other
+// kernel traces with top_n = 0.  127 nodes = the top 7 levels of the
+// breadth-first numbered top of the binned-SAH hierarchy, 8 KB.  Off by
+// default: the 8 KB per block come out of the SM's L1 (shared memory and L1
+// are one array), the pixel kernel's L1 hit rate fell from 79 % to 64 % and
+// the icosphere workload ran 9 % slower on GB300; the top nodes are L1-hot
+// without it.
 constexpr int kTopNodes = 127;
+#ifdef DRGB_TOP_SMEM
 static __shared__ float4 g_top_nodes[4 * kTopNodes];
 
 __device__ __forceinline__ void stage_top_nodes(const JobDev& J) {
   for (int i = threadIdx.x; i < 4 * J.top_n; i += blockDim.x) g_top_nodes[i] = __ldg(J.nodes + i);
   __syncthreads();
 }
+#else
+__device__ __forceinline__ void stage_top_nodes(const JobDev&) {}
+#endif
 
 // Nearest hit (ANY=false) or any hit (ANY=true) in [tNear, tFar).  Equal
 // distances resolve to the lowest flattened triangle index, which is the
@@ -602,12 +610,15 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
     if (node >= 0) {
 #ifndef DRGB_BVH4
       float4 n0, n1, n2, n3;
+#ifdef DRGB_TOP_SMEM
       if (node < J.top_n) {
         n0 = g_top_nodes[4 * node + 0];
         n1 = g_top_nodes[4 * node + 1];
         n2 = g_top_nodes[4 * node + 2];
         n3 = g_top_nodes[4 * node + 3];
-      } else {
+      } else
+#endif
+      {
         n0 = __ldg(J.nodes + 4 * node + 0);
         n1 = __ldg(J.nodes + 4 * node + 1);
         n2 = __ldg(J.nodes + 4 * node + 2);

@@ -44,7 +44,13 @@ __device__ __forceinline__ void edge_pmf_body(const JobDev& J, int view, int e) 
 // traffic off the chain: while thread 0 sums chunk c, warps 1-7 write chunk
 // c-1 out and stage chunk c+1.
 constexpr int CDF_THREADS = 256;
-constexpr int CDF_CHUNK = 2048;
+// 1,024 floats per chunk (12 KB for the three buffers): small enough that a
+// CDF block finds room on an SM beside the persistent pixel kernel (with
+// 2,048 it did not, and the side-stream CDF ran after the pixel pass).
+#ifndef DRGB_CDF_CHUNK
+#define DRGB_CDF_CHUNK 1024
+#endif
+constexpr int CDF_CHUNK = DRGB_CDF_CHUNK;
 constexpr int CDF_SMEM = 3 * CDF_CHUNK;  // floats of 16-byte aligned shared memory the caller provides
 __device__ __forceinline__ void edge_cdf_body(const JobDev& J, int view, float* sbuf) {
   const int tid = threadIdx.x;

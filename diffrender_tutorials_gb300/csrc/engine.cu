@@ -423,11 +423,11 @@ void sync_dev(Job& J) {
   d.nodes4 = J.nodes4.p;
   d.tri = J.tri.p;
   d.leaf_of = J.leaf_of.p;
-  // the binned-SAH topology numbers its nodes breadth first (top levels first)
-#ifdef DRGB_NO_TOP_STAGE
-  d.top_n = 0;
-#else
+  // the binned-SAH topology numbers its top levels first (breadth first)
+#ifdef DRGB_TOP_SMEM
   d.top_n = J.topo_builder == 1 ? std::min(std::max(J.n_tris - 1, 0), kTopNodes) : 0;
+#else
+  d.top_n = 0;
 #endif
   d.root = J.root;
   d.trace_bruteforce = J.trace_bruteforce;
