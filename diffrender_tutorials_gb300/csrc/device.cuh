@@ -489,10 +489,10 @@ __device__ __forceinline__ float cull_bound(float t) { return t + fabsf(t) * 4e-
 // per block (stage_top_nodes) before their first traversal; every other
 // kernel traces with top_n = 0.  127 nodes = the top 7 levels of the
 // breadth-first numbered top of the binned-SAH hierarchy, 8 KB.  Off by
-// default: the 8 KB per block come out of the SM's L1 (shared memory and L1
-// are one array), the pixel kernel's L1 hit rate fell from 79 % to 64 % and
-// the icosphere workload ran 9 % slower on GB300; the top nodes are L1-hot
-// without it.
+// default: the icosphere workload ran 9 % slower with it on GB300 (a branch
+// on every node visit and the staging, for nodes that are L1 hits anyway;
+// the pixel kernel's L1 hit rate fell from 79 % to 64 % as those hits left
+// L1).  A smaller shared footprint alone (below) changed nothing.
 constexpr int kTopNodes = 127;
 #ifdef DRGB_TOP_SMEM
 static __shared__ float4 g_top_nodes[4 * kTopNodes];

@@ -301,12 +301,22 @@ constexpr int px_min_blocks(int mode, bool det, bool hits) {
 template <int MODE, bool DET, bool HITS>
 __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
                                                        int n_items, int* counter, const int flags) {
+  // Shared memory per block stays small: what the block does not take
+  // stays L1 for the traversal's node and triangle loads (shared memory and
+  // L1 are one array per SM).  The forward colours and the adjoint's scatter
+  // scratch are never live together, so they share one buffer; the
+  // Hammersley points are read through L1.
+  constexpr int kWarpScratch = PX_MAX_SAMPLES * 3 > 9 * 32 ? PX_MAX_SAMPLES * 3 : 9 * 32;
   __shared__ JobDev sJ_all[PX_WARPS];
   __shared__ CamDev sC_all[PX_WARPS];
-  __shared__ float s_col_all[PX_WARPS][PX_MAX_SAMPLES * 3];
   __shared__ float4 s_adj_all[PX_WARPS][32];
-  __shared__ float s_ham_all[PX_WARPS][2 * 64];
+#ifndef DRGB_PX_SMEM_WIDE
+  __shared__ float s_buf_all[PX_WARPS][kWarpScratch];
+#else
+  __shared__ float s_col_all[PX_WARPS][PX_MAX_SAMPLES * 3];
   __shared__ float wscr_all[PX_WARPS][9 * 32];
+  __shared__ float s_ham_all[PX_WARPS][2 * 64];
+#endif
 #ifdef DRGB_SEED_HITS
   __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
 #endif
@@ -314,10 +324,15 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
-  float* s_col = s_col_all[warp];
   float4* s_adj = s_adj_all[warp];
-  float* s_ham = s_ham_all[warp];
+#ifndef DRGB_PX_SMEM_WIDE
+  float* s_col = s_buf_all[warp];  // forward: sample colours
+  float* wscr = s_buf_all[warp];   // adjoint: scatter scratch
+#else
+  float* s_col = s_col_all[warp];
   float* wscr = wscr_all[warp];
+  float* s_ham = s_ham_all[warp];
+#endif
 #ifdef DRGB_SEED_HITS
   int* s_hit = s_hit_all[warp];
 #endif
@@ -333,7 +348,9 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
       int* dst = reinterpret_cast<int*>(&J);
       for (int i = lane; i < (int)(sizeof(JobDev) / sizeof(int)); i += 32) dst[i] = src[i];
       __syncwarp();
+#ifdef DRGB_PX_SMEM_WIDE
       for (int i = lane; i < 2 * J.spp && i < 128; i += 32) s_ham[i] = J.ham[i];
+#endif
       cur_job = item.x;
       cur_view = -1;
     }
@@ -448,8 +465,13 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
             val = mk(a.x, a.y, a.z) / (float)S;
             act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
           }
+#ifndef DRGB_PX_SMEM_WIDE
+          sx = (float)px + __ldg(J.ham + 2 * k);
+          sy = (float)py + __ldg(J.ham + 2 * k + 1);
+#else
           sx = (float)px + s_ham[2 * k];
           sy = (float)py + s_ham[2 * k + 1];
+#endif
           const int64_t pix = (int64_t)py * W + px;
           key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
         }
@@ -468,8 +490,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         int seed = -1;
 #ifdef DRGB_SEED_HITS
         if ((flags & PX_FWD) && act) {
-          const int gx = min(sq - 1, (int)(s_ham[2 * k] * (float)sq));
-          const int gy = min(sq - 1, (int)(s_ham[2 * k + 1] * (float)sq));
+          const int gx = min(sq - 1, (int)(__ldg(J.ham + 2 * k) * (float)sq));
+          const int gy = min(sq - 1, (int)(__ldg(J.ham + 2 * k + 1) * (float)sq));
           seed = s_hit[p * S + gy * sq + gx];
         }
 #endif
