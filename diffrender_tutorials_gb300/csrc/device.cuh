@@ -492,7 +492,7 @@ __device__ __forceinline__ float cull_bound(float t) { return t + fabsf(t) * 4e-
 // default: the icosphere workload ran 9 % slower with it on GB300 (a branch
 // on every node visit and the staging, for nodes that are L1 hits anyway;
 // the pixel kernel's L1 hit rate fell from 79 % to 64 % as those hits left
-// L1).  A smaller shared footprint alone (below) changed nothing.
+// L1).  A smaller shared footprint alone changed nothing.
 constexpr int kTopNodes = 127;
 #ifdef DRGB_TOP_SMEM
 static __shared__ float4 g_top_nodes[4 * kTopNodes];
@@ -624,9 +624,6 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
         n2 = __ldg(J.nodes + 4 * node + 2);
         n3 = __ldg(J.nodes + 4 * node + 3);
       }
-#ifdef DRGB_CULL_PER_VISIT
-      hi_t = cull_bound(best.t);
-#endif
       n_box += 2;
       const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, inv, oi, lo_t, hi_t);
       const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, inv, oi, lo_t, hi_t);

@@ -37,7 +37,6 @@ constexpr bool kPixelWarp = false;
 // lane order, then add it with one atomic each (or, in deterministic mode,
 // lane 0 writes the group's 3 records at rec_base + rec_n; rec_n: records of
 // this work item so far, warp-uniform).
-#ifndef DRGB_SCATTER_LEADER
 template <bool DET>
 __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
                                                       const float c[9], float* wscr, int64_t rec_base, int& rec_n) {
@@ -90,59 +89,6 @@ __device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, 
   }
   __syncwarp();
 }
-#else
-// -DDRGB_SCATTER_LEADER: the group's lowest lane sums all 9 values alone.
-template <bool DET>
-__device__ __forceinline__ void scatter_vertex_colors(const JobDev& J, int tri, int gA, int gB, int gC,
-                                                      const float c[9], float* wscr, int64_t rec_base, int& rec_n) {
-  const int lane = threadIdx.x & 31;
-  const unsigned peers = __match_any_sync(0xffffffffu, tri);
-  const int leader = __ffs(peers) - 1;
-#pragma unroll
-  for (int i = 0; i < 9; i++) wscr[i * 32 + lane] = c[i];
-  __syncwarp();
-  float s[9];
-  float* g = nullptr;
-  int a = 0, bb = 0, cc = 0;
-  if (tri >= 0 && lane == leader) {
-#pragma unroll
-    for (int i = 0; i < 9; i++) s[i] = 0.0f;
-    unsigned m = peers;
-    while (m) {
-      const int l = __ffs(m) - 1;
-      m &= m - 1;
-#pragma unroll
-      for (int i = 0; i < 9; i++) s[i] += wscr[i * 32 + l];
-    }
-    const int b = __ldg(J.tri_v + tri).w;
-    const BlockDev bd = J.blocks[b];
-    const MeshDev& md = J.meshes[bd.mesh];
-    if (md.dslot >= 0) {
-      g = J.grad + md.g_base + md.color_off;
-      a = gA - bd.vert_off; bb = gB - bd.vert_off; cc = gC - bd.vert_off;
-    }
-  }
-  if (DET && J.det) {
-    const unsigned writers = __ballot_sync(0xffffffffu, g != nullptr);
-    if (g) {
-      const int64_t slot = rec_base + rec_n + 3 * __popc(writers & ((1u << lane) - 1u));
-      const uint32_t k0 = (uint32_t)(g - J.grad);
-      J.rec_key[slot + 0] = k0 + 3 * a;
-      J.rec_val[slot + 0] = make_float4(s[0], s[1], s[2], 0.0f);
-      J.rec_key[slot + 1] = k0 + 3 * bb;
-      J.rec_val[slot + 1] = make_float4(s[3], s[4], s[5], 0.0f);
-      J.rec_key[slot + 2] = k0 + 3 * cc;
-      J.rec_val[slot + 2] = make_float4(s[6], s[7], s[8], 0.0f);
-    }
-    rec_n += 3 * __popc(writers);
-  } else if (g) {
-    atomicAdd(g + 3 * a + 0, s[0]); atomicAdd(g + 3 * a + 1, s[1]); atomicAdd(g + 3 * a + 2, s[2]);
-    atomicAdd(g + 3 * bb + 0, s[3]); atomicAdd(g + 3 * bb + 1, s[4]); atomicAdd(g + 3 * bb + 2, s[5]);
-    atomicAdd(g + 3 * cc + 0, s[6]); atomicAdd(g + 3 * cc + 1, s[7]); atomicAdd(g + 3 * cc + 2, s[8]);
-  }
-  __syncwarp();
-}
-#endif
 
 // sample_bilinear_clamp_3f_grad (shade_common.cpp:23-46): the four taps
 // and their weights; data points at the texture's gradient block.
@@ -310,13 +256,7 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   __shared__ JobDev sJ_all[PX_WARPS];
   __shared__ CamDev sC_all[PX_WARPS];
   __shared__ float4 s_adj_all[PX_WARPS][32];
-#ifndef DRGB_PX_SMEM_WIDE
   __shared__ float s_buf_all[PX_WARPS][kWarpScratch];
-#else
-  __shared__ float s_col_all[PX_WARPS][PX_MAX_SAMPLES * 3];
-  __shared__ float wscr_all[PX_WARPS][9 * 32];
-  __shared__ float s_ham_all[PX_WARPS][2 * 64];
-#endif
 #ifdef DRGB_SEED_HITS
   __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
 #endif
@@ -325,14 +265,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
   float4* s_adj = s_adj_all[warp];
-#ifndef DRGB_PX_SMEM_WIDE
   float* s_col = s_buf_all[warp];  // forward: sample colours
   float* wscr = s_buf_all[warp];   // adjoint: scatter scratch
-#else
-  float* s_col = s_col_all[warp];
-  float* wscr = wscr_all[warp];
-  float* s_ham = s_ham_all[warp];
-#endif
 #ifdef DRGB_SEED_HITS
   int* s_hit = s_hit_all[warp];
 #endif
@@ -348,9 +282,6 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
       int* dst = reinterpret_cast<int*>(&J);
       for (int i = lane; i < (int)(sizeof(JobDev) / sizeof(int)); i += 32) dst[i] = src[i];
       __syncwarp();
-#ifdef DRGB_PX_SMEM_WIDE
-      for (int i = lane; i < 2 * J.spp && i < 128; i += 32) s_ham[i] = J.ham[i];
-#endif
       cur_job = item.x;
       cur_view = -1;
     }
@@ -465,13 +396,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
             val = mk(a.x, a.y, a.z) / (float)S;
             act = !(val.x == 0.0f && val.y == 0.0f && val.z == 0.0f);
           }
-#ifndef DRGB_PX_SMEM_WIDE
           sx = (float)px + __ldg(J.ham + 2 * k);
           sy = (float)py + __ldg(J.ham + 2 * k + 1);
-#else
-          sx = (float)px + s_ham[2 * k];
-          sy = (float)py + s_ham[2 * k + 1];
-#endif
           const int64_t pix = (int64_t)py * W + px;
           key = ((uint32_t)view * 0x9E3779B9u) ^ 0x5bd1e995u ^ ((uint32_t)(pix * 64 + k) * 2654435761u);
         }
