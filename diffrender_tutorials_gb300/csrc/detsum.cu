@@ -27,6 +27,7 @@ constexpr int DS_THREADS = 256;
 constexpr int DS_PER_THREAD = 8;
 constexpr int DS_CHUNK = DS_THREADS * DS_PER_THREAD;  // regions per block of the count scan
 constexpr int DS_GRID = 512;                           // blocks of the radix sort
+constexpr int DS_TR_BLOCKS = 256;                      // blocks of the dense transform sums
 
 __device__ __forceinline__ int64_t region_slot(int64_t r, int item_count, int item_cap) {
   return r < item_count ? r * item_cap
@@ -322,14 +323,73 @@ void det_buffers(Job& J, cudaStream_t s) {
   J.det_hist.reserve(256 * DS_GRID);
   J.det_frag.reserve(2 * ((std::max<int64_t>(1, cap) + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK));
   J.det_n.reserve(1);
+  // A single transform block among the differentiable meshes (one mesh, one
+  // instance): its 12 values per edge sample are summed densely in a fixed
+  // order instead of going through the sort as 4 records per sample.
+  int blocks = 0;
+  J.det_tr_key = -1;
+  for (const DLayout& L : J.dlay) {
+    blocks += L.instances;
+    if (L.instances == 1) J.det_tr_key = (int)(L.base + L.tr_off);
+  }
+  if (blocks != 1 || J.dev.edge_samples <= 0) J.det_tr_key = -1;
+#ifdef DRGB_NO_DENSE_TR
+  J.det_tr_key = -1;
+#endif
+  if (J.det_tr_key >= 0) {
+    J.det_tr.reserve(12 * (size_t)J.n_views * J.dev.edge_samples);
+    J.det_tr_part.reserve(12 * (size_t)DS_TR_BLOCKS);
+  }
   J.dev.det = 1;
   J.dev.rec_key = J.rec_key.p;
   J.dev.rec_val = J.rec_val.p;
   J.dev.rec_count = J.rec_count.p;
+  J.dev.det_tr = J.det_tr_key >= 0 ? J.det_tr.p : nullptr;
+  J.dev.det_tr_key = J.det_tr_key;
 }
 
 void launch_det_clear(const Job& J, cudaStream_t s) {
   DRGB_CUDA(cudaMemsetAsync(J.rec_count.p, 0, sizeof(int) * std::max<int64_t>(1, det_regions(J)), s));
+  if (J.det_tr_key >= 0)
+    DRGB_CUDA(cudaMemsetAsync(J.det_tr.p, 0, sizeof(float) * 12 * (size_t)J.n_views * J.dev.edge_samples, s));
+}
+
+// Dense transform sums: block b adds samples [b*chunk, (b+1)*chunk) (thread t
+// every DS_THREADS-th one from t, then a fixed tree), the last kernel adds
+// the block sums in block order into the gradient.
+__global__ void __launch_bounds__(DS_THREADS) k_ds_tr_blocks(const float* tr, int64_t n, float* part) {
+  __shared__ float red[12][DS_THREADS];
+  const int64_t chunk = (n + DS_TR_BLOCKS - 1) / DS_TR_BLOCKS;
+  const int64_t b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  float acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) acc[k] = 0.0f;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += DS_THREADS) {
+    const float4* T = reinterpret_cast<const float4*>(tr + 12 * i);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const float4 v = T[q];
+      acc[4 * q] += v.x; acc[4 * q + 1] += v.y; acc[4 * q + 2] += v.z; acc[4 * q + 3] += v.w;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 12; k++) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int h = DS_THREADS / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+#pragma unroll
+      for (int k = 0; k < 12; k++) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x < 12) part[12 * blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_ds_tr_final(const float* part, float* grad, int key) {
+  const int k = threadIdx.x;
+  if (k >= 12) return;
+  float s = 0.0f;
+  for (int b = 0; b < DS_TR_BLOCKS; b++) s += part[12 * b + k];
+  grad[key + k] += s;
 }
 
 void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
@@ -357,6 +417,12 @@ void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
                                                                     J.rec_val.p, J.grad.p, J.det_frag.p);
   k_ds_seg_final<<<1, 32, 0, s>>>(J.det_n.p, J.det_frag.p, J.grad.p);
   count_launch(2);
+  if (J.det_tr_key >= 0) {
+    k_ds_tr_blocks<<<DS_TR_BLOCKS, DS_THREADS, 0, s>>>(J.det_tr.p, (int64_t)J.n_views * J.dev.edge_samples,
+                                                      J.det_tr_part.p);
+    k_ds_tr_final<<<1, 32, 0, s>>>(J.det_tr_part.p, J.grad.p, J.det_tr_key);
+    count_launch(2);
+  }
 }
 
 }  // namespace drgb

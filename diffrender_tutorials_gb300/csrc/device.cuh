@@ -170,6 +170,8 @@ struct JobDev {
   uint32_t* rec_key;
   float4* rec_val;
   int* rec_count;            // records per region: work items, then (view, sample) edge regions
+  float* det_tr;             // deterministic mode with one transform block: 12 floats per edge sample
+  int det_tr_key;            // (view, sample order), summed in a fixed order into grad[det_tr_key + 0..11]
   // stored adjoint hits (one float4 {t, u, v, triangle} per adjoint sample)
   float4* hit_buf;
 };

@@ -243,19 +243,28 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
         tr[11] = 1 * dv0_dz + 1 * dv1_dz;
         target = J.grad + md.g_base + md.tr_off + 12 * mi.y;
         if (DET && J.det) {
-          // six records in the sample's own slots, in a fixed order
+          // the records in the sample's own slots, in a fixed order
           const int64_t slot = edge_rec_slot(J, view, i);
           const uint32_t kp = (uint32_t)(g - J.grad), kt = (uint32_t)(target - J.grad);
           J.rec_key[slot + 0] = kp + 3 * ed.z;
           J.rec_val[slot + 0] = make_float4(d0.x, d0.y, d0.z, 0.0f);
           J.rec_key[slot + 1] = kp + 3 * ed.w;
           J.rec_val[slot + 1] = make_float4(d1.x, d1.y, d1.z, 0.0f);
+          if (J.det_tr) {
+            // the job's only transform block: 12 dense values per sample,
+            // summed later in a fixed order without sorting
+            float4* T = reinterpret_cast<float4*>(J.det_tr + ((int64_t)view * J.edge_samples + i) * 12);
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
-            J.rec_key[slot + 2 + k] = kt + 3 * k;
-            J.rec_val[slot + 2 + k] = make_float4(tr[3 * k], tr[3 * k + 1], tr[3 * k + 2], 0.0f);
+            for (int k = 0; k < 3; k++) T[k] = make_float4(tr[4 * k], tr[4 * k + 1], tr[4 * k + 2], tr[4 * k + 3]);
+            J.rec_count[edge_region(J, view, i)] = 2;
+          } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              J.rec_key[slot + 2 + k] = kt + 3 * k;
+              J.rec_val[slot + 2 + k] = make_float4(tr[3 * k], tr[3 * k + 1], tr[3 * k + 2], 0.0f);
+            }
+            J.rec_count[edge_region(J, view, i)] = kEdgeRecords;
           }
-          J.rec_count[edge_region(J, view, i)] = kEdgeRecords;
           target = nullptr;
         }
       }

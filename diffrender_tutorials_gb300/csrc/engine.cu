@@ -469,6 +469,8 @@ void sync_dev(Job& J) {
   d.rec_key = J.rec_key.p;
   d.rec_val = J.rec_val.p;
   d.rec_count = J.rec_count.p;
+  d.det_tr = d.det && J.det_tr_key >= 0 ? J.det_tr.p : nullptr;
+  d.det_tr_key = J.det_tr_key;
   d.hit_buf = J.hit_buf.p;
 }
 

@@ -227,6 +227,8 @@ struct Job {
   DevBuf<float4> rec_val;
   DevBuf<int> rec_count, det_idx[2], det_n;
   DevBuf<DetFrag> det_frag;
+  DevBuf<float> det_tr, det_tr_part;  // one transform block: dense per-sample values, block sums
+  int det_tr_key = -1;                // its gradient index (-1: transform records instead)
   // work items
   std::vector<int4> h_pixel_items;
   int n_tiles_x = 0, n_tiles_y = 0;
