@@ -215,7 +215,7 @@ def read_traffic():
     return None
 
 
-BVH_BUILDERS = {"lbvh": 0, "sah": 1}
+BVH_BUILDERS = {"lbvh": 0, "sah": 1, "two_level": 2, "flat_sah": 3}
 
 
 def drgb_arm(args, w, ws, rank, local, pg):
@@ -483,6 +483,109 @@ def stress_problem(n_tris=200_000, res=1024, seed=0):
     return ts, isc, cams
 
 
+def instances_problem(n_inst=64, sub=4, res=512, views=4, seed=0):
+    """One icosphere (sub 4: 5,120 triangles) instanced on a 4x4x4 grid: scale
+    0.35, translations chosen so that the traced spheres (the instance
+    transform is applied twice, as the reference's brute-force caster does)
+    sit 0.5 apart with radius 0.12.  The initial scene moves every instance
+    by N(0, 0.02) per axis; ring cameras."""
+    import diffrender_tutorials_gb300 as D
+    rng = np.random.default_rng(seed)
+    mesh = D.make_icosphere(sub, seed=1)
+    s = 0.35
+    side = round(n_inst ** (1 / 3))
+    true_tr, init_tr = [], []
+    for i in range(n_inst):
+        c = np.array([i % side, (i // side) % side, i // (side * side)], np.float64)
+        c = (c - (side - 1) / 2) * 0.5
+        for lst, off in ((true_tr, 0.0), (init_tr, rng.normal(0.0, 0.02, 3))):
+            m = np.eye(4, dtype=np.float32)
+            m[0, 0] = m[1, 1] = m[2, 2] = s
+            m[:3, 3] = (c / (1 + s) + off).astype(np.float32)
+            lst.append(m)
+    ts, isc = D.Scene(), D.Scene()
+    ts.add_mesh(mesh, true_tr)
+    isc.add_mesh(mesh, init_tr)
+    cams = D.ring_cameras(views, 3.0, res, res)
+    return ts, isc, cams
+
+
+def instances_arm(args, ws, rank, local, pg):
+    """Instanced scene (64 instances of a 5,120-triangle icosphere, point
+    light, 4 views at 512x512, 16 spp), instance transforms optimised: the
+    flat binned-SAH hierarchy over all 327,680 triangles against the two-level
+    build (one hierarchy per mesh, shared by its instances, under one over the
+    instances).  Per builder: the commit (flatten + host build + refit), the
+    iteration rate with refits only, and with a rebuild every 10 iterations."""
+    import time
+    import torch
+    import diffrender_tutorials_gb300 as D
+    from diffrender_tutorials_gb300 import build as B
+    from diffrender_tutorials_gb300 import native as N
+    B.build()
+    torch.cuda.set_device(local)
+    ts, isc, cams = instances_problem()
+    S = D.SHADING_MODEL.LAMBERT_POINT_VCOLOR
+    spp = 16
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+    r.commit(ts)
+    tgt = r.render(ts, cams)
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.0, transforms_lr=0.002)
+    p.flags = D.OptimizerParameters._OPT_TFM
+    n_tri = sum(m.face_count * len(t) for m, t in zip(isc.meshes, isc.transforms))
+    out = {}
+    for label, builder in (("lbvh", 0), ("flat_sah", 3), ("two_level", 1)):  # 1: the default, two-level here
+        commit_ms = []
+        for _ in range(3):  # a new renderer each time: a commit of the same triangles keeps the topology
+            rb = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+            rb.set_option(N.OPT_BVH_BUILDER, builder)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rb.commit(isc)
+            torch.cuda.synchronize()
+            commit_ms.append((time.perf_counter() - t0) * 1e3)
+            del rb
+        res = {"commit_ms": float(np.median(commit_ms))}
+        for period in (0, 10):
+            ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+            ro.set_option(N.OPT_BVH_BUILDER, builder)
+            ro.set_option(N.OPT_BVH_REBUILD, period)
+            opt = D.CreateSimpleOptimizer()
+            opt.Init(isc, ro, cams, tgt, p)
+            stream = torch.cuda.ExternalStream(ro.stream(), device=local)
+            for _ in range(args.warmup):
+                opt.run_async(1)
+            torch.cuda.synchronize()
+            with ClockSampler(local) as clk:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    opt.run_async(args.steps)
+                    e1.record(stream)
+                torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            key = "refit_only" if period == 0 else "rebuild_every_10"
+            res[key] = {"value": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "clocks": clk.summary()}
+            if period == 0:
+                res[key]["phases_ms"] = opt.profile(2)
+            del opt, ro
+        out[label] = res
+    best = out["two_level"]["rebuild_every_10"]
+    line = {
+        "metric": "fwd+adjoint iters/s", "value": best["value"], "unit": "iters/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (instanced icosphere grid)",
+        "config": {"workload": f"instances64_icosphere5120_pointlight_4views_512x512_16spp", "triangles": n_tri,
+                   "instances": 64, "optimised": "instance transforms", "bvh_rebuild_period": 10,
+                   "l2": "inputs larger than L2 (flattened scene + hierarchy ~60 MB, image buffers ~50 MB)",
+                   "parallelism": "replicas"},
+        "builders": out,
+        "clocks": best["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def fd_check(r, isc, cams, tgt, grad_pos, coords, h=1e-3):
     """Central finite differences of the loss at `coords` (flat vertex
     coordinate indices of mesh 0) against the gradient's position block."""
@@ -747,7 +850,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="drgb", choices=["drgb", "reference"])
-    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve", "stress"])
+    ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve", "stress", "instances"])
     ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
     ap.add_argument("--bvh", default="sah", choices=sorted(BVH_BUILDERS), help="hierarchy builder")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
@@ -759,8 +862,8 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)
     ws, rank, local, pg = dist_setup()
-    if args.workload == "stress":
-        stress_arm(args, ws, rank, local, pg)
+    if args.workload in ("stress", "instances"):
+        (stress_arm if args.workload == "stress" else instances_arm)(args, ws, rank, local, pg)
         if pg is not None:
             pg.destroy_process_group()
         return

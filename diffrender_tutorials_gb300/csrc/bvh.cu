@@ -492,12 +492,13 @@ void rebuild_bvh(Job& J, cudaStream_t s) {
   refit_bvh(J, s);
 }
 
-static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int n, std::vector<float4>& links,
-                         std::vector<int>& perm, std::vector<int>& leaf_parent, std::vector<int>& node_parent);
+static void host_topology(int builder, const float4* pos, const float* block_tr, const std::vector<int4>& tri_v,
+                          const std::vector<BlockDev>& blocks, int n_vertices, int n, std::vector<float4>& links,
+                          std::vector<int>& perm, std::vector<int>& leaf_parent, std::vector<int>& node_parent);
 
 void rebuild_bvh_begin(Job& J, cudaStream_t s) {
   const int n = J.n_tris;
-  if (J.bvh_builder != 1 || n <= 1) {  // a device build blocks nothing
+  if (J.bvh_builder == 0 || n <= 1) {  // a device build blocks nothing
     rebuild_bvh(J, s);
     return;
   }
@@ -507,6 +508,9 @@ void rebuild_bvh_begin(Job& J, cudaStream_t s) {
   if (!T.ev) DRGB_CUDA(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
   T.pos.reserve((size_t)J.n_vertices);
   DRGB_CUDA(cudaMemcpyAsync(T.pos.p, J.pos.p, sizeof(float4) * J.n_vertices, cudaMemcpyDeviceToHost, s));
+  T.block_tr.reserve(32 * (size_t)J.n_blocks);
+  DRGB_CUDA(cudaMemcpyAsync(T.block_tr.p, J.block_tr.p, sizeof(float) * 32 * J.n_blocks, cudaMemcpyDeviceToHost, s));
+  T.builder = J.bvh_builder;
   DRGB_CUDA(cudaEventRecord(T.ev, s));
   T.stage = 1;
 }
@@ -525,10 +529,13 @@ void rebuild_bvh_poll(Job& J, cudaStream_t s) {
     T.node_parent.reserve(n - 1);
     TopoRebuild* t = &T;
     const std::vector<int4>* tri_v = &J.h_tri_v;
-    T.task = std::async(std::launch::async, [t, tri_v, n] {
+    const std::vector<BlockDev>* blocks = &J.h_blocks;
+    const int nv = J.n_vertices;
+    T.task = std::async(std::launch::async, [t, tri_v, blocks, nv, n] {
       std::vector<float4> links;
       std::vector<int> perm, leaf_parent, node_parent;
-      sah_topology(t->pos.p, *tri_v, n, links, perm, leaf_parent, node_parent);
+      host_topology(t->builder, t->pos.p, t->block_tr.p, *tri_v, *blocks, nv, n, links, perm, leaf_parent,
+                    node_parent);
       std::fill(t->nodes.p, t->nodes.p + 4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
       for (int i = 0; i < n - 1; i++) t->nodes.p[4 * (size_t)i + 3] = links[i];
       std::memcpy(t->perm.p, perm.data(), sizeof(int) * n);
@@ -547,7 +554,7 @@ void rebuild_bvh_poll(Job& J, cudaStream_t s) {
     DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, T.node_parent.p, sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
     refit_bvh(J, s);
     J.topo_tri_v = J.h_tri_v;
-    J.topo_builder = 1;
+    J.topo_builder = T.builder;
     T.stage = 0;
   }
 }
@@ -567,28 +574,25 @@ void refit_bvh(Job& J, cudaStream_t s) {
 #endif
 }
 
-// Binned SAH build of the hierarchy's topology on the host (16 bins per
-// axis over the triangle centroids, one triangle per leaf); the boxes are
-// filled by the device refit, exactly as for the LBVH.  Outputs the child
-// links of every internal node (root 0), the leaf permutation and the
-// parent arrays.
-static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int n,
-                         std::vector<float4>& links, std::vector<int>& perm, std::vector<int>& leaf_parent,
-                         std::vector<int>& node_parent) {
-  struct Item {
-    float lo[3], hi[3], c[3];
-  };
-  std::vector<Item> items((size_t)n);
-  for (int t = 0; t < n; t++) {
-    const int4 tv = tri_v[t];
-    const float4 a = pos[tv.x], b = pos[tv.y], c = pos[tv.z];
-    Item& it = items[t];
-    const float xa[3] = {a.x, a.y, a.z}, xb[3] = {b.x, b.y, b.z}, xc[3] = {c.x, c.y, c.z};
-    for (int k = 0; k < 3; k++) {
-      it.lo[k] = std::min(xa[k], std::min(xb[k], xc[k]));
-      it.hi[k] = std::max(xa[k], std::max(xb[k], xc[k]));
-      it.c[k] = 0.5f * (it.lo[k] + it.hi[k]);
-    }
+// Binned SAH build of a hierarchy's topology on the host (16 bins per axis
+// over the item centroids, one item per leaf); the boxes are filled by the
+// device refit, exactly as for the LBVH.  Outputs the child links of every
+// internal node (root 0; a leaf child is ~slot), the leaf permutation (slot
+// -> item) and the parent arrays.  Leaf slots and internal nodes are numbered
+// in the order the build reaches them.
+struct SahItem {
+  float lo[3], hi[3], c[3];
+};
+
+static void sah_tree(const std::vector<SahItem>& items, std::vector<float4>& links, std::vector<int>& perm,
+                     std::vector<int>& leaf_parent, std::vector<int>& node_parent) {
+  const int n = (int)items.size();
+  if (n < 2) {
+    links.assign(1, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    perm.assign((size_t)n, 0);
+    leaf_parent.assign((size_t)n, -1);
+    node_parent.assign(1, -1);
+    return;
   }
   std::vector<int> idx((size_t)n);
   for (int t = 0; t < n; t++) idx[t] = t;
@@ -628,7 +632,7 @@ static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int 
           bhi[q][k] = -1e30f;
         }
       for (int i = t.b; i < t.e; i++) {
-        const Item& it = items[idx[i]];
+        const SahItem& it = items[idx[i]];
         const int q = std::min(NB - 1, (int)((it.c[ax] - cmin[ax]) / ext * NB));
         cnt[q]++;
         for (int k = 0; k < 3; k++) {
@@ -699,9 +703,54 @@ static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int 
     std::memcpy(&l.y, &child[1], sizeof(int));
     links[t.node] = l;
   }
-  // The top levels of the hierarchy take node ids 0..K-1 in breadth-first
-  // order (the range kernels stage in shared memory); every other node keeps
-  // its depth-first order after them, so that a subtree stays contiguous.
+}
+
+// A flattened vertex as traced: after its block's transform (host copy of
+// traced_vertex; the build needs no exact value).
+static void traced_host(const float4* pos, const float* block_tr, int b, int g, float w[3]) {
+  const float4 p = pos[g];
+  const float* m = block_tr + 32 * (size_t)b;
+  w[0] = p.x * m[0] + p.y * m[4] + p.z * m[8] + m[12];
+  w[1] = p.x * m[1] + p.y * m[5] + p.z * m[9] + m[13];
+  w[2] = p.x * m[2] + p.y * m[6] + p.z * m[10] + m[14];
+}
+
+// Items of n triangles: boxes of their vertices as traced.
+static void tri_items(const float4* pos, const float* block_tr, const int4* tri_v, int n, std::vector<SahItem>& items) {
+  items.resize((size_t)n);
+  for (int t = 0; t < n; t++) {
+    const int4 tv = tri_v[t];
+    float xa[3], xb[3], xc[3];
+    traced_host(pos, block_tr, tv.w, tv.x, xa);
+    traced_host(pos, block_tr, tv.w, tv.y, xb);
+    traced_host(pos, block_tr, tv.w, tv.z, xc);
+    SahItem& it = items[t];
+    for (int k = 0; k < 3; k++) {
+      it.lo[k] = std::min(xa[k], std::min(xb[k], xc[k]));
+      it.hi[k] = std::max(xa[k], std::max(xb[k], xc[k]));
+      it.c[k] = 0.5f * (it.lo[k] + it.hi[k]);
+    }
+  }
+}
+
+static void renumber_top(int n, std::vector<float4>& links, std::vector<int>& leaf_parent,
+                         std::vector<int>& node_parent);
+
+// One SAH hierarchy over every triangle of the scene.
+static void sah_topology(const float4* pos, const float* block_tr, const std::vector<int4>& tri_v, int n,
+                         std::vector<float4>& links, std::vector<int>& perm, std::vector<int>& leaf_parent,
+                         std::vector<int>& node_parent) {
+  std::vector<SahItem> items;
+  tri_items(pos, block_tr, tri_v.data(), n, items);
+  sah_tree(items, links, perm, leaf_parent, node_parent);
+  renumber_top(n, links, leaf_parent, node_parent);
+}
+
+// The top levels of the hierarchy take node ids 0..K-1 in breadth-first
+// order (the range kernels stage in shared memory); every other node keeps
+// its depth-first order after them, so that a subtree stays contiguous.
+static void renumber_top(int n, std::vector<float4>& links, std::vector<int>& leaf_parent,
+                         std::vector<int>& node_parent) {
 #ifdef DRGB_NO_RENUMBER
   return;
 #endif
@@ -740,6 +789,130 @@ static void sah_topology(const float4* pos, const std::vector<int4>& tri_v, int 
   links.swap(nl);
   node_parent.swap(np);
   for (int k = 0; k < n; k++) leaf_parent[k] = new_id[leaf_parent[k]];
+}
+
+
+// Two-level build for instanced scenes: one SAH hierarchy per mesh over its
+// first instance's triangles, shared by every instance of the mesh, and an
+// SAH hierarchy over the instances (their boxes as traced, after the block
+// transform); each leaf of the top hierarchy is replaced by a copy of its
+// mesh's hierarchy with the instance's triangle and node offsets.  The
+// result is one binary hierarchy over world-space boxes and triangles with
+// the layout of the flat build (n - 1 internal nodes), so that the traversal
+// and its hit arithmetic do not change: only the build is per mesh, and the
+// top levels follow the instances.  Cost: one SAH build per mesh plus one
+// over the instances, against one over every instance's triangles.
+static void two_level_topology(const float4* pos, const float* block_tr, const std::vector<int4>& tri_v,
+                               const std::vector<BlockDev>& blocks, int n_vertices, int n,
+                               std::vector<float4>& links, std::vector<int>& perm, std::vector<int>& leaf_parent,
+                               std::vector<int>& node_parent) {
+  const int nb = (int)blocks.size();
+  auto tri_end = [&](int b) { return b + 1 < nb ? blocks[b + 1].tri_off : n; };
+  auto vert_end = [&](int b) { return b + 1 < nb ? blocks[b + 1].vert_off : n_vertices; };
+  // per-mesh hierarchies over local triangle ids (the mesh's index order)
+  struct Bottom {
+    std::vector<float4> links;
+    std::vector<int> perm, leaf_parent, node_parent;
+    bool built = false;
+  };
+  int n_meshes = 0;
+  for (const BlockDev& bd : blocks) n_meshes = std::max(n_meshes, bd.mesh + 1);
+  std::vector<Bottom> bottom((size_t)n_meshes);
+  std::vector<int> inst;  // blocks with triangles: the top hierarchy's items
+  std::vector<SahItem> items;
+  for (int b = 0; b < nb; b++) {
+    const int t0 = blocks[b].tri_off, nt = tri_end(b) - t0;
+    if (nt <= 0) continue;
+    inst.push_back(b);
+    Bottom& B = bottom[blocks[b].mesh];
+    if (B.built) continue;
+    tri_items(pos, block_tr, tri_v.data() + t0, nt, items);
+    sah_tree(items, B.links, B.perm, B.leaf_parent, B.node_parent);
+    B.built = true;
+  }
+  // the instances, boxed as traced
+  std::vector<SahItem> top(inst.size());
+  for (size_t i = 0; i < inst.size(); i++) {
+    const int b = inst[i];
+    SahItem& it = top[i];
+    for (int k = 0; k < 3; k++) {
+      it.lo[k] = 1e30f;
+      it.hi[k] = -1e30f;
+    }
+    for (int g = blocks[b].vert_off; g < vert_end(b); g++) {
+      float w[3];
+      traced_host(pos, block_tr, b, g, w);
+      for (int k = 0; k < 3; k++) {
+        it.lo[k] = std::min(it.lo[k], w[k]);
+        it.hi[k] = std::max(it.hi[k], w[k]);
+      }
+    }
+    for (int k = 0; k < 3; k++) it.c[k] = 0.5f * (it.lo[k] + it.hi[k]);
+  }
+  std::vector<float4> tl;
+  std::vector<int> tperm, tleaf_parent, tnode_parent;
+  sah_tree(top, tl, tperm, tleaf_parent, tnode_parent);
+  const int ni = (int)inst.size();
+  links.assign((size_t)std::max(n - 1, 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  perm.assign((size_t)n, 0);
+  leaf_parent.assign((size_t)n, -1);
+  node_parent.assign((size_t)std::max(n - 1, 1), -1);
+  auto get = [](const float4& l, int side) {
+    int c;
+    std::memcpy(&c, side ? &l.y : &l.x, sizeof(int));
+    return c;
+  };
+  auto set = [](float4& l, int side, int c) { std::memcpy(side ? &l.y : &l.x, &c, sizeof(int)); };
+  for (int i = 0; i < ni - 1; i++) {
+    links[i] = tl[i];
+    node_parent[i] = tnode_parent[i];
+  }
+  int next_node = std::max(ni - 1, 0), next_leaf = 0;
+  for (int slot = 0; slot < ni; slot++) {  // the top hierarchy's leaves, in build order
+    const int b = inst[tperm[slot]];
+    const Bottom& B = bottom[blocks[b].mesh];
+    const int t0 = blocks[b].tri_off, nt = tri_end(b) - t0;
+    const int node0 = next_node, leaf0 = next_leaf;
+    for (int i = 0; i < nt - 1; i++) {
+      float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      for (int side = 0; side < 2; side++) {
+        const int c = get(B.links[i], side);
+        set(l, side, c >= 0 ? c + node0 : ~(~c + leaf0));
+      }
+      links[node0 + i] = l;
+      node_parent[node0 + i] = B.node_parent[i] >= 0 ? B.node_parent[i] + node0 : -1;
+    }
+    for (int k = 0; k < nt; k++) {
+      perm[leaf0 + k] = t0 + B.perm[k];
+      leaf_parent[leaf0 + k] = nt > 1 ? B.leaf_parent[k] + node0 : -1;
+    }
+    next_node += nt - 1;
+    next_leaf += nt;
+    // hang the instance's root where the top hierarchy had its leaf
+    const int root = nt > 1 ? node0 : ~leaf0;
+    const int p = ni > 1 ? tleaf_parent[slot] : -1;
+    if (p >= 0) {
+      set(links[p], get(tl[p], 0) == ~slot ? 0 : 1, root);  // the side in the unmodified top hierarchy
+      if (nt > 1) node_parent[node0] = p;
+      else leaf_parent[leaf0] = p;
+    }
+  }
+  renumber_top(n, links, leaf_parent, node_parent);
+}
+
+// The host builders: 2 the two-level build, 3 one SAH hierarchy over every
+// triangle, 1 the two-level build when a mesh has several instances (one
+// instance per mesh: a single mesh gives the same hierarchy either way, and
+// meshes that overlap in space are better split by triangles).
+static void host_topology(int builder, const float4* pos, const float* block_tr, const std::vector<int4>& tri_v,
+                          const std::vector<BlockDev>& blocks, int n_vertices, int n, std::vector<float4>& links,
+                          std::vector<int>& perm, std::vector<int>& leaf_parent, std::vector<int>& node_parent) {
+  bool instanced = false;
+  for (const BlockDev& bd : blocks) instanced |= bd.inst > 0;
+  if (builder == 2 || (builder == 1 && instanced))
+    two_level_topology(pos, block_tr, tri_v, blocks, n_vertices, n, links, perm, leaf_parent, node_parent);
+  else
+    sah_topology(pos, block_tr, tri_v, n, links, perm, leaf_parent, node_parent);
 }
 
 // triangle -> leaf slot, for traversals seeded with a candidate triangle
@@ -792,13 +965,17 @@ static void build_topology(Job& J, cudaStream_t s) {
     return;
   }
   J.root = 0;
-  if (J.bvh_builder == 1) {
+  if (J.bvh_builder != 0) {
     std::vector<float4> pos((size_t)J.n_vertices);
+    std::vector<float> block_tr(32 * (size_t)J.n_blocks);
     DRGB_CUDA(cudaMemcpyAsync(pos.data(), J.pos.p, sizeof(float4) * pos.size(), cudaMemcpyDeviceToHost, s));
+    DRGB_CUDA(cudaMemcpyAsync(block_tr.data(), J.block_tr.p, sizeof(float) * block_tr.size(), cudaMemcpyDeviceToHost,
+                              s));
     DRGB_CUDA(cudaStreamSynchronize(s));
     std::vector<float4> links;
     std::vector<int> perm, leaf_parent, node_parent;
-    sah_topology(pos.data(), J.h_tri_v, n, links, perm, leaf_parent, node_parent);
+    host_topology(J.bvh_builder, pos.data(), block_tr.data(), J.h_tri_v, J.h_blocks, J.n_vertices, n, links, perm,
+                  leaf_parent, node_parent);
     std::vector<float4> nodes(4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (int i = 0; i < n - 1; i++) nodes[4 * (size_t)i + 3] = links[i];
     DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice, s));
@@ -807,7 +984,7 @@ static void build_topology(Job& J, cudaStream_t s) {
     DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, node_parent.data(), sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
     DRGB_CUDA(cudaStreamSynchronize(s));
     J.topo_tri_v = J.h_tri_v;
-    J.topo_builder = 1;
+    J.topo_builder = J.bvh_builder;
     return;
   }
   for (int b = 0; b < 2; b++) {

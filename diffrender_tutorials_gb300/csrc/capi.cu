@@ -101,7 +101,8 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
       }
       case DRGB_OPT_USE_GRAPH: r->use_graph = value ? 1 : 0; break;
       case DRGB_OPT_BVH_BUILDER:
-        require(value == 0 || value == 1, "hierarchy builder: 0 (LBVH) or 1 (binned SAH)");
+        require(value >= 0 && value <= 3,
+                "hierarchy builder: 0 (LBVH), 1 (binned SAH, two-level when instanced), 2 (two-level), 3 (flat SAH)");
         r->job.bvh_builder = (int)value;  // used from the next commit on
         break;
       case DRGB_OPT_BVH_REBUILD:

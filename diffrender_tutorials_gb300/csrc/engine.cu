@@ -425,7 +425,7 @@ void sync_dev(Job& J) {
   d.leaf_of = J.leaf_of.p;
   // the binned-SAH topology numbers its top levels first (breadth first)
 #ifdef DRGB_TOP_SMEM
-  d.top_n = J.topo_builder == 1 ? std::min(std::max(J.n_tris - 1, 0), kTopNodes) : 0;
+  d.top_n = J.topo_builder >= 1 ? std::min(std::max(J.n_tris - 1, 0), kTopNodes) : 0;
 #else
   d.top_n = 0;
 #endif

@@ -99,7 +99,9 @@ struct HostBuf {
 struct TopoRebuild {
   int stage = 0;  // 0 idle, 1 positions in flight, 2 topology being built
   cudaEvent_t ev = nullptr;
+  int builder = 1;  // the host builder in use
   HostBuf<float4> pos, nodes;
+  HostBuf<float> block_tr;
   HostBuf<int> perm, leaf_parent, node_parent;
   std::future<void> task;
   ~TopoRebuild() {

@@ -69,8 +69,11 @@ enum {
   DRGB_OPT_PIXEL_GRID = 7,       /* blocks per SM of the persistent pixel kernel (default 8) */
   DRGB_OPT_EDGE_GRID = 8,        /* blocks per SM of the persistent edge-shading kernel (default 8) */
   DRGB_OPT_BVH_BUILDER = 9,      /* hierarchy topology from the next commit on: 0 LBVH from Morton codes on
-                                    the device, 1 (default) binned SAH on the host; boxes are refitted on the
-                                    device either way, and a commit of the same triangles keeps the topology */
+                                    the device; binned SAH on the host: 1 (default) two-level when a mesh has
+                                    several instances, else one hierarchy; 2 always two-level (one hierarchy
+                                    per mesh, shared by its instances, under one over the instances); 3 always
+                                    one hierarchy over every triangle.  Boxes are refitted on the device
+                                    either way, and a commit of the same triangles keeps the topology */
   DRGB_OPT_BVH_REBUILD = 10      /* optimiser (and batch, for every job): rebuild the hierarchy topology from
                                     the current vertices every N iterations (default 100; 0: refit only).
                                     Refitted boxes of moving vertices overlap more and more (icosphere
