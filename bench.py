@@ -664,6 +664,27 @@ def stress_arm(args, ws, rank, local, pg):
                           "phases_ms": opt.profile(2), "clocks": clk.summary(),
                           "hit_buffer_bytes_per_iter": (2 * 16 * n_samples) if hits else 0}
         del opt, ro
+    # a long run: 200 iterations with the default hierarchy rebuild every 100
+    # (host SAH of 200k triangles, overlapped with the next 50 iterations)
+    # against refits only
+    long_run = {}
+    for period in (0, 100):
+        ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
+        ro.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
+        ro.set_option(N.OPT_BVH_REBUILD, period)
+        opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, ro, cams, tgt, p)
+        stream = torch.cuda.ExternalStream(ro.stream(), device=local)
+        opt.run_async(args.warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            opt.run_async(200)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        long_run["rebuild_every_100" if period else "refit_only"] = 200 / (e0.elapsed_time(e1) / 1e3)
+        del opt, ro
     # gradient at the initial mesh and the finite-difference check
     r.commit(isc)
     ds = D.DScene(r, [0])
@@ -692,6 +713,7 @@ def stress_arm(args, ws, rank, local, pg):
                    "l2": "inputs larger than L2 (scene + LBVH ~40 MB, image buffers ~50 MB, edge queue 16 MB)",
                    "parallelism": "replicas"},
         "adjoint": results,
+        "long_run_200_iters_per_s": long_run,
         "fd_check": {"h": 1e-3, "random_coords": fd_random, "silhouette_coords": fd_sil,
                      "note": "the method's position gradient is the edge (visibility) term only; the path "
                              "model's smooth dependence of shading on positions is not differentiated, as in "

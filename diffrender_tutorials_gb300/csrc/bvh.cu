@@ -496,6 +496,62 @@ static void host_topology(int builder, const float4* pos, const float* block_tr,
                           const std::vector<BlockDev>& blocks, int n_vertices, int n, std::vector<float4>& links,
                           std::vector<int>& perm, std::vector<int>& leaf_parent, std::vector<int>& node_parent);
 
+// The pieces of an overlapped rebuild: the current vertices copied out
+// behind the enqueued work, the topology built on a host thread into pinned
+// buffers, and copied in (and refitted) in stream order.
+static void topo_copy_out(Job& J, TopoRebuild& T, cudaStream_t s) {
+  if (!T.ev) DRGB_CUDA(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
+  T.pos.reserve((size_t)J.n_vertices);
+  DRGB_CUDA(cudaMemcpyAsync(T.pos.p, J.pos.p, sizeof(float4) * J.n_vertices, cudaMemcpyDeviceToHost, s));
+  T.block_tr.reserve(32 * (size_t)J.n_blocks);
+  DRGB_CUDA(cudaMemcpyAsync(T.block_tr.p, J.block_tr.p, sizeof(float) * 32 * J.n_blocks, cudaMemcpyDeviceToHost, s));
+  T.builder = J.bvh_builder;
+  DRGB_CUDA(cudaEventRecord(T.ev, s));
+  const int n = J.n_tris;
+  T.nodes.reserve(4 * (size_t)(n - 1));
+  T.perm.reserve(n);
+  T.leaf_parent.reserve(n);
+  T.node_parent.reserve(n - 1);
+}
+
+// wait_copy: the thread first waits for the copy-out (its device is `dev`).
+static void topo_start_build(Job& J, TopoRebuild& T, bool wait_copy) {
+  TopoRebuild* t = &T;
+  const std::vector<int4>* tri_v = &J.h_tri_v;
+  const std::vector<BlockDev>* blocks = &J.h_blocks;
+  const int nv = J.n_vertices, n = J.n_tris;
+  int dev = 0;
+  DRGB_CUDA(cudaGetDevice(&dev));
+  T.task = std::async(std::launch::async, [t, tri_v, blocks, nv, n, wait_copy, dev] {
+    if (wait_copy) {
+      DRGB_CUDA(cudaSetDevice(dev));
+      DRGB_CUDA(cudaEventSynchronize(t->ev));
+    }
+    std::vector<float4> links;
+    std::vector<int> perm, leaf_parent, node_parent;
+    host_topology(t->builder, t->pos.p, t->block_tr.p, *tri_v, *blocks, nv, n, links, perm, leaf_parent,
+                  node_parent);
+    std::fill(t->nodes.p, t->nodes.p + 4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (int i = 0; i < n - 1; i++) t->nodes.p[4 * (size_t)i + 3] = links[i];
+    std::memcpy(t->perm.p, perm.data(), sizeof(int) * n);
+    std::memcpy(t->leaf_parent.p, leaf_parent.data(), sizeof(int) * n);
+    std::memcpy(t->node_parent.p, node_parent.data(), sizeof(int) * (n - 1));
+  });
+}
+
+static void topo_copy_in(Job& J, TopoRebuild& T, cudaStream_t s) {
+  T.task.get();
+  const int n = J.n_tris;
+  DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, T.nodes.p, sizeof(float4) * 4 * (n - 1), cudaMemcpyHostToDevice, s));
+  DRGB_CUDA(cudaMemcpyAsync(J.perm.p, T.perm.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  DRGB_CUDA(cudaMemcpyAsync(J.leaf_parent.p, T.leaf_parent.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, T.node_parent.p, sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
+  refit_bvh(J, s);
+  J.topo_tri_v = J.h_tri_v;
+  J.topo_builder = T.builder;
+  T.stage = 0;
+}
+
 void rebuild_bvh_begin(Job& J, cudaStream_t s) {
   const int n = J.n_tris;
   if (J.bvh_builder == 0 || n <= 1) {  // a device build blocks nothing
@@ -505,13 +561,7 @@ void rebuild_bvh_begin(Job& J, cudaStream_t s) {
   if (!J.topo_async) J.topo_async.reset(new TopoRebuild());
   TopoRebuild& T = *J.topo_async;
   if (T.stage != 0) return;  // the previous one is still on its way
-  if (!T.ev) DRGB_CUDA(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
-  T.pos.reserve((size_t)J.n_vertices);
-  DRGB_CUDA(cudaMemcpyAsync(T.pos.p, J.pos.p, sizeof(float4) * J.n_vertices, cudaMemcpyDeviceToHost, s));
-  T.block_tr.reserve(32 * (size_t)J.n_blocks);
-  DRGB_CUDA(cudaMemcpyAsync(T.block_tr.p, J.block_tr.p, sizeof(float) * 32 * J.n_blocks, cudaMemcpyDeviceToHost, s));
-  T.builder = J.bvh_builder;
-  DRGB_CUDA(cudaEventRecord(T.ev, s));
+  topo_copy_out(J, T, s);
   T.stage = 1;
 }
 
@@ -522,41 +572,47 @@ void rebuild_bvh_poll(Job& J, cudaStream_t s) {
     const cudaError_t q = cudaEventQuery(T.ev);
     if (q == cudaErrorNotReady) return;
     DRGB_CUDA(q);
-    const int n = J.n_tris;
-    T.nodes.reserve(4 * (size_t)(n - 1));
-    T.perm.reserve(n);
-    T.leaf_parent.reserve(n);
-    T.node_parent.reserve(n - 1);
-    TopoRebuild* t = &T;
-    const std::vector<int4>* tri_v = &J.h_tri_v;
-    const std::vector<BlockDev>* blocks = &J.h_blocks;
-    const int nv = J.n_vertices;
-    T.task = std::async(std::launch::async, [t, tri_v, blocks, nv, n] {
-      std::vector<float4> links;
-      std::vector<int> perm, leaf_parent, node_parent;
-      host_topology(t->builder, t->pos.p, t->block_tr.p, *tri_v, *blocks, nv, n, links, perm, leaf_parent,
-                    node_parent);
-      std::fill(t->nodes.p, t->nodes.p + 4 * (size_t)(n - 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-      for (int i = 0; i < n - 1; i++) t->nodes.p[4 * (size_t)i + 3] = links[i];
-      std::memcpy(t->perm.p, perm.data(), sizeof(int) * n);
-      std::memcpy(t->leaf_parent.p, leaf_parent.data(), sizeof(int) * n);
-      std::memcpy(t->node_parent.p, node_parent.data(), sizeof(int) * (n - 1));
-    });
+    topo_start_build(J, T, false);
     T.stage = 2;
     return;
   }
-  if (T.stage == 2 && T.task.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
-    T.task.get();
-    const int n = J.n_tris;
-    DRGB_CUDA(cudaMemcpyAsync(J.nodes.p, T.nodes.p, sizeof(float4) * 4 * (n - 1), cudaMemcpyHostToDevice, s));
-    DRGB_CUDA(cudaMemcpyAsync(J.perm.p, T.perm.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    DRGB_CUDA(cudaMemcpyAsync(J.leaf_parent.p, T.leaf_parent.p, sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    DRGB_CUDA(cudaMemcpyAsync(J.node_parent.p, T.node_parent.p, sizeof(int) * (n - 1), cudaMemcpyHostToDevice, s));
-    refit_bvh(J, s);
-    J.topo_tri_v = J.h_tri_v;
-    J.topo_builder = T.builder;
-    T.stage = 0;
+  if (T.stage == 2 && T.task.wait_for(std::chrono::seconds(0)) == std::future_status::ready) topo_copy_in(J, T, s);
+}
+
+// The optimiser's rebuild, overlapped but deterministic: started after one
+// iteration (the vertices of that iteration) and applied after a fixed later
+// one, waiting there if the host build has not finished, so that the
+// topology each iteration uses does not depend on timing.
+void rebuild_bvh_start(Job& J, cudaStream_t s) {
+  const int n = J.n_tris;
+  if (J.bvh_builder == 0 || n <= 1) {  // a device build blocks nothing
+    rebuild_bvh(J, s);
+    return;
   }
+  if (!J.topo_async) J.topo_async.reset(new TopoRebuild());
+  TopoRebuild& T = *J.topo_async;
+  if (T.stage == 3) topo_copy_in(J, T, s);  // the previous one first
+  rebuild_bvh_discard(J);
+  topo_copy_out(J, T, s);
+  topo_start_build(J, T, true);
+  T.stage = 3;
+}
+
+void rebuild_bvh_apply(Job& J, cudaStream_t s) {
+  if (J.topo_async && J.topo_async->stage == 3) topo_copy_in(J, *J.topo_async, s);
+}
+
+void rebuild_bvh_discard(Job& J) {
+  if (!J.topo_async) return;
+  TopoRebuild& T = *J.topo_async;
+  if (T.task.valid()) {
+    try {
+      T.task.get();
+    } catch (...) {  // the build is dropped, its error with it
+    }
+  }
+  if (T.stage == 1 && T.ev) cudaEventSynchronize(T.ev);  // the copy-out still writes the pinned buffers
+  T.stage = 0;
 }
 
 void refit_bvh(Job& J, cudaStream_t s) {

@@ -435,17 +435,27 @@ int drgb_optimizer_run_async(drgb_renderer* r, int64_t n_iters) {
       O.losses = std::move(nb);
       r->graph_valid = false;
     }
-    // iterations up to the next hierarchy rebuild, then the rebuild (host
-    // SAH build from the current vertices; the device pointers stay the same,
-    // so the captured graph stays valid)
-    const int64_t period = r->bvh_rebuild;
+    // Hierarchy rebuilds: after every `period` iterations a host SAH build
+    // from the current vertices starts on a host thread, behind the enqueued
+    // iterations; `period / 2` iterations later its topology is copied in
+    // (waiting for the build if needed).  The device pointers stay the same,
+    // so the captured graph stays valid, and the iteration at which a
+    // topology takes over depends only on the iteration count, not on timing.
+    const int64_t period = r->bvh_rebuild, lag = period / 2;
     while (n_iters > 0) {
       int64_t n = n_iters;
-      if (period > 0) n = std::min<int64_t>(n, period - O.host_iter % period);
+      if (period > 0) {
+        const int64_t ph = O.host_iter % period;
+        n = std::min<int64_t>(n, ph < lag ? lag - ph : period - ph);
+      }
       enqueue_opt_iterations(r, n);
       O.host_iter += n;
       n_iters -= n;
-      if (period > 0 && O.host_iter % period == 0) rebuild_bvh(J, r->stream);
+      if (period > 0) {
+        const int64_t ph = O.host_iter % period;
+        if (ph == 0) rebuild_bvh_start(J, r->stream);
+        if (ph == lag) rebuild_bvh_apply(J, r->stream);
+      }
     }
   });
 }

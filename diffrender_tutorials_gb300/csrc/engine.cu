@@ -125,6 +125,7 @@ static void hammersley(int n, float* out) {
 void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   if (!scene || scene->n_meshes < 0 || (scene->n_meshes > 0 && !scene->meshes))
     throw CudaError("scene descriptor is null or malformed", DRGB_ERR_INVALID);
+  rebuild_bvh_discard(J);  // a host build in progress reads the triangle lists replaced here
   const int nm = scene->n_meshes;
   J.meshes.clear();
   J.meshes.resize(nm);

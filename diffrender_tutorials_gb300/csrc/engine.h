@@ -97,7 +97,7 @@ struct HostBuf {
 // thread builds the SAH topology, and the new topology is copied in and
 // refitted in stream order a few steps later.
 struct TopoRebuild {
-  int stage = 0;  // 0 idle, 1 positions in flight, 2 topology being built
+  int stage = 0;  // 0 idle, 1 positions in flight, 2 topology being built, 3 an optimiser rebuild in progress
   cudaEvent_t ev = nullptr;
   int builder = 1;  // the host builder in use
   HostBuf<float4> pos, nodes;
@@ -246,6 +246,9 @@ void commit_scene(Job& J, cudaStream_t s);             // flatten + LBVH build +
 void rebuild_bvh(Job& J, cudaStream_t s);              // new topology from the current vertices + refit
 void rebuild_bvh_begin(Job& J, cudaStream_t s);        // the same, overlapped with later steps...
 void rebuild_bvh_poll(Job& J, cudaStream_t s);         // ...advanced between steps, never blocking
+void rebuild_bvh_start(Job& J, cudaStream_t s);        // optimiser: built from this iteration's vertices...
+void rebuild_bvh_apply(Job& J, cudaStream_t s);        // ...and used from a fixed later iteration on
+void rebuild_bvh_discard(Job& J);                      // drop a rebuild in progress (waits for its thread)
 void build_bvh(Job& J, cudaStream_t s);                // topology (Morton, sort, Karras)
 void refit_bvh(Job& J, cudaStream_t s);
 void setup_views(Job& J, const drgb_camera* cams, int n_views);

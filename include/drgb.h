@@ -76,6 +76,9 @@ enum {
                                     either way, and a commit of the same triangles keeps the topology */
   DRGB_OPT_BVH_REBUILD = 10      /* optimiser (and batch, for every job): rebuild the hierarchy topology from
                                     the current vertices every N iterations (default 100; 0: refit only).
+                                    The host build overlaps the following iterations; the optimiser uses the
+                                    new topology from N/2 iterations after the start on (fixed, not timing
+                                    dependent), a batch from the first step after the build completes.
                                     Refitted boxes of moving vertices overlap more and more (icosphere
                                     workload: 55 box tests per ray after 500 steps against 47 with
                                     rebuilds); the hit set does not depend on the topology. */

@@ -167,6 +167,35 @@ def test_hierarchy_rebuilds_leave_the_trajectory_unchanged():
         assert diff.max() <= 2.5 * lr, (k, float(diff.max()))
 
 
+def test_optimizer_rebuild_schedule_does_not_depend_on_run_calls():
+    """The optimiser's overlapped rebuild starts after every `period`
+    iterations and its topology takes over `period / 2` iterations later,
+    whatever the host's timing: one Run(10) and the same iterations in four
+    calls (run_async included) give the same bits, and so does a period of
+    1 (built and used at once)."""
+    name, mode, spp, ts, isc, cams = problems()[0]
+    st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+    r0 = D.MakeDifferentialRenderer(st)
+    r0.commit(ts)
+    tgt = r0.render(ts, cams)
+    out = {}
+    for period, chunks in ((4, (10,)), (4, (1, 3, 2, 4)), (1, (10,)), (1, (3, 7))):
+        r = D.MakeDifferentialRenderer(st)
+        r.set_option(N.OPT_DETERMINISTIC, 1)
+        r.set_option(N.OPT_BVH_REBUILD, period)
+        opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, r, cams, tgt, opt_params(mode))
+        for k, c in enumerate(chunks):
+            if k == 1:
+                opt.run_async(c)   # enqueued only; the next call continues behind it
+            else:
+                opt.Run(c)
+        out[(period, chunks)] = opt.current_scene().meshes[0].vertices
+    for period in (4, 1):
+        a, b = [v for (p, _), v in out.items() if p == period]
+        assert np.array_equal(a, b), period
+
+
 def test_overlapped_rebuilds_with_jobs_leaving_mid_pipeline():
     """Rebuild every step in a batch (the overlapped pipeline is always in
     flight) while jobs are removed and added between steps: the remaining
