@@ -169,11 +169,15 @@ __device__ __forceinline__ void queue_append(int4* queue, int* count, int cap, b
 
 // Shading and chain rule of queue entries [q0, q0+32) (one per lane).  DET:
 // the deterministic-mode variant (records for jobs that have record buffers).
-template <bool DET>
+// PAIRS: two lanes per entry, the even one shading the inside point and the
+// odd one the outside point in the same traversal call (16 entries per
+// warp); else one lane per entry shades both points in turn.
+template <bool DET, bool PAIRS = false>
 __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* queue, int n, int q0,
                                                 const int* order = nullptr) {
   const int lane = threadIdx.x & 31;
-  const int q = q0 + lane;
+  const int side = PAIRS ? (lane & 1) : 0;
+  const int q = PAIRS ? q0 + (lane >> 1) : q0 + lane;
   float tr[12];
 #pragma unroll
   for (int k = 0; k < 12; k++) tr[k] = 0.0f;
@@ -199,12 +203,22 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
     const float coutx = px + 1e-3f * nx, couty = py + 1e-3f * ny;
     const uint32_t key_in = 0xA511E9B3u ^ ((uint32_t)(i * 2u) * 2654435761u);
     const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
-    const f3 color_in = shade_generic(J, cam, cinx, ciny, key_in);
-    const f3 color_out = shade_generic(J, cam, coutx, couty, key_out);
+    f3 color_in, color_out;
+    if (PAIRS) {
+      const f3 mine = shade_generic(J, cam, side ? coutx : cinx, side ? couty : ciny, side ? key_out : key_in);
+      const unsigned pair = 3u << (lane & ~1);  // both lanes of an entry take this branch
+      const f3 other = mk(__shfl_xor_sync(pair, mine.x, 1), __shfl_xor_sync(pair, mine.y, 1),
+                          __shfl_xor_sync(pair, mine.z, 1));
+      color_in = side ? other : mine;
+      color_out = side ? mine : other;
+    } else {
+      color_in = shade_generic(J, cam, cinx, ciny, key_in);
+      color_out = shade_generic(J, cam, coutx, couty, key_out);
+    }
     const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
     const float weight = 1.0f / (pdf * (float)J.edge_samples);
     const float adjv = dot(color_in - color_out, mk(ad.x, ad.y, ad.z));
-    if (adjv * adjv > 0.0f) {
+    if (side == 0 && adjv * adjv > 0.0f) {  // (PAIRS: the even lane applies the chain rule)
       const float d0x = (1 - t) * nx * adjv * weight, d0y = (1 - t) * ny * adjv * weight;
       const float d1x = t * nx * adjv * weight, d1y = t * ny * adjv * weight;
       const f3 v0 = ld3(J.pos, ed.x), v1 = ld3(J.pos, ed.y);
@@ -328,22 +342,23 @@ __global__ void k_edge_select(const JobDev* jobs, int job) {
 // the queue count), so warps that drew cheap samples take more and the launch
 // ends without a tail of idle SMs; -DDRGB_EDGE_STATIC strides statically.
 // `order` (may be null) is the shading order of the entries.
-template <bool DET>
+template <bool DET, bool PAIRS = false>
 __device__ __forceinline__ void edge_shade_loop(const JobDev* jobs, const int4* queue, int n, int* work,
                                                 const int* order) {
+  constexpr int kPerWarp = PAIRS ? 16 : 32;
 #ifdef DRGB_EDGE_STATIC
   (void)work;
-  const int stride = gridDim.x * blockDim.x;
-  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; q0 < n; q0 += stride)
-    edge_shade_warp<DET>(jobs, queue, n, q0, order);
+  const int stride = gridDim.x * blockDim.x / 32 * kPerWarp;
+  for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * kPerWarp; q0 < n; q0 += stride)
+    edge_shade_warp<DET, PAIRS>(jobs, queue, n, q0, order);
 #else
   const int lane = threadIdx.x & 31;
   while (true) {
     int q0 = 0;
-    if (lane == 0) q0 = atomicAdd(work, 32);
+    if (lane == 0) q0 = atomicAdd(work, kPerWarp);
     q0 = __shfl_sync(0xffffffffu, q0, 0);
     if (q0 >= n) break;
-    edge_shade_warp<DET>(jobs, queue, n, q0, order);
+    edge_shade_warp<DET, PAIRS>(jobs, queue, n, q0, order);
   }
 #endif
 }
@@ -370,12 +385,30 @@ __global__ void k_b_queue_keys(const JobDev* jobs, const int4* queue, const int*
 
 // Single job: the queue, its counter and its capacity are the job's own;
 // `order` (may be null) is the shading order of the queue entries.
-template <bool DET>
+template <bool DET, bool PAIRS>
 __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(const JobDev* jobs, int job,
                                                                               const int* order) {
   const JobDev& J = jobs[job];
   stage_top_nodes(J);
-  edge_shade_loop<DET>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
+  edge_shade_loop<DET, PAIRS>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
+}
+
+// Lane pairs for the path model, whose two points cost alike but vary a lot
+// from sample to sample (GB300, 200k-triangle stress workload: edge pass
+// 4.34 -> 4.03 ms); one lane per entry for the others, where the inside point
+// of a silhouette sample hits and casts a shadow ray and the outside point
+// misses (point-light icosphere: 1.50 ms against 2.10 ms with pairs).
+static void launch_shade_job(const JobDev* d_jobs, int job, int mode, int grid, const int* order, bool det,
+                             cudaStream_t s) {
+  grid = std::max(1, grid);
+  const bool pairs = mode == PATH_DIFFUSE;
+  if (det) {
+    if (pairs) k_edge_shade_job<true, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
+    else k_edge_shade_job<true, false><<<grid, 256, 0, s>>>(d_jobs, job, order);
+  } else {
+    if (pairs) k_edge_shade_job<false, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
+    else k_edge_shade_job<false, false><<<grid, 256, 0, s>>>(d_jobs, job, order);
+  }
 }
 
 // Sort keys of the queue entries: (view, edge), so that neighbouring lanes
@@ -455,18 +488,17 @@ void launch_edges_prep(const JobDev* d_jobs, int job, int n_edges, int n_views, 
 
 // The rest, which reads the adjoint image: selection, ordering, shading.
 void launch_edges_rest(const JobDev* d_jobs, int job, int n_edges, int n_views, int edge_samples, int* queue_count,
-                       int shade_grid, cudaStream_t s, bool det, const Job* Jq) {
+                       int shade_grid, cudaStream_t s, bool det, const Job* Jq, int mode) {
   if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
   DRGB_CUDA(cudaMemsetAsync(queue_count, 0, 2 * sizeof(int), s));  // queue count, shading counter
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   const int* order = Jq ? sort_queue(d_jobs, job, *Jq, shade_grid, s) : nullptr;
-  if (det) k_edge_shade_job<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
-  else k_edge_shade_job<false><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
+  launch_shade_job(d_jobs, job, mode, shade_grid, order, det, s);
   count_launch(2);
 }
 
 void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
-                      int* queue_count, int shade_grid, cudaStream_t s, bool det, const Job* Jq) {
+                      int* queue_count, int shade_grid, cudaStream_t s, bool det, const Job* Jq, int mode) {
   if (n_edges <= 0 || n_views <= 0 || edge_samples <= 0) return;
   k_edge_project<<<dim3((n_vertices + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   k_edge_pmf<<<dim3((n_edges + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
@@ -475,15 +507,14 @@ void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, i
   k_edge_select<<<dim3((edge_samples + 255) / 256, n_views), 256, 0, s>>>(d_jobs, job);
   // the queue, its counter and capacity are read from the job on the device
   const int* order = Jq ? sort_queue(d_jobs, job, *Jq, shade_grid, s) : nullptr;
-  if (det) k_edge_shade_job<true><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
-  else k_edge_shade_job<false><<<std::max(1, shade_grid), 256, 0, s>>>(d_jobs, job, order);
+  launch_shade_job(d_jobs, job, mode, shade_grid, order, det, s);
   count_launch(5);
 }
 
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s) {
   if (J.n_edges <= 0 || J.n_views <= 0) return;
   launch_edges_raw(d_jobs, job, J.n_edges, J.n_views, J.n_vertices, J.dev.edge_samples, J.queue_count.p, shade_grid,
-                   s, J.det != 0, &J);
+                   s, J.det != 0, &J, J.mode);
 }
 
 // Edge pass of every job of a batch; the shared queue holds (view, sample,

@@ -286,7 +286,7 @@ void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, in
 void launch_edges(const JobDev* d_jobs, int job, const Job& J, int shade_grid, cudaStream_t s);
 void launch_edges_prep(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, cudaStream_t s);
 void launch_edges_rest(const JobDev* d_jobs, int job, int n_edges, int n_views, int edge_samples, int* queue_count,
-                       int shade_grid, cudaStream_t s, bool det, const Job* Jq);
+                       int shade_grid, cudaStream_t s, bool det, const Job* Jq, int mode);
 // Blocks of the (atomic-scatter) pixel kernel of a model that one SM holds
 // at a time (its register budget).
 int pixel_blocks_resident(int mode);

@@ -33,7 +33,7 @@
 namespace drgb {
 
 void launch_edges_raw(const JobDev* d_jobs, int job, int n_edges, int n_views, int n_vertices, int edge_samples,
-                      int* queue_count, int shade_grid, cudaStream_t s, bool det, const Job* Jq);
+                      int* queue_count, int shade_grid, cudaStream_t s, bool det, const Job* Jq, int mode);
 
 constexpr size_t kScratchBytes = 32u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -295,7 +295,8 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
                   r->px_grid(), s, J.mode);
     launch_loss_finalize(d_job, 1, s);
     if (edge_samples > 0)
-      launch_edges_raw(d_job, 0, E, n_views, J.n_vertices, edge_samples, counters, r->edge_grid(), s, false, nullptr);
+      launch_edges_raw(d_job, 0, E, n_views, J.n_vertices, edge_samples, counters, r->edge_grid(), s, false, nullptr,
+                       J.mode);
     uint32_t f = 0;
     DRGB_CUDA(cudaMemcpyAsync(&f, J.err.p, sizeof(f), cudaMemcpyDeviceToHost, s));
     DRGB_CUDA(cudaStreamSynchronize(s));

@@ -257,7 +257,7 @@ struct drgb_renderer {
       launch_loss_finalize(d_job.p, 1, stream);
       DRGB_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
       launch_edges_rest(d_job.p, 0, J.n_edges, J.n_views, J.dev.edge_samples, J.queue_count.p, edge_grid(), stream,
-                        false, &J);
+                        false, &J, J.mode);
     } else {
       pixel_pass(flags);
       launch_loss_finalize(d_job.p, 1, stream);

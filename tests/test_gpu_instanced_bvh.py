@@ -137,3 +137,43 @@ def test_two_level_rebuilds_of_moving_instances():
     cam = D.CamInfo(origin=(0.4, 0.5, 3.0), width=512, height=512)
     xy = np.random.default_rng(6).uniform(0, 512, size=(300000, 2)).astype(np.float32)
     assert_hits_match(r.cast_rays(cam, xy), bf.cast_rays(cam, xy))
+
+
+@pytest.mark.parametrize("builder", [0, 1, 2, 3])
+def test_degenerate_instancing_equals_bruteforce(builder):
+    """A one-triangle mesh with 7 instances (the top hierarchy's leaves are
+    single triangles), a mesh with vertices but no triangles, 3 instances,
+    and a two-triangle quad; hits against the brute-force caster, and a
+    gradient through the edge pass."""
+    rng = np.random.default_rng(11)
+    sc = D.Scene()
+    tri = D.TriangleMesh(np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], np.float32), np.array([0, 1, 2], np.uint32),
+                         colors=np.eye(3, dtype=np.float32))
+    trs = []
+    for k in range(7):
+        m = np.eye(4, dtype=np.float32)
+        m[:3, :3] = 0.3 * rot(*rng.uniform(0, 2 * math.pi, 3))
+        m[:3, 3] = rng.uniform(-0.5, 0.5, 3)
+        trs.append(m)
+    sc.add_mesh(tri, trs)
+    empty = D.TriangleMesh(np.zeros((3, 3), np.float32), np.zeros(0, np.uint32), colors=np.ones((3, 3), np.float32))
+    sc.add_mesh(empty, [np.eye(4, dtype=np.float32)] * 3)
+    quad = D.TriangleMesh(np.array([[-2, -2, -1], [2, -2, -1], [2, 2, -1], [-2, 2, -1]], np.float32),
+                          np.array([0, 1, 2, 0, 2, 3], np.uint32), colors=rng.uniform(0, 1, (4, 3)).astype(np.float32))
+    sc.add_mesh(quad)
+    cam = D.CamInfo(origin=(0.2, 0.1, 3.0), width=256, height=256)
+    xy = np.random.default_rng(12).uniform(0, 256, size=(100000, 2)).astype(np.float32)
+    a, b = renderer(2, 1, builder), renderer(2, 1, bruteforce=True)
+    a.commit(sc)
+    b.commit(sc)
+    ha, hb = a.cast_rays(cam, xy), b.cast_rays(cam, xy)
+    assert (hb["geom"][hb["prim"] != 0xFFFFFFFF] == 0).mean() > 0.005   # the small triangles are hit
+    same = np.ones(xy.shape[0], bool)
+    for k in ("prim", "inst", "geom", "t", "u", "v"):
+        same &= ha[k] == hb[k]
+    assert (~same).sum() <= 1e-3 * xy.shape[0]
+    cams = [cam]
+    adj = np.random.default_rng(13).normal(0, 0.5, 256 * 256 * 3).astype(np.float32)
+    ds = D.DScene(a, [0, 2])
+    a.d_render(sc, cams, adj, 256 * 256, ds)
+    assert np.isfinite(ds.data).all() and np.abs(ds.data).max() > 0
