@@ -196,6 +196,33 @@ def test_optimizer_rebuild_schedule_does_not_depend_on_run_calls():
         assert np.array_equal(a, b), period
 
 
+def test_optimizer_reinit_while_a_rebuild_is_in_flight():
+    """Run(5) with a rebuild every 4 iterations leaves one in flight (started
+    after iteration 4, due after 6); a new Init on the same renderer drops it
+    (waiting for its host thread) and then runs exactly as a fresh
+    optimiser does."""
+    name, mode, spp, ts, isc, cams = problems()[0]
+    st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+    r0 = D.MakeDifferentialRenderer(st)
+    r0.commit(ts)
+    tgt = r0.render(ts, cams)
+    out = []
+    for reuse in (True, False):
+        r = D.MakeDifferentialRenderer(st)
+        r.set_option(N.OPT_DETERMINISTIC, 1)
+        r.set_option(N.OPT_BVH_REBUILD, 4)
+        opt = D.CreateSimpleOptimizer()
+        if reuse:
+            opt.Init(isc, r, cams, tgt, opt_params(mode))
+            opt.Run(5)
+            opt = D.CreateSimpleOptimizer()
+        opt.Init(isc, r, cams, tgt, opt_params(mode))
+        opt.Run(7)
+        out.append((np.array(opt.losses), opt.current_scene().meshes[0].vertices))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_overlapped_rebuilds_with_jobs_leaving_mid_pipeline():
     """Rebuild every step in a batch (the overlapped pipeline is always in
     flight) while jobs are removed and added between steps: the remaining
