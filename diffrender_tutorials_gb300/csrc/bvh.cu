@@ -1,4 +1,4 @@
-// Scene flattening and the device-built LBVH.
+// Scene flattening and the hierarchy over the flattened triangles.
 //
 // prepare_scene() is the device counterpart of Scene::prepare_for_render
 // (common_src/scene_utils.cpp:98-173): it applies each instance transform to
@@ -9,12 +9,18 @@
 // exact.  Each triangle is stored as (A, B-A, C-A): the same differences the
 // caster forms, so the intersection arithmetic is unchanged.
 //
-// build_bvh() builds a linear BVH (Karras 2012: Morton codes of triangle
-// centroids, LSD radix sort, binary radix tree).  Only the topology is built
-// here; refit_bvh() recomputes every box bottom-up and is run after each
-// parameter update, since vertex positions move but the mesh topology does
-// not.  Boxes are padded so that the traversal never culls a triangle the
-// brute-force test would accept.
+// build_bvh() builds the topology of a binary hierarchy, one triangle per
+// leaf, with one of three builders: a binned SAH on the host over every
+// triangle; the two-level build for instanced scenes (one SAH per mesh,
+// shared by its instances, under one over the instances, the shape of the
+// reference's Embree scene, raytrace_src/raytrace3d_embree.cpp:35-50); or a
+// linear BVH on the device (Karras 2012: Morton codes of triangle centroids,
+// LSD radix sort, binary radix tree).  refit_bvh() recomputes every box
+// bottom-up and runs after each parameter update, since vertex positions
+// move but the triangles do not; the rebuild_bvh_* functions renew the
+// topology from moved vertices, overlapped with later work.  Boxes are
+// padded so that the traversal never culls a triangle the brute-force test
+// would accept.
 #include <algorithm>
 #include <chrono>
 #include <climits>
