@@ -380,7 +380,11 @@ def batch_arm(args, ws, rank, local, pg):
     from diffrender_tutorials_gb300 import workloads as WL
     B.build()
     torch.cuda.set_device(local)
-    specs = WL.batch_jobs(args.jobs, seed=0)
+    if args.batch_mix == "small":  # jobs too small to fill the GPU alone
+        specs = WL.batch_jobs(args.jobs, seed=0, tri_range=(200, 3_000), resolutions=(64, 96, 128), spps=(4, 8),
+                              views=(1, 2))
+    else:
+        specs = WL.batch_jobs(args.jobs, seed=0)
     setups = []
     for sp in specs:
         ts, isc = D.Scene(), D.Scene()
@@ -453,7 +457,8 @@ def batch_arm(args, ws, rank, local, pg):
         "metric": "batched fwd+adjoint job-iterations/s", "value": batched, "unit": "job-iters/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced spheres)",
-        "config": {"workload": f"batch{n}_displaced_spheres_lambert_pointlight", "jobs": n,
+        "config": {"workload": f"batch{n}_{'small_' if args.batch_mix == 'small' else ''}displaced_spheres_lambert_pointlight",
+                   "jobs": n,
                    "triangles_min": min(tris), "triangles_max": max(tris),
                    "resolutions": sorted({sp.cams[0].width for *_, sp in setups}),
                    "spp": sorted({sp.spp for *_, sp in setups}), "l2": "flushed (256 MiB write) before every step",
@@ -876,6 +881,8 @@ def main():
     ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
     ap.add_argument("--bvh", default="sah", choices=sorted(BVH_BUILDERS), help="hierarchy builder")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
+    ap.add_argument("--batch-mix", default="c4", choices=["c4", "small"],
+                    help="batch: the uneven 64-job mix (c4) or small jobs that cannot fill the GPU alone")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device memory budget")
@@ -891,7 +898,7 @@ def main():
         return
     if args.workload in ("batch", "serve"):
         if args.jobs is None:
-            args.jobs = 64 if args.workload == "batch" else 16
+            args.jobs = (256 if args.batch_mix == "small" else 64) if args.workload == "batch" else 16
         (batch_arm if args.workload == "batch" else serve_arm)(args, ws, rank, local, pg)
         if pg is not None:
             pg.destroy_process_group()
