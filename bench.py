@@ -380,7 +380,7 @@ def batch_arm(args, ws, rank, local, pg):
     from diffrender_tutorials_gb300 import workloads as WL
     B.build()
     torch.cuda.set_device(local)
-    if args.batch_mix == "small":  # jobs too small to fill the GPU alone
+    if args.mix == "small":  # jobs too small to fill the GPU alone
         specs = WL.batch_jobs(args.jobs, seed=0, tri_range=(200, 3_000), resolutions=(64, 96, 128), spps=(4, 8),
                               views=(1, 2))
     else:
@@ -457,7 +457,7 @@ def batch_arm(args, ws, rank, local, pg):
         "metric": "batched fwd+adjoint job-iterations/s", "value": batched, "unit": "job-iters/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced spheres)",
-        "config": {"workload": f"batch{n}_{'small_' if args.batch_mix == 'small' else ''}displaced_spheres_lambert_pointlight",
+        "config": {"workload": f"batch{n}_{'small_' if args.mix == 'small' else ''}displaced_spheres_lambert_pointlight",
                    "jobs": n,
                    "triangles_min": min(tris), "triangles_max": max(tris),
                    "resolutions": sorted({sp.cams[0].width for *_, sp in setups}),
@@ -733,7 +733,11 @@ def serve_setups(args, local):
     """The Poisson trace with its target images rendered from the true meshes."""
     import diffrender_tutorials_gb300 as D
     from diffrender_tutorials_gb300 import workloads as WL
-    specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate)
+    if args.mix == "small":
+        specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate, tri_range=(200, 3_000), res_range=(64, 192),
+                                 views=(1, 2), steps=(50, 200))
+    else:
+        specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate)
     out = []
     for sp in specs:
         ts, isc = D.Scene(), D.Scene()
@@ -842,7 +846,8 @@ def serve_arm(args, ws, rank, local, pg):
         "steps": total_iters, "warmup": args.warmup, "ms_per_step": 1e3 / served, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Poisson trace of displaced-sphere optimisation jobs)",
-        "config": {"workload": f"serve{n}_poisson{args.rate:g}_displaced_spheres", "jobs": n, "rate_per_s": args.rate,
+        "config": {"workload": f"serve{n}_{'small_' if args.mix == 'small' else ''}poisson{args.rate:g}_displaced_spheres",
+                   "jobs": n, "rate_per_s": args.rate,
                    "triangles": [min(tris), max(tris)], "resolution": [min(res), max(res)],
                    "views": [min(len(sp.cams) for *_, sp in setups), max(len(sp.cams) for *_, sp in setups)],
                    "steps_per_job": [min(sp.steps for *_, sp in setups), max(sp.steps for *_, sp in setups)],
@@ -881,8 +886,9 @@ def main():
     ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
     ap.add_argument("--bvh", default="sah", choices=sorted(BVH_BUILDERS), help="hierarchy builder")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
-    ap.add_argument("--batch-mix", default="c4", choices=["c4", "small"],
-                    help="batch: the uneven 64-job mix (c4) or small jobs that cannot fill the GPU alone")
+    ap.add_argument("--mix", default="c4", choices=["c4", "small"],
+                    help="batch / serve: the configured job mix, or small jobs that cannot fill the GPU alone "
+                         "(batch: 256 jobs; serve: 128 jobs at 200/s, 32 slots)")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: Poisson arrival rate, jobs/s")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device memory budget")
@@ -898,7 +904,13 @@ def main():
         return
     if args.workload in ("batch", "serve"):
         if args.jobs is None:
-            args.jobs = (256 if args.batch_mix == "small" else 64) if args.workload == "batch" else 16
+            args.jobs = (256 if args.mix == "small" else 64) if args.workload == "batch" else \
+                (128 if args.mix == "small" else 16)
+        if args.workload == "serve" and args.mix == "small":
+            if args.rate == 20.0:
+                args.rate = 200.0
+            if args.slots == 8:
+                args.slots = 32
         (batch_arm if args.workload == "batch" else serve_arm)(args, ws, rank, local, pg)
         if pg is not None:
             pg.destroy_process_group()
