@@ -185,7 +185,9 @@ struct Job {
   int bvh_builder = 1;
   std::vector<int4> h_tri_v, topo_tri_v;
   int topo_builder = -1;
-  std::unique_ptr<TopoRebuild> topo_async;  // overlapped rebuild in progress (batches)
+  // overlapped rebuild in progress (optimiser or batch); declared after what its host thread reads, so that
+  // it is destroyed, and waits for that thread, first
+  std::unique_ptr<TopoRebuild> topo_async;
   // edges (topology; one list per differentiable-mesh set)
   DevBuf<int4> edges;   // v0, v1, vn0, vn1
   DevBuf<int2> edge_mi; // mesh, instance
