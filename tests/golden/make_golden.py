@@ -277,5 +277,70 @@ def main():
     save("optimize_cube_vc", **items, **prefixed("out.", out))
 
 
+def _moved(mesh, m):
+    v = np.c_[mesh.vertices.astype(np.float64), np.ones(len(mesh.vertices))] @ m.T
+    return TriangleMesh(v[:, :3].astype(np.float32), mesh.indices.copy(), colors=mesh.colors.copy())
+
+
+def _rot(axis, deg):
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    m = np.eye(4)
+    i, j = (0, 2) if axis == "y" else (0, 1)
+    m[i, i], m[j, j] = c, c
+    m[i, j], m[j, i] = (s, -s) if axis == "y" else (-s, s)
+    return m
+
+
+def _translate(x, y, z):
+    m = np.eye(4)
+    m[:3, 3] = (x, y, z)
+    return m
+
+
+def convergence():
+    """300-iteration runs in the shape of the reference's TESTS 2.1, 2.2 and
+    2.4 (src/tests.cpp:144-260): the triangle and pyramid of
+    src/scenes.cpp:69-117,190-238 restated (turned and moved apart between
+    start and target), three cameras around at distance 5
+    (create_cameras_around), 256x256, 16 spp, "Adam" with the tests'
+    learning rates and otherwise default parameters.  Kept: the inputs, the
+    final error and the last iteration's mesh."""
+    build_ref.build(verbose=True)
+    tri = TriangleMesh(np.array([[0, 1, 0], [1, -1, 1], [-1, -1, 1]], np.float32), np.array([0, 1, 2], np.uint32),
+                       colors=np.ones((3, 3), np.float32))
+    pyr = TriangleMesh(np.array([[0, 1, 0], [-1, -1, 1], [1, -1, 1], [1, -1, -1], [-1, -1, -1]], np.float32),
+                       np.array([0, 1, 2, 0, 2, 3, 0, 3, 4, 0, 4, 1], np.uint32),
+                       colors=np.array([[1, 0, 0], [1, 1, 0], [0, 0, 1], [0, 1, 0], [0, 1, 1]], np.float32))
+    lift = _translate(0, 0.5, 0)
+    half = np.diag([0.5, 0.5, 0.5, 1.0])
+    tri_pair = (_moved(tri, lift @ _rot("y", -40)), _moved(tri, lift @ _rot("y", 30)))
+    pyr_init = _moved(pyr, half @ lift @ _rot("y", -40) @ _rot("z", -30))
+    pyr_init.colors[:] = 0.25
+    pyr_pair = (pyr_init, _moved(pyr, half @ lift @ _rot("y", 50)))
+    ry = 2 * math.pi / 3
+    cams = [Cam((-5 * math.sin(ry * (i - 1)), 0.0, -5 * math.cos(ry * (i - 1))), 256, 256) for i in range(3)]
+    iters = 300
+    for name, (init, target), mode, tex_lr in (("converge_triangle_sil", tri_pair, 1, 0.1),
+                                               ("converge_pyramid_sil", pyr_pair, 1, 0.1),
+                                               ("converge_pyramid_vc", pyr_pair, 2, 0.0)):
+        tscene, iscene = Scene(), Scene()
+        tscene.add_mesh(target)
+        iscene.add_mesh(init)
+        tgt = run({"task": np.array([2], np.int32), "mode": np.array([mode], np.int32),
+                   "spp": np.array([16], np.int32), **scene_items(tscene), **cam_items(cams)})["images"]
+        items = {"task": np.array([5], np.int32), "mode": np.array([mode], np.int32), "spp": np.array([16], np.int32),
+                 **scene_items(iscene), **cam_items(cams), "targets": tgt, "iters": np.array([iters], np.int32),
+                 "opt_alg": np.array([4], np.int32), "opt_pos_lr": np.array([0.05], np.float32),
+                 "opt_tex_lr": np.array([tex_lr], np.float32), "dmesh_ids": np.array([0], np.int32)}
+        out = run(items)
+        last = f"it{iters - 1}."
+        keep = {k: v for k, v in out.items() if k in ("final_error", "n_iters") or k.startswith(last)}
+        save(name, **items, **prefixed("out.", keep))
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "convergence":
+        convergence()
+    else:
+        main()
