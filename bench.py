@@ -897,6 +897,16 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)
     ws, rank, local, pg = dist_setup()
+    if args.impl == "reference" and args.workload not in WORKLOADS:
+        # the reference's CPU path is timed on the single-job workloads only
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "workload": args.workload,
+                              "unavailable": "the reference arm times the reference's CPU d_render_and_compare on "
+                                             "the single-job workloads (" + ", ".join(sorted(WORKLOADS)) + ")"}),
+                  flush=True)
+        if pg is not None:
+            pg.destroy_process_group()
+        return
     if args.workload in ("stress", "instances"):
         (stress_arm if args.workload == "stress" else instances_arm)(args, ws, rank, local, pg)
         if pg is not None:
