@@ -149,9 +149,10 @@ __global__ void __launch_bounds__(DS_THREADS) k_ds_scatter(const uint32_t* kin, 
 // lane's range is a whole segment (the keys are sorted) and goes straight to
 // the gradient; the lane's first and last runs are fragments.  Lane 0 merges
 // the 32 lanes' fragments in lane order the same way, leaving the chunk's
-// first and last runs as fragments in two slots per chunk; one warp finally
-// merges those in chunk order.  The association order of every sum depends
-// only on the record count and the sorted keys.
+// first and last runs as fragments in two slots per chunk.  A second pass
+// merges those fragments in order the same way (chunks of 2,048 slots), and
+// one warp merges that pass's fragments.  The association order of every
+// sum depends only on the record count and the sorted keys.
 constexpr int DS_SEG_LANE = 64;
 constexpr int DS_SEG_CHUNK = 32 * DS_SEG_LANE;
 
@@ -233,10 +234,14 @@ __device__ __forceinline__ void merge_lane_frags(const DetFrag* f, float* grad, 
   }
 }
 
+// FRAGS: the input is the previous level's chunk fragments (two slots per
+// chunk of the *n_ptr sorted records) instead of the records.
+template <bool FRAGS>
 __global__ void __launch_bounds__(DS_THREADS) k_ds_seg_chunks(const uint32_t* key, const int* idx, const int* n_ptr,
-                                                              const float4* val, float* grad, DetFrag* chunk_frags) {
+                                                              const float4* val, const DetFrag* in, float* grad,
+                                                              DetFrag* chunk_frags) {
   __shared__ DetFrag sf[DS_THREADS / 32][64];
-  const int n = *n_ptr;
+  const int n = FRAGS ? 2 * ((*n_ptr + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK) : *n_ptr;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n_chunks = (n + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK;
   const int warps = gridDim.x * (DS_THREADS / 32);
@@ -244,8 +249,14 @@ __global__ void __launch_bounds__(DS_THREADS) k_ds_seg_chunks(const uint32_t* ke
     const int b = min(n, c * DS_SEG_CHUNK + lane * DS_SEG_LANE), e = min(n, b + DS_SEG_LANE);
     DetFrag f0, f1;
     seq_runs([&](int i, uint32_t& k, float4& v) {
-      k = key[i];
-      v = val[idx[i]];
+      if (FRAGS) {
+        const DetFrag g = in[i];
+        k = g.key;
+        v = make_float4(g.x, g.y, g.z, 0.0f);
+      } else {
+        k = key[i];
+        v = val[idx[i]];
+      }
     }, b, e, grad, f0, f1);
     sf[w][2 * lane] = f0;
     sf[w][2 * lane + 1] = f1;
@@ -260,13 +271,14 @@ __global__ void __launch_bounds__(DS_THREADS) k_ds_seg_chunks(const uint32_t* ke
   }
 }
 
-// One warp: the chunks' fragments in chunk order, lanes over contiguous
+// One warp: the second level's fragments in order, lanes over contiguous
 // ranges of slots, then lane 0.
 __global__ void __launch_bounds__(32) k_ds_seg_final(const int* n_ptr, const DetFrag* chunk_frags, float* grad) {
   __shared__ DetFrag sf[64];
   const int n = *n_ptr;
   const int lane = threadIdx.x;
-  const int slots = 2 * ((n + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK);
+  const int slots1 = 2 * ((n + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK);
+  const int slots = 2 * ((slots1 + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK);
   const int per = (slots + 31) / 32;
   const int b = min(slots, lane * per), e = min(slots, b + per);
   DetFrag f0, f1;
@@ -304,6 +316,14 @@ int64_t det_regions(const Job& J) { return (int64_t)J.dev.item_count + (int64_t)
 
 // Buffers of the deterministic mode for the current views, work items and
 // edge-sample count (grow-only).
+// Fragment slots of the first level (two per chunk of records, at the
+// record capacity); the second level's follow them.
+static int64_t det_frag_l1(const Job& J) {
+  const int64_t cap = (int64_t)J.dev.item_count * J.dev.rec_item_cap +
+                      (int64_t)J.n_views * J.dev.edge_samples * kEdgeRecords;
+  return 2 * ((std::max<int64_t>(1, cap) + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK);
+}
+
 void det_buffers(Job& J, cudaStream_t s) {
   (void)s;
   const int NS = J.tile_w * J.tile_h * J.S;
@@ -321,7 +341,8 @@ void det_buffers(Job& J, cudaStream_t s) {
   }
   J.det_part.reserve(std::max<int64_t>(1, (regions + DS_CHUNK - 1) / DS_CHUNK));
   J.det_hist.reserve(256 * DS_GRID);
-  J.det_frag.reserve(2 * ((std::max<int64_t>(1, cap) + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK));
+  const int64_t l1 = det_frag_l1(J);
+  J.det_frag.reserve(l1 + 2 * ((l1 + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK));
   J.det_n.reserve(1);
   // A single transform block among the differentiable meshes (one mesh, one
   // instance): its 12 values per edge sample are summed densely in a fixed
@@ -413,10 +434,15 @@ void launch_det_reduce(const Job& J, int sm_count, cudaStream_t s) {
     count_launch(2);
     cur ^= 1;
   }
-  k_ds_seg_chunks<<<std::max(1, sm_count) * 8, DS_THREADS, 0, s>>>(J.det_key[cur].p, J.det_idx[cur].p, J.det_n.p,
-                                                                    J.rec_val.p, J.grad.p, J.det_frag.p);
-  k_ds_seg_final<<<1, 32, 0, s>>>(J.det_n.p, J.det_frag.p, J.grad.p);
-  count_launch(2);
+  // three levels: chunks of records, chunks of their fragments, one warp
+  DetFrag* l2 = J.det_frag.p + det_frag_l1(J);
+  k_ds_seg_chunks<false><<<std::max(1, sm_count) * 8, DS_THREADS, 0, s>>>(J.det_key[cur].p, J.det_idx[cur].p,
+                                                                           J.det_n.p, J.rec_val.p, nullptr, J.grad.p,
+                                                                           J.det_frag.p);
+  k_ds_seg_chunks<true><<<std::max(1, sm_count), DS_THREADS, 0, s>>>(nullptr, nullptr, J.det_n.p, nullptr,
+                                                                      J.det_frag.p, J.grad.p, l2);
+  k_ds_seg_final<<<1, 32, 0, s>>>(J.det_n.p, l2, J.grad.p);
+  count_launch(3);
   if (J.det_tr_key >= 0) {
     k_ds_tr_blocks<<<DS_TR_BLOCKS, DS_THREADS, 0, s>>>(J.det_tr.p, (int64_t)J.n_views * J.dev.edge_samples,
                                                       J.det_tr_part.p);
