@@ -198,7 +198,7 @@ struct drgb_batch {
       qkey[b].reserve(queue.n);
       qidx[b].reserve(queue.n);
     }
-    qhist.reserve(256 * (size_t)kSortGrid);
+    qhist.reserve(scan_scratch(256 * (size_t)kSortGrid));
     qn.reserve(1);
     qbits = 1;
     while (qbits < 32 && (1ull << qbits) < std::max<uint64_t>(1, key_base)) qbits++;

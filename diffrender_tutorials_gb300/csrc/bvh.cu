@@ -163,68 +163,116 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* keys, in
 // counters, 16 consecutive ones per thread (four 16-byte loads, so a warp
 // reads 2 KB contiguously), a warp-shuffle scan of the thread sums, and a
 // carry from tile to tile.  hist must be 16-byte aligned (a buffer start).
-__global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* hist, int m) {
-  __shared__ uint32_t wsum[32];
+// Exclusive scan of the tile hist[base, base + 16384) in place (1024 threads,
+// 16 counters each), offset by `carry`; returns the tile's total.
+__device__ __forceinline__ uint32_t scan_tile(uint32_t* hist, int m, int base, uint32_t carry, uint32_t* wsum) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  uint32_t carry = 0;
-  for (int base = 0; base < m; base += 1024 * 16) {
-    const int i0 = base + tid * 16;
-    uint32_t v[16];
-    if (i0 + 16 <= m) {
-      const uint4* p = reinterpret_cast<const uint4*>(hist + i0);
+  const int i0 = base + tid * 16;
+  uint32_t v[16];
+  if (i0 + 16 <= m) {
+    const uint4* p = reinterpret_cast<const uint4*>(hist + i0);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const uint4 x = p[q];
-        v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 16; k++) v[k] = i0 + k < m ? hist[i0 + k] : 0u;
+    for (int q = 0; q < 4; q++) {
+      const uint4 x = p[q];
+      v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
     }
-    uint32_t sum = 0;
+  } else {
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const uint32_t x = v[k];
-      v[k] = sum;
-      sum += x;
-    }
-    uint32_t inc = sum;
+    for (int k = 0; k < 16; k++) v[k] = i0 + k < m ? hist[i0 + k] : 0u;
+  }
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    const uint32_t x = v[k];
+    v[k] = sum;
+    sum += x;
+  }
+  uint32_t inc = sum;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = wsum[lane];
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
-      if (lane >= off) inc += y;
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += y;
     }
-    if (lane == 31) wsum[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = wsum[lane];
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t before = carry + (warp ? wsum[warp - 1] : 0u) + (inc - sum);
+  if (i0 + 16 <= m) {
+    uint4* p = reinterpret_cast<uint4*>(hist + i0);
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
-        if (lane >= off) w += y;
-      }
-      wsum[lane] = w;
+    for (int q = 0; q < 4; q++)
+      p[q] = make_uint4(v[4 * q] + before, v[4 * q + 1] + before, v[4 * q + 2] + before, v[4 * q + 3] + before);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+      if (i0 + k < m) hist[i0 + k] = v[k] + before;
+  }
+  const uint32_t total = wsum[31];
+  __syncthreads();  // wsum is rewritten by the next tile
+  return total;
+}
+
+constexpr int RS_SCAN_TILE = 1024 * 16;
+
+__global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* hist, int m) {
+  __shared__ uint32_t wsum[32];
+  uint32_t carry = 0;
+  for (int base = 0; base < m; base += RS_SCAN_TILE) carry += scan_tile(hist, m, base, carry, wsum);
+}
+
+// Several tiles: one block scans each tile on its own and keeps its total in
+// the slot past the counters; a second pass adds the totals of the tiles
+// before it to every counter of a tile.
+__global__ void __launch_bounds__(1024) k_rs_scan_tiles(uint32_t* hist, int m, uint32_t* totals) {
+  __shared__ uint32_t wsum[32];
+  const uint32_t t = scan_tile(hist, m, blockIdx.x * RS_SCAN_TILE, 0u, wsum);
+  if (threadIdx.x == 0) totals[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(1024) k_rs_scan_offsets(uint32_t* hist, int m, const uint32_t* totals) {
+  __shared__ uint32_t off;
+  if (threadIdx.x == 0) {
+    uint32_t o = 0;
+    for (int b = 0; b < (int)blockIdx.x; b++) o += totals[b];
+    off = o;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) return;
+  const int i0 = blockIdx.x * RS_SCAN_TILE + threadIdx.x * 16;
+  if (i0 + 16 <= m) {
+    uint4* p = reinterpret_cast<uint4*>(hist + i0);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint4 x = p[q];
+      p[q] = make_uint4(x.x + off, x.y + off, x.z + off, x.w + off);
     }
-    __syncthreads();
-    const uint32_t before = carry + (warp ? wsum[warp - 1] : 0u) + (inc - sum);
-    if (i0 + 16 <= m) {
-      uint4* p = reinterpret_cast<uint4*>(hist + i0);
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        p[q] = make_uint4(v[4 * q] + before, v[4 * q + 1] + before, v[4 * q + 2] + before, v[4 * q + 3] + before);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 16; k++)
-        if (i0 + k < m) hist[i0 + k] = v[k] + before;
-    }
-    carry += wsum[31];
-    __syncthreads();  // wsum is rewritten by the next tile
+  } else {
+    for (int k = 0; k < 16; k++)
+      if (i0 + k < m) hist[i0 + k] += off;
   }
 }
 
+// `hist` has room for scan_scratch(m) counters: m, then one total per tile.
 void launch_rs_scan(uint32_t* hist, int m, cudaStream_t s) {
-  k_rs_scan<<<1, 1024, 0, s>>>(hist, m);
-  count_launch();
+  const int tiles = (m + RS_SCAN_TILE - 1) / RS_SCAN_TILE;
+  if (tiles <= 1) {
+    k_rs_scan<<<1, 1024, 0, s>>>(hist, m);
+    count_launch();
+    return;
+  }
+  uint32_t* totals = hist + ((m + 3) & ~3);
+  k_rs_scan_tiles<<<tiles, 1024, 0, s>>>(hist, m, totals);
+  k_rs_scan_offsets<<<tiles, 1024, 0, s>>>(hist, m, totals);
+  count_launch(2);
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* kin, const int* vin, uint32_t* kout,

@@ -339,8 +339,8 @@ void det_buffers(Job& J, cudaStream_t s) {
     J.det_key[b].reserve(std::max<int64_t>(1, cap));
     J.det_idx[b].reserve(std::max<int64_t>(1, cap));
   }
-  J.det_part.reserve(std::max<int64_t>(1, (regions + DS_CHUNK - 1) / DS_CHUNK));
-  J.det_hist.reserve(256 * DS_GRID);
+  J.det_part.reserve(scan_scratch((size_t)std::max<int64_t>(1, (regions + DS_CHUNK - 1) / DS_CHUNK)));
+  J.det_hist.reserve(scan_scratch(256 * DS_GRID));
   const int64_t l1 = det_frag_l1(J);
   J.det_frag.reserve(l1 + 2 * ((l1 + DS_SEG_CHUNK - 1) / DS_SEG_CHUNK));
   J.det_n.reserve(1);

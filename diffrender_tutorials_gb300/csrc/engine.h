@@ -279,6 +279,9 @@ CamDev make_cam(const drgb_camera& c);
 // PX_HIT_STORE: adjoint pass that only traces and stores the primary hits;
 // PX_HIT_LOAD: adjoint pass that reads them instead of tracing.
 enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8, PX_HIT_STORE = 16, PX_HIT_LOAD = 32 };
+// Counters a buffer scanned by launch_rs_scan needs for m counters: the m
+// counters (rounded up to 4) and one total per 16,384-counter tile.
+inline size_t scan_scratch(size_t m) { return ((m + 3) & ~(size_t)3) + (m + 16383) / 16384; }
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
                    cudaStream_t s, int mode, bool det = false);
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);

@@ -149,7 +149,7 @@ struct drgb_renderer {
       J.qkey[b].reserve(J.queue.n);
       J.qidx[b].reserve(J.queue.n);
     }
-    J.qhist.reserve(256 * (size_t)kSortGrid);
+    J.qhist.reserve(scan_scratch(256 * (size_t)kSortGrid));
     J.qn.reserve(1);
 #endif
     J.dev.edge_samples = edge_samples;
