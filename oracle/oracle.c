@@ -25,6 +25,7 @@
 #endif
 
 #define REF_THREADS 14 /* MAXTHREADS, src/drender.h:12 */
+#define ORC_CHUNK 16   /* triangles per vectorised step of the brute-force caster */
 
 typedef struct { float x, y, z; } f3;
 typedef struct { float x, y; } f2;
@@ -295,6 +296,11 @@ typedef struct {
   int* tri_prim;
   f3 *ta, *te1, *te2;
   int* tri_gid; /* 3 global vertex ids per traced triangle */
+  /* the same triangles structure-of-arrays, padded to a multiple of
+   * ORC_CHUNK with zero triangles (determinant 0 -> never accepted): 9 arrays
+   * of n_pad floats {ax ay az e1x e1y e1z e2x e2y e2z} */
+  int n_pad;
+  float* soa;
 } prep_t;
 
 static const float* mesh_tr(const orc_mesh* m, int j, float* tmp) {
@@ -314,6 +320,7 @@ static void prep_free(prep_t* s) {
   free(s->pos); free(s->orig); free(s->col); free(s->nrm); free(s->tng); free(s->tc);
   free(s->tr); free(s->tr_inv);
   free(s->tri_block); free(s->tri_prim); free(s->ta); free(s->te1); free(s->te2); free(s->tri_gid);
+  free(s->soa);
   memset(s, 0, sizeof(*s));
 }
 
@@ -398,6 +405,16 @@ static void prep_build(prep_t* s, const orc_mesh* meshes, int n_meshes) {
       s->tri_gid[3 * t + 2] = C;
     }
   }
+  s->n_pad = (ntri + ORC_CHUNK - 1) / ORC_CHUNK * ORC_CHUNK;
+  s->soa = (float*)calloc(9 * (size_t)(s->n_pad > 0 ? s->n_pad : 1), sizeof(float));
+  for (t = 0; t < ntri; t++) {
+    const f3 q[3] = {s->ta[t], s->te1[t], s->te2[t]};
+    for (int k = 0; k < 3; k++) {
+      s->soa[(size_t)(3 * k + 0) * s->n_pad + t] = q[k].x;
+      s->soa[(size_t)(3 * k + 1) * s->n_pad + t] = q[k].y;
+      s->soa[(size_t)(3 * k + 2) * s->n_pad + t] = q[k].z;
+    }
+  }
 }
 
 /* get_index(mesh, inst, k) with the caster's identity instance mapping (scene.h:168-171). */
@@ -411,36 +428,70 @@ static inline int get_index(const prep_t* s, int mesh, int inst, int k) {
  * ------------------------------------------------------------------------- */
 typedef struct { uint32_t prim, inst, geom; float t, u, v; } hit_t;
 
-static hit_t nearest_hit(const prep_t* s, f3 pos, f3 dir, float tNear, float tFar) {
-  hit_t h = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, tFar, 0.0f, 0.0f};
-  for (int t = 0; t < s->n_tris; t++) {
-    const f3 edge1 = s->te1[t], edge2 = s->te2[t];
+/* The Moller-Trumbore test of raytrace3d_bf.cpp:127-138 for ORC_CHUNK
+ * consecutive triangles: each lane performs the reference's scalar IEEE
+ * operations in the reference's order (no contraction), so the values are
+ * those of the scalar loop; ok[k] holds every acceptance test except the
+ * running `t < best`, which the callers apply in triangle order. */
+static inline int mt_chunk(const prep_t* s, int t0, f3 pos, f3 dir, float tNear, float tFar, float* tt, float* uu,
+                           float* vv, int* ok) {
+  const size_t np = (size_t)s->n_pad;
+  const float *ax = s->soa + t0, *ay = ax + np, *az = ay + np;
+  const float *e1x = az + np, *e1y = e1x + np, *e1z = e1y + np;
+  const float *e2x = e1z + np, *e2y = e2x + np, *e2z = e2y + np;
+  int any = 0;
+  for (int k = 0; k < ORC_CHUNK; k++) {
+    const f3 edge1 = v3(e1x[k], e1y[k], e1z[k]), edge2 = v3(e2x[k], e2y[k], e2z[k]);
     const f3 pvec = cross3(dir, edge2);
-    const f3 tvec = sub3(pos, s->ta[t]);
+    const f3 tvec = sub3(pos, v3(ax[k], ay[k], az[k]));
     const f3 qvec = cross3(tvec, edge1);
     const float e1dpv = dot3(edge1, pvec);
-    const float signv = signf_ref(e1dpv);
+    const float signv = (e1dpv == 0.0f) ? 0.0f : ((e1dpv < 0.0f) ? -1.0f : 1.0f); /* signf_ref */
     const float invDet = signv / maxf_ref(signv * e1dpv, 1e-6f);
     const float v = dot3(tvec, pvec) * invDet;
     const float u = dot3(qvec, dir) * invDet;
-    const float tt = dot3(edge2, qvec) * invDet;
-    if (v > 0.0f && u > 0.0f && (u + v < 1.0f) && tt > tNear && tt < h.t) {
-      const int b = s->tri_block[t];
-      const int mesh = s->block_mesh[b];
-      h.t = tt;
-      h.geom = (uint32_t)mesh;
-      h.inst = (uint32_t)(b - s->mesh_block0[mesh]);
-      h.prim = (uint32_t)s->tri_prim[t];
-      h.u = u;
-      h.v = v;
+    const float t = dot3(edge2, qvec) * invDet;
+    const int a = (v > 0.0f) & (u > 0.0f) & (u + v < 1.0f) & (t > tNear) & (t < tFar);
+    tt[k] = t;
+    uu[k] = u;
+    vv[k] = v;
+    ok[k] = a;
+    any |= a;
+  }
+  return any;
+}
+
+static hit_t nearest_hit(const prep_t* s, f3 pos, f3 dir, float tNear, float tFar) {
+  hit_t h = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, tFar, 0.0f, 0.0f};
+  float tt[ORC_CHUNK], uu[ORC_CHUNK], vv[ORC_CHUNK];
+  int ok[ORC_CHUNK];
+  for (int t0 = 0; t0 < s->n_pad; t0 += ORC_CHUNK) {
+    if (!mt_chunk(s, t0, pos, dir, tNear, tFar, tt, uu, vv, ok)) continue;
+    for (int k = 0; k < ORC_CHUNK; k++) {
+      if (ok[k] && tt[k] < h.t) { /* the brute-force loop's order and strict < */
+        const int t = t0 + k;
+        const int b = s->tri_block[t];
+        const int mesh = s->block_mesh[b];
+        h.t = tt[k];
+        h.geom = (uint32_t)mesh;
+        h.inst = (uint32_t)(b - s->mesh_block0[mesh]);
+        h.prim = (uint32_t)s->tri_prim[t];
+        h.u = uu[k];
+        h.v = vv[k];
+      }
     }
   }
   return h;
 }
 
+/* Whether nearest_hit would report a hit: the first accepted triangle
+ * decides, so the scan stops there. */
 static int any_hit(const prep_t* s, f3 pos, f3 dir, float tNear, float tFar) {
-  hit_t h = nearest_hit(s, pos, dir, tNear, tFar);
-  return h.prim != 0xFFFFFFFFu;
+  float tt[ORC_CHUNK], uu[ORC_CHUNK], vv[ORC_CHUNK];
+  int ok[ORC_CHUNK];
+  for (int t0 = 0; t0 < s->n_pad; t0 += ORC_CHUNK)
+    if (mt_chunk(s, t0, pos, dir, tNear, tFar, tt, uu, vv, ok)) return 1;
+  return 0;
 }
 
 static void camera_ray(const float* cam, float x, float y, f3* ro, f3* rd) {
@@ -684,7 +735,7 @@ static f3 shade(const ctx_t* c, f2 sp) {
       const f3 to_light = scl3(light_dir, -1.0f);
       const float ndl = maxf_ref(0.0f, dot3(n, to_light));
       /* (colour * vis) * 0 is 0 for either visibility: trace only when lit */
-      float sh = (ndl > 0.0f && nearest_hit(s, surf_pos, to_light, 0.0f, 1e9f).prim != 0xFFFFFFFFu) ? 0.0f : 1.0f;
+      float sh = (ndl > 0.0f && any_hit(s, surf_pos, to_light, 0.0f, 1e9f)) ? 0.0f : 1.0f;
       f3 lit = scl3(scl3(light_color, sh), ndl);
       return mul3(add3(lit, ambient), diffuse);
     }
@@ -731,7 +782,7 @@ static f3 shade(const ctx_t* c, f2 sp) {
         term = maxf_ref(0.0f, dot3(n, to_light)) + ggx;
       }
       /* (colour * vis) * 0 is 0 for either visibility: trace only when lit */
-      const float sh = (term != 0.0f && nearest_hit(s, surf_pos, to_light, 0.0f, 1e9f).prim != 0xFFFFFFFFu) ? 0.0f : 1.0f;
+      const float sh = (term != 0.0f && any_hit(s, surf_pos, to_light, 0.0f, 1e9f)) ? 0.0f : 1.0f;
       const f3 lit = scl3(scl3(light_color, sh), term);
       return mul3(add3(lit, scl3(v3(1, 1, 1), Ka)), diffuse);
     }

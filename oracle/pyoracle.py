@@ -20,14 +20,17 @@ LAMBERT_POINT_VCOLOR, PATH_DIFFUSE = 16, 17
 
 def build(force=False):
     """Compile oracle.c with gcc (-ffp-contract=off keeps the reference's
-    rounding on hosts whose compilers fuse multiply-adds by default)."""
+    rounding on hosts whose compilers fuse multiply-adds by default;
+    -fno-trapping-math only lets gcc turn the caster's compares into vector
+    selects, it changes no value)."""
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "oracle.c")
     hdr = os.path.join(HERE, "oracle.h")
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
         return LIB
     tmp = LIB + ".tmp"
-    subprocess.check_call(["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+    subprocess.check_call(["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+                           "-fno-trapping-math", "-fPIC",
                            "-shared", "-Wall", "-Wno-unused-function", src, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
     return LIB

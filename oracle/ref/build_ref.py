@@ -134,7 +134,8 @@ def _oracle_object():
     src, hdr = os.path.join(ORACLE, "oracle.c"), os.path.join(ORACLE, "oracle.h")
     obj = os.path.join(BIN, "oracle.o")
     if _stale(obj, [src, hdr, __file__]):
-        subprocess.check_call(["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-w", "-c",
+        subprocess.check_call(["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+                               "-fno-trapping-math", "-w", "-c",
                                src, "-o", obj])
     return obj
 
