@@ -153,7 +153,8 @@ def cpu_sample(w, reps=1):
     scams = [D.CamInfo(origin=c.origin, target=c.target, up=c.up, width=sres, height=sres) for c in cams[:sv]]
     cores = os.cpu_count() or 1
     factor = (w["res"] * w["res"] * w["views"]) / (sres * sres * sv)
-    what = f"{sv} view(s) at {sres}x{sres} of the same scene, extrapolated x{factor:g}"
+    what = (f"{sv} view(s) at {sres}x{sres} of the same scene, extrapolated x{factor:g}" if factor != 1 else
+            f"the full workload ({sv} view(s) at {sres}x{sres}), not extrapolated")
     O.set_threads(cores)
     tgt = O.render(ts, scams, w["mode"], w["spp"])
     exe = None
@@ -172,9 +173,10 @@ def cpu_sample(w, reps=1):
         for _ in range(reps):
             dt += float(refrun.run(exe, items)["seconds"][0])
         dt /= reps
-        # the reference runs its loops on at most 14 OpenMP threads (MAXTHREADS, src/drender.h:12)
-        return dt * factor, factor, min(cores, 14), "reference", what + " (reference d_render_and_compare, " \
-            "brute-force caster, OpenMP)"
+        # the reference runs its loops on 14 OpenMP threads (MAXTHREADS, src/drender.h:12) whatever the
+        # host has: more threads than cores when the host has fewer than 14
+        return dt * factor, factor, 14, "reference", what + f" (reference d_render_and_compare, " \
+            f"brute-force caster, OpenMP: 14 threads on {cores} host cores)"
     t0 = time.perf_counter()
     for _ in range(reps):
         O.d_render_and_compare(isc, scams, w["mode"], w["spp"], tgt, sres * sres)
@@ -194,11 +196,21 @@ def reference_arm(args, w, ws, rank, pg):
         times.append(t)
     mean = sum(times) / len(times)
     val = 1.0 / mean
+    # the small workload (cube, 256x256, one view) timed at its full size, not extrapolated
+    cube = WORKLOADS["cube"]
+    cube_t = [cpu_sample(cube)[0] for _ in range(max(3, min(args.steps, 10)))]
     line = {"impl": "reference", "metric": "fwd+adjoint iters/s", "value": val, "unit": "iters/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "parallelism": "replicas"},
-            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc},
+            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc,
+                             "host_cores": os.cpu_count() or 1},
+            "extrapolation": {"factor": factor, "sample_ms_per_step": mean * 1e3 / factor,
+                              "note": "each step times one bounded sample of the workload (one reduced view) and "
+                                      "scales it by pixels x views; ms_per_step is the scaled figure"},
+            "cube_full_size": {"workload": cube["name"], "value": 1.0 / (sum(cube_t) / len(cube_t)),
+                               "unit": "iters/s", "ms_per_step": 1e3 * sum(cube_t) / len(cube_t),
+                               "steps": len(cube_t), "extrapolated": False},
             "e2e": {"value": val, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -263,7 +275,13 @@ def drgb_arm(args, w, ws, rank, local, pg):
     value = ws * args.steps / (total_ms / 1e3)
     losses = opt.losses
 
-    # e2e: the public C-ABI call with host buffers (pinned), one call per step
+    # e2e: the reference's call sequence through the public C ABI with host
+    # buffers, one iteration per step: drgb_commit of the scene (the
+    # reference's d_render_and_compare commits the scene it is given on every
+    # call, src/drender.h:176; here a commit of the same triangles uploads the
+    # mesh, flattens it and refits the hierarchy), then
+    # drgb_d_render_and_compare (targets in from pinned memory, gradient and
+    # loss out)
     r2 = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
     r2.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
     r2.commit(isc)
@@ -273,15 +291,19 @@ def drgb_arm(args, w, ws, rank, local, pg):
     ds.data = torch.zeros(ds.data.size, dtype=torch.float32, pin_memory=True).numpy()
     edge_samples = w["res"] * w["res"]
     for _ in range(max(1, args.warmup)):
+        r2.commit(isc)
         r2.d_render_and_compare(isc, cams, tg_pinned, edge_samples, ds)
     e2e_ms = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
+        r2.commit(isc)
         r2.d_render_and_compare(isc, cams, tg_pinned, edge_samples, ds)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_total = allmax(pg, sum(e2e_ms))
     e2e_value = ws * args.steps / (e2e_total / 1e3)
-    h2d = tg_pinned.nbytes + 168 * len(cams)
+    scene_bytes = sum(a.nbytes for m in isc.meshes for a in (m.vertices, m.indices, m.colors, m.normals, m.tc)
+                      if a is not None) + sum(64 * len(t) for t in isc.transforms)
+    h2d = scene_bytes + tg_pinned.nbytes + 168 * len(cams)
     d2h = ds.data.nbytes + 4
 
     # the same iteration with the deterministic gradient reduction
@@ -346,7 +368,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "api": "drgb_d_render_and_compare (host pointers, pinned)",
+                "api": "drgb_commit (scene from host memory) + drgb_d_render_and_compare (host pointers, pinned)",
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
         "gpu_launches": int(launches),
         "phases_ms": prof,
@@ -363,28 +385,68 @@ def drgb_arm(args, w, ws, rank, local, pg):
                           "ops_per_iter": ops},
         "final_loss": losses[-1] if losses else None,
     }
+    del opt, r, r2
+    if w is WORKLOADS["icosphere"] and not args.no_patterns:
+        # the small workload at its own size (the reference arm times it at full size too)
+        line["cube"] = single_job_rate(WORKLOADS["cube"], local, args.steps, args.warmup)
+        # the batched and served forms against the plain one-job-at-a-time path on the same GPU:
+        # 64 uneven jobs, and a Poisson trace of 16 jobs at 20 jobs/s with an HBM budget of 150 GB
+        line["batched"] = batch_measure(local, 64, max(3, min(args.steps, 5)), min(args.warmup, 3))
+        line["served"] = serve_measure(local, 16, 0, 20.0, min(args.warmup, 3))
     if ws == 1 and rank == 0 and not args.no_cpu_baseline:
         t, factor, cores, kind, desc = cpu_sample(w)
-        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc}
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "iters/s", "cores": cores, "kind": kind, "sample": desc,
+                                "host_cores": os.cpu_count() or 1}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def batch_arm(args, ws, rank, local, pg):
-    """64 uneven optimisation jobs: batched (one fused launch sequence per
-    iteration, CUDA graph) against the plain path (each job's own iteration
-    graph, one job at a time)."""
+def single_job_rate(w, local, steps, warmup):
+    """Optimiser iterations/s of one job of workload w (graph replays timed
+    with CUDA events on the renderer's stream, L2 flushed before each)."""
     import torch
     import diffrender_tutorials_gb300 as D
-    from diffrender_tutorials_gb300 import build as B
+    ts, isc, cams = make_problem(w)
+    S = D.SHADING_MODEL(w["mode"])
+    r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
+    r.commit(ts)
+    targets = r.render(ts, cams)
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.01)
+    p.base_lr = 0.01
+    p.flags = D.OptimizerParameters._OPT_POS | D.OptimizerParameters._OPT_COL
+    opt = D.CreateSimpleOptimizer()
+    opt.Init(isc, r, cams, targets, p)
+    opt.autotune(2)
+    stream = torch.cuda.ExternalStream(r.stream(), device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    opt.run_async(warmup)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            opt.run_async(1)
+            e1.record(stream)
+    torch.cuda.synchronize()
+    ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    return {"workload": w["name"], "value": steps / (sum(ms) / 1e3), "unit": "iters/s",
+            "ms_per_step": sum(ms) / steps, "steps": steps}
+
+
+def batch_measure(local, jobs, steps, warmup, mix="c4"):
+    """64 uneven optimisation jobs: batched (one fused launch sequence per
+    iteration, CUDA graph) against the plain path (each job's own iteration
+    graph, one job at a time).  Returns the measurement as a dict."""
+    import torch
+    import diffrender_tutorials_gb300 as D
     from diffrender_tutorials_gb300 import workloads as WL
-    B.build()
     torch.cuda.set_device(local)
-    if args.mix == "small":  # jobs too small to fill the GPU alone
-        specs = WL.batch_jobs(args.jobs, seed=0, tri_range=(200, 3_000), resolutions=(64, 96, 128), spps=(4, 8),
+    if mix == "small":  # jobs too small to fill the GPU alone
+        specs = WL.batch_jobs(jobs, seed=0, tri_range=(200, 3_000), resolutions=(64, 96, 128), spps=(4, 8),
                               views=(1, 2))
     else:
-        specs = WL.batch_jobs(args.jobs, seed=0)
+        specs = WL.batch_jobs(jobs, seed=0)
     setups = []
     for sp in specs:
         ts, isc = D.Scene(), D.Scene()
@@ -407,15 +469,15 @@ def batch_arm(args, ws, rank, local, pg):
     for isc, cams, tgt, sp in setups:
         b.add_job(isc, cams, tgt, D.DiffRenderSettings(D.SHADING_MODEL(sp.mode), sp.spp), params())
     tuned = b.autotune(2)
-    b.run(args.warmup)
+    b.run(warmup)
     bs = torch.cuda.ExternalStream(b.stream(), device=local)
-    st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     k0 = D.kernel_launches()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         with torch.cuda.stream(bs):
-            for i in range(args.steps):
+            for i in range(steps):
                 flush.zero_()
                 st[i].record(bs)
                 b.run_async(1)
@@ -426,7 +488,8 @@ def batch_arm(args, ws, rank, local, pg):
     step_ms = [s.elapsed_time(e) for s, e in zip(st, en)]
     batched_ms = sum(step_ms)
     n = len(setups)
-    batched = n * args.steps / (batched_ms / 1e3)
+    batched = n * steps / (batched_ms / 1e3)
+    del b
     # plain: one job at a time
     opts = []
     for isc, cams, tgt, sp in setups:
@@ -434,11 +497,12 @@ def batch_arm(args, ws, rank, local, pg):
         o = D.CreateSimpleOptimizer()
         o.Init(isc, r, cams, tgt, params())
         o.autotune(2)
-        o.run_async(args.warmup)
+        o.run_async(warmup)
         opts.append((r, o))
     torch.cuda.synchronize()
     plain_ms = 0.0
-    for i in range(args.steps):
+    job_ms = []
+    for i in range(steps):
         # L2 flushed once per step, as for the batched arm (not before every job)
         flush.zero_()
         torch.cuda.synchronize()
@@ -450,26 +514,40 @@ def batch_arm(args, ws, rank, local, pg):
                 o.run_async(1)
                 e1.record(s)
             e1.synchronize()
-            plain_ms += e0.elapsed_time(e1)
-    plain = n * args.steps / (plain_ms / 1e3)
+            job_ms.append(e0.elapsed_time(e1))
+            plain_ms += job_ms[-1]
+    del opts
+    plain = n * steps / (plain_ms / 1e3)
     tris = [sp.triangles for _, _, _, sp in setups]
-    line = {
-        "metric": "batched fwd+adjoint job-iterations/s", "value": batched, "unit": "job-iters/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced spheres)",
-        "config": {"workload": f"batch{n}_{'small_' if args.mix == 'small' else ''}displaced_spheres_lambert_pointlight",
-                   "jobs": n,
-                   "triangles_min": min(tris), "triangles_max": max(tris),
+    return {
+        "value": batched, "unit": "job-iters/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": batched_ms / steps,
+        "config": {"workload": f"batch{n}_{'small_' if mix == 'small' else ''}displaced_spheres_lambert_pointlight",
+                   "jobs": n, "triangles_min": min(tris), "triangles_max": max(tris),
                    "resolutions": sorted({sp.cams[0].width for *_, sp in setups}),
                    "spp": sorted({sp.spp for *_, sp in setups}), "l2": "flushed (256 MiB write) before every step",
-                   "parallelism": "replicas", "autotuned": tuned,
-                   "plain_autotuned": "each job's tile and grids by drgb_optimizer_autotune"},
-        "plain": {"value": plain, "unit": "job-iters/s", "ms_per_step": plain_ms / args.steps,
+                   "autotuned": tuned, "plain_autotuned": "each job's tile and grids by drgb_optimizer_autotune"},
+        "plain": {"value": plain, "unit": "job-iters/s", "ms_per_step": plain_ms / steps,
+                  "latency_ms": {"job_iteration_p50": float(np.percentile(job_ms, 50)),
+                                 "job_iteration_p99": float(np.percentile(job_ms, 99))},
                   "how": "each job's own iteration graph, one job at a time; L2 flushed once per step of all jobs"},
         "speedup_vs_plain": batched / plain,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "clocks": clk.summary(), "gpu_launches": int(launches),
     }
+
+
+def batch_arm(args, ws, rank, local, pg):
+    from diffrender_tutorials_gb300 import build as B
+    B.build()
+    m = batch_measure(local, args.jobs, args.steps, args.warmup, args.mix)
+    line = {"metric": "batched fwd+adjoint job-iterations/s", "value": m.pop("value"), "unit": m.pop("unit"),
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded displaced spheres)", "config": dict(m.pop("config"), parallelism="replicas")}
+    m.pop("steps")
+    m.pop("warmup")
+    line.update(m)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -729,15 +807,15 @@ def stress_arm(args, ws, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
-def serve_setups(args, local):
+def serve_setups(local, jobs, seed, rate, mix="c5"):
     """The Poisson trace with its target images rendered from the true meshes."""
     import diffrender_tutorials_gb300 as D
     from diffrender_tutorials_gb300 import workloads as WL
-    if args.mix == "small":
-        specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate, tri_range=(200, 3_000), res_range=(64, 192),
+    if mix == "small":
+        specs = WL.serving_trace(jobs, seed=seed, rate=rate, tri_range=(200, 3_000), res_range=(64, 192),
                                  views=(1, 2), steps=(50, 200))
     else:
-        specs = WL.serving_trace(args.jobs, seed=args.seed, rate=args.rate)
+        specs = WL.serving_trace(jobs, seed=seed, rate=rate)
     out = []
     for sp in specs:
         ts, isc = D.Scene(), D.Scene()
@@ -759,30 +837,28 @@ def serve_params(sp):
     return p
 
 
-def serve_arm(args, ws, rank, local, pg):
+def serve_measure(local, jobs, seed, rate, warmup, budget_gb=150.0, slots=8, mix="c5"):
     """Poisson arrivals of optimisation jobs (wall clock): the serving loop
     (continuous batching, admission by memory budget) against the plain path
     (each job alone with its own optimiser, first come first served), on the
     same trace.  Per-iteration latency = device time of the step that ran the
-    iteration; per-job latency = completion - arrival."""
+    iteration; per-job latency = completion - arrival.  Returns a dict."""
     import torch
     import diffrender_tutorials_gb300 as D
-    from diffrender_tutorials_gb300 import build as B
-    B.build()
     torch.cuda.set_device(local)
-    setups = serve_setups(args, local)
+    setups = serve_setups(local, jobs, seed, rate, mix)
     n = len(setups)
     total_iters = sum(sp.steps for *_, sp in setups)
     # warm-up: load the kernels and the graph path once
     warm = D.OptimizationServer(device=local)
     for isc, cams, tgt, st, sp in setups[:2]:
-        warm.submit(isc, cams, tgt, st, serve_params(sp), args.warmup)
+        warm.submit(isc, cams, tgt, st, serve_params(sp), warmup)
     warm.wait(0)
     warm.close()
     torch.cuda.synchronize()
 
     # served
-    srv = D.OptimizationServer(device=local, hbm_budget_bytes=int(args.budget_gb * 1e9), max_jobs=args.slots)
+    srv = D.OptimizationServer(device=local, hbm_budget_bytes=int(budget_gb * 1e9), max_jobs=slots)
     k0 = D.kernel_launches()
     h2d = 0
     with ClockSampler(local) as clk:
@@ -841,21 +917,18 @@ def serve_arm(args, ws, rank, local, pg):
     pct = lambda xs, q: float(np.percentile(np.asarray(xs, np.float64), q))  # noqa: E731
     tris = [sp.triangles for *_, sp in setups]
     res = [sp.cams[0].width for *_, sp in setups]
-    line = {
-        "metric": "served fwd+adjoint iters/s", "value": served, "unit": "iters/s", "n_gpus": ws,
-        "steps": total_iters, "warmup": args.warmup, "ms_per_step": 1e3 / served, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded Poisson trace of displaced-sphere optimisation jobs)",
-        "config": {"workload": f"serve{n}_{'small_' if args.mix == 'small' else ''}poisson{args.rate:g}_displaced_spheres",
-                   "jobs": n, "rate_per_s": args.rate,
+    return {
+        "value": served, "unit": "iters/s", "steps": total_iters, "warmup": warmup,
+        "ms_per_step": 1e3 / served,
+        "config": {"workload": f"serve{n}_{'small_' if mix == 'small' else ''}poisson{rate:g}_displaced_spheres",
+                   "jobs": n, "rate_per_s": rate,
                    "triangles": [min(tris), max(tris)], "resolution": [min(res), max(res)],
                    "views": [min(len(sp.cams) for *_, sp in setups), max(len(sp.cams) for *_, sp in setups)],
                    "steps_per_job": [min(sp.steps for *_, sp in setups), max(sp.steps for *_, sp in setups)],
                    "models": sorted({D.SHADING_MODEL(sp.mode).name for *_, sp in setups}),
-                   "hbm_budget_gb": args.budget_gb, "slots": args.slots or "unlimited",
+                   "hbm_budget_gb": budget_gb, "slots": slots or "unlimited",
                    "l2": f"not flushed: back-to-back steps over a resident working set of "
-                         f"{stats['bytes_peak'] / 1e9:.2f} GB (> L2)",
-                   "parallelism": "replicas"},
+                         f"{stats['bytes_peak'] / 1e9:.2f} GB (> L2)"},
         "latency_ms": {"iteration_p50": pct(it_lat, 50), "iteration_p99": pct(it_lat, 99),
                        "job_p50": 1e3 * pct(job_lat, 50), "job_p99": 1e3 * pct(job_lat, 99)},
         "plain": {"value": plain, "unit": "iters/s", "how": "each job alone with its own optimiser graph, "
@@ -872,6 +945,19 @@ def serve_arm(args, ws, rank, local, pg):
                 "api": "drgb_server_submit/wait (host inputs copied at submission, results copied back)"},
         "clocks": clk.summary(), "gpu_launches": int(launches),
     }
+
+
+def serve_arm(args, ws, rank, local, pg):
+    from diffrender_tutorials_gb300 import build as B
+    B.build()
+    m = serve_measure(local, args.jobs, args.seed, args.rate, args.warmup, args.budget_gb, args.slots, args.mix)
+    line = {"metric": "served fwd+adjoint iters/s", "value": m.pop("value"), "unit": m.pop("unit"), "n_gpus": ws,
+            "steps": m.pop("steps"), "warmup": args.warmup, "ms_per_step": m.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Poisson trace of displaced-sphere optimisation jobs)",
+            "config": dict(m.pop("config"), parallelism="replicas")}
+    m.pop("warmup")
+    line.update(m)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -894,6 +980,8 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device memory budget")
     ap.add_argument("--slots", type=int, default=8, help="serving: resident jobs at most (0: no limit)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-patterns", action="store_true",
+                    help="default workload: leave out the batched, served and cube measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 1)
     ws, rank, local, pg = dist_setup()

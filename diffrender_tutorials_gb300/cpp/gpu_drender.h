@@ -27,8 +27,10 @@
 namespace diff_render {
 
 // Renderer on CUDA device `device`.  Models: SILHOUETTE, VERTEX_COLOR,
-// TEXTURE_COLOR, LAMBERT (the reference's numbering); others print an error
-// and the renderer stays unusable.
+// TEXTURE_COLOR, LAMBERT, PHONG, GGX (the reference's numbering), and the
+// point-light vertex-albedo (16) and diffuse path (17) models that have no
+// reference counterpart.  PATH_TEST and any other number print an error and
+// the renderer stays unusable.
 std::shared_ptr<IDiffRender> MakeGpuDifferentialRenderer(const DiffRenderSettings& settings, int device = 0);
 
 // OptSimple's loop with every iteration (render, loss, gradients, update,

@@ -140,6 +140,16 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         if (r->d_job.p) r->push_dev();
         break;
       }
+      case DRGB_OPT_TRACE_STEP_LIMIT:
+        require(value >= 0 && value <= (1 << 24), "traversal step limit: 1..16777216 (0: the default, 16777216)");
+        r->job.trace_limit = value ? (int)value : (1 << 24);
+        if (r->d_job.p) r->push_dev();
+        break;
+      case DRGB_OPT_EDGE_JACOBIAN:
+        require(value == 0 || value == 1, "edge Jacobian: 0 (the reference's edge_grad) or 1 (full 2x3)");
+        r->job.edge_exact = (int)value;
+        if (r->d_job.p) r->push_dev();
+        break;
       default: throw CudaError("unknown option", DRGB_ERR_INVALID);
     }
     r->graph_valid = false;

@@ -77,6 +77,7 @@ struct MeshDev {
   int64_t g_base;     // offset of this mesh's DMesh block in the flat gradient
   int pos_off, color_off, tex_off, tr_off;
   int n_vertices, n_instances;
+  int block0;         // flattened block of instance 0 (the instances' blocks follow it)
 };
 
 struct ModelParams {
@@ -104,6 +105,7 @@ struct JobDev {
   const BlockDev* blocks;
   const MeshDev* meshes;
   const float* tr_inv0;  // inverse transforms of mesh 0 (16 per instance)
+  const float* block_tr; // per block: transform (16, column-major), inverse transpose (16)
   // BVH: internal nodes (4 float4 each) and leaf triangles in leaf order
   const float4* nodes;
   const float4* tri;     // 3 float4 per leaf: (A, id bits), (e1), (e2)
@@ -120,6 +122,7 @@ struct JobDev {
                          // are read from the block's shared copy; 0: none staged
   const int* leaf_of;    // flattened triangle -> its leaf slot in `tri`
   int trace_bruteforce;  // 1: test every triangle (reference loop order)
+  int trace_limit;       // node pops per ray before the traversal gives up and raises ERR_TRAVERSAL_LIMIT
   // model
   int mode;
   int spp;               // requested spp (Hammersley count)
@@ -158,6 +161,7 @@ struct JobDev {
   int queue_cap;
   int edge_samples;
   const float* rnd;         // 2 * edge_samples replayed random numbers
+  int edge_exact;           // 1: full 2x3 screen Jacobian through the instance's own transform
   uint32_t edge_key_base;   // first queue-sort key of this job in a batch
   // optional work counters (rays, box tests, triangle tests); null normally
   unsigned long long* work;
@@ -728,7 +732,7 @@ __device__ DRGB_TRACE_ATTR bool trace(const JobDev& J, f3 o, f3 d, float tNear, 
     }
     if (sp == 0) break;
     node = DRGB_POP();
-    if (++guard > (1 << 24)) {
+    if (++guard > J.trace_limit) {
       atomicOr(J.err, ERR_TRAVERSAL_LIMIT);
       break;
     }

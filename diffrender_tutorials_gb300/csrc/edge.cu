@@ -224,16 +224,35 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
       const f3 v0 = ld3(J.pos, ed.x), v1 = ld3(J.pos, ed.y);
       const f3 g0x = vs_grad(cam, v0, false), g0y = vs_grad(cam, v0, true);
       const f3 g1x = vs_grad(cam, v1, false), g1y = vs_grad(cam, v1, true);
-      const float dv0_dx = g0x.x * d0x, dv0_dy = g0y.y * d0y, dv0_dz = (g0x.z * d0x + g0y.z * d0y);
-      const float dv1_dx = g1x.x * d1x, dv1_dy = g1y.y * d1y, dv1_dz = (g1x.z * d1x + g1y.z * d1y);
+      // world-space gradient of the two endpoints: the reference keeps dx/dX
+      // and dy/dY only for the x and y components (drender.cpp:45-51); the
+      // exact form is the full (dx,dy)/(X,Y,Z) Jacobian transposed
+      const bool exact = J.edge_exact;
+      const float dv0_dx = exact ? g0x.x * d0x + g0y.x * d0y : g0x.x * d0x;
+      const float dv0_dy = exact ? g0x.y * d0x + g0y.y * d0y : g0y.y * d0y;
+      const float dv0_dz = (g0x.z * d0x + g0y.z * d0y);
+      const float dv1_dx = exact ? g1x.x * d1x + g1y.x * d1y : g1x.x * d1x;
+      const float dv1_dy = exact ? g1x.y * d1x + g1y.y * d1y : g1y.y * d1y;
+      const float dv1_dz = (g1x.z * d1x + g1y.z * d1y);
       const MeshDev& md = J.meshes[mi.x];
       if (md.dslot >= 0) {
-        const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
         float* g = J.grad + md.g_base + md.pos_off;
-        const f3 d0 = mk(M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz,
-                         M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
-        const f3 d1 = mk(M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz,
-                         M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+        f3 d0, d1;
+        if (exact) {
+          // to mesh-local positions: the transpose of the edge's own instance
+          // transform (world = T * local)
+          const float* T = J.block_tr + 32 * (md.block0 + mi.y);
+          d0 = mk(T[0] * dv0_dx + T[1] * dv0_dy + T[2] * dv0_dz, T[4] * dv0_dx + T[5] * dv0_dy + T[6] * dv0_dz,
+                  T[8] * dv0_dx + T[9] * dv0_dy + T[10] * dv0_dz);
+          d1 = mk(T[0] * dv1_dx + T[1] * dv1_dy + T[2] * dv1_dz, T[4] * dv1_dx + T[5] * dv1_dy + T[6] * dv1_dz,
+                  T[8] * dv1_dx + T[9] * dv1_dy + T[10] * dv1_dz);
+        } else {
+          const float* M = J.tr_inv0 + 16 * mi.y;  // get_transform_inv(0)[inst]
+          d0 = mk(M[0] * dv0_dx + M[4] * dv0_dy + M[8] * dv0_dz, M[1] * dv0_dx + M[5] * dv0_dy + M[9] * dv0_dz,
+                  M[2] * dv0_dx + M[6] * dv0_dy + M[10] * dv0_dz);
+          d1 = mk(M[0] * dv1_dx + M[4] * dv1_dy + M[8] * dv1_dz, M[1] * dv1_dx + M[5] * dv1_dy + M[9] * dv1_dz,
+                  M[2] * dv1_dx + M[6] * dv1_dy + M[10] * dv1_dz);
+        }
         if (!(DET && J.det)) {
           atomicAdd(g + ed.z * 3 + 0, d0.x);
           atomicAdd(g + ed.z * 3 + 1, d0.y);

@@ -305,18 +305,17 @@ int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<
   return off;
 }
 
-// Unique edges of the differentiable meshes ordered by (v0, v1) global ids,
-// the first inserted kept on duplicates (std::set<Edge>, drender.h:244-299).
-void build_edges(Job& J) {
+// Unique edges of the meshes of `lay` ordered by (v0, v1) global ids, the
+// first inserted kept on duplicates (std::set<Edge>, drender.h:244-299);
+// insertion runs over meshes, then instances, then triangles.
+void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi) {
   std::vector<int> key;
-  for (auto& L : J.dlay) key.push_back(L.mesh_id);
+  for (auto& L : lay) key.push_back(L.mesh_id);
   std::sort(key.begin(), key.end());
-  if (key == J.edge_ids_key && (J.n_edges > 0 || key.empty())) return;
   struct E {
-    int v0, v1, vn0, vn1, mesh, inst, order;
+    int v0, v1, vn0, vn1, mesh, inst;
   };
   std::vector<E> all;
-  int order = 0;
   for (int m = 0; m < (int)J.meshes.size(); m++) {
     if (!std::binary_search(key.begin(), key.end(), m)) continue;
     const MeshState& M = J.meshes[m];
@@ -330,8 +329,8 @@ void build_edges(Job& J) {
         for (int e = 0; e < 3; e++) {
           const int a = n[e], c = n[(e + 1) % 3];
           const int ga = off + a, gc = off + c;
-          if (ga < gc) all.push_back(E{ga, gc, a, c, m, j, order++});
-          else all.push_back(E{gc, ga, c, a, m, j, order++});
+          if (ga < gc) all.push_back(E{ga, gc, a, c, m, j});
+          else all.push_back(E{gc, ga, c, a, m, j});
         }
       }
     }
@@ -339,18 +338,34 @@ void build_edges(Job& J) {
   std::stable_sort(all.begin(), all.end(), [](const E& x, const E& y) {
     return x.v0 != y.v0 ? x.v0 < y.v0 : x.v1 < y.v1;
   });
+  ed.clear();
+  mi.clear();
+  for (const E& e : all) {
+    if (!ed.empty() && ed.back().x == e.v0 && ed.back().y == e.v1) continue;
+    ed.push_back(make_int4(e.v0, e.v1, e.vn0, e.vn1));
+    mi.push_back(make_int2(e.mesh, e.inst));
+  }
+}
+
+void build_edges(Job& J) {
+  std::vector<int> key;
+  for (auto& L : J.dlay) key.push_back(L.mesh_id);
+  std::sort(key.begin(), key.end());
+  if (key == J.edge_ids_key && (J.n_edges > 0 || key.empty())) return;
   std::vector<int4> ed;
   std::vector<int2> mi;
-  for (size_t i = 0; i < all.size(); i++) {
-    if (!ed.empty() && ed.back().x == all[i].v0 && ed.back().y == all[i].v1) continue;
-    ed.push_back(make_int4(all[i].v0, all[i].v1, all[i].vn0, all[i].vn1));
-    mi.push_back(make_int2(all[i].mesh, all[i].inst));
-  }
+  edge_list(J, J.dlay, ed, mi);
   J.n_edges = (int)ed.size();
   J.edges.upload(ed.data(), ed.size(), 0);
   J.edge_mi.upload(mi.data(), mi.size(), 0);
   DRGB_CUDA(cudaStreamSynchronize(0));
   J.edge_ids_key = key;
+}
+
+int first_block(const Job& J, int mesh) {
+  for (int b = 0; b < J.n_blocks; b++)
+    if (J.h_blocks[b].mesh == mesh) return b;
+  return 0;
 }
 
 void set_dscene(Job& J, const int32_t* ids, int n_ids) {
@@ -372,6 +387,7 @@ void set_dscene(Job& J, const int32_t* ids, int n_ids) {
     d.tr_off = 0;
     d.n_vertices = M.nv;
     d.n_instances = M.n_inst;
+    d.block0 = first_block(J, (int)m);
   }
   for (size_t k = 0; k < J.dlay.size(); k++) {
     const DLayout& L = J.dlay[k];
@@ -420,6 +436,7 @@ void sync_dev(Job& J) {
   d.blocks = J.blocks.p;
   d.meshes = J.meshdev.p;
   d.tr_inv0 = J.tr_inv0.p;
+  d.block_tr = J.block_tr.p;
   d.nodes = J.nodes.p;
   d.nodes4 = J.nodes4.p;
   d.tri = J.tri.p;
@@ -432,6 +449,8 @@ void sync_dev(Job& J) {
 #endif
   d.root = J.root;
   d.trace_bruteforce = J.trace_bruteforce;
+  d.trace_limit = J.trace_limit;
+  d.edge_exact = J.edge_exact;
   d.mode = J.mode;
   d.spp = J.spp;
   d.sq = J.sq;
@@ -499,6 +518,17 @@ static void prng_stream(int seed, int count, float* out) {
   }
 }
 
+void edge_random_host(int n, std::vector<float>& h) {
+  h.assign(2 * (size_t)std::max(n, 1), 0.0f);
+  const int T = 14;
+  const int64_t q = n / T, r = n % T;
+  for (int k = 0; k < T; k++) {
+    const int64_t b = q * k + std::min<int64_t>(k, r);
+    const int64_t cnt = q + (k < r ? 1 : 0);
+    if (cnt > 0) prng_stream(7777 + k * k + 1, (int)(2 * cnt), h.data() + 2 * b);
+  }
+}
+
 const float* edge_random_table(int n, cudaStream_t s) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, DevBuf<float>*> cache;
@@ -507,14 +537,8 @@ const float* edge_random_table(int n, cudaStream_t s) {
   std::lock_guard<std::mutex> lk(mu);
   auto it = cache.find({dev, n});
   if (it != cache.end()) return it->second->p;
-  std::vector<float> h(2 * (size_t)std::max(n, 1), 0.0f);
-  const int T = 14;
-  const int64_t q = n / T, r = n % T;
-  for (int k = 0; k < T; k++) {
-    const int64_t b = q * k + std::min<int64_t>(k, r);
-    const int64_t cnt = q + (k < r ? 1 : 0);
-    if (cnt > 0) prng_stream(7777 + k * k + 1, (int)(2 * cnt), h.data() + 2 * b);
-  }
+  std::vector<float> h;
+  edge_random_host(n, h);
   auto* buf = new DevBuf<float>();
   buf->upload(h.data(), h.size(), s);
   DRGB_CUDA(cudaStreamSynchronize(s));

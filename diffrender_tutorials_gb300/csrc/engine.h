@@ -154,6 +154,8 @@ struct Job {
   int spp = 1, sq = 1, S = 1;
   ModelParams mp{};
   int trace_bruteforce = 0;
+  int trace_limit = 1 << 24;  // node pops per ray (DRGB_OPT_TRACE_STEP_LIMIT)
+  int edge_exact = 0;         // DRGB_OPT_EDGE_JACOBIAN
   int tile_w = 4, tile_h = 4;
   // scene
   bool committed = false;
@@ -257,6 +259,10 @@ void setup_views(Job& J, const drgb_camera* cams, int n_views);
 void sync_dev(Job& J);
 void set_dscene(Job& J, const int32_t* ids, int n_ids);
 void build_edges(Job& J);
+// Flattened block of instance 0 of a mesh (its instances' blocks follow).
+int first_block(const Job& J, int mesh);
+// The edge list of the meshes of `lay` (host vectors; build_edges uploads it).
+void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi);
 int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out,
                        int64_t* alloc_total = nullptr);
 // TransformR::to_mat on the host (column-major, LiteMath's rounding).
@@ -315,5 +321,7 @@ constexpr int kSortGrid = 512;  // blocks of sort_pairs_device (its histogram ha
 
 // edge random table shared by every job with the same sample count
 const float* edge_random_table(int n, cudaStream_t s);
+// The same 2n replayed random numbers in a host vector.
+void edge_random_host(int n, std::vector<float>& out);
 
 }  // namespace drgb

@@ -1,12 +1,12 @@
 // drgb_d_render_and_compare_noalloc: forward + loss + interior adjoint + edge
 // term without allocating GPU memory during the call.
 //
-// Who needs it: callers that may not call cudaMalloc while they run -- code
-// that records work into a CUDA stream capture (a cudaMalloc during capture
-// invalidates it), engines that hand out all device memory from their own
-// pool or budget and forbid allocations after start-up, and latency-bound
-// loops where an allocation (and the device synchronisation it can cause)
-// is too costly.  drgb_d_render_and_compare_device grows its per-call
+// Who needs it: programs that hand out all device memory from a pool or
+// budget of their own and forbid allocations once they run -- an engine or
+// a server that sizes its HBM at start-up and treats a later cudaMalloc as
+// an error -- and loops that must not pay for an allocation, nor for the
+// device-wide synchronisation that cudaMalloc and cudaFree can cause, in
+// the middle of a run.  drgb_d_render_and_compare_device grows its per-call
 // buffers with cudaMalloc on first use; this variant takes every per-call
 // buffer from one fixed array compiled into the library instead.
 //
@@ -15,17 +15,21 @@
 //    images, edge-sample queue, tile partials, projected vertices, edge
 //    sampler, random streams) need more is rejected with DRGB_ERR_INVALID;
 //    roughly one 512x512 view with 262,144 edge samples fits;
-//  * every GPU that loads the library reserves the array until the process
-//    exits;
+//  * the first call on a device looks the array's device address up with
+//    cudaGetSymbolAddress (the CUDA runtime may load the array onto that
+//    device only then); make that first call before any stream capture.
+//    From then on the array stays on the device until the process exits;
 //  * all calls share the one array and it keeps the previous call's
 //    contents: each call clears what must start at zero (the caller's
 //    gradient vector, the sample-queue and work-queue counters) and rewrites
 //    the rest, so calls that overlap on the GPU -- from two host threads, or
 //    enqueued on different streams without ordering -- race on it;
-//  * the first call on a device looks the array's device address up with
-//    cudaGetSymbolAddress; make that first call before any stream capture.
-// The renderer itself (scene, LBVH, model constants) must have been committed
-// beforehand; that set-up allocates as usual.
+//  * host cost per call: the edge list (a sort of 3 x triangles entries) and
+//    the 2 x edge_samples replayed random numbers are rebuilt on the host and
+//    copied from pageable memory, and the call waits for its stream at the
+//    end to read the kernels' error flag.
+// The renderer itself (scene, hierarchy, model constants) must have been
+// committed beforehand; that set-up allocates as usual.
 #include <mutex>
 
 #include "renderer.h"
@@ -67,69 +71,6 @@ struct Carve {
   }
 };
 
-// Unique edges of the differentiable meshes ordered by (v0, v1), the first
-// inserted kept (same list as the allocating path builds).
-void host_edges(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi) {
-  std::vector<int> key;
-  for (auto& L : lay) key.push_back(L.mesh_id);
-  std::sort(key.begin(), key.end());
-  struct E {
-    int v0, v1, vn0, vn1, mesh, inst;
-  };
-  std::vector<E> all;
-  for (int b = 0; b < J.n_blocks; b++) {
-    const BlockDev& bd = J.h_blocks[b];
-    if (!std::binary_search(key.begin(), key.end(), bd.mesh)) continue;
-    const MeshState& M = J.meshes[bd.mesh];
-    for (int k = 0; k + 2 < M.ni; k += 3) {
-      const int n[3] = {(int)M.h_indices[k], (int)M.h_indices[k + 1], (int)M.h_indices[k + 2]};
-      for (int e = 0; e < 3; e++) {
-        const int a = n[e], c = n[(e + 1) % 3];
-        const int ga = bd.vert_off + a, gc = bd.vert_off + c;
-        if (ga < gc) all.push_back(E{ga, gc, a, c, bd.mesh, bd.inst});
-        else all.push_back(E{gc, ga, c, a, bd.mesh, bd.inst});
-      }
-    }
-  }
-  std::stable_sort(all.begin(), all.end(), [](const E& x, const E& y) {
-    return x.v0 != y.v0 ? x.v0 < y.v0 : x.v1 < y.v1;
-  });
-  ed.clear();
-  mi.clear();
-  for (const E& e : all) {
-    if (!ed.empty() && ed.back().x == e.v0 && ed.back().y == e.v1) continue;
-    ed.push_back(make_int4(e.v0, e.v1, e.vn0, e.vn1));
-    mi.push_back(make_int2(e.mesh, e.inst));
-  }
-}
-
-// Replayed edge-sampler streams (prng stream 7777+k^2+1 of each of the 14
-// static OpenMP blocks), written into a host vector.
-void host_random_table(int n, std::vector<float>& out) {
-  out.assign(2 * (size_t)std::max(n, 1), 0.0f);
-  const int T = 14;
-  const int64_t q = n / T, r = n % T;
-  for (int k = 0; k < T; k++) {
-    const int64_t b = q * k + std::min<int64_t>(k, r);
-    const int64_t cnt = q + (k < r ? 1 : 0);
-    const uint32_t us = (uint32_t)(7777 + k * k + 1);
-    uint32_t sx = us * (us * us * 15731u + 74323u) + 871483u;
-    uint32_t sy = us * (us * us * 13734u + 37828u) + 234234u;
-    for (int i = 0; i < (int)(us % 7u); i++) {
-      const uint32_t x = sx * 17u + sy * 13123u;
-      sx = (x << 13) ^ x;
-      sy ^= (x << 7);
-    }
-    for (int64_t j = 0; j < 2 * cnt; j++) {
-      const uint32_t x = sx * 17u + sy * 13123u;
-      sx = (x << 13) ^ x;
-      sy ^= (x << 7);
-      const uint32_t tmp = (x * (x * x * 15731u + 74323u) + 871483u);
-      out[2 * b + j] = (float)tmp * (1.0f / 4294967296.0f);
-    }
-  }
-}
-
 }  // namespace
 }  // namespace drgb
 
@@ -169,7 +110,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     std::vector<MeshDev> md(J.meshes.size());
     for (size_t m = 0; m < J.meshes.size(); m++) {
       const MeshState& M = J.meshes[m];
-      md[m] = MeshDev{M.texture.p, M.tex_w, M.tex_h, M.tex_c, -1, 0, 0, -1, -1, 0, M.nv, M.n_inst};
+      md[m] = MeshDev{M.texture.p, M.tex_w, M.tex_h, M.tex_c, -1, 0, 0, -1, -1, 0, M.nv, M.n_inst, first_block(J, (int)m)};
     }
     for (size_t k = 0; k < lay.size(); k++) {
       MeshDev& d = md[lay[k].mesh_id];
@@ -182,10 +123,10 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     }
     std::vector<int4> ed;
     std::vector<int2> emi;
-    host_edges(J, lay, ed, emi);
+    edge_list(J, lay, ed, emi);
     const int E = (int)ed.size();
     std::vector<float> rnd;
-    if (edge_samples > 0) host_random_table(edge_samples, rnd);
+    if (edge_samples > 0) edge_random_host(edge_samples, rnd);
 
     // ---- carve the scratch array ----
     Carve c;
@@ -227,12 +168,15 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.blocks = J.blocks.p;
     d.meshes = reinterpret_cast<const MeshDev*>(base + o_md);
     d.tr_inv0 = J.tr_inv0.p;
+    d.block_tr = J.block_tr.p;
     d.nodes = J.nodes.p;
     d.nodes4 = J.nodes4.p;
     d.tri = J.tri.p;
     d.leaf_of = J.leaf_of.p;
     d.root = J.root;
     d.trace_bruteforce = J.trace_bruteforce;
+    d.trace_limit = J.trace_limit;
+    d.edge_exact = J.edge_exact;
     d.mode = J.mode;
     d.spp = J.spp;
     d.sq = J.sq;

@@ -104,7 +104,7 @@ __device__ DRGB_TRACE_ATTR bool trace_warp(const JobDev& J, f3 o, f3 d, float tN
     if (sp == 0) break;
     sp--;
     node = __shfl_sync(FULL, sp < 32 ? s0 : s1, sp & 31);
-    if (++guard > (1 << 24)) {
+    if (++guard > J.trace_limit) {
       if (lane == 0) atomicOr(J.err, ERR_TRAVERSAL_LIMIT);
       break;
     }
@@ -227,6 +227,31 @@ __device__ __forceinline__ float rnd01(uint32_t a, uint32_t b, uint32_t c) {
   return (float)(h >> 8) * (1.0f / 16777216.0f);
 }
 
+// sin and cos of 2*pi*x for x in [0, 1) (the bounce azimuth).  x*4 and its
+// nearest integer q are exact, so is f = 4x - q in [-1/2, 1/2]; a = f*pi/2
+// then lies in [-pi/4, pi/4], where the Taylor series of sin to a^9 and of
+// cos to a^10 are accurate to 2e-9, and the quadrant q turns (sin a, cos a)
+// into (sin, cos) of the full angle.  Plain multiplies and adds in a fixed
+// order (no contraction): the oracle evaluates the same sequence, so both
+// sides draw bit-identical bounce directions, which the math library's
+// sinf/cosf (different on host and device) would not give.
+__device__ __forceinline__ void sincos_turns(float x, float* s, float* c) {
+  const float x4 = x * 4.0f;
+  const float q = rintf(x4);
+  const float a = (x4 - q) * 1.57079633f;
+  const float a2 = a * a;
+  const float ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f +
+                                                                                   a2 * 2.75573188e-6f))));
+  const float pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
+                                                                                          a2 * -2.75573188e-7f))));
+  switch (((int)q) & 3) {
+    case 0: *s = ps; *c = pc; break;
+    case 1: *s = pc; *c = -ps; break;
+    case 2: *s = -ps; *c = -pc; break;
+    default: *s = -pc; *c = ps; break;
+  }
+}
+
 // Fixed-depth diffuse path tracer (same definition as the oracle's
 // path_diffuse): point light, Lambert BRDF, cosine-weighted bounces.
 // `alive` = the camera ray hit; the bounce loop runs the same number of
@@ -283,12 +308,13 @@ __device__ inline f3 path_diffuse_p(const JobDev& J, const Surf& first, uint32_t
     if (hitb) {
       const float r1 = rnd01(key, (uint32_t)bounce, J.mp.seed);
       const float r2 = rnd01(key, (uint32_t)bounce + 1000u, J.mp.seed);
-      const float phi = 6.28318531f * r1;
+      float sphi, cphi;
+      sincos_turns(r1, &sphi, &cphi);  // azimuth 2*pi*r1
       const float sr = sqrtf(r2);
       const f3 a = fabsf(n.x) > 0.5f ? mk(0, 1, 0) : mk(1, 0, 0);
       const f3 ex = normalize(cross(a, n));
       const f3 ey = cross(n, ex);
-      const float lx = sr * cosf(phi), ly = sr * sinf(phi), lz = sqrtf(ref_max(0.0f, 1.0f - r2));
+      const float lx = sr * cphi, ly = sr * sphi, lz = sqrtf(ref_max(0.0f, 1.0f - r2));
       rd = normalize((ex * lx + ey * ly) + n * lz);
       ro = p;
       beta_na = bounce == 0 ? beta_na : beta_na * alb;

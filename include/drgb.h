@@ -74,7 +74,7 @@ enum {
                                     per mesh, shared by its instances, under one over the instances); 3 always
                                     one hierarchy over every triangle.  Boxes are refitted on the device
                                     either way, and a commit of the same triangles keeps the topology */
-  DRGB_OPT_BVH_REBUILD = 10      /* optimiser (and batch, for every job): rebuild the hierarchy topology from
+  DRGB_OPT_BVH_REBUILD = 10,     /* optimiser (and batch, for every job): rebuild the hierarchy topology from
                                     the current vertices every N iterations (default 100; 0: refit only).
                                     The host build overlaps the following iterations; the optimiser uses the
                                     new topology from N/2 iterations after the start on (fixed, not timing
@@ -82,6 +82,16 @@ enum {
                                     Refitted boxes of moving vertices overlap more and more (icosphere
                                     workload: 55 box tests per ray after 500 steps against 47 with
                                     rebuilds); the hit set does not depend on the topology. */
+  DRGB_OPT_TRACE_STEP_LIMIT = 11, /* node visits one ray may make before its traversal gives up (default and
+                                    maximum 16,777,216).  A ray that reaches the limit stops with the nearest
+                                    hit found so far and the call returns DRGB_ERR_KERNEL ("traversal step
+                                    limit"); the renderer stays usable.  The reference has no such bound: its
+                                    caster loops over every triangle (raytrace3d_bf.cpp:102-156). */
+  DRGB_OPT_EDGE_JACOBIAN = 12    /* chain rule of the edge term from pixel to vertex positions: 0 (default)
+                                    the reference's edge_grad (drender.cpp:31-87): dx/dX and dy/dY only for
+                                    the x and y components, through mesh 0's inverse transform; 1 the full
+                                    2x3 Jacobian of each endpoint's pixel position, through the transpose of
+                                    the edge's own instance transform (exact for any camera and instance) */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -201,16 +211,19 @@ int drgb_d_render_and_compare_device(drgb_renderer* r, const drgb_camera* cams, 
 /* No counterpart in the reference.  The same computation and outputs as
  * drgb_d_render_and_compare_device (gradient vector and loss written to
  * caller-owned device memory), for callers that cannot allocate GPU memory
- * while they run: code recording into a CUDA stream capture, engines that
- * own all device memory through a fixed pool, latency-bound loops.  The call
- * itself makes no cudaMalloc/cudaFree; its per-call buffers come from one
- * 32 MiB array compiled into the library (reserved on every GPU that loads
- * it, until exit).  Calls needing more (roughly: beyond one 512x512 view
- * with 262,144 edge samples) return DRGB_ERR_INVALID.  All calls share that
- * array, so calls that overlap on the GPU race; the first call on a device
- * looks its address up and should come before any stream capture.  The
- * scene must have been committed (drgb_commit) beforehand; returns after
- * the results are in device memory. */
+ * while they run: programs that take all device memory from a pool or
+ * budget of their own and forbid cudaMalloc after start-up, and loops that
+ * must not pay for an allocation (or the synchronisation it can cause)
+ * mid-run.  The call makes no cudaMalloc/cudaFree; its per-call buffers come
+ * from one 32 MiB array compiled into the library.  The first call on a
+ * device looks the array's address up (the runtime may load the array onto
+ * the device then; it stays until exit); make that first call before any
+ * stream capture.  Calls needing more than the array (roughly: beyond one
+ * 512x512 view with 262,144 edge samples) return DRGB_ERR_INVALID.  All
+ * calls share the array, so calls that overlap on the GPU race.  Each call
+ * rebuilds the edge list and the replayed random numbers on the host, copies
+ * them from pageable memory and waits for the renderer's stream before it
+ * returns.  The scene must have been committed (drgb_commit) beforehand. */
 int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_camera* cams, const float* d_targets,
                                       int n_views, int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids,
                                       float* d_dscene, float* d_loss);

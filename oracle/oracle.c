@@ -541,6 +541,7 @@ void orc_default_model_params(orc_model_params* p) {
   p->ambient = 0.1f;
   p->path_depth = 2;
   p->seed = 1u;
+  p->edge_jacobian = 0;
 }
 
 /* sample_bilinear_clamp_3f, shade_common.cpp:3-21 */
@@ -641,6 +642,28 @@ static float lpv_factor(const ctx_t* c, const surf_t* sf) {
   return vis * c->mp->light_intensity * ndl / d2 + c->mp->ambient;
 }
 
+/* sin and cos of 2*pi*x, x in [0, 1): exact quadrant split (x*4, its nearest
+ * integer q and 4x - q are exact), Taylor series of sin to a^9 and cos to
+ * a^10 on a = (4x - q)*pi/2 in [-pi/4, pi/4] (error < 2e-9), rotated by the
+ * quadrant.  The CUDA path evaluates the same operations in the same order,
+ * so the bounce directions are bit-identical on both sides. */
+static void sincos_turns(float x, float* s, float* c) {
+  const float x4 = x * 4.0f;
+  const float q = rintf(x4);
+  const float a = (x4 - q) * 1.57079633f;
+  const float a2 = a * a;
+  const float ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f +
+                                                                                   a2 * 2.75573188e-6f))));
+  const float pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
+                                                                                          a2 * -2.75573188e-7f))));
+  switch (((int)q) & 3) {
+    case 0: *s = ps; *c = pc; break;
+    case 1: *s = pc; *c = -ps; break;
+    case 2: *s = -ps; *c = -pc; break;
+    default: *s = -pc; *c = ps; break;
+  }
+}
+
 /* Fixed-depth diffuse path tracer (no reference counterpart; structure of
  * shade<PATH_TEST>, shade_path_test.cpp:232-282, with a counter-based RNG
  * and `path_depth` bounces).  Returns radiance and the albedo-weighted
@@ -689,12 +712,13 @@ static f3 path_diffuse(const ctx_t* c, const surf_t* first, uint32_t sample_key,
     /* cosine-weighted bounce: throughput *= albedo (pdf cancels cos/pi) */
     const float r1 = rnd01(sample_key, (uint32_t)bounce, c->mp->seed);
     const float r2 = rnd01(sample_key, (uint32_t)bounce + 1000u, c->mp->seed);
-    const float phi = 6.28318531f * r1;
+    float sphi, cphi;
+    sincos_turns(r1, &sphi, &cphi); /* azimuth 2*pi*r1 */
     const float sr = sqrtf(r2);
     const f3 a = fabsf(n.x) > 0.5f ? v3(0, 1, 0) : v3(1, 0, 0);
     const f3 ex = norm3(cross3(a, n));
     const f3 ey = cross3(n, ex);
-    const float lx = sr * cosf(phi), ly = sr * sinf(phi), lz = sqrtf(maxf_ref(0.0f, 1.0f - r2));
+    const float lx = sr * cphi, ly = sr * sphi, lz = sqrtf(maxf_ref(0.0f, 1.0f - r2));
     rd = norm3(add3(add3(scl3(ex, lx), scl3(ey, ly)), scl3(n, lz)));
     ro = p;
     beta_noalb0 = bounce == 0 ? beta_noalb0 : mul3(beta_noalb0, alb);
@@ -1212,22 +1236,44 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
       vs_grad(cam, v0_3d, 1, g0y);
       vs_grad(cam, v1_3d, 0, g1x);
       vs_grad(cam, v1_3d, 1, g1y);
-      const float dv0_dx = g0x[0] * d0x;
-      const float dv0_dy = g0y[1] * d0y;
+      const int exact = mp->edge_jacobian != 0;
+      float dv0_dx, dv0_dy, dv1_dx, dv1_dy;
+      if (exact) {
+        /* no reference counterpart: the full Jacobian of the endpoint's pixel
+         * position, transposed (world-space gradient of each endpoint) */
+        dv0_dx = g0x[0] * d0x + g0y[0] * d0y;
+        dv0_dy = g0x[1] * d0x + g0y[1] * d0y;
+        dv1_dx = g1x[0] * d1x + g1y[0] * d1y;
+        dv1_dy = g1x[1] * d1x + g1y[1] * d1y;
+      } else {
+        dv0_dx = g0x[0] * d0x;
+        dv0_dy = g0y[1] * d0y;
+        dv1_dx = g1x[0] * d1x;
+        dv1_dy = g1y[1] * d1y;
+      }
       const float dv0_dz = (g0x[2] * d0x + g0y[2] * d0y);
-      const float dv1_dx = g1x[0] * d1x;
-      const float dv1_dy = g1y[1] * d1y;
       const float dv1_dz = (g1x[2] * d1x + g1y[2] * d1y);
       const int slot = dm->by_mesh[ed.mesh];
-      const float* tr = tr_inv0 + 16 * ed.inst; /* get_transform_inv(0)[inst] */
       const f3 v0o = s->orig[ed.v0], v1o = s->orig[ed.v1];
       float* P = my_pos + pos_base[slot];
-      P[ed.vn0 * 3 + 0] += M(tr, 0, 0) * dv0_dx + M(tr, 0, 1) * dv0_dy + M(tr, 0, 2) * dv0_dz;
-      P[ed.vn0 * 3 + 1] += M(tr, 1, 0) * dv0_dx + M(tr, 1, 1) * dv0_dy + M(tr, 1, 2) * dv0_dz;
-      P[ed.vn0 * 3 + 2] += M(tr, 2, 0) * dv0_dx + M(tr, 2, 1) * dv0_dy + M(tr, 2, 2) * dv0_dz;
-      P[ed.vn1 * 3 + 0] += M(tr, 0, 0) * dv1_dx + M(tr, 0, 1) * dv1_dy + M(tr, 0, 2) * dv1_dz;
-      P[ed.vn1 * 3 + 1] += M(tr, 1, 0) * dv1_dx + M(tr, 1, 1) * dv1_dy + M(tr, 1, 2) * dv1_dz;
-      P[ed.vn1 * 3 + 2] += M(tr, 2, 0) * dv1_dx + M(tr, 2, 1) * dv1_dy + M(tr, 2, 2) * dv1_dz;
+      if (exact) {
+        /* world = T * local: the transpose of the edge's own instance transform */
+        const float* T = s->tr + 16 * (s->mesh_block0[ed.mesh] + ed.inst);
+        P[ed.vn0 * 3 + 0] += M(T, 0, 0) * dv0_dx + M(T, 1, 0) * dv0_dy + M(T, 2, 0) * dv0_dz;
+        P[ed.vn0 * 3 + 1] += M(T, 0, 1) * dv0_dx + M(T, 1, 1) * dv0_dy + M(T, 2, 1) * dv0_dz;
+        P[ed.vn0 * 3 + 2] += M(T, 0, 2) * dv0_dx + M(T, 1, 2) * dv0_dy + M(T, 2, 2) * dv0_dz;
+        P[ed.vn1 * 3 + 0] += M(T, 0, 0) * dv1_dx + M(T, 1, 0) * dv1_dy + M(T, 2, 0) * dv1_dz;
+        P[ed.vn1 * 3 + 1] += M(T, 0, 1) * dv1_dx + M(T, 1, 1) * dv1_dy + M(T, 2, 1) * dv1_dz;
+        P[ed.vn1 * 3 + 2] += M(T, 0, 2) * dv1_dx + M(T, 1, 2) * dv1_dy + M(T, 2, 2) * dv1_dz;
+      } else {
+        const float* tr = tr_inv0 + 16 * ed.inst; /* get_transform_inv(0)[inst] */
+        P[ed.vn0 * 3 + 0] += M(tr, 0, 0) * dv0_dx + M(tr, 0, 1) * dv0_dy + M(tr, 0, 2) * dv0_dz;
+        P[ed.vn0 * 3 + 1] += M(tr, 1, 0) * dv0_dx + M(tr, 1, 1) * dv0_dy + M(tr, 1, 2) * dv0_dz;
+        P[ed.vn0 * 3 + 2] += M(tr, 2, 0) * dv0_dx + M(tr, 2, 1) * dv0_dy + M(tr, 2, 2) * dv0_dz;
+        P[ed.vn1 * 3 + 0] += M(tr, 0, 0) * dv1_dx + M(tr, 0, 1) * dv1_dy + M(tr, 0, 2) * dv1_dz;
+        P[ed.vn1 * 3 + 1] += M(tr, 1, 0) * dv1_dx + M(tr, 1, 1) * dv1_dy + M(tr, 1, 2) * dv1_dz;
+        P[ed.vn1 * 3 + 2] += M(tr, 2, 0) * dv1_dx + M(tr, 2, 1) * dv1_dy + M(tr, 2, 2) * dv1_dz;
+      }
       float* T = my_tr + tr_base[slot] + 12 * ed.inst;
       T[0] += v0o.x * dv0_dx + v1o.x * dv1_dx;
       T[1] += v0o.y * dv0_dx + v1o.y * dv1_dx;

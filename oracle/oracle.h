@@ -66,6 +66,9 @@ typedef struct orc_model_params {
   float ambient;
   int32_t path_depth; /* bounces after the primary hit */
   uint32_t seed;
+  /* edge-term chain rule: 0 the reference's edge_grad (drender.cpp:31-87),
+   * 1 the full 2x3 screen Jacobian through the instance's own transform */
+  int32_t edge_jacobian;
 } orc_model_params;
 
 void orc_default_model_params(orc_model_params* p);

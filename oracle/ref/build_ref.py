@@ -28,8 +28,11 @@ import shutil
 import subprocess
 import sys
 
-REF_ROOT = os.environ.get("DRGB_REFERENCE_ROOT", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout: $DRGB_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's root
+REF_ROOT = os.environ.get("DRGB_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference"))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 # objects and binaries per machine architecture (the source copy is shared)

@@ -89,11 +89,14 @@ def test_path_model_gradient_vs_oracle():
     imgs = np.zeros(tgt.size, np.float32)
     loss = r.d_render_and_compare(isc, cams, tgt, 40 * 40, ds, out_images=imgs)
     oloss, ods, oimgs = O.d_render_and_compare(isc, cams, 17, 4, tgt, 40 * 40)
-    # transcendental functions differ in the last bit between libm and CUDA,
-    # which moves a few bounce directions
-    assert np.abs(imgs - oimgs).mean() < 1e-4
-    assert loss == pytest.approx(oloss, rel=1e-2)
-    assert_grad_close(ds.data, ods, ds.layout, edge_tol=5e-2, interior_tol=1e-2)
+    # the bounce directions come from the same counter-based random numbers
+    # and the same sin/cos polynomial on both sides, so the images agree
+    # per pixel
+    diff = np.abs(imgs - oimgs)
+    print(f"path model vs oracle: image max abs {diff.max():.3g} ({int((diff > 0).sum())} values differ)")
+    assert diff.max() <= 1e-4, (float(diff.max()), int((diff > 0).sum()))
+    assert loss == pytest.approx(oloss, rel=1e-5)
+    assert_grad_close(ds.data, ods, ds.layout)
 
 
 def silhouette_coords(isc, cams, n, rng):

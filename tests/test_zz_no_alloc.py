@@ -1,9 +1,16 @@
 """drgb_d_render_and_compare_noalloc against drgb_d_render_and_compare_device.
 
 The no-allocation entry point serves callers that cannot allocate GPU memory
-while they run (stream capture, fixed memory pools); it must produce the same
-loss and gradient as the allocating device-pointer entry point, call after
-call, and allocate nothing.  This file is collected last on purpose.
+while they run (programs that take all device memory from their own pool or
+budget, loops that must not pay for an allocation mid-run).  It must produce
+the same loss and gradient as the allocating device-pointer entry point,
+call after call, and allocate nothing.  Both entry points shade the same
+edge list with the same replayed random numbers and the same samples; only
+the order of the float atomics differs, so the results agree to float
+rounding.  The first call on a device may load the library's fixed array
+onto it (the runtime does that when its address is looked up), so the
+no-allocation check is made on the second call.  This file is collected last
+on purpose.
 """
 import ctypes as C
 
@@ -16,8 +23,7 @@ from diffrender_tutorials_gb300.api import make_cameras
 
 pytestmark = pytest.mark.gpu
 
-EDGE_TOL = 1e-2      # relative L2, position/transform block (edge term)
-INTERIOR_TOL = 1e-3  # relative L2, colour block (interior term)
+TOL = 1e-5  # relative L2 of each gradient block: the same sums in another atomic order
 
 
 def _rel(a, b):
@@ -70,8 +76,8 @@ def test_noalloc_matches_device_entry_point():
         edge_got = np.concatenate([got[pos:pos + 3 * nv], got[tr:tr + 12]])
         edge_ref = np.concatenate([ref[pos:pos + 3 * nv], ref[tr:tr + 12]])
         assert np.abs(edge_ref).max() > 0
-        assert _rel(edge_got, edge_ref) <= EDGE_TOL, (call, _rel(edge_got, edge_ref))
-        assert _rel(got[col:col + 3 * nv], ref[col:col + 3 * nv]) <= INTERIOR_TOL, call
+        assert _rel(edge_got, edge_ref) <= TOL, (call, _rel(edge_got, edge_ref))
+        assert _rel(got[col:col + 3 * nv], ref[col:col + 3 * nv]) <= TOL, call
 
 
 def test_noalloc_rejects_oversized_calls():
