@@ -16,7 +16,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdrgb.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["bvh.cu", "render.cu", "edge.cu", "optim.cu", "engine.cu", "capi.cu", "noalloc.cu", "batch.cu", "serve.cu", "detsum.cu"]
+SOURCES = ["bvh.cu", "render.cu", "edge.cu", "optim.cu", "engine.cu", "capi.cu", "noalloc.cu", "batch.cu", "serve.cu", "detsum.cu",
+           "raster.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

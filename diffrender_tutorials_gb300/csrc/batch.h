@@ -96,6 +96,7 @@ struct drgb_batch {
       Job& J = r->job;
       JobDev d = J.dev;
       d.top_n = 0;  // batched kernels stage no job's top levels
+      d.vis_fwd = d.vis_adj = nullptr;  // batched pixel kernels trace their samples
       d.edge_key_base = (uint32_t)key_base;
       key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
       if (mode_groups.empty() || mode_groups.back().mode != J.mode)
@@ -130,6 +131,7 @@ struct drgb_batch {
       A.tc = J.tc.p;
       A.tri_v = J.tri_v.p;
       A.perm = J.perm.p;
+      A.leaf_of = J.leaf_of.p;
       A.tri = J.tri.p;
       A.nodes = J.nodes.p;
       A.nodes4 = J.nodes4.p;

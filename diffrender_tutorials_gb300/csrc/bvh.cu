@@ -360,10 +360,15 @@ __device__ __forceinline__ void write_child(float4* nodes, int parent, int slot,
   }
 }
 
+// Leaf k: its triangle's traced vertices (A, e1, e2) and, in leaf_of, the
+// leaf slot of that triangle (refreshed with every refit, so it follows any
+// topology change); then the boxes up the tree.
 __device__ __forceinline__ void leaf_refit_body(int k, const int* perm, int n, const int4* tri_v, const float4* pos,
                                                 const float* block_tr, float4* tri, float4* nodes,
-                                                const int* leaf_parent, const int* node_parent, int* counters) {
+                                                const int* leaf_parent, const int* node_parent, int* counters,
+                                                int* leaf_of) {
   const int t = perm[k];
+  leaf_of[t] = k;
   const int4 tv = tri_v[t];
   const f3 A = traced_vertex(pos, block_tr, tv.w, tv.x);
   const f3 B = traced_vertex(pos, block_tr, tv.w, tv.y);
@@ -402,10 +407,10 @@ __device__ __forceinline__ void leaf_refit_body(int k, const int* perm, int n, c
 
 __global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const float4* pos, const float* block_tr,
                                float4* tri, float4* nodes, const int* leaf_parent, const int* node_parent,
-                               int* counters) {
+                               int* counters, int* leaf_of) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  leaf_refit_body(k, perm, n, tri_v, pos, block_tr, tri, nodes, leaf_parent, node_parent, counters);
+  leaf_refit_body(k, perm, n, tri_v, pos, block_tr, tri, nodes, leaf_parent, node_parent, counters, leaf_of);
 }
 
 // 4-wide node of binary internal node p (layout in JobDev::nodes4; used by
@@ -488,7 +493,7 @@ __global__ void k_b_refit(const JobAux* aux, const Seg* segs, int nseg) {
   if (k >= sg.count) return;
   const JobAux& A = aux[sg.job];
   leaf_refit_body(k, A.perm, A.n_tris, A.tri_v, A.pos, A.block_tr, A.tri, A.nodes, A.leaf_parent, A.node_parent,
-                  A.counters);
+                  A.counters, A.leaf_of);
 }
 
 // segment table over the jobs' internal node counts
@@ -674,7 +679,7 @@ void refit_bvh(Job& J, cudaStream_t s) {
   if (n == 0) return;
   if (n > 1) DRGB_CUDA(cudaMemsetAsync(J.counters.p, 0, sizeof(int) * (n - 1), s));
   k_leaves_refit<<<(n + 127) / 128, 128, 0, s>>>(J.perm.p, n, J.tri_v.p, J.pos.p, J.block_tr.p, J.tri.p, J.nodes.p,
-                                                 J.leaf_parent.p, J.node_parent.p, J.counters.p);
+                                                 J.leaf_parent.p, J.node_parent.p, J.counters.p, J.leaf_of.p);
   count_launch();
 #ifdef DRGB_BVH4
   if (n > 1) {
@@ -1025,12 +1030,6 @@ static void host_topology(int builder, const float4* pos, const float* block_tr,
     sah_topology(pos, block_tr, tri_v, n, links, perm, leaf_parent, node_parent);
 }
 
-// triangle -> leaf slot, for traversals seeded with a candidate triangle
-__global__ void k_leaf_of(const int* perm, int n, int* leaf_of) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) leaf_of[perm[k]] = k;
-}
-
 static void build_topology(Job& J, cudaStream_t s);
 
 void build_bvh(Job& J, cudaStream_t s) {
@@ -1041,13 +1040,6 @@ void build_bvh(Job& J, cudaStream_t s) {
                                                            sizeof(int4) * J.h_tri_v.size()) == 0);
   if (J.topo_builder == J.bvh_builder && same_tris && J.nodes.p && J.perm.p) return;
   build_topology(J, s);
-#ifdef DRGB_SEED_HITS
-  J.leaf_of.alloc(std::max(n, 1));
-  if (n > 0) {
-    k_leaf_of<<<(n + 255) / 256, 256, 0, s>>>(J.perm.p, n, J.leaf_of.p);
-    count_launch();
-  }
-#endif
 }
 
 static void build_topology(Job& J, cudaStream_t s) {
@@ -1055,6 +1047,7 @@ static void build_topology(Job& J, cudaStream_t s) {
   J.topo_builder = -1;
   J.tri.alloc(3 * (size_t)std::max(n, 1));
   J.perm.alloc(std::max(n, 1));
+  J.leaf_of.alloc(std::max(n, 1));
   J.leaf_parent.alloc(std::max(n, 1));
   J.nodes.alloc(4 * (size_t)std::max(n - 1, 1));
 #ifdef DRGB_BVH4

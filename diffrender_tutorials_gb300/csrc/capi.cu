@@ -27,6 +27,10 @@ std::string t_err_message() { return t_err; }
 
 static void check_renderer(drgb_renderer* r) { require(r != nullptr, "null renderer"); }
 
+namespace drgb {
+void launch_rs_scan(uint32_t* hist, int m, cudaStream_t s);
+}  // namespace drgb
+
 extern "C" {
 
 int drgb_abi_version(void) { return DRGB_ABI_VERSION; }
@@ -38,6 +42,18 @@ int drgb_last_error(char* buf, size_t len) {
 }
 
 int64_t drgb_kernel_launches(void) { return g_launches.load(); }
+
+int drgb_debug_exclusive_scan(const uint32_t* counts, int n, uint32_t* out) {
+  return guard([&] {
+    require(counts && out && n >= 1, "null array or empty scan");
+    DevBuf<uint32_t> d;
+    d.alloc(scan_scratch((size_t)n));
+    DRGB_CUDA(cudaMemcpy(d.p, counts, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    launch_rs_scan(d.p, n, 0);
+    DRGB_CUDA(cudaGetLastError());
+    DRGB_CUDA(cudaMemcpy(out, d.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+  });
+}
 
 int drgb_camera_look_at(const float origin[3], const float target[3], const float up[3], float width, float height,
                         float fov_rad, float znear, float zfar, drgb_camera* out) {
@@ -150,6 +166,19 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         r->job.edge_exact = (int)value;
         if (r->d_job.p) r->push_dev();
         break;
+      case DRGB_OPT_PRIMARY_RASTER:
+        require(value == 0 || value == 1, "primary visibility: 0 (hierarchy traversal) or 1 (raster pass)");
+        r->job.raster = (int)value;
+        if (r->d_job.p && r->job.n_views > 0) {
+          r->raster_buffers();
+          r->push_dev();
+        }
+        break;
+      case DRGB_OPT_EDGE_SET:
+        require(value == 0 || value == 1, "edge set: 0 (every edge, the reference's) or 1 (silhouette edges)");
+        r->job.edge_sil = (int)value;
+        if (r->d_job.p) r->push_dev();
+        break;
       default: throw CudaError("unknown option", DRGB_ERR_INVALID);
     }
     r->graph_valid = false;
@@ -193,8 +222,10 @@ int drgb_render(drgb_renderer* r, const drgb_camera* cams, int n_views, float* i
     r->views(cams, n_views, false);
     const int64_t npx = r->n_pixels();
     J.images.reserve(3 * (size_t)npx);
+    r->raster_buffers();
     r->push_dev();
-    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_FWD | PX_IMG,
+    const int vis = r->raster_pass(PX_FWD);
+    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, PX_FWD | PX_IMG | vis,
                   r->px_grid(), r->stream, J.mode);
     DRGB_CUDA(cudaMemcpyAsync(images, J.images.p, sizeof(float) * 3 * npx, cudaMemcpyDeviceToHost, r->stream));
     r->check_flags();
@@ -622,8 +653,9 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
     save.alloc(std::max<int64_t>(1, J.grad_alloc));
     DRGB_CUDA(cudaMemcpyAsync(save.p, J.grad.p, save.bytes(), cudaMemcpyDeviceToDevice, r->stream));
     DRGB_CUDA(cudaMemsetAsync(J.grad.p, 0, save.bytes(), r->stream));
-    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags, r->px_grid(),
-                  r->stream, J.mode);
+    const int vis = r->raster_pass(flags);  // its candidate tests count as rays and triangle tests
+    launch_pixels(r->d_job.p, r->d_items.p, (int)J.h_pixel_items.size(), r->d_counter.p, flags | vis,
+                  r->px_grid(), r->stream, J.mode);
     if (J.dev.edge_samples > 0) launch_edges(r->d_job.p, 0, J, r->edge_grid(), r->stream);
     int shaded = 0;
     DRGB_CUDA(cudaMemcpyAsync(&shaded, J.queue_count.p, sizeof(int), cudaMemcpyDeviceToHost, r->stream));

@@ -43,6 +43,7 @@ constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 enum ErrFlag : uint32_t {
   ERR_STACK_OVERFLOW = 1u,
   ERR_TRAVERSAL_LIMIT = 2u,
+  ERR_VISIBILITY = 8u,  // a rasterised hit names a triangle the leaf arrays do not hold where expected
   ERR_BAD_INDEX = 4u,
 };
 
@@ -152,6 +153,8 @@ struct JobDev {
   // edge sampling (edge_derivatives, drender.h:235-425)
   const int4* edges;        // v0, v1 (global ids), vn0, vn1 (mesh-local ids)
   const int2* edge_mi;      // mesh, instance
+  const int2* edge_tris;    // the two flattened triangles sharing the edge (-1: boundary edge)
+  int edge_sil;             // 1: per view, only silhouette and boundary edges are sampled
   int n_edges;
   float4* proj;             // per view per vertex: pixel x, pixel y, world z
   float* pmf;               // per view n_edges
@@ -178,6 +181,12 @@ struct JobDev {
   int det_tr_key;            // (view, sample order), summed in a fixed order into grad[det_tr_key + 0..11]
   // stored adjoint hits (one float4 {t, u, v, triangle} per adjoint sample)
   float4* hit_buf;
+  // rasterised primary visibility: per forward / adjoint sample the minimum
+  // {t bits, triangle} of the hits found by the raster pass, or ~0 (null:
+  // the samples are traced through the hierarchy)
+  unsigned long long* vis_fwd;
+  unsigned long long* vis_adj;
+  const uint32_t* ra_state;  // bit 0 set: the raster pass wrote nothing this call
 };
 
 // Record slots a work item of NS samples may fill (deterministic mode):
@@ -239,6 +248,7 @@ struct JobAux {
   float2* tc;
   const int4* tri_v;
   const int* perm;
+  int* leaf_of;
   float4* tri;
   float4* nodes;
   float4* nodes4;

@@ -29,11 +29,33 @@ __device__ __forceinline__ void edge_project_body(const JobDev& J, int view, int
   J.proj[(int64_t)view * J.n_vertices + v] = make_float4(ox, oy, p.z, 0.0f);
 }
 
+// Whether a flattened triangle faces the eye (its winding's normal points
+// towards it).
+__device__ __forceinline__ bool faces_eye(const JobDev& J, int tri, f3 eye) {
+  const int4 tv = __ldg(J.tri_v + tri);
+  const f3 a = ld3(J.pos, tv.x);
+  return dot(cross(ld3(J.pos, tv.y) - a, ld3(J.pos, tv.z) - a), a - eye) < 0.0f;
+}
+
+// Sampling weight of an edge: the 3-D length of its projected endpoints
+// (build_edge_sampler, drender.cpp:5-22).  Silhouette mode (no reference
+// counterpart; the reference samples every edge, drender.h:274-285): an
+// edge whose two triangles both face the eye, or both face away, gets
+// weight 0 and is never drawn; silhouette and boundary edges keep theirs.
 __device__ __forceinline__ void edge_pmf_body(const JobDev& J, int view, int e) {
   const int4 ed = __ldg(J.edges + e);
   const float4* P = J.proj + (int64_t)view * J.n_vertices;
   const float4 a = P[ed.x], b = P[ed.y];
-  J.pmf[(int64_t)view * J.n_edges + e] = length(mk(b.x - a.x, b.y - a.y, b.z - a.z));
+  float w = length(mk(b.x - a.x, b.y - a.y, b.z - a.z));
+  if (J.edge_sil) {
+    const int2 tt = __ldg(J.edge_tris + e);
+    if (tt.y >= 0) {
+      const float* m = J.cams[view].wv_inv;
+      const f3 eye = mk(m[12], m[13], m[14]);  // the camera position in world space
+      if (faces_eye(J, tt.x, eye) == faces_eye(J, tt.y, eye)) w = 0.0f;
+    }
+  }
+  J.pmf[(int64_t)view * J.n_edges + e] = w;
 }
 
 // One block (CDF_THREADS): cdf[k+1] = pmf[k] + cdf[k] in edge order, then
@@ -141,6 +163,8 @@ __device__ __forceinline__ bool edge_select_test(const JobDev& J, int view, int 
   const float rnd0 = __ldg(J.rnd + 2 * i), rnd1 = __ldg(J.rnd + 2 * i + 1);
   const float* cdf = J.cdf + (int64_t)view * (J.n_edges + 1);
   edge_id = clampi(upper_bound_idx(cdf, J.n_edges + 1, rnd0) - 1, 0, J.n_edges - 1);
+  // silhouette mode: a view without silhouette edges has no samples
+  if (J.edge_sil && !(J.pmf[(int64_t)view * J.n_edges + edge_id] > 0.0f)) return false;
   const int4 ed = __ldg(J.edges + edge_id);
   const float4* P = J.proj + (int64_t)view * J.n_vertices;
   const float4 a = P[ed.x], b = P[ed.y];

@@ -307,13 +307,16 @@ int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<
 
 // Unique edges of the meshes of `lay` ordered by (v0, v1) global ids, the
 // first inserted kept on duplicates (std::set<Edge>, drender.h:244-299);
-// insertion runs over meshes, then instances, then triangles.
-void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi) {
+// insertion runs over meshes, then instances, then triangles.  `tris` (may
+// be null) receives the flattened ids of the first two triangles that share
+// each edge (-1 where an edge has only one: a boundary edge).
+void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi,
+               std::vector<int2>* tris) {
   std::vector<int> key;
   for (auto& L : lay) key.push_back(L.mesh_id);
   std::sort(key.begin(), key.end());
   struct E {
-    int v0, v1, vn0, vn1, mesh, inst;
+    int v0, v1, vn0, vn1, mesh, inst, tri;
   };
   std::vector<E> all;
   for (int m = 0; m < (int)J.meshes.size(); m++) {
@@ -323,14 +326,14 @@ void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>&
       int b = -1;
       for (int q = 0; q < J.n_blocks; q++)
         if (J.h_blocks[q].mesh == m && J.h_blocks[q].inst == j) b = q;
-      const int off = J.h_blocks[b].vert_off;
+      const int off = J.h_blocks[b].vert_off, toff = J.h_blocks[b].tri_off;
       for (int k = 0; k + 2 < M.ni; k += 3) {
         const int n[3] = {(int)M.h_indices[k], (int)M.h_indices[k + 1], (int)M.h_indices[k + 2]};
         for (int e = 0; e < 3; e++) {
           const int a = n[e], c = n[(e + 1) % 3];
           const int ga = off + a, gc = off + c;
-          if (ga < gc) all.push_back(E{ga, gc, a, c, m, j});
-          else all.push_back(E{gc, ga, c, a, m, j});
+          if (ga < gc) all.push_back(E{ga, gc, a, c, m, j, toff + k / 3});
+          else all.push_back(E{gc, ga, c, a, m, j, toff + k / 3});
         }
       }
     }
@@ -340,10 +343,15 @@ void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>&
   });
   ed.clear();
   mi.clear();
+  if (tris) tris->clear();
   for (const E& e : all) {
-    if (!ed.empty() && ed.back().x == e.v0 && ed.back().y == e.v1) continue;
+    if (!ed.empty() && ed.back().x == e.v0 && ed.back().y == e.v1) {
+      if (tris && tris->back().y < 0) tris->back().y = e.tri;
+      continue;
+    }
     ed.push_back(make_int4(e.v0, e.v1, e.vn0, e.vn1));
     mi.push_back(make_int2(e.mesh, e.inst));
+    if (tris) tris->push_back(make_int2(e.tri, -1));
   }
 }
 
@@ -353,11 +361,12 @@ void build_edges(Job& J) {
   std::sort(key.begin(), key.end());
   if (key == J.edge_ids_key && (J.n_edges > 0 || key.empty())) return;
   std::vector<int4> ed;
-  std::vector<int2> mi;
-  edge_list(J, J.dlay, ed, mi);
+  std::vector<int2> mi, tris;
+  edge_list(J, J.dlay, ed, mi, &tris);
   J.n_edges = (int)ed.size();
   J.edges.upload(ed.data(), ed.size(), 0);
   J.edge_mi.upload(mi.data(), mi.size(), 0);
+  J.edge_tris.upload(tris.data(), tris.size(), 0);
   DRGB_CUDA(cudaStreamSynchronize(0));
   J.edge_ids_key = key;
 }
@@ -476,6 +485,11 @@ void sync_dev(Job& J) {
   d.tile_h = J.tile_h;
   d.edges = J.edges.p;
   d.edge_mi = J.edge_mi.p;
+  d.edge_tris = J.edge_tris.p;
+  d.edge_sil = J.edge_sil;
+  d.vis_fwd = J.raster_on ? J.vis[0].p : nullptr;
+  d.vis_adj = J.raster_on ? J.vis[1].p : nullptr;
+  d.ra_state = J.ra_state.p;
   d.n_edges = J.n_edges;
   d.proj = J.proj.p;
   d.pmf = J.pmf.p;

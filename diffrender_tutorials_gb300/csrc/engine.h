@@ -156,6 +156,14 @@ struct Job {
   int trace_bruteforce = 0;
   int trace_limit = 1 << 24;  // node pops per ray (DRGB_OPT_TRACE_STEP_LIMIT)
   int edge_exact = 0;         // DRGB_OPT_EDGE_JACOBIAN
+  int edge_sil = 0;           // DRGB_OPT_EDGE_SET
+  int raster = 1;             // DRGB_OPT_PRIMARY_RASTER
+  bool raster_on = false;     // raster buffers set up for the current views (see renderer::raster_buffers)
+  DevBuf<unsigned long long> vis[2];  // rasterised visibility of forward / adjoint samples
+  DevBuf<uint32_t> ra_tiles;          // triangles per screen tile, then their offsets (scan)
+  DevBuf<uint32_t> ra_cursor;         // per tile fill cursor
+  DevBuf<uint32_t> ra_state;          // bit 0: the tile lists did not fit ra_list
+  DevBuf<int> ra_list;                // per tile the triangles (leaf slots) whose footprint overlaps it
   int tile_w = 4, tile_h = 4;
   // scene
   bool committed = false;
@@ -193,6 +201,7 @@ struct Job {
   // edges (topology; one list per differentiable-mesh set)
   DevBuf<int4> edges;   // v0, v1, vn0, vn1
   DevBuf<int2> edge_mi; // mesh, instance
+  DevBuf<int2> edge_tris;  // the two flattened triangles sharing the edge (-1: boundary edge)
   int n_edges = 0;
   std::vector<int> edge_ids_key;  // dmesh ids the list was built for
   // views
@@ -262,7 +271,8 @@ void build_edges(Job& J);
 // Flattened block of instance 0 of a mesh (its instances' blocks follow).
 int first_block(const Job& J, int mesh);
 // The edge list of the meshes of `lay` (host vectors; build_edges uploads it).
-void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi);
+void edge_list(const Job& J, const std::vector<DLayout>& lay, std::vector<int4>& ed, std::vector<int2>& mi,
+               std::vector<int2>* tris = nullptr);
 int64_t compute_layout(const Job& J, const int32_t* ids, int n_ids, std::vector<DLayout>& out,
                        int64_t* alloc_total = nullptr);
 // TransformR::to_mat on the host (column-major, LiteMath's rounding).
@@ -284,13 +294,24 @@ CamDev make_cam(const drgb_camera& c);
 // Pixel kernel flags
 // PX_HIT_STORE: adjoint pass that only traces and stores the primary hits;
 // PX_HIT_LOAD: adjoint pass that reads them instead of tracing.
-enum PixelFlags : int { PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8, PX_HIT_STORE = 16, PX_HIT_LOAD = 32 };
+// PX_VIS: the raster pass of this call filled the job's visibility buffers
+// (the pixel kernel reads them instead of tracing camera rays).
+enum PixelFlags : int {
+  PX_FWD = 1, PX_LOSS = 2, PX_ADJ = 4, PX_IMG = 8, PX_HIT_STORE = 16, PX_HIT_LOAD = 32, PX_VIS = 64
+};
 // Counters a buffer scanned by launch_rs_scan needs for m counters: the m
 // counters (rounded up to 4) and one total per 16,384-counter tile.
 inline size_t scan_scratch(size_t m) { return ((m + 3) & ~(size_t)3) + (m + 16383) / 16384; }
 void launch_pixels(const JobDev* d_jobs, const int4* d_items, int n_items, int* d_counter, int flags, int grid,
                    cudaStream_t s, int mode, bool det = false);
 void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
+// Rasterised primary visibility of the forward (passes & 1) and adjoint
+// (passes & 2) samples of a single job's views, over ntx x nty tiles of
+// tw x th pixels per view.
+void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int nty, int tw, int th, cudaStream_t s);
+// Raster tile of tw x th pixels for S samples per pixel.
+void raster_tile(int S, int& tw, int& th);
+void launch_rs_scan(uint32_t* hist, int m, cudaStream_t s);
 void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s);
 void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, int64_t n, uint32_t* prim,
                  uint32_t* inst, uint32_t* geom, float* t, float* u, float* v, cudaStream_t s);

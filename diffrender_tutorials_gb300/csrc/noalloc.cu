@@ -122,8 +122,8 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
       d.tr_off = lay[k].tr_off;
     }
     std::vector<int4> ed;
-    std::vector<int2> emi;
-    edge_list(J, lay, ed, emi);
+    std::vector<int2> emi, etris;
+    edge_list(J, lay, ed, emi, &etris);
     const int E = (int)ed.size();
     std::vector<float> rnd;
     if (edge_samples > 0) edge_random_host(edge_samples, rnd);
@@ -143,6 +143,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     const size_t o_queue = c.take<int4>((size_t)n_views * std::max(1, edge_samples));
     const size_t o_edges = c.take<int4>(std::max(1, E));
     const size_t o_emi = c.take<int2>(std::max(1, E));
+    const size_t o_etri = c.take<int2>(std::max(1, E));
     const size_t o_rnd = c.take<float>(std::max<size_t>(1, rnd.size()));
     const size_t o_lblk = c.take<double>((size_t)n_views * kLossBlocks);
     const size_t o_cnt = c.take<int>(4);
@@ -203,6 +204,8 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.item_count = (int)items.size();
     d.edges = reinterpret_cast<const int4*>(base + o_edges);
     d.edge_mi = reinterpret_cast<const int2*>(base + o_emi);
+    d.edge_tris = reinterpret_cast<const int2*>(base + o_etri);
+    d.edge_sil = J.edge_sil;
     d.n_edges = E;
     d.proj = reinterpret_cast<float4*>(base + o_proj);
     d.pmf = reinterpret_cast<float*>(base + o_pmf);
@@ -230,6 +233,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     put(o_md, md.data(), sizeof(MeshDev) * md.size());
     put(o_edges, ed.data(), sizeof(int4) * ed.size());
     put(o_emi, emi.data(), sizeof(int2) * emi.size());
+    put(o_etri, etris.data(), sizeof(int2) * etris.size());
     if (edge_samples > 0) put(o_rnd, rnd.data(), sizeof(float) * rnd.size());
     if (grad_total > 0) DRGB_CUDA(cudaMemsetAsync(d_dscene, 0, sizeof(float) * grad_total, s));
     DRGB_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int), s));

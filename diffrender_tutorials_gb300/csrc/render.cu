@@ -146,7 +146,8 @@ __device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, 
 template <int MODE, bool DET, bool HITS>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
                                            uint32_t key, float* wscr, int64_t rec_base, int& rec_n,
-                                           const float4* stored, int seed) {
+                                           const float4* stored, int seed, bool use_vis,
+                                           unsigned long long vkey) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   bool hit;
@@ -166,6 +167,8 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
       s.C = tv.z;
       s.block = tv.w;
     }
+  } else if (use_vis) {
+    hit = cast_vis(J, cam, x, y, active, vkey, s);
   } else {
     hit = cast_p<kPixelWarp>(J, cam, x, y, active, s, seed);
   }
@@ -267,6 +270,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
 #endif
   stage_top_nodes(jobs[0]);  // a single job's top levels (none for a batch)
+  // a single job whose raster pass resolved this launch's camera samples
+  const bool vis_ok = (flags & PX_VIS) && jobs[0].ra_state && !(*jobs[0].ra_state & 1u);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
@@ -328,7 +333,10 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, &ht);
         if (s < NS) s_hit[s] = act ? ht : -1;
 #else
-        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act);
+        const bool use_vis = vis_ok && J.vis_fwd != nullptr;
+        const unsigned long long vk =
+            act && use_vis ? J.vis_fwd[(J.img_off[view] + (int64_t)py * W + px) * S + k] : ~0ull;
+        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, nullptr, use_vis, vk);
 #endif
         if (act) c = sc / (float)S;
         if (s < NS) {
@@ -427,7 +435,10 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
           seed = s_hit[p * S + gy * sq + gx];
         }
 #endif
-        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed);
+        const bool use_vis = vis_ok && J.vis_adj != nullptr;
+        const unsigned long long vk =
+            act && use_vis ? J.vis_adj[(J.img_off[view] + (int64_t)py * W + px) * S + k] : ~0ull;
+        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed, use_vis, vk);
       }
       if (DET && J.det && lane == 0 && !store_hits) J.rec_count[it - J.item_base] = rec_n;
     }

@@ -156,6 +156,76 @@ struct drgb_renderer {
     J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
     if (J.det) det_buffers(J, stream);
     if (J.store_hits) hit_buffers();
+    raster_buffers();
+  }
+
+  // Rasterised primary visibility (DRGB_OPT_PRIMARY_RASTER) for the current
+  // views: one 64-bit key per forward and per adjoint sample, the screen
+  // tiles and their triangle lists.  raster_on tells sync_dev to hand the
+  // buffers to the pixel kernel; call before push_dev.  Off for the
+  // brute-force caster (the reference's loop, kept for parity) and for
+  // stored adjoint hits.
+  void raster_geometry(int& tw, int& th, int& ntx, int& nty) const {
+    raster_tile(job.S, tw, th);
+    int W = 1, H = 1;
+    for (auto& c : job.h_cams) {
+      W = std::max(W, (int)c.width);
+      H = std::max(H, (int)c.height);
+    }
+    ntx = (W + tw - 1) / tw;
+    nty = (H + th - 1) / th;
+  }
+  void raster_buffers() {
+    Job& J = job;
+    const bool on = J.raster && !J.trace_bruteforce && !J.store_hits && J.n_tris > 0 && J.n_views > 0;
+    if (on) {
+      const size_t samples = (size_t)n_pixels() * J.S;
+      J.vis[0].reserve(samples);
+      J.vis[1].reserve(samples);
+      int tw, th, ntx, nty;
+      raster_geometry(tw, th, ntx, nty);
+      const size_t n_tiles = (size_t)J.n_views * ntx * nty;
+      J.ra_tiles.reserve(scan_scratch(n_tiles + 1));
+      J.ra_cursor.reserve(n_tiles);
+      J.ra_state.reserve(1);
+      J.ra_list.reserve(std::max<size_t>(1u << 20, (size_t)16 * J.n_views * J.n_tris));
+    }
+    J.raster_on = on;
+  }
+
+  // The raster pass for the samples a pixel-kernel launch with `flags`
+  // traces.  Returns PX_VIS when it ran (add it to that launch's flags), 0
+  // when the samples are to be traced: raster off, or the device job does
+  // not hold the current, large enough buffers.
+  int raster_pass(int flags) {
+    Job& J = job;
+    const int passes = ((flags & PX_FWD) ? 1 : 0) | ((flags & PX_ADJ) ? 2 : 0);
+    if (!J.raster_on || !passes) return 0;
+    const size_t samples = (size_t)n_pixels() * J.S;
+    int tw, th, ntx, nty;
+    raster_geometry(tw, th, ntx, nty);
+    const size_t n_tiles = (size_t)J.n_views * ntx * nty;
+    if (J.dev.vis_fwd != J.vis[0].p || J.dev.vis_adj != J.vis[1].p || J.dev.ra_state != J.ra_state.p ||
+        J.vis[0].n < samples || J.vis[1].n < samples || J.ra_tiles.n < scan_scratch(n_tiles + 1) ||
+        J.ra_cursor.n < n_tiles || !J.ra_list.p)
+      return 0;
+    launch_raster(d_job.p, J, passes, ntx, nty, tw, th, stream);
+    return PX_VIS;
+  }
+
+  // After a synchronised call: lists that did not fit double their room for
+  // the next call (that call traced its camera rays instead).
+  void raster_grow() {
+    Job& J = job;
+    if (!J.raster_on || !J.ra_state.p) return;
+    uint32_t st = 0;
+    DRGB_CUDA(cudaMemcpy(&st, J.ra_state.p, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st & 1u) {
+      J.ra_list.alloc(2 * J.ra_list.n);
+      DRGB_CUDA(cudaMemset(J.ra_state.p, 0, sizeof(uint32_t)));
+      graph_valid = false;
+      push_dev();
+    }
   }
 
   // One float4 per adjoint sample of every work item (stored-hit mode).
@@ -171,6 +241,7 @@ struct drgb_renderer {
     Job& J = job;
     const bool hits = J.store_hits && J.hit_buf.p && (flags & PX_ADJ);
     const int n = (int)J.h_pixel_items.size();
+    flags |= raster_pass(flags);
     if (hits) launch_pixels(d_job.p, d_items.p, n, d_counter.p, PX_ADJ | PX_HIT_STORE, px_grid(), stream, J.mode, J.det);
     launch_pixels(d_job.p, d_items.p, n, d_counter.p, flags | (hits ? PX_HIT_LOAD : 0), px_grid(), stream, J.mode,
                   J.det);
@@ -200,12 +271,14 @@ struct drgb_renderer {
     uint32_t f = 0;
     DRGB_CUDA(cudaMemcpyAsync(&f, job.err.p, sizeof(f), cudaMemcpyDeviceToHost, stream));
     DRGB_CUDA(cudaStreamSynchronize(stream));
+    raster_grow();
     if (f) {
       DRGB_CUDA(cudaMemsetAsync(job.err.p, 0, sizeof(uint32_t), stream));
       DRGB_CUDA(cudaStreamSynchronize(stream));
       std::string m = "kernel error flags " + std::to_string(f);
       if (f & ERR_STACK_OVERFLOW) m += " (traversal stack overflow)";
       if (f & ERR_TRAVERSAL_LIMIT) m += " (traversal step limit)";
+      if (f & ERR_VISIBILITY) m += " (rasterised visibility out of step with the hierarchy's leaves)";
       throw CudaError(m, DRGB_ERR_KERNEL);
     }
   }
@@ -253,6 +326,7 @@ struct drgb_renderer {
       DRGB_CUDA(cudaEventRecord(ev_join, side));
       // one SM slot per CDF block stays free of the persistent pixel kernel
       const int grid = std::max(1, std::min(px_grid(), sm_count * px_resident - J.n_views));
+      flags |= raster_pass(flags);
       launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, grid, stream, J.mode, J.det);
       launch_loss_finalize(d_job.p, 1, stream);
       DRGB_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));

@@ -153,6 +153,46 @@ __device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float
   return hit;
 }
 
+// The camera ray of a sample whose nearest hit the raster pass found
+// (key = {t bits, flattened triangle}, ~0 for none): the reference's
+// Moller-Trumbore test on that triangle gives t, u, v bit-identical to the
+// traversal's.
+__device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, float x, float y, bool active,
+                                         unsigned long long key, Surf& s) {
+  camera_ray(cam, x, y, s.ro, s.rd);
+  s.h.t = 1e9f;
+  s.h.tri = -1;
+  s.h.u = s.h.v = 0.0f;
+  s.A = s.B = s.C = 0;
+  s.block = 0;
+  if (!active || key == ~0ull) return false;
+  const int id = (int)(uint32_t)key;
+  if (id < 0 || id >= J.n_tris) {
+    atomicOr(J.err, ERR_VISIBILITY);
+    return false;
+  }
+  const int k = __ldg(J.leaf_of + id);
+  const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+  float t, u, v;
+  add_work(J, 0, 1);
+  // the leaf must hold that triangle, and the test accepts it again (same
+  // ray, same operands); anything else is an error, not a miss
+  if (__float_as_int(a.w) != id || !mt_test(s.ro, s.rd, f4to3(a), f4to3(e1), f4to3(e2), 0.0f, t, u, v)) {
+    atomicOr(J.err, ERR_VISIBILITY);
+    return false;
+  }
+  s.h.t = t;
+  s.h.u = u;
+  s.h.v = v;
+  s.h.tri = id;
+  const int4 tv = __ldg(J.tri_v + id);
+  s.A = tv.x;
+  s.B = tv.y;
+  s.C = tv.z;
+  s.block = tv.w;
+  return true;
+}
+
 __device__ __forceinline__ bool cast(const JobDev& J, const CamDev& cam, float x, float y, Surf& s) {
   return cast_p<false>(J, cam, x, y, true, s);
 }
@@ -369,12 +409,14 @@ __device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
 }
 
 // hit_tri (may be null) receives the camera ray's triangle, -1 on a miss.
+// use_vis (uniform over the launch): the camera ray's hit is the sample's
+// rasterised visibility key vkey instead of a traversal.
 template <int MODE, bool WARP>
 __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active,
-                             int* hit_tri = nullptr) {
+                             int* hit_tri = nullptr, bool use_vis = false, unsigned long long vkey = ~0ull) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
-  const bool hit = cast_p<WARP>(J, cam, x, y, active, s);
+  const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s) : cast_p<WARP>(J, cam, x, y, active, s);
   if (hit_tri) *hit_tri = hit ? s.h.tri : -1;
   const float u = s.h.u, v = s.h.v;
   switch (mode) {

@@ -16,7 +16,7 @@ DRGB_OK = 0
 # renderer / batch options (drgb_renderer_set_option, drgb_batch_set_option)
 OPT_TRACE_BRUTEFORCE, OPT_TILE_W, OPT_TILE_H, OPT_USE_GRAPH, OPT_DETERMINISTIC, OPT_ADJOINT_HITS = 1, 2, 3, 4, 5, 6
 OPT_PIXEL_GRID, OPT_EDGE_GRID, OPT_BVH_BUILDER, OPT_BVH_REBUILD = 7, 8, 9, 10
-OPT_TRACE_STEP_LIMIT, OPT_EDGE_JACOBIAN = 11, 12
+OPT_TRACE_STEP_LIMIT, OPT_EDGE_JACOBIAN, OPT_EDGE_SET, OPT_PRIMARY_RASTER = 11, 12, 13, 14
 ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_STATE, ERR_KERNEL, ERR_UNSUPPORTED, ERR_NO_DEVICE = -1, -2, -3, -4, -5, -6, -7
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
           -5: "kernel error flag", -6: "unsupported", -7: "no CUDA device"}
@@ -79,6 +79,7 @@ _SIGS = {
     "drgb_abi_version": (C.c_int, []),
     "drgb_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "drgb_kernel_launches": (C.c_int64, []),
+    "drgb_debug_exclusive_scan": (C.c_int, [VP, C.c_int, VP]),
     "drgb_camera_look_at": (C.c_int, [VP, VP, VP, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                       C.POINTER(Camera)]),
     "drgb_renderer_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(VP)]),

@@ -87,11 +87,27 @@ enum {
                                     hit found so far and the call returns DRGB_ERR_KERNEL ("traversal step
                                     limit"); the renderer stays usable.  The reference has no such bound: its
                                     caster loops over every triangle (raytrace3d_bf.cpp:102-156). */
-  DRGB_OPT_EDGE_JACOBIAN = 12    /* chain rule of the edge term from pixel to vertex positions: 0 (default)
+  DRGB_OPT_EDGE_JACOBIAN = 12,   /* chain rule of the edge term from pixel to vertex positions: 0 (default)
                                     the reference's edge_grad (drender.cpp:31-87): dx/dX and dy/dY only for
                                     the x and y components, through mesh 0's inverse transform; 1 the full
                                     2x3 Jacobian of each endpoint's pixel position, through the transpose of
                                     the edge's own instance transform (exact for any camera and instance) */
+  DRGB_OPT_EDGE_SET = 13,        /* edges the boundary term samples: 0 (default) every edge of the
+                                    differentiable meshes, in proportion to projected length (the reference,
+                                    drender.h:274-285,306-345); 1 per view only silhouette edges (one adjacent
+                                    triangle faces the camera, the other faces away) and boundary edges.
+                                    Where shading is continuous across edges (interpolated normals and
+                                    colours) the other edges contribute only the O(1e-3 px) offset of the
+                                    two shading points, so the samples go where the image is discontinuous;
+                                    with per-face colours or textures edges inside the silhouette carry real
+                                    discontinuities and mode 0 is required */
+  DRGB_OPT_PRIMARY_RASTER = 14   /* nearest hits of the forward and adjoint camera samples of a single
+                                    renderer: 1 (default) a raster pass -- every triangle runs the
+                                    reference's ray/triangle test on the samples its projection covers
+                                    (with a margin), keeping per sample the nearest hit, ties to the lowest
+                                    triangle as the reference's loop does; 0 each sample's ray through the
+                                    hierarchy.  Same hits either way; off for the brute-force caster and
+                                    stored adjoint hits.  Costs 16 bytes per sample of the views */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -163,6 +179,11 @@ int drgb_abi_version(void);
 int drgb_last_error(char* buf, size_t len);
 /* Number of kernels this library launched since load (all threads). */
 int64_t drgb_kernel_launches(void);
+/* Test hook, no counterpart in the reference: the device exclusive scan of
+ * n 32-bit counters that the radix sorts of the hierarchy build, the
+ * edge-sample queue and the deterministic reduction use (host arrays in and
+ * out, current device, synchronous). */
+int drgb_debug_exclusive_scan(const uint32_t* counts, int n, uint32_t* out);
 
 /* ---- renderer: IDiffRender (src/virtual_drender.h:14-26) ----------------- */
 

@@ -542,6 +542,7 @@ void orc_default_model_params(orc_model_params* p) {
   p->path_depth = 2;
   p->seed = 1u;
   p->edge_jacobian = 0;
+  p->edge_set = 0;
 }
 
 /* sample_bilinear_clamp_3f, shade_common.cpp:3-21 */
@@ -1038,7 +1039,7 @@ static void interior_derivatives(const prep_t* s, const dmap_t* dm, int mode, in
 /* ---------------------------------------------------------------------------
  * Edge sampling (drender.h:235-425, drender.cpp:5-87, functions.cpp:21-163).
  * ------------------------------------------------------------------------- */
-typedef struct { int v0, v1, vn0, vn1, mesh, inst; } edge_t;
+typedef struct { int v0, v1, vn0, vn1, mesh, inst, tri0, tri1; } edge_t; /* tri0/1: adjacent traced triangles (-1: none) */
 
 static int edge_cmp(const void* a, const void* b) {
   const edge_t* x = (const edge_t*)a;
@@ -1110,10 +1111,14 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
     if (dm->by_mesh[i] >= 0) ne_all += 3 * (s->meshes[i].n_indices / 3) * s->meshes[i].n_instances;
   edge_t* E = (edge_t*)malloc(sizeof(edge_t) * (ne_all > 0 ? ne_all : 1));
   int ne = 0;
+  int tri_base = 0; /* first traced triangle of the current (mesh, instance) block */
   for (int i = 0; i < s->n_meshes; i++) {
-    if (dm->by_mesh[i] < 0) continue;
     const orc_mesh* m = s->meshes + i;
-    for (int j = 0; j < m->n_instances; j++) {
+    if (dm->by_mesh[i] < 0) {
+      tri_base += m->n_instances * (m->n_indices / 3);
+      continue;
+    }
+    for (int j = 0; j < m->n_instances; j++, tri_base += m->n_indices / 3) {
       for (int k = 0; k + 2 < m->n_indices; k += 3) {
         int g[3] = {get_index(s, i, j, k), get_index(s, i, j, k + 1), get_index(s, i, j, k + 2)};
         int n[3] = {(int)m->indices[k], (int)m->indices[k + 1], (int)m->indices[k + 2]};
@@ -1124,6 +1129,8 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
           else { ed.v0 = g[b]; ed.vn0 = n[b]; ed.v1 = g[a]; ed.vn1 = n[a]; }
           ed.mesh = i;
           ed.inst = j;
+          ed.tri0 = tri_base + k / 3;
+          ed.tri1 = -1;
           E[ne++] = ed;
         }
       }
@@ -1154,7 +1161,10 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
     int u = 0;
     for (int k = 0; k < ne; k++) {
       const edge_t* e = &E[order[k]];
-      if (u > 0 && T[u - 1].v0 == e->v0 && T[u - 1].v1 == e->v1) continue;
+      if (u > 0 && T[u - 1].v0 == e->v0 && T[u - 1].v1 == e->v1) {
+        if (T[u - 1].tri1 < 0) T[u - 1].tri1 = e->tri0;
+        continue;
+      }
       T[u++] = *e;
     }
     memcpy(E, T, sizeof(edge_t) * u);
@@ -1170,6 +1180,18 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
     const f3 a = v3(p2[3 * E[k].v0], p2[3 * E[k].v0 + 1], p2[3 * E[k].v0 + 2]);
     const f3 b = v3(p2[3 * E[k].v1], p2[3 * E[k].v1 + 1], p2[3 * E[k].v1 + 2]);
     pmf[k] = len3(sub3(b, a));
+    if (mp->edge_set == 1 && E[k].tri1 >= 0) {
+      /* silhouette edges only (no reference counterpart): both triangles
+       * facing the eye, or both facing away, give the edge weight 0 */
+      const f3 eye = v3(cam[64 + 12], cam[64 + 13], cam[64 + 14]); /* wv_inv * (0,0,0,1) */
+      int facing[2];
+      for (int q = 0; q < 2; q++) {
+        const int t = q ? E[k].tri1 : E[k].tri0;
+        const f3 A = s->pos[s->tri_gid[3 * t]], B = s->pos[s->tri_gid[3 * t + 1]], C = s->pos[s->tri_gid[3 * t + 2]];
+        facing[q] = dot3(cross3(sub3(B, A), sub3(C, A)), sub3(A, eye)) < 0.0f;
+      }
+      if (facing[0] == facing[1]) pmf[k] = 0.0f;
+    }
     cdf[k + 1] = pmf[k] + cdf[k];
   }
   const float length_sum = cdf[ne];
@@ -1201,6 +1223,7 @@ static void edge_derivatives(const prep_t* s, const dmap_t* dm, int mode, const 
         if (rnd0 < cdf[mid]) hi = mid; else lo = mid + 1;
       }
       const int edge_id = clampi(lo - 1, 0, ne - 1);
+      if (mp->edge_set == 1 && !(pmf[edge_id] > 0.0f)) continue; /* no silhouette edge in this view */
       const edge_t ed = E[edge_id];
       const float pm = pmf[edge_id];
       const f2 v0 = v2(p2[3 * ed.v0], p2[3 * ed.v0 + 1]);

@@ -69,6 +69,9 @@ typedef struct orc_model_params {
   /* edge-term chain rule: 0 the reference's edge_grad (drender.cpp:31-87),
    * 1 the full 2x3 screen Jacobian through the instance's own transform */
   int32_t edge_jacobian;
+  /* edges the boundary term samples: 0 every edge (the reference), 1 only
+   * silhouette and boundary edges of each view */
+  int32_t edge_set;
 } orc_model_params;
 
 void orc_default_model_params(orc_model_params* p);

@@ -46,7 +46,8 @@ class OrcMesh(C.Structure):
 
 class OrcModelParams(C.Structure):
     _fields_ = [("light_pos", C.c_float * 3), ("light_intensity", C.c_float), ("ambient", C.c_float),
-                ("path_depth", C.c_int32), ("seed", C.c_uint32), ("edge_jacobian", C.c_int32)]
+                ("path_depth", C.c_int32), ("seed", C.c_uint32), ("edge_jacobian", C.c_int32),
+                ("edge_set", C.c_int32)]
 
 
 class OrcOptParams(C.Structure):
@@ -93,9 +94,11 @@ class _Scene:
         self.n = len(scene.meshes)
 
 
-def model_params(light_pos=(3.0, 3.0, 3.0), intensity=10.0, ambient=0.1, path_depth=2, seed=1, edge_jacobian=0):
+def model_params(light_pos=(3.0, 3.0, 3.0), intensity=10.0, ambient=0.1, path_depth=2, seed=1, edge_jacobian=0,
+                 edge_set=0):
     p = OrcModelParams()
     p.edge_jacobian = edge_jacobian
+    p.edge_set = edge_set
     p.light_pos[:] = light_pos
     p.light_intensity = intensity
     p.ambient = ambient
