@@ -97,6 +97,8 @@ struct drgb_batch {
       JobDev d = J.dev;
       d.top_n = 0;  // batched kernels stage no job's top levels
       d.vis_fwd = d.vis_adj = nullptr;  // batched pixel kernels trace their samples
+      d.sh_grid = nullptr;
+      d.ra_tiles = nullptr;
       d.edge_key_base = (uint32_t)key_base;
       key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
       if (mode_groups.empty() || mode_groups.back().mode != J.mode)

@@ -405,10 +405,14 @@ __device__ __forceinline__ void leaf_refit_body(int k, const int* perm, int n, c
   }
 }
 
+// `light`, `tiles_state` (may be null): the light-space cells and the
+// raster pass's tile lists no longer hold the geometry.
 __global__ void k_leaves_refit(const int* perm, int n, const int4* tri_v, const float4* pos, const float* block_tr,
                                float4* tri, float4* nodes, const int* leaf_parent, const int* node_parent,
-                               int* counters, int* leaf_of) {
+                               int* counters, int* leaf_of, LightGrid* light, uint32_t* tiles_state) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0 && light) light->valid = 0;
+  if (k == 0 && tiles_state) *tiles_state &= ~2u;
   if (k >= n) return;
   leaf_refit_body(k, perm, n, tri_v, pos, block_tr, tri, nodes, leaf_parent, node_parent, counters, leaf_of);
 }
@@ -679,7 +683,8 @@ void refit_bvh(Job& J, cudaStream_t s) {
   if (n == 0) return;
   if (n > 1) DRGB_CUDA(cudaMemsetAsync(J.counters.p, 0, sizeof(int) * (n - 1), s));
   k_leaves_refit<<<(n + 127) / 128, 128, 0, s>>>(J.perm.p, n, J.tri_v.p, J.pos.p, J.block_tr.p, J.tri.p, J.nodes.p,
-                                                 J.leaf_parent.p, J.node_parent.p, J.counters.p, J.leaf_of.p);
+                                                 J.leaf_parent.p, J.node_parent.p, J.counters.p, J.leaf_of.p,
+                                                 J.sh_grid.p, J.ra_state.p);
   count_launch();
 #ifdef DRGB_BVH4
   if (n > 1) {

@@ -181,6 +181,13 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         break;
       default: throw CudaError("unknown option", DRGB_ERR_INVALID);
     }
+    // the raster pass depends on the caster, stored hits and deterministic mode
+    if ((option == DRGB_OPT_TRACE_BRUTEFORCE || option == DRGB_OPT_DETERMINISTIC ||
+         option == DRGB_OPT_ADJOINT_HITS) && r->d_job.p && r->job.n_views > 0) {
+      r->set_device();
+      r->raster_buffers();
+      r->push_dev();
+    }
     r->graph_valid = false;
   });
 }

@@ -89,6 +89,21 @@ struct ModelParams {
   uint32_t seed;
 };
 
+// Light-space grid of the point light's shadow rays: a view from the light
+// position toward the scene's bounding sphere.  A point q maps to grid
+// coordinates (dot(q-L, u)/z * scale + half, dot(q-L, v)/z * scale + half)
+// with z = dot(q-L, w); every point of the sphere has z > 0 and lands in
+// [0, G) x [0, G).  ok = 0: the light is inside (or too close to) the
+// sphere, and shadow rays are traced.
+struct LightGrid {
+  float lx, ly, lz;  // light position
+  float ux, uy, uz, vx, vy, vz, wx, wy, wz;
+  float scale, half;
+  int G, ok;
+  int valid;     // the cell lists hold the current geometry (cleared by every refit)
+  int overflow;  // the lists did not fit their buffer
+};
+
 // One render job: a committed scene, its BVH, views and buffers.  All
 // pointers are device pointers.
 struct JobDev {
@@ -186,7 +201,20 @@ struct JobDev {
   // the samples are traced through the hierarchy)
   unsigned long long* vis_fwd;
   unsigned long long* vis_adj;
-  const uint32_t* ra_state;  // bit 0 set: the raster pass wrote nothing this call
+  const uint32_t* ra_state;  // bit 0: the raster pass wrote nothing this call; bit 1: its tile lists
+                             // hold the current geometry (cleared by every refit)
+  // the raster pass's screen tiles (tw x th pixels, ntx x nty per view): per
+  // (view, tile) the list offsets ([count] = total), the (view, leaf) entries
+  // and their footprints (4 float4 each); null when there is no raster pass
+  const uint32_t* ra_tiles;
+  const int* ra_list;
+  const float4* ra_rec;
+  int ra_tw, ra_th, ra_ntx, ra_nty;
+  // point-light shadow rays through light-space cells (null: traced)
+  const LightGrid* sh_grid;
+  const uint32_t* sh_cells;  // per cell the offset of its list, [G*G] = total
+  const int* sh_list;        // triangle leaf slots
+  const float4* sh_rec;      // per leaf slot its light-space footprint (box, three edge lines)
 };
 
 // Record slots a work item of NS samples may fill (deterministic mode):

@@ -229,15 +229,15 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
     const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
     f3 color_in, color_out;
     if (PAIRS) {
-      const f3 mine = shade_generic(J, cam, side ? coutx : cinx, side ? couty : ciny, side ? key_out : key_in);
+      const f3 mine = shade_generic(J, cam, side ? coutx : cinx, side ? couty : ciny, side ? key_out : key_in, view);
       const unsigned pair = 3u << (lane & ~1);  // both lanes of an entry take this branch
       const f3 other = mk(__shfl_xor_sync(pair, mine.x, 1), __shfl_xor_sync(pair, mine.y, 1),
                           __shfl_xor_sync(pair, mine.z, 1));
       color_in = side ? other : mine;
       color_out = side ? mine : other;
     } else {
-      color_in = shade_generic(J, cam, cinx, ciny, key_in);
-      color_out = shade_generic(J, cam, coutx, couty, key_out);
+      color_in = shade_generic(J, cam, cinx, ciny, key_in, view);
+      color_out = shade_generic(J, cam, coutx, couty, key_out, view);
     }
     const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
     const float weight = 1.0f / (pdf * (float)J.edge_samples);

@@ -490,6 +490,23 @@ void sync_dev(Job& J) {
   d.vis_fwd = J.raster_on ? J.vis[0].p : nullptr;
   d.vis_adj = J.raster_on ? J.vis[1].p : nullptr;
   d.ra_state = J.ra_state.p;
+  d.ra_tiles = J.raster_on ? J.ra_tiles.p : nullptr;
+  d.ra_list = J.ra_list.p;
+  d.ra_rec = J.ra_rec.p;
+  raster_tile(J.S, d.ra_tw, d.ra_th);
+  {
+    int W = 1, H = 1;
+    for (auto& c : J.h_cams) {
+      W = std::max(W, (int)c.width);
+      H = std::max(H, (int)c.height);
+    }
+    d.ra_ntx = (W + d.ra_tw - 1) / d.ra_tw;
+    d.ra_nty = (H + d.ra_th - 1) / d.ra_th;
+  }
+  d.sh_grid = J.shadow_on ? J.sh_grid.p : nullptr;
+  d.sh_cells = J.sh_cells.p;
+  d.sh_list = J.sh_list.p;
+  d.sh_rec = J.sh_rec.p;
   d.n_edges = J.n_edges;
   d.proj = J.proj.p;
   d.pmf = J.pmf.p;

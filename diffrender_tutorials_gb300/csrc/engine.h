@@ -163,7 +163,13 @@ struct Job {
   DevBuf<uint32_t> ra_tiles;          // triangles per screen tile, then their offsets (scan)
   DevBuf<uint32_t> ra_cursor;         // per tile fill cursor
   DevBuf<uint32_t> ra_state;          // bit 0: the tile lists did not fit ra_list
-  DevBuf<int> ra_list;                // per tile the triangles (leaf slots) whose footprint overlaps it
+  DevBuf<int> ra_list;                // per tile the (view, leaf) footprints that overlap it
+  DevBuf<float4> ra_rec;              // per (view, leaf) its footprint (4 float4)
+  bool shadow_on = false;             // light-space cells for point-light shadow rays (renderer::raster_buffers)
+  DevBuf<LightGrid> sh_grid;
+  DevBuf<uint32_t> sh_cells, sh_cursor;
+  DevBuf<int> sh_list;
+  DevBuf<float4> sh_rec;
   int tile_w = 4, tile_h = 4;
   // scene
   bool committed = false;
@@ -311,6 +317,9 @@ void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
 void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int nty, int tw, int th, cudaStream_t s);
 // Raster tile of tw x th pixels for S samples per pixel.
 void raster_tile(int S, int& tw, int& th);
+// Light-space cells (G x G) of point-light shadow rays for the current geometry.
+void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s);
+int light_grid_size(int n_tris);
 void launch_rs_scan(uint32_t* hist, int m, cudaStream_t s);
 void launch_adj_convert(const JobDev* d_job, int64_t n_pixels, cudaStream_t s);
 void launch_cast(const JobDev* d_job, const CamDev* d_cam, const float* d_xy, int64_t n, uint32_t* prim,

@@ -9,9 +9,10 @@
 //   bin     : per (view, triangle) a conservative screen footprint -- the
 //             projected triangle grown by RA_MARGIN pixels -- and the tiles
 //             its box overlaps; per tile a count, an exclusive scan, then
-//             the lists (triangle leaf slots) filled through per-tile cursors;
+//             the lists (view, triangle) filled through per-tile cursors;
 //   resolve : one block per (view, tile).  The tile's triangles are staged
-//             in shared memory with their screen edge lines; every thread
+//             in shared memory with the screen edge lines the binning pass
+//             stored for them; every thread
 //             takes samples of the tile, builds the sample's camera ray once
 //             (camera_ray, the reference's arithmetic) and runs the
 //             reference's Moller-Trumbore test (mt_test) on each staged
@@ -31,6 +32,8 @@
 // fit sets the state word, the resolve pass then writes nothing and the
 // pixel kernel traces its samples (same results), and the renderer doubles
 // the capacity for the next call.
+#include <cmath>
+
 #include "engine.h"
 
 namespace drgb {
@@ -109,13 +112,21 @@ __device__ __forceinline__ void ra_tiles(const RaTri& r, int tw, int th, int ntx
   ty1 = min(nty - 1, (int)floorf(r.y1) / th);
 }
 
-// PASS 0: count triangles per tile; PASS 1: fill the lists.  Thread j =
-// (view, leaf slot), view-major.  `tiles` = per view ntx*nty counters, then
+// A footprint as the resolve pass reads it: box, then the three edge lines
+// (all zero when unusable: 0 >= 0 holds), 16 floats.
+struct __align__(16) RaRec {
+  float4 box;         // x0, x1, y0, y1
+  float4 l0, l1, l2;  // nx, ny, c, unused
+};
+
+// PASS 0: each (view, leaf slot) thread j (view-major) stores its footprint
+// record in `rec[j]` and counts itself in every tile its box overlaps;
+// PASS 1: fills the lists with j.  `tiles` = per view ntx*nty counters, then
 // (scanned) offsets with the total at [n_tiles]; `cursor` per tile; `list`
 // of `cap` slots; `state` bit 0 set when the lists do not fit.
 template <int PASS>
 __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint32_t* tiles, uint32_t* cursor,
-                      int* list, uint32_t cap, uint32_t* state) {
+                      int* list, uint32_t cap, uint32_t* state, RaRec* rec) {
   const JobDev& J = jobs[0];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= J.n_views * J.n_tris) return;
@@ -126,7 +137,16 @@ __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint
     return;
   }
   RaTri r;
-  if (!ra_setup(J, J.cams[view], leaf, r)) return;
+  const bool ok = ra_setup(J, J.cams[view], leaf, r);
+  if (PASS == 0) {
+    RaRec q;
+    q.box = ok ? make_float4(r.x0, r.x1, r.y0, r.y1) : make_float4(1.0f, 0.0f, 1.0f, 0.0f);
+    q.l0 = make_float4(r.nx[0], r.ny[0], r.c[0], 0.0f);
+    q.l1 = make_float4(r.nx[1], r.ny[1], r.c[1], 0.0f);
+    q.l2 = make_float4(r.nx[2], r.ny[2], r.c[2], 0.0f);
+    rec[j] = q;
+  }
+  if (!ok) return;
   int tx0, tx1, ty0, ty1;
   ra_tiles(r, tw, th, ntx, nty, tx0, tx1, ty0, ty1);
   const int base = view * ntx * nty;
@@ -137,20 +157,64 @@ __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint
         atomicAdd(tiles + t, 1u);
       } else {
         const uint32_t pos = tiles[t] + atomicAdd(cursor + t, 1u);
-        list[pos] = leaf;
+        list[pos] = j;
       }
     }
 }
 
+// Sample s of a tile in pass `pass`: its pixel, index and position (the
+// pixel kernel's float operations).
+__device__ __forceinline__ bool ra_sample(const JobDev& J, int pass, int s, int tile_samples, int tx, int ty,
+                                          int tw, int th, int W, int H, int& px, int& py, int& k, float& x,
+                                          float& y) {
+  const int S = J.S, sq = J.sq;
+  const int p = s / S;
+  k = s - p * S;
+  px = tx * tw + p % tw;
+  py = ty * th + p / tw;
+  x = y = 0.0f;
+  if (!(s < tile_samples && px < W && py < H)) return false;
+  if (pass == 0) {
+    const int dy = k / sq, dx = k - dy * sq;
+    x = (float)px + (dx + 0.5f) / (float)sq;
+    y = (float)py + (dy + 0.5f) / (float)sq;
+  } else {
+    x = (float)px + __ldg(J.ham + 2 * k);
+    y = (float)py + __ldg(J.ham + 2 * k + 1);
+  }
+  return true;
+}
+
+// Nearest-hit update of one sample against staged triangle c.
+__device__ __forceinline__ void ra_test(const float4* s_a, const float4* s_e1, const float4* s_e2,
+                                        const RaRec* s_rec, int c, bool act, float x, float y, f3 ro, f3 rd,
+                                        unsigned long long& best, unsigned& n_tests) {
+  if (!act) return;
+  const RaRec& q = s_rec[c];
+  if (!(x >= q.box.x && x <= q.box.y && y >= q.box.z && y <= q.box.w)) return;
+  if (!(q.l0.x * x + q.l0.y * y + q.l0.z >= 0.0f && q.l1.x * x + q.l1.y * y + q.l1.z >= 0.0f &&
+        q.l2.x * x + q.l2.y * y + q.l2.z >= 0.0f))
+    return;
+  const float4 a = s_a[c];
+  float tt, u, v;
+  n_tests++;
+  if (mt_test(ro, rd, f4to3(a), f4to3(s_e1[c]), f4to3(s_e2[c]), 0.0f, tt, u, v) && tt < 1e9f) {
+    const unsigned long long key = ((unsigned long long)__float_as_uint(tt) << 32) | (uint32_t)__float_as_int(a.w);
+    best = key < best ? key : best;
+  }
+}
+
 // One block per (view, tile): the nearest hit of every forward (passes & 1)
-// and adjoint (passes & 2) sample of the tile's pixels.
+// and adjoint (passes & 2) sample of the tile's pixels.  The tile's
+// triangles are staged once per RA_STAGE for both passes; a thread holds
+// one forward and one adjoint sample (tiles of at most RA_THREADS samples),
+// whose two independent tests interleave.  Larger tiles (more than
+// RA_THREADS samples per pixel) take their samples RA_THREADS at a time.
 __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int passes, int tw, int th, int ntx,
                                                         int nty, const uint32_t* tiles, const int* list,
-                                                        const uint32_t* state) {
+                                                        const uint32_t* state, const RaRec* rec) {
   __shared__ float4 s_a[RA_STAGE], s_e1[RA_STAGE], s_e2[RA_STAGE];  // A | id bits, e1, e2
-  __shared__ float s_box[RA_STAGE][4];
-  __shared__ float s_lin[RA_STAGE][9];
-  __shared__ int s_lines[RA_STAGE];
+  __shared__ RaRec s_rec[RA_STAGE];
   if (*state & 1u) return;  // lists did not fit: the pixel kernel traces
   const JobDev& J = jobs[0];
   const int b = blockIdx.x;
@@ -159,86 +223,214 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
   const int ty = t / ntx, tx = t - ty * ntx;
   const CamDev& cam = J.cams[view];
   const int W = (int)cam.width, H = (int)cam.height;
-  const int S = J.S, sq = J.sq;
+  const int S = J.S;
   const uint32_t l0 = tiles[b], l1 = tiles[b + 1];
   const int n_list = (int)(l1 - l0);
   const int64_t vbase = J.img_off[view];
   const int tile_samples = tw * th * S;
-  for (int pass = 0; pass < 2; pass++) {
-    if (!((passes >> pass) & 1)) continue;
-    unsigned long long* vis = pass == 0 ? J.vis_fwd : J.vis_adj;
-    // every sample of the tile is written: a miss as ~0
-    for (int s0 = 0; s0 < tile_samples; s0 += RA_THREADS) {
-      const int s = s0 + threadIdx.x;
-      const int p = s / S, k = s - p * S;
-      const int px = tx * tw + p % tw, py = ty * th + p / tw;
-      const bool act = s < tile_samples && px < W && py < H;
-      float x = 0.0f, y = 0.0f;
-      if (act) {
-        if (pass == 0) {
-          const int dy = k / sq, dx = k - dy * sq;
-          x = (float)px + (dx + 0.5f) / (float)sq;  // the pixel kernel's grid position
-          y = (float)py + (dy + 0.5f) / (float)sq;
-        } else {
-          x = (float)px + __ldg(J.ham + 2 * k);
-          y = (float)py + __ldg(J.ham + 2 * k + 1);
-        }
+  const bool fwd = passes & 1, adj = (passes >> 1) & 1;
+  for (int s0 = 0; s0 < tile_samples; s0 += RA_THREADS) {
+    const int s = s0 + threadIdx.x;
+    int px0, py0, k0, px1, py1, k1;
+    float x0, y0, x1, y1;
+    const bool a0 = fwd && ra_sample(J, 0, s, tile_samples, tx, ty, tw, th, W, H, px0, py0, k0, x0, y0);
+    const bool a1 = adj && ra_sample(J, 1, s, tile_samples, tx, ty, tw, th, W, H, px1, py1, k1, x1, y1);
+    f3 ro0 = mk(0.0f, 0.0f, 0.0f), rd0 = mk(0.0f, 0.0f, 1.0f), ro1 = ro0, rd1 = rd0;
+    if (n_list > 0) {
+      if (a0) camera_ray(cam, x0, y0, ro0, rd0);
+      if (a1) camera_ray(cam, x1, y1, ro1, rd1);
+    }
+    unsigned long long b0 = ~0ull, b1 = ~0ull;
+    unsigned n_tests = 0;
+    for (int c0 = 0; c0 < n_list; c0 += RA_STAGE) {
+      const int nc = min(RA_STAGE, n_list - c0);
+      if (c0 > 0 || s0 > 0) __syncthreads();  // the previous stage is no longer read
+      if ((int)threadIdx.x < nc) {
+        const int j = list[l0 + c0 + threadIdx.x];
+        const int leaf = j - view * J.n_tris;
+        s_a[threadIdx.x] = __ldg(J.tri + 3 * leaf);
+        s_e1[threadIdx.x] = __ldg(J.tri + 3 * leaf + 1);
+        s_e2[threadIdx.x] = __ldg(J.tri + 3 * leaf + 2);
+        s_rec[threadIdx.x] = rec[j];
       }
-      f3 ro = mk(0.0f, 0.0f, 0.0f), rd = mk(0.0f, 0.0f, 1.0f);
-      if (act && n_list > 0) camera_ray(cam, x, y, ro, rd);
-      unsigned long long best = ~0ull;
-      unsigned n_tests = 0;
-      for (int c0 = 0; c0 < n_list; c0 += RA_STAGE) {
-        const int nc = min(RA_STAGE, n_list - c0);
-        __syncthreads();  // the previous stage is no longer read
-        if ((int)threadIdx.x < nc) {
-          const int leaf = list[l0 + c0 + threadIdx.x];
-          RaTri r;
-          const bool ok = ra_setup(J, cam, leaf, r);
-          s_a[threadIdx.x] = __ldg(J.tri + 3 * leaf);
-          s_e1[threadIdx.x] = __ldg(J.tri + 3 * leaf + 1);
-          s_e2[threadIdx.x] = __ldg(J.tri + 3 * leaf + 2);
-          // an empty box (x0 > x1) for a footprint that turned out empty
-          s_box[threadIdx.x][0] = ok ? r.x0 : 1.0f;
-          s_box[threadIdx.x][1] = ok ? r.x1 : 0.0f;
-          s_box[threadIdx.x][2] = ok ? r.y0 : 1.0f;
-          s_box[threadIdx.x][3] = ok ? r.y1 : 0.0f;
-          s_lines[threadIdx.x] = ok && r.edge_test;
-#pragma unroll
-          for (int e = 0; e < 3; e++) {
-            s_lin[threadIdx.x][3 * e + 0] = r.nx[e];
-            s_lin[threadIdx.x][3 * e + 1] = r.ny[e];
-            s_lin[threadIdx.x][3 * e + 2] = r.c[e];
-          }
-        }
-        __syncthreads();
-        if (act) {
-          for (int c = 0; c < nc; c++) {
-            if (!(x >= s_box[c][0] && x <= s_box[c][1] && y >= s_box[c][2] && y <= s_box[c][3])) continue;
-            if (s_lines[c]) {
-              const float* L = s_lin[c];
-              if (!(L[0] * x + L[1] * y + L[2] >= 0.0f && L[3] * x + L[4] * y + L[5] >= 0.0f &&
-                    L[6] * x + L[7] * y + L[8] >= 0.0f))
-                continue;
-            }
-            const float4 a = s_a[c];
-            float tt, u, v;
-            n_tests++;
-            if (mt_test(ro, rd, f4to3(a), f4to3(s_e1[c]), f4to3(s_e2[c]), 0.0f, tt, u, v) && tt < 1e9f) {
-              const unsigned long long key =
-                  ((unsigned long long)__float_as_uint(tt) << 32) | (uint32_t)__float_as_int(a.w);
-              best = key < best ? key : best;
-            }
-          }
-        }
-      }
-      if (act) vis[(vbase + (int64_t)py * W + px) * S + k] = best;
-      if (J.work && act && n_list > 0) {
-        atomicAdd(J.work + 0, 1ull);  // the sample's camera ray
-        atomicAdd(J.work + 2, (unsigned long long)n_tests);
+      __syncthreads();
+      for (int c = 0; c < nc; c++) {
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, n_tests);
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, n_tests);
       }
     }
+    // every sample of the tile is written: a miss as ~0
+    if (a0) J.vis_fwd[(vbase + (int64_t)py0 * W + px0) * S + k0] = b0;
+    if (a1) J.vis_adj[(vbase + (int64_t)py1 * W + px1) * S + k1] = b1;
+    if (J.work && n_list > 0 && (a0 || a1)) {
+      atomicAdd(J.work + 0, (unsigned long long)(a0 + a1));  // the samples' camera rays
+      atomicAdd(J.work + 2, (unsigned long long)n_tests);
+    }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Shadow rays toward the point light (LAMBERT_POINT_VCOLOR, PATH_DIFFUSE).
+// Every shadow ray runs from a surface point p to the light, so in a view
+// from the light the whole segment sits at p's grid position: the triangles
+// it can meet are those whose light-space footprint holds that position.
+// The grid covers the scene's bounding sphere (from the leaf triangles); a
+// light inside or near the sphere leaves the grid unusable (ok = 0) and the
+// rays are traced.  Lists per cell as for the camera tiles.
+// ---------------------------------------------------------------------------
+constexpr int SH_THREADS = 1024;
+
+__global__ void __launch_bounds__(SH_THREADS) k_light_grid(const JobDev* jobs, LightGrid* g, int G) {
+  __shared__ float red[6][SH_THREADS / 32];
+  const JobDev& J = jobs[0];
+  const float inf = __int_as_float(0x7f800000);
+  float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+  for (int k = threadIdx.x; k < J.n_tris; k += SH_THREADS) {
+    const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+    const float P[3][3] = {{a.x, a.y, a.z}, {a.x + e1.x, a.y + e1.y, a.z + e1.z}, {a.x + e2.x, a.y + e2.y, a.z + e2.z}};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        lo[c] = fminf(lo[c], P[i][c]);
+        hi[c] = fmaxf(hi[c], P[i][c]);
+      }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+    if (lane == 0) {
+      red[c][warp] = lo[c];
+      red[3 + c][warp] = hi[c];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < SH_THREADS / 32; w++)
+    for (int c = 0; c < 3; c++) {
+      red[c][0] = fminf(red[c][0], red[c][w]);
+      red[3 + c][0] = fmaxf(red[3 + c][0], red[3 + c][w]);
+    }
+  LightGrid q;
+  q.lx = J.mp.light_pos[0];
+  q.ly = J.mp.light_pos[1];
+  q.lz = J.mp.light_pos[2];
+  const float cx = 0.5f * (red[0][0] + red[3][0]), cy = 0.5f * (red[1][0] + red[4][0]),
+              cz = 0.5f * (red[2][0] + red[5][0]);
+  const float ex = red[3][0] - red[0][0], ey = red[4][0] - red[1][0], ez = red[5][0] - red[2][0];
+  const float r = 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) * 1.001f + 1e-6f;
+  float wx = cx - q.lx, wy = cy - q.ly, wz = cz - q.lz;
+  const float d = sqrtf(wx * wx + wy * wy + wz * wz);
+  q.G = G;
+  q.valid = 0;
+  q.overflow = 0;
+  q.ok = J.n_tris > 0 && d > 1.05f * r && isfinite(d);
+  if (q.ok) {
+    wx /= d; wy /= d; wz /= d;
+    // u = normalize(up x w), v = w x u, up the axis least aligned with w
+    const bool yup = fabsf(wy) < 0.9f;
+    const float upx = yup ? 0.0f : 1.0f, upy = yup ? 1.0f : 0.0f;
+    float ux = upy * wz, uy = -upx * wz, uz = upx * wy - upy * wx;
+    const float ul = sqrtf(ux * ux + uy * uy + uz * uz);
+    ux /= ul; uy /= ul; uz /= ul;
+    q.ux = ux; q.uy = uy; q.uz = uz;
+    q.vx = wy * uz - wz * uy; q.vy = wz * ux - wx * uz; q.vz = wx * uy - wy * ux;
+    q.wx = wx; q.wy = wy; q.wz = wz;
+    const float sn = r / d;
+    const float tn = sn / sqrtf(1.0f - sn * sn) * 1.02f;  // tangent of the cone around the sphere
+    q.half = 0.5f * (float)G;
+    q.scale = q.half / tn;
+  } else {
+    q.ux = q.uy = q.uz = q.vx = q.vy = q.vz = q.wx = q.wy = q.wz = 0.0f;
+    q.half = q.scale = 0.0f;
+  }
+  *g = q;
+}
+
+// PASS 0: footprint record of leaf k and its cell counts; PASS 1: the lists.
+template <int PASS>
+__global__ void k_light_bin(const JobDev* jobs, LightGrid* g, uint32_t* cells, uint32_t* cursor, int* list,
+                            uint32_t cap, float4* rec) {
+  const JobDev& J = jobs[0];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= J.n_tris || !g->ok) return;
+  const int G = g->G;
+  if (PASS == 1 && cells[G * G] > cap) {
+    if (k == 0) g->overflow = 1;
+    return;
+  }
+  const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+  const f3 P[3] = {f4to3(a), mk(a.x + e1.x, a.y + e1.y, a.z + e1.z), mk(a.x + e2.x, a.y + e2.y, a.z + e2.z)};
+  float sa[3], sb[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) light_project(*g, P[i], sa[i], sb[i]);
+  const float x0 = fminf(sa[0], fminf(sa[1], sa[2])) - RA_MARGIN, x1 = fmaxf(sa[0], fmaxf(sa[1], sa[2])) + RA_MARGIN;
+  const float y0 = fminf(sb[0], fminf(sb[1], sb[2])) - RA_MARGIN, y1 = fmaxf(sb[0], fmaxf(sb[1], sb[2])) + RA_MARGIN;
+  if (PASS == 0) {
+    float4 L[3] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+    const float area2 = (sa[1] - sa[0]) * (sb[2] - sb[0]) - (sb[1] - sb[0]) * (sa[2] - sa[0]);
+    if (fabsf(area2) > 1e-6f) {
+      const float sg = area2 > 0.0f ? 1.0f : -1.0f;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int j = i == 2 ? 0 : i + 1;
+        const float dx = sa[j] - sa[i], dy = sb[j] - sb[i];
+        const float inv = 1.0f / sqrtf(dx * dx + dy * dy);
+        const float nx = -dy * inv * sg, ny = dx * inv * sg;
+        L[i] = make_float4(nx, ny, -(nx * sa[i] + ny * sb[i]) + RA_MARGIN, 0.0f);
+      }
+    }
+    rec[4 * k + 0] = make_float4(x0, x1, y0, y1);
+    rec[4 * k + 1] = L[0];
+    rec[4 * k + 2] = L[1];
+    rec[4 * k + 3] = L[2];
+  }
+  const int cx0 = min(G - 1, max(0, (int)floorf(x0))), cx1 = min(G - 1, max(0, (int)floorf(x1)));
+  const int cy0 = min(G - 1, max(0, (int)floorf(y0))), cy1 = min(G - 1, max(0, (int)floorf(y1)));
+  for (int cy = cy0; cy <= cy1; cy++)
+    for (int cx = cx0; cx <= cx1; cx++) {
+      const int c = cy * G + cx;
+      if (PASS == 0) {
+        atomicAdd(cells + c, 1u);
+      } else {
+        const uint32_t pos = cells[c] + atomicAdd(cursor + c, 1u);
+        list[pos] = k;
+      }
+    }
+}
+
+__global__ void k_light_valid(LightGrid* g) { g->valid = g->ok && !g->overflow; }
+
+// Light-space cells of the current geometry (grid G x G).
+void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s) {
+  LightGrid* g = J.sh_grid.p;
+  const int n_cells = G * G;
+  DRGB_CUDA(cudaMemsetAsync(J.sh_cells.p, 0, sizeof(uint32_t) * (n_cells + 1), s));
+  DRGB_CUDA(cudaMemsetAsync(J.sh_cursor.p, 0, sizeof(uint32_t) * n_cells, s));
+  k_light_grid<<<1, SH_THREADS, 0, s>>>(d_job, g, G);
+  const int grid = (J.n_tris + 255) / 256;
+  k_light_bin<0><<<grid, 256, 0, s>>>(d_job, g, J.sh_cells.p, J.sh_cursor.p, J.sh_list.p, (uint32_t)J.sh_list.n,
+                                      J.sh_rec.p);
+  launch_rs_scan(J.sh_cells.p, n_cells + 1, s);
+  k_light_bin<1><<<grid, 256, 0, s>>>(d_job, g, J.sh_cells.p, J.sh_cursor.p, J.sh_list.p, (uint32_t)J.sh_list.n,
+                                      J.sh_rec.p);
+  k_light_valid<<<1, 1, 0, s>>>(g);
+  count_launch(4);
+}
+
+// Cells per side of the light grid for n triangles (a few cells each).
+int light_grid_size(int n_tris) {
+  int G = (int)(2.0 * std::sqrt((double)std::max(1, n_tris)));
+  return std::min(1024, std::max(32, (G + 7) / 8 * 8));
+}
+
+// The lists hold the current geometry unless they did not fit.
+__global__ void k_tiles_valid(uint32_t* state) {
+  if (!(*state & 1u)) *state |= 2u;
 }
 
 // Tile shape for S samples per pixel: square, at most RA_THREADS samples.
@@ -259,11 +451,15 @@ void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int n
   DRGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * n_tiles, s));
   DRGB_CUDA(cudaMemsetAsync(state, 0, sizeof(uint32_t), s));
   const int grid = (tasks + 255) / 256;
-  k_bin<0><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state);
+  RaRec* rec = reinterpret_cast<RaRec*>(J.ra_rec.p);
+  k_bin<0><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state,
+                                rec);
   launch_rs_scan(tiles, n_tiles + 1, s);
-  k_bin<1><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state);
-  k_resolve<<<n_tiles, RA_THREADS, 0, s>>>(d_job, passes, tw, th, ntx, nty, tiles, J.ra_list.p, state);
-  count_launch(3);
+  k_bin<1><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state,
+                                rec);
+  k_resolve<<<n_tiles, RA_THREADS, 0, s>>>(d_job, passes, tw, th, ntx, nty, tiles, J.ra_list.p, state, rec);
+  k_tiles_valid<<<1, 1, 0, s>>>(state);
+  count_launch(4);
 }
 
 }  // namespace drgb

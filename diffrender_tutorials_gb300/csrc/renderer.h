@@ -177,7 +177,11 @@ struct drgb_renderer {
   }
   void raster_buffers() {
     Job& J = job;
-    const bool on = J.raster && !J.trace_bruteforce && !J.store_hits && J.n_tris > 0 && J.n_views > 0;
+    // deterministic mode promises the same bits alone, in a batch and in the
+    // server, whose kernels trace: it traces too (the raster pass and the
+    // traversal find the same hits except the reference caster's
+    // clamped-determinant ones, which each finds only by chance)
+    const bool on = J.raster && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 && J.n_views > 0;
     if (on) {
       const size_t samples = (size_t)n_pixels() * J.S;
       J.vis[0].reserve(samples);
@@ -189,8 +193,20 @@ struct drgb_renderer {
       J.ra_cursor.reserve(n_tiles);
       J.ra_state.reserve(1);
       J.ra_list.reserve(std::max<size_t>(1u << 20, (size_t)16 * J.n_views * J.n_tris));
+      J.ra_rec.reserve((size_t)4 * J.n_views * J.n_tris);
     }
     J.raster_on = on;
+    // point-light shadow rays (the models with the point light)
+    const bool sh = on && (J.mode == LAMBERT_POINT_VCOLOR || J.mode == PATH_DIFFUSE);
+    if (sh) {
+      const int G = light_grid_size(J.n_tris);
+      J.sh_grid.reserve(1);
+      J.sh_cells.reserve(scan_scratch((size_t)G * G + 1));
+      J.sh_cursor.reserve((size_t)G * G);
+      J.sh_list.reserve(std::max<size_t>(1u << 20, (size_t)16 * J.n_tris));
+      J.sh_rec.reserve((size_t)4 * J.n_tris);
+    }
+    J.shadow_on = sh;
   }
 
   // The raster pass for the samples a pixel-kernel launch with `flags`
@@ -207,9 +223,19 @@ struct drgb_renderer {
     const size_t n_tiles = (size_t)J.n_views * ntx * nty;
     if (J.dev.vis_fwd != J.vis[0].p || J.dev.vis_adj != J.vis[1].p || J.dev.ra_state != J.ra_state.p ||
         J.vis[0].n < samples || J.vis[1].n < samples || J.ra_tiles.n < scan_scratch(n_tiles + 1) ||
-        J.ra_cursor.n < n_tiles || !J.ra_list.p)
+        J.ra_cursor.n < n_tiles || !J.ra_list.p || J.ra_rec.n < (size_t)4 * J.n_views * J.n_tris) {
+      // nothing built for this call: no stale list may be read either
+      if (J.ra_state.p) DRGB_CUDA(cudaMemsetAsync(J.ra_state.p, 0, sizeof(uint32_t), stream));
+      if (J.sh_grid.p) DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), stream));
       return 0;
+    }
     launch_raster(d_job.p, J, passes, ntx, nty, tw, th, stream);
+    const int G = light_grid_size(J.n_tris);
+    if (J.shadow_on && J.dev.sh_grid == J.sh_grid.p && J.sh_cells.n >= scan_scratch((size_t)G * G + 1) &&
+        J.sh_cursor.n >= (size_t)G * G && J.sh_rec.n >= (size_t)4 * J.n_tris && J.sh_list.p)
+      launch_light_grid(d_job.p, J, G, stream);
+    else if (J.sh_grid.p)
+      DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), stream));
     return PX_VIS;
   }
 
@@ -225,6 +251,16 @@ struct drgb_renderer {
       DRGB_CUDA(cudaMemset(J.ra_state.p, 0, sizeof(uint32_t)));
       graph_valid = false;
       push_dev();
+    }
+    if (J.shadow_on && J.sh_grid.p) {
+      LightGrid g;
+      DRGB_CUDA(cudaMemcpy(&g, J.sh_grid.p, sizeof(g), cudaMemcpyDeviceToHost));
+      if (g.overflow) {
+        J.sh_list.alloc(2 * J.sh_list.n);
+        DRGB_CUDA(cudaMemset(J.sh_grid.p, 0, sizeof(LightGrid)));
+        graph_valid = false;
+        push_dev();
+      }
     }
   }
 

@@ -193,6 +193,67 @@ __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, flo
   return true;
 }
 
+// Whether a camera ray of `view` at image position (x, y) can use the
+// raster pass's tile lists (built for this call's geometry; the footprints
+// are clipped to the image, so only positions inside it).
+__device__ __forceinline__ bool tiles_usable(const JobDev& J, const CamDev& cam, float x, float y) {
+  return J.ra_tiles && (*J.ra_state & 2u) && x >= 0.0f && x < cam.width && y >= 0.0f && y < cam.height;
+}
+
+// The nearest hit of the camera ray of `view` at (x, y) among the triangles
+// of its screen tile: the reference's test on each footprint holding the
+// point, the smallest {t, flattened triangle} kept (the traversal's tie
+// rule); t, u, v are those the test computed.
+__device__ __forceinline__ bool cast_tiles(const JobDev& J, const CamDev& cam, int view, float x, float y,
+                                           bool active, Surf& s) {
+  camera_ray(cam, x, y, s.ro, s.rd);
+  s.h.t = 1e9f;
+  s.h.tri = -1;
+  s.h.u = s.h.v = 0.0f;
+  s.A = s.B = s.C = 0;
+  s.block = 0;
+  if (!active) return false;
+  const int tx = min(J.ra_ntx - 1, (int)x / J.ra_tw), ty = min(J.ra_nty - 1, (int)y / J.ra_th);
+  const int b = (view * J.ra_nty + ty) * J.ra_ntx + tx;
+  const uint32_t i0 = __ldg(J.ra_tiles + b), i1 = __ldg(J.ra_tiles + b + 1);
+  unsigned long long best = ~0ull;
+  float bu = 0.0f, bv = 0.0f;
+  unsigned n_tri = 0;
+  for (uint32_t i = i0; i < i1; i++) {
+    const int j = __ldg(J.ra_list + i);
+    const float4 box = __ldg(J.ra_rec + 4 * j);
+    if (!(x >= box.x && x <= box.y && y >= box.z && y <= box.w)) continue;
+    const float4 q0 = __ldg(J.ra_rec + 4 * j + 1), q1 = __ldg(J.ra_rec + 4 * j + 2), q2 = __ldg(J.ra_rec + 4 * j + 3);
+    if (!(q0.x * x + q0.y * y + q0.z >= 0.0f && q1.x * x + q1.y * y + q1.z >= 0.0f &&
+          q2.x * x + q2.y * y + q2.z >= 0.0f))
+      continue;
+    const int k = j - view * J.n_tris;
+    const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+    float t, u, v;
+    n_tri++;
+    if (mt_test(s.ro, s.rd, f4to3(a), f4to3(e1), f4to3(e2), 0.0f, t, u, v) && t < 1e9f) {
+      const unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | (uint32_t)__float_as_int(a.w);
+      if (key < best) {
+        best = key;
+        bu = u;
+        bv = v;
+      }
+    }
+  }
+  add_work(J, 0, n_tri);
+  if (best == ~0ull) return false;
+  s.h.t = __uint_as_float((uint32_t)(best >> 32));
+  s.h.u = bu;
+  s.h.v = bv;
+  s.h.tri = (int)(uint32_t)best;
+  const int4 tv = __ldg(J.tri_v + s.h.tri);
+  s.A = tv.x;
+  s.B = tv.y;
+  s.C = tv.z;
+  s.block = tv.w;
+  return true;
+}
+
 __device__ __forceinline__ bool cast(const JobDev& J, const CamDev& cam, float x, float y, Surf& s) {
   return cast_p<false>(J, cam, x, y, true, s);
 }
@@ -235,6 +296,55 @@ __device__ __forceinline__ float2 interp_tc(const JobDev& J, const Surf& s) {
 #else
 #define DRGB_LPV_ATTR __noinline__
 #endif
+// Grid coordinates of a point in the light's view (LightGrid).
+__device__ __forceinline__ void light_project(const LightGrid& g, f3 q, float& a, float& b) {
+  const float dx = q.x - g.lx, dy = q.y - g.ly, dz = q.z - g.lz;
+  const float z = dx * g.wx + dy * g.wy + dz * g.wz;
+  a = (dx * g.ux + dy * g.uy + dz * g.uz) / z * g.scale + g.half;
+  b = (dx * g.vx + dy * g.vy + dz * g.vz) / z * g.scale + g.half;
+}
+
+// Whether the shadow ray (p, l) toward the point light meets a triangle at
+// 0 < t < tfar: the reference's test (mt_test, any hit) on the triangles
+// whose light-space footprint holds p's grid position.  Every point of the
+// segment from p to the light has that grid position, so the triangles the
+// segment crosses are all among them (the footprints carry a margin of
+// 0.125 cells for rounding).  The caller checks that the grid is usable.
+__device__ __forceinline__ bool light_occluded(const JobDev& J, f3 p, f3 l, float tfar) {
+  const LightGrid& g = *J.sh_grid;
+  float a, b;
+  light_project(g, p, a, b);
+  const int cx = min(g.G - 1, max(0, (int)a)), cy = min(g.G - 1, max(0, (int)b));
+  const int c = cy * g.G + cx;
+  const uint32_t i0 = __ldg(J.sh_cells + c), i1 = __ldg(J.sh_cells + c + 1);
+  unsigned n_tri = 0;
+  bool occ = false;
+  for (uint32_t i = i0; i < i1 && !occ; i++) {
+    const int k = __ldg(J.sh_list + i);
+    const float4 box = __ldg(J.sh_rec + 4 * k);
+    if (!(a >= box.x && a <= box.y && b >= box.z && b <= box.w)) continue;
+    const float4 q0 = __ldg(J.sh_rec + 4 * k + 1), q1 = __ldg(J.sh_rec + 4 * k + 2), q2 = __ldg(J.sh_rec + 4 * k + 3);
+    if (!(q0.x * a + q0.y * b + q0.z >= 0.0f && q1.x * a + q1.y * b + q1.z >= 0.0f &&
+          q2.x * a + q2.y * b + q2.z >= 0.0f))
+      continue;
+    const float4 A = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
+    float t, u, v;
+    n_tri++;
+    occ = mt_test(p, l, f4to3(A), f4to3(e1), f4to3(e2), 0.0f, t, u, v) && t < tfar;
+  }
+  add_work(J, 0, n_tri);
+  return occ;
+}
+
+// Shadow ray toward the point light: the light-space cells when they hold
+// the current geometry, else the hierarchy.
+template <bool WARP>
+__device__ __forceinline__ bool point_shadow(const JobDev& J, f3 p, f3 l, float tfar, bool active) {
+  if (!WARP && J.sh_grid && J.sh_grid->valid) return active && light_occluded(J, p, l, tfar);
+  Hit sh;
+  return trace_p<true, WARP>(J, p, l, 0.0f, tfar, active, sh);
+}
+
 template <bool WARP>
 __device__ DRGB_LPV_ATTR float lpv_factor_p(const JobDev& J, const Surf& s, bool hit) {
   f3 p = mk(0.0f, 0.0f, 0.0f), l = mk(0.0f, 0.0f, 1.0f);
@@ -249,8 +359,7 @@ __device__ DRGB_LPV_ATTR float lpv_factor_p(const JobDev& J, const Surf& s, bool
     l = L / dist;
     ndl = ref_max(0.0f, dot(n, l));
   }
-  Hit sh;
-  const float vis = trace_p<true, WARP>(J, p, l, 0.0f, dist, hit && ndl > 0.0f, sh) ? 0.0f : 1.0f;
+  const float vis = point_shadow<WARP>(J, p, l, dist, hit && ndl > 0.0f) ? 0.0f : 1.0f;
   return vis * J.mp.light_intensity * ndl / d2 + J.mp.ambient;
 }
 
@@ -337,8 +446,7 @@ __device__ inline f3 path_diffuse_p(const JobDev& J, const Surf& first, uint32_t
       l = Lv / dist;
       ndl = ref_max(0.0f, dot(n, l));
     }
-    Hit sh;
-    const bool occluded = trace_p<true, WARP>(J, p, l, 0.0f, dist, hitb && ndl > 0.0f, sh);
+    const bool occluded = point_shadow<WARP>(J, p, l, dist, hitb && ndl > 0.0f);
     if (hitb && ndl > 0.0f && !occluded) {
       const float k = I * ndl / (d2 * 3.14159265f);
       L = L + (beta * alb) * k;
@@ -411,12 +519,17 @@ __device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
 // hit_tri (may be null) receives the camera ray's triangle, -1 on a miss.
 // use_vis (uniform over the launch): the camera ray's hit is the sample's
 // rasterised visibility key vkey instead of a traversal.
+// view >= 0: the camera ray may come from the raster pass's tile lists of
+// that view (see tiles_usable).
 template <int MODE, bool WARP>
 __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active,
-                             int* hit_tri = nullptr, bool use_vis = false, unsigned long long vkey = ~0ull) {
+                             int* hit_tri = nullptr, bool use_vis = false, unsigned long long vkey = ~0ull,
+                             int view = -1) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
-  const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s) : cast_p<WARP>(J, cam, x, y, active, s);
+  const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s)
+                   : (!WARP && view >= 0 && tiles_usable(J, cam, x, y)) ? cast_tiles(J, cam, view, x, y, active, s)
+                                                                       : cast_p<WARP>(J, cam, x, y, active, s);
   if (hit_tri) *hit_tri = hit ? s.h.tri : -1;
   const float u = s.h.u, v = s.h.v;
   switch (mode) {
@@ -497,13 +610,14 @@ __device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y,
 // The generic shader as one out-of-line function (callers that shade
 // several points keep a single copy of every model's code).
 #ifdef DRGB_EDGE_SHADE_NOINLINE
-static __device__ __noinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key) {
-  return shade_p<0, false>(J, cam, x, y, key, true);
+static __device__ __noinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key,
+                                                int view = -1) {
+  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, ~0ull, view);
 }
 #else
 static __device__ __forceinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y,
-                                                   uint32_t key) {
-  return shade_p<0, false>(J, cam, x, y, key, true);
+                                                   uint32_t key, int view = -1) {
+  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, ~0ull, view);
 }
 #endif
 

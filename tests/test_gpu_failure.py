@@ -27,6 +27,9 @@ def scene_and_cams():
 def test_traversal_step_limit_returns_kernel_error_and_recovers():
     s, cams = scene_and_cams()
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL.LAMBERT_POINT_VCOLOR, 4))
+    # camera samples and point-light shadow rays through the hierarchy (the
+    # raster pass and the light-space cells resolve them without traversal)
+    r.set_option(N.OPT_PRIMARY_RASTER, 0)
     r.commit(s)
     good = r.render(s, cams).reshape(-1)
     assert np.array_equal(good, O.render(s, cams, 16, 4))
@@ -51,6 +54,7 @@ def test_traversal_step_limit_in_the_optimiser_loop():
     surfaces from Run, and a later Run with the default bound succeeds."""
     s, cams = scene_and_cams()
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL.LAMBERT_POINT_VCOLOR, 4))
+    r.set_option(N.OPT_PRIMARY_RASTER, 0)  # every ray through the hierarchy
     r.commit(s)
     tgt = r.render(s, cams)
     init = D.Scene()
