@@ -103,6 +103,46 @@ __device__ __forceinline__ bool ra_setup(const JobDev& J, const CamDev& cam, int
   return true;
 }
 
+// A lower bound on the distance from `o` of any point of triangle P: the
+// distance to its centroid less its largest vertex distance, shrunk by a
+// relative 1e-5 and 1e-6 for rounding (0 when o is that close).  A hit on
+// the triangle at ray parameter t (unit direction) has t >= this bound, so a
+// query that already holds a hit nearer than the bound can skip it.
+__device__ __forceinline__ float dist_lower_bound(const f3 P[3], float ox, float oy, float oz) {
+  const float cx = (P[0].x + P[1].x + P[2].x) * (1.0f / 3.0f), cy = (P[0].y + P[1].y + P[2].y) * (1.0f / 3.0f),
+              cz = (P[0].z + P[1].z + P[2].z) * (1.0f / 3.0f);
+  float rb = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float dx = P[i].x - cx, dy = P[i].y - cy, dz = P[i].z - cz;
+    rb = fmaxf(rb, sqrtf(dx * dx + dy * dy + dz * dz));
+  }
+  const float dx = cx - ox, dy = cy - oy, dz = cz - oz;
+  const float lb = sqrtf(dx * dx + dy * dy + dz * dz) - rb * 1.0001f;
+  return lb > 0.0f ? lb * (1.0f - 1e-5f) - 1e-6f : 0.0f;
+}
+
+// Orders each list (lengths 2..64; longer ones stay unsorted) by the lower
+// bound in rec[4 * entry + 1].w, nearest first, so the queries meet the
+// triangles that can win first and skip the rest by one comparison.
+__global__ void k_sort_lists(const uint32_t* offs, int n_lists, int* list, const float4* rec, uint32_t cap) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_lists || offs[n_lists] > cap) return;  // lists that did not fit were not filled
+  const uint32_t i0 = offs[b], n = offs[b + 1] - i0;
+  if (n < 2 || n > 64) return;
+  int* L = list + i0;
+  for (uint32_t i = 1; i < n; i++) {
+    const int e = L[i];
+    const float key = rec[4 * e + 1].w;
+    int j = (int)i - 1;
+    while (j >= 0 && rec[4 * L[j] + 1].w > key) {
+      L[j + 1] = L[j];
+      j--;
+    }
+    L[j + 1] = e;
+  }
+}
+
 // Tile range of a footprint (tiles of tw x th pixels, ntx x nty per view).
 __device__ __forceinline__ void ra_tiles(const RaTri& r, int tw, int th, int ntx, int nty, int& tx0, int& tx1,
                                          int& ty0, int& ty1) {
@@ -116,7 +156,7 @@ __device__ __forceinline__ void ra_tiles(const RaTri& r, int tw, int th, int ntx
 // (all zero when unusable: 0 >= 0 holds), 16 floats.
 struct __align__(16) RaRec {
   float4 box;         // x0, x1, y0, y1
-  float4 l0, l1, l2;  // nx, ny, c, unused
+  float4 l0, l1, l2;  // nx, ny, c; l0.w: lower bound on the hit distance (dist_lower_bound)
 };
 
 // PASS 0: each (view, leaf slot) thread j (view-major) stores its footprint
@@ -137,11 +177,16 @@ __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint
     return;
   }
   RaTri r;
-  const bool ok = ra_setup(J, J.cams[view], leaf, r);
+  const CamDev& cam = J.cams[view];
+  const bool ok = ra_setup(J, cam, leaf, r);
   if (PASS == 0) {
+    const float4 a = __ldg(J.tri + 3 * leaf), e1 = __ldg(J.tri + 3 * leaf + 1), e2 = __ldg(J.tri + 3 * leaf + 2);
+    const f3 P[3] = {f4to3(a), mk(a.x + e1.x, a.y + e1.y, a.z + e1.z), mk(a.x + e2.x, a.y + e2.y, a.z + e2.z)};
+    // the camera rays start at wv_inv * (0,0,0,1) (camera_ray)
+    const float lb = dist_lower_bound(P, cam.wv_inv[12], cam.wv_inv[13], cam.wv_inv[14]);
     RaRec q;
     q.box = ok ? make_float4(r.x0, r.x1, r.y0, r.y1) : make_float4(1.0f, 0.0f, 1.0f, 0.0f);
-    q.l0 = make_float4(r.nx[0], r.ny[0], r.c[0], 0.0f);
+    q.l0 = make_float4(r.nx[0], r.ny[0], r.c[0], lb);
     q.l1 = make_float4(r.nx[1], r.ny[1], r.c[1], 0.0f);
     q.l2 = make_float4(r.nx[2], r.ny[2], r.c[2], 0.0f);
     rec[j] = q;
@@ -191,6 +236,8 @@ __device__ __forceinline__ void ra_test(const float4* s_a, const float4* s_e1, c
                                         unsigned long long& best, unsigned& n_tests) {
   if (!act) return;
   const RaRec& q = s_rec[c];
+  // no hit on this triangle can be nearer than the best so far (~0: none yet, NaN compares false)
+  if (q.l0.w > __uint_as_float((uint32_t)(best >> 32))) return;
   if (!(x >= q.box.x && x <= q.box.y && y >= q.box.z && y <= q.box.w)) return;
   if (!(q.l0.x * x + q.l0.y * y + q.l0.z >= 0.0f && q.l1.x * x + q.l1.y * y + q.l1.z >= 0.0f &&
         q.l2.x * x + q.l2.y * y + q.l2.z >= 0.0f))
@@ -384,6 +431,8 @@ __global__ void k_light_bin(const JobDev* jobs, LightGrid* g, uint32_t* cells, u
         L[i] = make_float4(nx, ny, -(nx * sa[i] + ny * sb[i]) + RA_MARGIN, 0.0f);
       }
     }
+    // shadow rays end at the light: a triangle no nearer to it than the ray's origin is not in the way
+    L[0].w = dist_lower_bound(P, g->lx, g->ly, g->lz);
     rec[4 * k + 0] = make_float4(x0, x1, y0, y1);
     rec[4 * k + 1] = L[0];
     rec[4 * k + 2] = L[1];
@@ -418,8 +467,10 @@ void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s)
   launch_rs_scan(J.sh_cells.p, n_cells + 1, s);
   k_light_bin<1><<<grid, 256, 0, s>>>(d_job, g, J.sh_cells.p, J.sh_cursor.p, J.sh_list.p, (uint32_t)J.sh_list.n,
                                       J.sh_rec.p);
+  k_sort_lists<<<(n_cells + 255) / 256, 256, 0, s>>>(J.sh_cells.p, n_cells, J.sh_list.p, J.sh_rec.p,
+                                                      (uint32_t)J.sh_list.n);
   k_light_valid<<<1, 1, 0, s>>>(g);
-  count_launch(4);
+  count_launch(5);
 }
 
 // Cells per side of the light grid for n triangles (a few cells each).
@@ -457,9 +508,11 @@ void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int n
   launch_rs_scan(tiles, n_tiles + 1, s);
   k_bin<1><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state,
                                 rec);
+  k_sort_lists<<<(n_tiles + 255) / 256, 256, 0, s>>>(tiles, n_tiles, J.ra_list.p, J.ra_rec.p,
+                                                     (uint32_t)J.ra_list.n);
   k_resolve<<<n_tiles, RA_THREADS, 0, s>>>(d_job, passes, tw, th, ntx, nty, tiles, J.ra_list.p, state, rec);
   k_tiles_valid<<<1, 1, 0, s>>>(state);
-  count_launch(4);
+  count_launch(5);
 }
 
 }  // namespace drgb

@@ -221,9 +221,12 @@ __device__ __forceinline__ bool cast_tiles(const JobDev& J, const CamDev& cam, i
   unsigned n_tri = 0;
   for (uint32_t i = i0; i < i1; i++) {
     const int j = __ldg(J.ra_list + i);
+    const float4 q0 = __ldg(J.ra_rec + 4 * j + 1);
+    // no hit on it can be nearer than the best so far (none yet: NaN compares false)
+    if (q0.w > __uint_as_float((uint32_t)(best >> 32))) continue;
     const float4 box = __ldg(J.ra_rec + 4 * j);
     if (!(x >= box.x && x <= box.y && y >= box.z && y <= box.w)) continue;
-    const float4 q0 = __ldg(J.ra_rec + 4 * j + 1), q1 = __ldg(J.ra_rec + 4 * j + 2), q2 = __ldg(J.ra_rec + 4 * j + 3);
+    const float4 q1 = __ldg(J.ra_rec + 4 * j + 2), q2 = __ldg(J.ra_rec + 4 * j + 3);
     if (!(q0.x * x + q0.y * y + q0.z >= 0.0f && q1.x * x + q1.y * y + q1.z >= 0.0f &&
           q2.x * x + q2.y * y + q2.z >= 0.0f))
       continue;
@@ -321,9 +324,11 @@ __device__ __forceinline__ bool light_occluded(const JobDev& J, f3 p, f3 l, floa
   bool occ = false;
   for (uint32_t i = i0; i < i1 && !occ; i++) {
     const int k = __ldg(J.sh_list + i);
+    const float4 q0 = __ldg(J.sh_rec + 4 * k + 1);
+    if (q0.w >= tfar) continue;  // no nearer to the light than p: not between them
     const float4 box = __ldg(J.sh_rec + 4 * k);
     if (!(a >= box.x && a <= box.y && b >= box.z && b <= box.w)) continue;
-    const float4 q0 = __ldg(J.sh_rec + 4 * k + 1), q1 = __ldg(J.sh_rec + 4 * k + 2), q2 = __ldg(J.sh_rec + 4 * k + 3);
+    const float4 q1 = __ldg(J.sh_rec + 4 * k + 2), q2 = __ldg(J.sh_rec + 4 * k + 3);
     if (!(q0.x * a + q0.y * b + q0.z >= 0.0f && q1.x * a + q1.y * b + q1.z >= 0.0f &&
           q2.x * a + q2.y * b + q2.z >= 0.0f))
       continue;
