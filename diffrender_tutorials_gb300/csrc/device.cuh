@@ -43,7 +43,7 @@ constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 enum ErrFlag : uint32_t {
   ERR_STACK_OVERFLOW = 1u,
   ERR_TRAVERSAL_LIMIT = 2u,
-  ERR_VISIBILITY = 8u,  // a rasterised hit names a triangle the leaf arrays do not hold where expected
+  ERR_VISIBILITY = 8u,  // a rasterised hit names a triangle the scene does not have
   ERR_BAD_INDEX = 4u,
 };
 
@@ -196,11 +196,11 @@ struct JobDev {
   int det_tr_key;            // (view, sample order), summed in a fixed order into grad[det_tr_key + 0..11]
   // stored adjoint hits (one float4 {t, u, v, triangle} per adjoint sample)
   float4* hit_buf;
-  // rasterised primary visibility: per forward / adjoint sample the minimum
-  // {t bits, triangle} of the hits found by the raster pass, or ~0 (null:
-  // the samples are traced through the hierarchy)
-  unsigned long long* vis_fwd;
-  unsigned long long* vis_adj;
+  // rasterised primary visibility: per forward / adjoint sample the nearest
+  // hit found by the raster pass, {t, u, v, triangle bits} (triangle -1: no
+  // hit); null: the samples are traced through the hierarchy
+  float4* vis_fwd;
+  float4* vis_adj;
   const uint32_t* ra_state;  // bit 0: the raster pass wrote nothing this call; bit 1: its tile lists
                              // hold the current geometry (cleared by every refit)
   // the raster pass's screen tiles (tw x th pixels, ntx x nty per view): per

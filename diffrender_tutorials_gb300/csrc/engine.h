@@ -159,7 +159,7 @@ struct Job {
   int edge_sil = 0;           // DRGB_OPT_EDGE_SET
   int raster = 1;             // DRGB_OPT_PRIMARY_RASTER
   bool raster_on = false;     // raster buffers set up for the current views (see renderer::raster_buffers)
-  DevBuf<unsigned long long> vis[2];  // rasterised visibility of forward / adjoint samples
+  DevBuf<float4> vis[2];              // rasterised visibility of forward / adjoint samples
   DevBuf<uint32_t> ra_tiles;          // triangles per screen tile, then their offsets (scan)
   DevBuf<uint32_t> ra_cursor;         // per tile fill cursor
   DevBuf<uint32_t> ra_state;          // bit 0: the tile lists did not fit ra_list

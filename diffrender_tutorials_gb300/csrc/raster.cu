@@ -19,9 +19,8 @@
 //             triangle whose footprint holds the sample, keeping the minimum
 //             {t bits, flattened triangle}: t > 0 orders as its float bits,
 //             equal t keeps the lowest triangle -- the brute-force loop's
-//             tie rule.  The key is written once per sample (no atomics).
-//
-// The pixel kernel then re-runs mt_test on the winning triangle for t, u, v.
+//             tie rule.  The hit {t, u, v, triangle} is written once per
+//             sample (no atomics), and the pixel kernel shades from it.
 // A hit that lies on its triangle projects inside it up to float rounding,
 // far below the margin, so every such hit is among the candidates and the
 // winner is the caster's nearest hit.  Not among them: the caster's
@@ -233,7 +232,7 @@ __device__ __forceinline__ bool ra_sample(const JobDev& J, int pass, int s, int 
 // Nearest-hit update of one sample against staged triangle c.
 __device__ __forceinline__ void ra_test(const float4* s_a, const float4* s_e1, const float4* s_e2,
                                         const RaRec* s_rec, int c, bool act, float x, float y, f3 ro, f3 rd,
-                                        unsigned long long& best, unsigned& n_tests) {
+                                        unsigned long long& best, float& bu, float& bv, unsigned& n_tests) {
   if (!act) return;
   const RaRec& q = s_rec[c];
   // no hit on this triangle can be nearer than the best so far (~0: none yet, NaN compares false)
@@ -247,8 +246,19 @@ __device__ __forceinline__ void ra_test(const float4* s_a, const float4* s_e1, c
   n_tests++;
   if (mt_test(ro, rd, f4to3(a), f4to3(s_e1[c]), f4to3(s_e2[c]), 0.0f, tt, u, v) && tt < 1e9f) {
     const unsigned long long key = ((unsigned long long)__float_as_uint(tt) << 32) | (uint32_t)__float_as_int(a.w);
-    best = key < best ? key : best;
+    if (key < best) {
+      best = key;
+      bu = u;
+      bv = v;
+    }
   }
+}
+
+// The hit record of a sample's best key: {t, u, v, triangle bits}, or a
+// miss {1e9, 0, 0, -1}.
+__device__ __forceinline__ float4 ra_hit(unsigned long long best, float u, float v) {
+  if (best == ~0ull) return make_float4(1e9f, 0.0f, 0.0f, __int_as_float(-1));
+  return make_float4(__uint_as_float((uint32_t)(best >> 32)), u, v, __int_as_float((int)(uint32_t)best));
 }
 
 // One block per (view, tile): the nearest hit of every forward (passes & 1)
@@ -288,6 +298,7 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
       if (a1) camera_ray(cam, x1, y1, ro1, rd1);
     }
     unsigned long long b0 = ~0ull, b1 = ~0ull;
+    float u0 = 0.0f, v0 = 0.0f, u1 = 0.0f, v1 = 0.0f;
     unsigned n_tests = 0;
     for (int c0 = 0; c0 < n_list; c0 += RA_STAGE) {
       const int nc = min(RA_STAGE, n_list - c0);
@@ -302,13 +313,13 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
       }
       __syncthreads();
       for (int c = 0; c < nc; c++) {
-        ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, n_tests);
-        ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, n_tests);
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, u0, v0, n_tests);
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, u1, v1, n_tests);
       }
     }
-    // every sample of the tile is written: a miss as ~0
-    if (a0) J.vis_fwd[(vbase + (int64_t)py0 * W + px0) * S + k0] = b0;
-    if (a1) J.vis_adj[(vbase + (int64_t)py1 * W + px1) * S + k1] = b1;
+    // every sample of the tile is written, a miss too
+    if (a0) J.vis_fwd[(vbase + (int64_t)py0 * W + px0) * S + k0] = ra_hit(b0, u0, v0);
+    if (a1) J.vis_adj[(vbase + (int64_t)py1 * W + px1) * S + k1] = ra_hit(b1, u1, v1);
     if (J.work && n_list > 0 && (a0 || a1)) {
       atomicAdd(J.work + 0, (unsigned long long)(a0 + a1));  // the samples' camera rays
       atomicAdd(J.work + 2, (unsigned long long)n_tests);

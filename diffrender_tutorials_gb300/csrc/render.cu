@@ -146,8 +146,7 @@ __device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, 
 template <int MODE, bool DET, bool HITS>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
                                            uint32_t key, float* wscr, int64_t rec_base, int& rec_n,
-                                           const float4* stored, int seed, bool use_vis,
-                                           unsigned long long vkey) {
+                                           const float4* stored, int seed, bool use_vis, float4 vkey) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   bool hit;
@@ -334,8 +333,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         if (s < NS) s_hit[s] = act ? ht : -1;
 #else
         const bool use_vis = vis_ok && J.vis_fwd != nullptr;
-        const unsigned long long vk =
-            act && use_vis ? J.vis_fwd[(J.img_off[view] + (int64_t)py * W + px) * S + k] : ~0ull;
+        const float4 vk = act && use_vis ? J.vis_fwd[(J.img_off[view] + (int64_t)py * W + px) * S + k]
+                                         : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, nullptr, use_vis, vk);
 #endif
         if (act) c = sc / (float)S;
@@ -436,8 +435,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         }
 #endif
         const bool use_vis = vis_ok && J.vis_adj != nullptr;
-        const unsigned long long vk =
-            act && use_vis ? J.vis_adj[(J.img_off[view] + (int64_t)py * W + px) * S + k] : ~0ull;
+        const float4 vk = act && use_vis ? J.vis_adj[(J.img_off[view] + (int64_t)py * W + px) * S + k]
+                                         : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed, use_vis, vk);
       }
       if (DET && J.det && lane == 0 && !store_hits) J.rec_count[it - J.item_base] = rec_n;

@@ -314,7 +314,7 @@ struct drgb_renderer {
       std::string m = "kernel error flags " + std::to_string(f);
       if (f & ERR_STACK_OVERFLOW) m += " (traversal stack overflow)";
       if (f & ERR_TRAVERSAL_LIMIT) m += " (traversal step limit)";
-      if (f & ERR_VISIBILITY) m += " (rasterised visibility out of step with the hierarchy's leaves)";
+      if (f & ERR_VISIBILITY) m += " (rasterised hit names a triangle the scene does not have)";
       throw CudaError(m, DRGB_ERR_KERNEL);
     }
   }

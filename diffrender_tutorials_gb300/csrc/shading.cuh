@@ -153,37 +153,26 @@ __device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float
   return hit;
 }
 
-// The camera ray of a sample whose nearest hit the raster pass found
-// (key = {t bits, flattened triangle}, ~0 for none): the reference's
-// Moller-Trumbore test on that triangle gives t, u, v bit-identical to the
-// traversal's.
+// The camera ray of a sample whose nearest hit the raster pass found:
+// hit = {t, u, v, triangle bits} (triangle -1: none), the values the
+// reference's ray/triangle test computed for that ray.
 __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, float x, float y, bool active,
-                                         unsigned long long key, Surf& s) {
+                                         float4 hit, Surf& s) {
   camera_ray(cam, x, y, s.ro, s.rd);
   s.h.t = 1e9f;
   s.h.tri = -1;
   s.h.u = s.h.v = 0.0f;
   s.A = s.B = s.C = 0;
   s.block = 0;
-  if (!active || key == ~0ull) return false;
-  const int id = (int)(uint32_t)key;
-  if (id < 0 || id >= J.n_tris) {
+  const int id = __float_as_int(hit.w);
+  if (!active || id < 0) return false;
+  if (id >= J.n_tris) {
     atomicOr(J.err, ERR_VISIBILITY);
     return false;
   }
-  const int k = __ldg(J.leaf_of + id);
-  const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
-  float t, u, v;
-  add_work(J, 0, 1);
-  // the leaf must hold that triangle, and the test accepts it again (same
-  // ray, same operands); anything else is an error, not a miss
-  if (__float_as_int(a.w) != id || !mt_test(s.ro, s.rd, f4to3(a), f4to3(e1), f4to3(e2), 0.0f, t, u, v)) {
-    atomicOr(J.err, ERR_VISIBILITY);
-    return false;
-  }
-  s.h.t = t;
-  s.h.u = u;
-  s.h.v = v;
+  s.h.t = hit.x;
+  s.h.u = hit.y;
+  s.h.v = hit.z;
   s.h.tri = id;
   const int4 tv = __ldg(J.tri_v + id);
   s.A = tv.x;
@@ -523,13 +512,14 @@ __device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
 
 // hit_tri (may be null) receives the camera ray's triangle, -1 on a miss.
 // use_vis (uniform over the launch): the camera ray's hit is the sample's
-// rasterised visibility key vkey instead of a traversal.
+// rasterised hit record vkey instead of a traversal (vkey is not read
+// otherwise).
 // view >= 0: the camera ray may come from the raster pass's tile lists of
 // that view (see tiles_usable).
 template <int MODE, bool WARP>
 __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active,
-                             int* hit_tri = nullptr, bool use_vis = false, unsigned long long vkey = ~0ull,
-                             int view = -1) {
+                             int* hit_tri = nullptr, bool use_vis = false,
+                             float4 vkey = float4{0.0f, 0.0f, 0.0f, 0.0f}, int view = -1) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s)
@@ -617,12 +607,12 @@ __device__ inline f3 shade(const JobDev& J, const CamDev& cam, float x, float y,
 #ifdef DRGB_EDGE_SHADE_NOINLINE
 static __device__ __noinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key,
                                                 int view = -1) {
-  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, ~0ull, view);
+  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, float4{0.0f, 0.0f, 0.0f, 0.0f}, view);
 }
 #else
 static __device__ __forceinline__ f3 shade_generic(const JobDev& J, const CamDev& cam, float x, float y,
                                                    uint32_t key, int view = -1) {
-  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, ~0ull, view);
+  return shade_p<0, false>(J, cam, x, y, key, true, nullptr, false, float4{0.0f, 0.0f, 0.0f, 0.0f}, view);
 }
 #endif
 
