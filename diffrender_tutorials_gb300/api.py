@@ -581,9 +581,10 @@ class OptimizationServer:
         return ms[:n], jobs[:n]
 
 
-def estimate_job_bytes(scene: Scene, cams: Sequence[CamInfo], mode: int = 0) -> int:
+def estimate_job_bytes(scene: Scene, cams: Sequence[CamInfo], mode: int = 0, spp: int = 16) -> int:
     h = _SceneHandle(scene)
-    return int(N.load().drgb_estimate_job_bytes(int(mode), C.byref(h.desc), make_cameras(list(cams)), len(cams)))
+    return int(N.load().drgb_estimate_job_bytes(int(mode), int(spp), C.byref(h.desc), make_cameras(list(cams)),
+                                                len(cams)))
 
 
 def kernel_launches() -> int:

@@ -96,9 +96,7 @@ struct drgb_batch {
       Job& J = r->job;
       JobDev d = J.dev;
       d.top_n = 0;  // batched kernels stage no job's top levels
-      d.vis_fwd = d.vis_adj = nullptr;  // batched pixel kernels trace their samples
-      d.sh_grid = nullptr;
-      d.ra_tiles = nullptr;
+      // a job's raster buffers and light cells (its own; see enqueue_iteration)
       d.edge_key_base = (uint32_t)key_base;
       key_base += (uint64_t)J.n_views * (uint64_t)std::max(0, J.n_edges);
       if (mode_groups.empty() || mode_groups.back().mode != J.mode)
@@ -224,9 +222,14 @@ struct drgb_batch {
       Job& J = jobs.at(id)->job;
       if (J.det && J.rec_key.p) launch_det_clear(J, stream);
     }
+    // each job's raster pass and light cells (jobs without them trace)
+    int vis = 0;
+    for (size_t j = 0; j < order.size(); j++)
+      vis |= jobs.at(order[j])->raster_pass(PX_FWD | PX_ADJ, d_jobs.p + j, stream);
     for (size_t g = 0; g < mode_groups.size(); g++)
       launch_pixels(d_jobs.p, d_items.p + mode_groups[g].begin, mode_groups[g].count, d_counter.p + g,
-                    PX_FWD | PX_LOSS | PX_ADJ, sm_count * px_blocks_per_sm, stream, mode_groups[g].mode, det_any);
+                    PX_FWD | PX_LOSS | PX_ADJ | vis, sm_count * px_blocks_per_sm, stream, mode_groups[g].mode,
+                    det_any);
     launch_loss_finalize(d_jobs.p, (int)order.size(), stream);
     launch_b_edges(d_jobs.p, seg_proj.p, n_proj, c_proj, seg_pmf.p, n_pmf, c_pmf, seg_pairs.p, n_pairs, seg_sel.p,
                    n_sel, c_sel, queue.p, queue_count.p, (int)queue.n, sm_count * edge_blocks_per_sm, stream,

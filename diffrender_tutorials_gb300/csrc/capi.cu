@@ -169,6 +169,7 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
       case DRGB_OPT_PRIMARY_RASTER:
         require(value == 0 || value == 1, "primary visibility: 0 (hierarchy traversal) or 1 (raster pass)");
         r->job.raster = (int)value;
+        r->job.raster_pick = -1;
         if (r->d_job.p && r->job.n_views > 0) {
           r->raster_buffers();
           r->push_dev();
@@ -595,6 +596,27 @@ int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, 
     r->set_device();
     Job& J = r->job;
     const int S = J.S;
+    float best = 1e30f;
+    // 0. camera samples and point-light shadow rays by the raster pass or by
+    //    traversal (the raster pass has a fixed cost that small calls do not
+    //    recover)
+    if (J.raster && !J.det && !J.trace_bruteforce && !J.store_hits) {
+      int pick = 1;
+      for (int k : {0, 1}) {
+        J.raster_pick = k;
+        r->raster_buffers();
+        r->push_dev();
+        r->graph_valid = false;
+        const float ms = time_gradient_passes(r, trial_iters);
+        if (ms < best) {
+          best = ms;
+          pick = k;
+        }
+      }
+      J.raster_pick = pick;
+      r->raster_buffers();
+      r->push_dev();
+    }
     // 1. work-item shape: 32 or 64 samples (one or two warp passes), at most 32 pixels
     std::vector<std::pair<int, int>> tiles;
     for (int n_samples : {32, 64}) {
@@ -602,7 +624,6 @@ int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, 
       for (int th = 1; th * th <= P; th *= 2)
         if (P % th == 0 && P / th >= th) tiles.emplace_back(P / th, th);
     }
-    float best = 1e30f;
     int bw = J.tile_w, bh = J.tile_h;
     for (auto [tw, th] : tiles) {
       r->apply_tile(tw, th);

@@ -158,6 +158,7 @@ struct Job {
   int edge_exact = 0;         // DRGB_OPT_EDGE_JACOBIAN
   int edge_sil = 0;           // DRGB_OPT_EDGE_SET
   int raster = 1;             // DRGB_OPT_PRIMARY_RASTER
+  int raster_pick = -1;       // the optimiser's autotuner's choice (-1: none, the size rule decides)
   bool raster_on = false;     // raster buffers set up for the current views (see renderer::raster_buffers)
   DevBuf<float4> vis[2];              // rasterised visibility of forward / adjoint samples
   DevBuf<uint32_t> ra_tiles;          // triangles per screen tile, then their offsets (scan)

@@ -163,16 +163,17 @@ struct __align__(16) RaRec {
 // PASS 1: fills the lists with j.  `tiles` = per view ntx*nty counters, then
 // (scanned) offsets with the total at [n_tiles]; `cursor` per tile; `list`
 // of `cap` slots; `state` bit 0 set when the lists do not fit.
+// One warp per (view, leaf): its lanes share the tiles of large footprints.
 template <int PASS>
 __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint32_t* tiles, uint32_t* cursor,
                       int* list, uint32_t cap, uint32_t* state, RaRec* rec) {
   const JobDev& J = jobs[0];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (j >= J.n_views * J.n_tris) return;
   const int view = j / J.n_tris, leaf = j - view * J.n_tris;
   const int n_tiles = J.n_views * ntx * nty;
   if (PASS == 1 && tiles[n_tiles] > cap) {
-    if (j == 0) atomicOr(state, 1u);
+    if (j == 0 && lane == 0) atomicOr(state, 1u);
     return;
   }
   RaTri r;
@@ -188,22 +189,23 @@ __global__ void k_bin(const JobDev* jobs, int tw, int th, int ntx, int nty, uint
     q.l0 = make_float4(r.nx[0], r.ny[0], r.c[0], lb);
     q.l1 = make_float4(r.nx[1], r.ny[1], r.c[1], 0.0f);
     q.l2 = make_float4(r.nx[2], r.ny[2], r.c[2], 0.0f);
-    rec[j] = q;
+    if (lane == 0) rec[j] = q;
   }
   if (!ok) return;
   int tx0, tx1, ty0, ty1;
   ra_tiles(r, tw, th, ntx, nty, tx0, tx1, ty0, ty1);
   const int base = view * ntx * nty;
-  for (int ty = ty0; ty <= ty1; ty++)
-    for (int tx = tx0; tx <= tx1; tx++) {
-      const int t = base + ty * ntx + tx;
-      if (PASS == 0) {
-        atomicAdd(tiles + t, 1u);
-      } else {
-        const uint32_t pos = tiles[t] + atomicAdd(cursor + t, 1u);
-        list[pos] = j;
-      }
+  const int nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
+  for (int q = lane; q < n; q += 32) {
+    const int ty = ty0 + q / nx, tx = tx0 + q % nx;
+    const int t = base + ty * ntx + tx;
+    if (PASS == 0) {
+      atomicAdd(tiles + t, 1u);
+    } else {
+      const uint32_t pos = tiles[t] + atomicAdd(cursor + t, 1u);
+      list[pos] = j;
     }
+  }
 }
 
 // Sample s of a tile in pass `pass`: its pixel, index and position (the
@@ -409,16 +411,17 @@ __global__ void __launch_bounds__(SH_THREADS) k_light_grid(const JobDev* jobs, L
   *g = q;
 }
 
-// PASS 0: footprint record of leaf k and its cell counts; PASS 1: the lists.
+// PASS 0: footprint record of leaf k and its cell counts; PASS 1: the
+// lists.  One warp per leaf.
 template <int PASS>
 __global__ void k_light_bin(const JobDev* jobs, LightGrid* g, uint32_t* cells, uint32_t* cursor, int* list,
                             uint32_t cap, float4* rec) {
   const JobDev& J = jobs[0];
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (k >= J.n_tris || !g->ok) return;
   const int G = g->G;
   if (PASS == 1 && cells[G * G] > cap) {
-    if (k == 0) g->overflow = 1;
+    if (k == 0 && lane == 0) g->overflow = 1;
     return;
   }
   const float4 a = __ldg(J.tri + 3 * k), e1 = __ldg(J.tri + 3 * k + 1), e2 = __ldg(J.tri + 3 * k + 2);
@@ -444,23 +447,25 @@ __global__ void k_light_bin(const JobDev* jobs, LightGrid* g, uint32_t* cells, u
     }
     // shadow rays end at the light: a triangle no nearer to it than the ray's origin is not in the way
     L[0].w = dist_lower_bound(P, g->lx, g->ly, g->lz);
-    rec[4 * k + 0] = make_float4(x0, x1, y0, y1);
-    rec[4 * k + 1] = L[0];
-    rec[4 * k + 2] = L[1];
-    rec[4 * k + 3] = L[2];
+    if (lane == 0) {
+      rec[4 * k + 0] = make_float4(x0, x1, y0, y1);
+      rec[4 * k + 1] = L[0];
+      rec[4 * k + 2] = L[1];
+      rec[4 * k + 3] = L[2];
+    }
   }
   const int cx0 = min(G - 1, max(0, (int)floorf(x0))), cx1 = min(G - 1, max(0, (int)floorf(x1)));
   const int cy0 = min(G - 1, max(0, (int)floorf(y0))), cy1 = min(G - 1, max(0, (int)floorf(y1)));
-  for (int cy = cy0; cy <= cy1; cy++)
-    for (int cx = cx0; cx <= cx1; cx++) {
-      const int c = cy * G + cx;
-      if (PASS == 0) {
-        atomicAdd(cells + c, 1u);
-      } else {
-        const uint32_t pos = cells[c] + atomicAdd(cursor + c, 1u);
-        list[pos] = k;
-      }
+  const int nx = cx1 - cx0 + 1, n = nx * (cy1 - cy0 + 1);
+  for (int q = lane; q < n; q += 32) {
+    const int c = (cy0 + q / nx) * G + cx0 + q % nx;
+    if (PASS == 0) {
+      atomicAdd(cells + c, 1u);
+    } else {
+      const uint32_t pos = cells[c] + atomicAdd(cursor + c, 1u);
+      list[pos] = k;
     }
+  }
 }
 
 __global__ void k_light_valid(LightGrid* g) { g->valid = g->ok && !g->overflow; }
@@ -472,7 +477,7 @@ void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s)
   DRGB_CUDA(cudaMemsetAsync(J.sh_cells.p, 0, sizeof(uint32_t) * (n_cells + 1), s));
   DRGB_CUDA(cudaMemsetAsync(J.sh_cursor.p, 0, sizeof(uint32_t) * n_cells, s));
   k_light_grid<<<1, SH_THREADS, 0, s>>>(d_job, g, G);
-  const int grid = (J.n_tris + 255) / 256;
+  const int grid = (int)(((int64_t)J.n_tris * 32 + 255) / 256);
   k_light_bin<0><<<grid, 256, 0, s>>>(d_job, g, J.sh_cells.p, J.sh_cursor.p, J.sh_list.p, (uint32_t)J.sh_list.n,
                                       J.sh_rec.p);
   launch_rs_scan(J.sh_cells.p, n_cells + 1, s);
@@ -512,7 +517,7 @@ void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int n
   DRGB_CUDA(cudaMemsetAsync(tiles, 0, sizeof(uint32_t) * (n_tiles + 1), s));
   DRGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * n_tiles, s));
   DRGB_CUDA(cudaMemsetAsync(state, 0, sizeof(uint32_t), s));
-  const int grid = (tasks + 255) / 256;
+  const int grid = (int)(((int64_t)tasks * 32 + 255) / 256);
   RaRec* rec = reinterpret_cast<RaRec*>(J.ra_rec.p);
   k_bin<0><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state,
                                 rec);

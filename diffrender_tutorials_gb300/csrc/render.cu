@@ -269,8 +269,7 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
   __shared__ int s_hit_all[PX_WARPS][PX_MAX_SAMPLES];  // forward hit triangle of each sample
 #endif
   stage_top_nodes(jobs[0]);  // a single job's top levels (none for a batch)
-  // a single job whose raster pass resolved this launch's camera samples
-  const bool vis_ok = (flags & PX_VIS) && jobs[0].ra_state && !(*jobs[0].ra_state & 1u);
+
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   JobDev& J = sJ_all[warp];
   CamDev& C = sC_all[warp];
@@ -302,6 +301,8 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
       cur_view = item.y;
     }
     __syncwarp();
+    // the item's job had its raster pass resolve this launch's camera samples
+    const bool vis_ok = (flags & PX_VIS) && J.ra_state && !(*J.ra_state & 1u);
     const int view = item.y, x0 = item.z, y0 = item.w;
     const int W = (int)C.width, H = (int)C.height;
     const int tw = J.tile_w;

@@ -181,9 +181,15 @@ struct drgb_renderer {
     // server, whose kernels trace: it traces too (the raster pass and the
     // traversal find the same hits except the reference caster's
     // clamped-determinant ones, which each finds only by chance)
-    const bool on = J.raster && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 && J.n_views > 0;
+    // small calls: the raster pass's fixed cost (about 15 launches) outweighs
+    // what it saves; measured on GB300, a 12-triangle cube at 256x256 x 16 spp
+    // and 5,120 triangles at 512x512 x 4 spp x 2 views break even (1-2 M
+    // samples).  The optimiser's autotuner times both ways instead.
+    const size_t samples = (size_t)n_pixels() * J.S;
+    const bool pays = J.raster_pick >= 0 ? J.raster_pick == 1 : (samples >= (2u << 20) && J.n_tris >= 64);
+    const bool on = J.raster && pays && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 &&
+                    J.n_views > 0;
     if (on) {
-      const size_t samples = (size_t)n_pixels() * J.S;
       J.vis[0].reserve(samples);
       J.vis[1].reserve(samples);
       int tw, th, ntx, nty;
@@ -192,7 +198,7 @@ struct drgb_renderer {
       J.ra_tiles.reserve(scan_scratch(n_tiles + 1));
       J.ra_cursor.reserve(n_tiles);
       J.ra_state.reserve(1);
-      J.ra_list.reserve(std::max<size_t>(1u << 20, (size_t)16 * J.n_views * J.n_tris));
+      J.ra_list.reserve(std::max<size_t>(1u << 16, (size_t)32 * J.n_views * J.n_tris));
       J.ra_rec.reserve((size_t)4 * J.n_views * J.n_tris);
     }
     J.raster_on = on;
@@ -203,18 +209,21 @@ struct drgb_renderer {
       J.sh_grid.reserve(1);
       J.sh_cells.reserve(scan_scratch((size_t)G * G + 1));
       J.sh_cursor.reserve((size_t)G * G);
-      J.sh_list.reserve(std::max<size_t>(1u << 20, (size_t)16 * J.n_tris));
+      J.sh_list.reserve(std::max<size_t>(1u << 16, (size_t)64 * J.n_tris));
       J.sh_rec.reserve((size_t)4 * J.n_tris);
     }
     J.shadow_on = sh;
   }
 
   // The raster pass for the samples a pixel-kernel launch with `flags`
-  // traces.  Returns PX_VIS when it ran (add it to that launch's flags), 0
+  // traces (on `st` for the device job `dj`: the renderer's own by default,
+  // a batch's copy of it otherwise).  Returns PX_VIS when it ran (add it to that launch's flags), 0
   // when the samples are to be traced: raster off, or the device job does
   // not hold the current, large enough buffers.
-  int raster_pass(int flags) {
+  int raster_pass(int flags, const JobDev* dj = nullptr, cudaStream_t st = nullptr) {
     Job& J = job;
+    if (!dj) dj = d_job.p;
+    if (!st) st = stream;
     const int passes = ((flags & PX_FWD) ? 1 : 0) | ((flags & PX_ADJ) ? 2 : 0);
     if (!J.raster_on || !passes) return 0;
     const size_t samples = (size_t)n_pixels() * J.S;
@@ -224,18 +233,19 @@ struct drgb_renderer {
     if (J.dev.vis_fwd != J.vis[0].p || J.dev.vis_adj != J.vis[1].p || J.dev.ra_state != J.ra_state.p ||
         J.vis[0].n < samples || J.vis[1].n < samples || J.ra_tiles.n < scan_scratch(n_tiles + 1) ||
         J.ra_cursor.n < n_tiles || !J.ra_list.p || J.ra_rec.n < (size_t)4 * J.n_views * J.n_tris) {
-      // nothing built for this call: no stale list may be read either
-      if (J.ra_state.p) DRGB_CUDA(cudaMemsetAsync(J.ra_state.p, 0, sizeof(uint32_t), stream));
-      if (J.sh_grid.p) DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), stream));
+      // nothing built for this call: no stale hit or list may be read either
+      // (state 0x01010101: bit 0 "wrote nothing" set, bit 1 "lists valid" clear)
+      if (J.ra_state.p) DRGB_CUDA(cudaMemsetAsync(J.ra_state.p, 1, sizeof(uint32_t), st));
+      if (J.sh_grid.p) DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), st));
       return 0;
     }
-    launch_raster(d_job.p, J, passes, ntx, nty, tw, th, stream);
+    launch_raster(dj, J, passes, ntx, nty, tw, th, st);
     const int G = light_grid_size(J.n_tris);
     if (J.shadow_on && J.dev.sh_grid == J.sh_grid.p && J.sh_cells.n >= scan_scratch((size_t)G * G + 1) &&
         J.sh_cursor.n >= (size_t)G * G && J.sh_rec.n >= (size_t)4 * J.n_tris && J.sh_list.p)
-      launch_light_grid(d_job.p, J, G, stream);
+      launch_light_grid(dj, J, G, st);
     else if (J.sh_grid.p)
-      DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), stream));
+      DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), st));
     return PX_VIS;
   }
 

@@ -17,6 +17,7 @@
 //
 // Host inputs are copied at submission, so a client can free them at once.
 // Times are on one steady clock that starts with the server.
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -94,7 +95,7 @@ struct Ticket {
   std::vector<std::vector<float>> out_v, out_col, out_tex, out_tr, out_rt;
 };
 
-int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_views) {
+int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_views, int spp, int mode) {
   int64_t V = 0, T = 0, VF = 0, TF = 0, tex = 0, inst = 0;
   for (int i = 0; i < s.n_meshes; i++) {
     const drgb_mesh_desc& m = s.meshes[i];
@@ -117,6 +118,18 @@ int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_
   b += px * (12 + 16 + 8 + 16 + 8);             // targets, adjoint, loss partials, edge queue, random table
   b += (V * 6 + tex + inst * 12) * 4 * 3;       // gradient, first and second moments
   b += 64 << 10;                                // tables, counters, loss history
+  // raster pass: a hit record per forward and adjoint sample, per (view,
+  // triangle) a footprint and room for 32 tile-list entries, tile offsets;
+  // the light-space cells of the point-light models (64 entries per triangle)
+  const int64_t S = (int64_t)std::max(1, (int)std::sqrt((float)std::max(1, spp))) *
+                    std::max(1, (int)std::sqrt((float)std::max(1, spp)));
+  // (the renderer's size rule: calls of fewer than 2 M camera samples trace)
+  if (px * S < (2 << 20) || TF < 64) return b;
+  b += px * S * 32 + TF * nv * (64 + 128) + (int64_t)(1 << 16) * 4 + px * 8 + 64;
+  if (mode == LAMBERT_POINT_VCOLOR || mode == PATH_DIFFUSE) {
+    const int64_t G = light_grid_size((int)std::min<int64_t>(TF, 1 << 30));
+    b += G * G * 8 + 16 + TF * (64 + 256) + (int64_t)(1 << 16) * 4 + 64;
+  }
   return b;
 }
 
@@ -340,11 +353,10 @@ static Ticket& find_ticket(drgb_server* s, int32_t id) {
 
 extern "C" {
 
-int64_t drgb_estimate_job_bytes(int shading_model, const drgb_scene_desc* scene, const drgb_camera* cams,
+int64_t drgb_estimate_job_bytes(int shading_model, int spp, const drgb_scene_desc* scene, const drgb_camera* cams,
                                 int n_views) {
-  (void)shading_model;
   if (!scene || !cams || n_views <= 0) return -1;
-  return estimate_bytes(*scene, cams, n_views);
+  return estimate_bytes(*scene, cams, n_views, spp, shading_model);
 }
 
 int drgb_server_create(const drgb_server_config* cfg, drgb_server** out) {
@@ -405,7 +417,7 @@ int drgb_server_submit(drgb_server* s, int shading_model, int spp, const drgb_mo
     t->info.state = DRGB_JOB_QUEUED;
     t->info.steps = n_steps;
     t->info.t_admit = t->info.t_done = -1.0;
-    t->info.device_bytes = estimate_bytes(*scene, cams, n_views);
+    t->info.device_bytes = estimate_bytes(*scene, cams, n_views, spp, shading_model);
     if (t->info.device_bytes > s->cfg.hbm_budget_bytes)
       throw CudaError("job needs more device memory than the whole budget", DRGB_ERR_OOM);
     {

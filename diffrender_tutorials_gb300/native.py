@@ -133,7 +133,7 @@ _SIGS = {
     "drgb_server_release": (C.c_int, [VP, C.c_int32]),
     "drgb_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
     "drgb_server_step_times": (C.c_int, [VP, C.c_int64, C.c_int64, VP, VP]),
-    "drgb_estimate_job_bytes": (C.c_int64, [C.c_int, C.POINTER(SceneDesc), C.POINTER(Camera), C.c_int]),
+    "drgb_estimate_job_bytes": (C.c_int64, [C.c_int, C.c_int, C.POINTER(SceneDesc), C.POINTER(Camera), C.c_int]),
     "drgb_optimizer_profile": (C.c_int, [VP, C.c_int, VP]),
     "drgb_count_work": (C.c_int, [VP, VP]),
     "drgb_optimizer_autotune": (C.c_int, [VP, C.c_int, VP, C.POINTER(C.c_float)]),

@@ -101,13 +101,17 @@ enum {
                                     two shading points, so the samples go where the image is discontinuous;
                                     with per-face colours or textures edges inside the silhouette carry real
                                     discontinuities and mode 0 is required */
-  DRGB_OPT_PRIMARY_RASTER = 14   /* nearest hits of the forward and adjoint camera samples of a single
-                                    renderer: 1 (default) a raster pass -- every triangle runs the
-                                    reference's ray/triangle test on the samples its projection covers
-                                    (with a margin), keeping per sample the nearest hit, ties to the lowest
-                                    triangle as the reference's loop does; 0 each sample's ray through the
-                                    hierarchy.  Same hits either way; off for the brute-force caster and
-                                    stored adjoint hits.  Costs 16 bytes per sample of the views */
+  DRGB_OPT_PRIMARY_RASTER = 14   /* camera rays and point-light shadow rays: 1 (default) by screen tiles
+                                    and light-space cells where that pays -- triangles are binned to the
+                                    tiles / cells their projection (with a margin) overlaps, and each ray
+                                    runs the reference's ray/triangle test on its tile's or cell's list,
+                                    keeping the nearest hit with ties to the lowest triangle, as the
+                                    reference's loop does; calls of fewer than about 2 M camera samples
+                                    trace, and drgb_optimizer_autotune times both ways; 0 every ray through
+                                    the hierarchy.  Same hits either way except the reference caster's
+                                    clamped-determinant hits, which each method finds only by chance.  Off
+                                    for the brute-force caster, stored adjoint hits and deterministic mode.
+                                    Costs 32 bytes per camera sample of the views */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -373,7 +377,7 @@ int drgb_server_get_stats(drgb_server* s, drgb_server_stats* out);
 /* Device time (ms) and resident job count of batched steps [first, first+n). */
 int drgb_server_step_times(drgb_server* s, int64_t first, int64_t n, float* ms, int32_t* jobs);
 /* Device bytes a job of this shape needs (an upper estimate used for admission). */
-int64_t drgb_estimate_job_bytes(int shading_model, const drgb_scene_desc* scene, const drgb_camera* cams,
+int64_t drgb_estimate_job_bytes(int shading_model, int spp, const drgb_scene_desc* scene, const drgb_camera* cams,
                                 int n_views);
 
 /* ---- measurement (no reference counterpart: the reference prints wall-clock

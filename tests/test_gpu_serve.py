@@ -98,7 +98,7 @@ def test_server_job_alone_and_in_mix_atomic_mode():
 
 def test_server_budget_and_slots():
     jobs = [job("cube", 100 + k) for k in range(5)]
-    est = D.estimate_job_bytes(jobs[0][0], jobs[0][1])
+    est = D.estimate_job_bytes(jobs[0][0], jobs[0][1], mode=int(D.SHADING_MODEL.VERTEX_COLOR), spp=16)
     # measured device bytes of one such job
     probe = D.OptimizationServer(worker=False)
     t = probe.submit(*jobs[4][:5], 1)
@@ -165,7 +165,7 @@ def test_server_estimate_covers_large_job():
     s = D.Scene()
     s.add_mesh(true)
     cams = D.ring_cameras(4, 3.0, 256, 256)
-    est = D.estimate_job_bytes(s, cams)
+    est = D.estimate_job_bytes(s, cams, mode=int(D.SHADING_MODEL.LAMBERT_POINT_VCOLOR), spp=4)
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(D.SHADING_MODEL.LAMBERT_POINT_VCOLOR, 4))
     r.commit(s)
     tgt = r.render(s, cams)
