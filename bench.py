@@ -325,7 +325,26 @@ def drgb_arm(args, w, ws, rank, local, pg):
     r.set_option(N.OPT_DETERMINISTIC, 0)
     deterministic = {"value": args.steps / (sum(det_ms) / 1e3), "unit": "iters/s",
                      "ms_per_step": sum(det_ms) / args.steps, "phases_ms": det_prof,
-                     "how": "DRGB_OPT_DETERMINISTIC: gradient records sorted by index, fixed-order sums"}
+                     "how": "DRGB_OPT_DETERMINISTIC: gradient records sorted by index, fixed-order sums "
+                            "(every ray traced, as in the batched engine)"}
+
+    # the same iteration sampling silhouette edges only (DRGB_OPT_EDGE_SET = 1)
+    r.set_option(N.OPT_EDGE_SET, 1)
+    for _ in range(args.warmup):
+        opt.run_async(1)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            opt.run_async(1)
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    sil_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    silhouette = {"value": args.steps / (sum(sil_ms) / 1e3), "unit": "iters/s",
+                  "ms_per_step": sum(sil_ms) / args.steps, "phases_ms": opt.profile(2),
+                  "how": "DRGB_OPT_EDGE_SET = 1: edge samples on silhouette and boundary edges only"}
+    r.set_option(N.OPT_EDGE_SET, 0)
 
     # roofline of the dominant kernel (fused forward/adjoint pixel kernel)
     prof = opt.profile(3)
@@ -340,11 +359,14 @@ def drgb_arm(args, w, ws, rank, local, pg):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     npix = w["res"] * w["res"] * w["views"]
     # algorithmic bytes of one pixel-kernel launch: targets read (12 B/px),
-    # adjoint written (16 B/px), scene data read once (pos/col/nrm/tc 56 B/vertex,
-    # triangles+indices 64 B/triangle, nodes 64 B/node), gradients written
+    # adjoint written (16 B/px), the raster pass's hit record of every forward
+    # and adjoint camera sample read (16 B each), scene data read once
+    # (pos/col/nrm/tc 56 B/vertex, triangles+indices 64 B/triangle, nodes
+    # 64 B/node), gradients written
     n_tri = sum(m.face_count for m in isc.meshes)
     n_v = sum(m.vertex_count for m in isc.meshes)
-    alg_bytes = npix * (12 + 16) + n_v * 56 + n_tri * (64 + 64) + n_v * 24
+    S_eff = int(math.isqrt(w["spp"])) ** 2
+    alg_bytes = npix * (12 + 16) + 2 * 16 * npix * S_eff + n_v * 56 + n_tri * (64 + 64) + n_v * 24
     px_s = prof["pixels"] / 1e3
     ach = alg_bytes / px_s / 1e9
     traffic = read_traffic()
@@ -352,8 +374,11 @@ def drgb_arm(args, w, ws, rank, local, pg):
     sm_mhz = clocks.get("sm_mhz") or 1900.0
     fp32_peak = sms * 128 * sm_mhz * 1e6 / 1e12  # T lane-ops/s, FMA counted once
     # FP32 lane-ops: 18 per slab test, 61 per Moller-Trumbore test, ~60 per
-    # ray for generation/shading, ~120 per shaded edge sample (edge_grad etc.)
-    ops = 18 * work["box_tests"] + 61 * work["tri_tests"] + 60 * work["rays"] + 120 * work["edge_samples"]
+    # ray for generation/shading, 19 per footprint test of a screen-tile or
+    # light-cell list (box: 4 compares, 3 edge lines: 2 mul, 2 add, 1 compare
+    # each), ~120 per shaded edge sample (edge_grad etc.)
+    ops = (18 * work["box_tests"] + 61 * work["tri_tests"] + 60 * work["rays"] + 19 * work["footprint_tests"] +
+           120 * work["edge_samples"])
     iter_s = prof["total"] / 1e3
     line = {
         "metric": "fwd+adjoint iters/s", "value": value, "unit": "iters/s", "n_gpus": ws, "steps": args.steps,
@@ -373,6 +398,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
         "gpu_launches": int(launches),
         "phases_ms": prof,
         "deterministic": deterministic,
+        "edge_set_silhouette": silhouette,
         "work_per_iter": work,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                      "traffic": traffic, "kernel": "k_pixels (forward+loss+interior adjoint)",

@@ -391,10 +391,11 @@ class IOptimizer:
                 "edge_blocks_per_sm": int(out[3]), "ms": float(ms.value)}
 
     def count_work(self):
-        """Rays, box tests, triangle tests and shaded edge samples of one iteration."""
-        out = np.zeros(4, np.uint64)
+        """Rays, box tests, triangle tests, shaded edge samples and footprint
+        tests of the tile and cell lists of one iteration."""
+        out = np.zeros(5, np.uint64)
         N.check(N.load().drgb_count_work(self._r._h, _ptr(out)))
-        return {k: int(v) for k, v in zip(("rays", "box_tests", "tri_tests", "edge_samples"), out)}
+        return {k: int(v) for k, v in zip(("rays", "box_tests", "tri_tests", "edge_samples", "footprint_tests"), out)}
 
     def current_scene(self) -> Scene:
         L, h = N.load(), self._r._h

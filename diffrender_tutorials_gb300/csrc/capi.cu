@@ -670,7 +670,7 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
     r->set_device();
     Job& J = r->job;
     DevBuf<unsigned long long> w;
-    w.alloc(4);
+    w.alloc(4);  // rays, box tests, triangle tests, footprint tests
     DRGB_CUDA(cudaMemsetAsync(w.p, 0, 4 * sizeof(unsigned long long), r->stream));
     JobDev d = J.dev;
     d.work = w.p;
@@ -696,6 +696,7 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts) {
     counts[1] = h[1];
     counts[2] = h[2];
     counts[3] = (uint64_t)std::max(0, shaded);
+    counts[4] = h[3];
     r->check_flags();
   });
 }

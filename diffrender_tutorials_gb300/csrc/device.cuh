@@ -181,7 +181,7 @@ struct JobDev {
   const float* rnd;         // 2 * edge_samples replayed random numbers
   int edge_exact;           // 1: full 2x3 screen Jacobian through the instance's own transform
   uint32_t edge_key_base;   // first queue-sort key of this job in a batch
-  // optional work counters (rays, box tests, triangle tests); null normally
+  // optional work counters (rays, box tests, triangle tests, footprint tests); null normally
   unsigned long long* work;
   // deterministic reduction: gradient contributions become records
   // {gradient index of 3 consecutive floats, value} in slots fixed by their
@@ -570,6 +570,17 @@ __device__ __forceinline__ void add_work(const JobDev& J, unsigned boxes, unsign
     atomicAdd(J.work + 0, 1ull);
     atomicAdd(J.work + 1, (unsigned long long)boxes);
     atomicAdd(J.work + 2, (unsigned long long)tris);
+  }
+}
+
+// Work of a ray resolved against a screen-tile or light-cell list: `fp`
+// footprint (box and edge-line) tests, `tris` ray/triangle tests; `ray`: it
+// counts as a ray (a camera ray built for it).
+__device__ __forceinline__ void add_list_work(const JobDev& J, bool ray, unsigned fp, unsigned tris) {
+  if (J.work) {
+    if (ray) atomicAdd(J.work + 0, 1ull);
+    if (tris) atomicAdd(J.work + 2, (unsigned long long)tris);
+    if (fp) atomicAdd(J.work + 3, (unsigned long long)fp);
   }
 }
 

@@ -234,11 +234,13 @@ __device__ __forceinline__ bool ra_sample(const JobDev& J, int pass, int s, int 
 // Nearest-hit update of one sample against staged triangle c.
 __device__ __forceinline__ void ra_test(const float4* s_a, const float4* s_e1, const float4* s_e2,
                                         const RaRec* s_rec, int c, bool act, float x, float y, f3 ro, f3 rd,
-                                        unsigned long long& best, float& bu, float& bv, unsigned& n_tests) {
+                                        unsigned long long& best, float& bu, float& bv, unsigned& n_tests,
+                                        unsigned& n_fp) {
   if (!act) return;
   const RaRec& q = s_rec[c];
   // no hit on this triangle can be nearer than the best so far (~0: none yet, NaN compares false)
   if (q.l0.w > __uint_as_float((uint32_t)(best >> 32))) return;
+  n_fp++;
   if (!(x >= q.box.x && x <= q.box.y && y >= q.box.z && y <= q.box.w)) return;
   if (!(q.l0.x * x + q.l0.y * y + q.l0.z >= 0.0f && q.l1.x * x + q.l1.y * y + q.l1.z >= 0.0f &&
         q.l2.x * x + q.l2.y * y + q.l2.z >= 0.0f))
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
     }
     unsigned long long b0 = ~0ull, b1 = ~0ull;
     float u0 = 0.0f, v0 = 0.0f, u1 = 0.0f, v1 = 0.0f;
-    unsigned n_tests = 0;
+    unsigned n_tests = 0, n_fp = 0;
     for (int c0 = 0; c0 < n_list; c0 += RA_STAGE) {
       const int nc = min(RA_STAGE, n_list - c0);
       if (c0 > 0 || s0 > 0) __syncthreads();  // the previous stage is no longer read
@@ -315,8 +317,8 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
       }
       __syncthreads();
       for (int c = 0; c < nc; c++) {
-        ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, u0, v0, n_tests);
-        ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, u1, v1, n_tests);
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, u0, v0, n_tests, n_fp);
+        ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, u1, v1, n_tests, n_fp);
       }
     }
     // every sample of the tile is written, a miss too
@@ -325,6 +327,7 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
     if (J.work && n_list > 0 && (a0 || a1)) {
       atomicAdd(J.work + 0, (unsigned long long)(a0 + a1));  // the samples' camera rays
       atomicAdd(J.work + 2, (unsigned long long)n_tests);
+      atomicAdd(J.work + 3, (unsigned long long)n_fp);
     }
   }
 }

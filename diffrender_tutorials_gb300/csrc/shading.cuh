@@ -164,6 +164,7 @@ __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, flo
   s.h.u = s.h.v = 0.0f;
   s.A = s.B = s.C = 0;
   s.block = 0;
+  if (active) add_list_work(J, true, 0, 0);
   const int id = __float_as_int(hit.w);
   if (!active || id < 0) return false;
   if (id >= J.n_tris) {
@@ -207,12 +208,13 @@ __device__ __forceinline__ bool cast_tiles(const JobDev& J, const CamDev& cam, i
   const uint32_t i0 = __ldg(J.ra_tiles + b), i1 = __ldg(J.ra_tiles + b + 1);
   unsigned long long best = ~0ull;
   float bu = 0.0f, bv = 0.0f;
-  unsigned n_tri = 0;
+  unsigned n_tri = 0, n_fp = 0;
   for (uint32_t i = i0; i < i1; i++) {
     const int j = __ldg(J.ra_list + i);
     const float4 q0 = __ldg(J.ra_rec + 4 * j + 1);
     // no hit on it can be nearer than the best so far (none yet: NaN compares false)
     if (q0.w > __uint_as_float((uint32_t)(best >> 32))) continue;
+    n_fp++;
     const float4 box = __ldg(J.ra_rec + 4 * j);
     if (!(x >= box.x && x <= box.y && y >= box.z && y <= box.w)) continue;
     const float4 q1 = __ldg(J.ra_rec + 4 * j + 2), q2 = __ldg(J.ra_rec + 4 * j + 3);
@@ -232,7 +234,7 @@ __device__ __forceinline__ bool cast_tiles(const JobDev& J, const CamDev& cam, i
       }
     }
   }
-  add_work(J, 0, n_tri);
+  add_list_work(J, true, n_fp, n_tri);
   if (best == ~0ull) return false;
   s.h.t = __uint_as_float((uint32_t)(best >> 32));
   s.h.u = bu;
@@ -309,12 +311,13 @@ __device__ __forceinline__ bool light_occluded(const JobDev& J, f3 p, f3 l, floa
   const int cx = min(g.G - 1, max(0, (int)a)), cy = min(g.G - 1, max(0, (int)b));
   const int c = cy * g.G + cx;
   const uint32_t i0 = __ldg(J.sh_cells + c), i1 = __ldg(J.sh_cells + c + 1);
-  unsigned n_tri = 0;
+  unsigned n_tri = 0, n_fp = 0;
   bool occ = false;
   for (uint32_t i = i0; i < i1 && !occ; i++) {
     const int k = __ldg(J.sh_list + i);
     const float4 q0 = __ldg(J.sh_rec + 4 * k + 1);
     if (q0.w >= tfar) continue;  // no nearer to the light than p: not between them
+    n_fp++;
     const float4 box = __ldg(J.sh_rec + 4 * k);
     if (!(a >= box.x && a <= box.y && b >= box.z && b <= box.w)) continue;
     const float4 q1 = __ldg(J.sh_rec + 4 * k + 2), q2 = __ldg(J.sh_rec + 4 * k + 3);
@@ -326,7 +329,7 @@ __device__ __forceinline__ bool light_occluded(const JobDev& J, f3 p, f3 l, floa
     n_tri++;
     occ = mt_test(p, l, f4to3(A), f4to3(e1), f4to3(e2), 0.0f, t, u, v) && t < tfar;
   }
-  add_work(J, 0, n_tri);
+  add_list_work(J, true, n_fp, n_tri);
   return occ;
 }
 

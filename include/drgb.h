@@ -388,8 +388,9 @@ int64_t drgb_estimate_job_bytes(int shading_model, int spp, const drgb_scene_des
  * step, [3] flatten+LBVH refit, [4] whole iteration. */
 int drgb_optimizer_profile(drgb_renderer* r, int n_iters, float* out_ms);
 /* Work of one optimiser iteration's pixel and edge passes, counted by an
- * instrumented replay: counts[0] rays traced, [1] ray/box tests,
- * [2] ray/triangle tests, [3] edge samples shaded. */
+ * instrumented replay: counts[0] rays (traced, or resolved against a screen
+ * tile or light cell), [1] ray/box tests, [2] ray/triangle tests, [3] edge
+ * samples shaded, [4] footprint tests of the tile and cell lists (5 entries). */
 int drgb_count_work(drgb_renderer* r, uint64_t* counts);
 
 /* ---- autotuning (no reference counterpart) ------------------------------
