@@ -228,6 +228,8 @@ def read_traffic():
 
 
 BVH_BUILDERS = {"lbvh": 0, "sah": 1, "two_level": 2, "flat_sah": 3}
+# camera and point-light shadow rays: hierarchy, tiles and cells where they pay (autotuned), always tiles and cells
+RASTER = {"off": 0, "auto": 1, "always": 2}
 
 
 def drgb_arm(args, w, ws, rank, local, pg):
@@ -241,6 +243,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
     S = D.SHADING_MODEL(w["mode"])
     r = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
     r.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
+    r.set_option(N.OPT_PRIMARY_RASTER, RASTER[args.raster])
     r.commit(ts)
     targets = r.render(ts, cams)
     p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.01)
@@ -284,6 +287,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
     # loss out)
     r2 = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, w["spp"]), device=local)
     r2.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
+    r2.set_option(N.OPT_PRIMARY_RASTER, RASTER[args.raster])
     r2.commit(isc)
     tg_pinned = torch.empty(targets.size, dtype=torch.float32, pin_memory=True).numpy()
     tg_pinned[:] = targets.reshape(-1)
@@ -997,6 +1001,8 @@ def main():
     ap.add_argument("--workload", default="icosphere", choices=sorted(WORKLOADS) + ["batch", "serve", "stress", "instances"])
     ap.add_argument("--res", type=int, default=1024, help="stress: view resolution")
     ap.add_argument("--bvh", default="sah", choices=sorted(BVH_BUILDERS), help="hierarchy builder")
+    ap.add_argument("--raster", default="auto", choices=sorted(RASTER),
+                    help="camera and point-light shadow rays by screen tiles and light cells (DRGB_OPT_PRIMARY_RASTER)")
     ap.add_argument("--jobs", type=int, default=None, help="jobs of the batch (64) or serving (16) workload")
     ap.add_argument("--mix", default="c4", choices=["c4", "small"],
                     help="batch / serve: the configured job mix, or small jobs that cannot fill the GPU alone "

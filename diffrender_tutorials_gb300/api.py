@@ -384,11 +384,11 @@ class IOptimizer:
     def autotune(self, trial_iters: int = 3) -> dict:
         """Picks the work-item shape and the persistent grid sizes by timing
         the gradient passes of the optimiser's views (the state is unchanged)."""
-        out = np.zeros(4, np.int32)
+        out = np.zeros(5, np.int32)
         ms = C.c_float(0.0)
         N.check(N.load().drgb_optimizer_autotune(self._r._h, int(trial_iters), _ptr(out), C.byref(ms)))
         return {"tile": (int(out[0]), int(out[1])), "pixel_blocks_per_sm": int(out[2]),
-                "edge_blocks_per_sm": int(out[3]), "ms": float(ms.value)}
+                "edge_blocks_per_sm": int(out[3]), "raster": bool(out[4]), "ms": float(ms.value)}
 
     def count_work(self):
         """Rays, box tests, triangle tests, shaded edge samples and footprint

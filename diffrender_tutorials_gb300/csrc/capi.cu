@@ -167,7 +167,8 @@ int drgb_renderer_set_option(drgb_renderer* r, int option, int64_t value) {
         if (r->d_job.p) r->push_dev();
         break;
       case DRGB_OPT_PRIMARY_RASTER:
-        require(value == 0 || value == 1, "primary visibility: 0 (hierarchy traversal) or 1 (raster pass)");
+        require(value >= 0 && value <= 2,
+                "camera and shadow rays: 0 (hierarchy traversal), 1 (tiles and cells where that pays), 2 (always)");
         r->job.raster = (int)value;
         r->job.raster_pick = -1;
         if (r->d_job.p && r->job.n_views > 0) {
@@ -600,7 +601,7 @@ int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, 
     // 0. camera samples and point-light shadow rays by the raster pass or by
     //    traversal (the raster pass has a fixed cost that small calls do not
     //    recover)
-    if (J.raster && !J.det && !J.trace_bruteforce && !J.store_hits) {
+    if (J.raster == 1 && !J.det && !J.trace_bruteforce && !J.store_hits) {
       int pick = 1;
       for (int k : {0, 1}) {
         J.raster_pick = k;
@@ -656,6 +657,7 @@ int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, 
       chosen[1] = J.tile_h;
       chosen[2] = r->px_blocks_per_sm;
       chosen[3] = r->edge_blocks_per_sm;
+      chosen[4] = J.raster_on ? 1 : 0;
     }
     if (best_ms) *best_ms = best;
   });

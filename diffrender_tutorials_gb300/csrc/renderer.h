@@ -186,7 +186,8 @@ struct drgb_renderer {
     // and 5,120 triangles at 512x512 x 4 spp x 2 views break even (1-2 M
     // samples).  The optimiser's autotuner times both ways instead.
     const size_t samples = (size_t)n_pixels() * J.S;
-    const bool pays = J.raster_pick >= 0 ? J.raster_pick == 1 : (samples >= (2u << 20) && J.n_tris >= 64);
+    const bool pays = J.raster == 2 ? true
+                      : J.raster_pick >= 0 ? J.raster_pick == 1 : (samples >= (2u << 20) && J.n_tris >= 64);
     const bool on = J.raster && pays && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 &&
                     J.n_views > 0;
     if (on) {

@@ -107,8 +107,9 @@ enum {
                                     runs the reference's ray/triangle test on its tile's or cell's list,
                                     keeping the nearest hit with ties to the lowest triangle, as the
                                     reference's loop does; calls of fewer than about 2 M camera samples
-                                    trace, and drgb_optimizer_autotune times both ways; 0 every ray through
-                                    the hierarchy.  Same hits either way except the reference caster's
+                                    trace, and drgb_optimizer_autotune times both ways; 2 tiles and cells
+                                    for every call (no size rule, not switched off by the autotuner); 0
+                                    every ray through the hierarchy.  Same hits either way except the reference caster's
                                     clamped-determinant hits, which each method finds only by chance.  Off
                                     for the brute-force caster, stored adjoint hits and deterministic mode.
                                     Costs 32 bytes per camera sample of the views */
@@ -398,8 +399,11 @@ int drgb_count_work(drgb_renderer* r, uint64_t* counts);
  * optimiser's state does not change) for candidate work-item shapes (32 or
  * 64 samples per item) and persistent grid sizes (2, 4, 8, 16 blocks per SM
  * for the pixel and the edge-shading kernels), by coordinate descent, and
- * keeps the fastest.  chosen (may be NULL) receives tile_w, tile_h, pixel
- * blocks per SM, edge blocks per SM; best_ms the mean time of the passes. */
+ * keeps the fastest; with DRGB_OPT_PRIMARY_RASTER = 1 it first times the
+ * camera and shadow rays by tiles and cells against traversal.  chosen (may
+ * be NULL) receives 5 values: tile_w, tile_h, pixel blocks per SM, edge
+ * blocks per SM, 1 if tiles and cells are used; best_ms the mean time of the
+ * passes. */
 int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, float* best_ms);
 /* The same for a batch: the grid sizes of its shared launches (2 ints). */
 int drgb_batch_autotune(drgb_batch* b, int trial_iters, int32_t* chosen, float* best_ms);
