@@ -35,6 +35,7 @@ class SHADING_MODEL(enum.IntEnum):
     LAMBERT = 4
     PHONG = 5
     GGX = 6
+    PATH_TEST = 7              # path tracer of shade_path_test.cpp, counter-based random numbers
     LAMBERT_POINT_VCOLOR = 16  # point light + per-vertex albedo (no reference counterpart)
     PATH_DIFFUSE = 17          # fixed-depth diffuse path tracer (no reference counterpart)
 

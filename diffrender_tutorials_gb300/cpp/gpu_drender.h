@@ -27,10 +27,12 @@
 namespace diff_render {
 
 // Renderer on CUDA device `device`.  Models: SILHOUETTE, VERTEX_COLOR,
-// TEXTURE_COLOR, LAMBERT, PHONG, GGX (the reference's numbering), and the
+// TEXTURE_COLOR, LAMBERT, PHONG, GGX and PATH_TEST (the reference's
+// numbering; PATH_TEST draws from a counter-based generator in place of
+// rand(), so its images agree with the reference's in expectation), and the
 // point-light vertex-albedo (16) and diffuse path (17) models that have no
-// reference counterpart.  PATH_TEST and any other number print an error and
-// the renderer stays unusable.
+// reference counterpart.  Any other number prints an error and the renderer
+// stays unusable.
 std::shared_ptr<IDiffRender> MakeGpuDifferentialRenderer(const DiffRenderSettings& settings, int device = 0);
 
 // OptSimple's loop with every iteration (render, loss, gradients, update,

@@ -128,6 +128,7 @@ struct drgb_batch {
       A.orig = J.orig.p;
       A.col = J.col.p;
       A.nrm = J.nrm.p;
+      A.tan = J.tan.p;
       A.tc = J.tc.p;
       A.tri_v = J.tri_v.p;
       A.perm = J.perm.p;

@@ -53,7 +53,7 @@ __global__ void k_block_tr(const BlockDev* blocks, int n_blocks, const float* co
 // Flattened vertex arrays (prepare_for_render's per-instance loop).
 __device__ __forceinline__ void flatten_body(int g, const int* vblock, const BlockDev* blocks, const MeshSrc* src,
                                              const float* block_tr, float4* pos, float4* orig, float4* col,
-                                             float4* nrm, float2* tc) {
+                                             float4* nrm, float2* tc, float4* tan) {
   const int b = vblock[g];
   const BlockDev bd = blocks[b];
   const int k = g - bd.vert_off;
@@ -71,13 +71,17 @@ __device__ __forceinline__ void flatten_body(int g, const int* vblock, const Blo
     nrm[g] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
   }
   tc[g] = s.tc ? make_float2(s.tc[2 * k], s.tc[2 * k + 1]) : make_float2(0.0f, 0.0f);
+  if (tan) {  // tangents by the inverse transpose, default (0,1,0) (scene_utils.cpp:133,167-168)
+    const f3 tt = s.tan ? mat_pt(tr + 16, mk(s.tan[3 * k], s.tan[3 * k + 1], s.tan[3 * k + 2])) : mk(0.0f, 1.0f, 0.0f);
+    tan[g] = make_float4(tt.x, tt.y, tt.z, 0.0f);
+  }
 }
 
 __global__ void k_flatten(const int* vblock, int n, const BlockDev* blocks, const MeshSrc* src, const float* block_tr,
-                          float4* pos, float4* orig, float4* col, float4* nrm, float2* tc) {
+                          float4* pos, float4* orig, float4* col, float4* nrm, float2* tc, float4* tan) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
-  flatten_body(g, vblock, blocks, src, block_tr, pos, orig, col, nrm, tc);
+  flatten_body(g, vblock, blocks, src, block_tr, pos, orig, col, nrm, tc, tan);
 }
 
 // ---------------------------------------------------------------------------
@@ -481,7 +485,7 @@ __global__ void k_b_flatten(const JobAux* aux, const Seg* segs, int nseg) {
   const int g = (blockIdx.x - sg.begin) * blockDim.x + threadIdx.x;
   if (g >= sg.count) return;
   const JobAux& A = aux[sg.job];
-  flatten_body(g, A.vblock, A.blocks, A.src, A.block_tr, A.pos, A.orig, A.col, A.nrm, A.tc);
+  flatten_body(g, A.vblock, A.blocks, A.src, A.block_tr, A.pos, A.orig, A.col, A.nrm, A.tc, A.tan);
 }
 
 __global__ void k_b_zero_counters(const JobAux* aux, const Seg* segs, int nseg) {
@@ -531,7 +535,8 @@ void flatten_scene(Job& J, cudaStream_t s) {
   if (J.n_vertices == 0) return;
   k_block_tr<<<(J.n_blocks + 63) / 64, 64, 0, s>>>(J.blocks.p, J.n_blocks, J.tr_tab.p, J.block_tr.p);
   k_flatten<<<(J.n_vertices + 255) / 256, 256, 0, s>>>(J.vblock.p, J.n_vertices, J.blocks.p, J.src_tab.p,
-                                                      J.block_tr.p, J.pos.p, J.orig.p, J.col.p, J.nrm.p, J.tc.p);
+                                                      J.block_tr.p, J.pos.p, J.orig.p, J.col.p, J.nrm.p, J.tc.p,
+                                                      J.tan.p);
   count_launch(2);
 }
 

@@ -69,7 +69,7 @@ int drgb_renderer_create(int shading_model, int spp, int device, drgb_renderer**
     *out = nullptr;
     switch (shading_model) {
       case DRGB_SILHOUETTE: case DRGB_VERTEX_COLOR: case DRGB_TEXTURE_COLOR: case DRGB_LAMBERT: case DRGB_PHONG:
-      case DRGB_GGX:
+      case DRGB_GGX: case DRGB_PATH_TEST:
       case DRGB_LAMBERT_POINT_VCOLOR: case DRGB_PATH_DIFFUSE: break;
       default: throw CudaError("unknown shading model " + std::to_string(shading_model), DRGB_ERR_UNSUPPORTED);
     }

@@ -24,6 +24,7 @@ enum Model : int {
   LAMBERT = 4,
   PHONG = 5,
   GGX = 6,
+  PATH_TEST = 7,
   LAMBERT_POINT_VCOLOR = 16,
   PATH_DIFFUSE = 17,
 };
@@ -32,8 +33,10 @@ __host__ __device__ inline bool model_has_color(int m) {
   return m == VERTEX_COLOR || m == LAMBERT_POINT_VCOLOR || m == PATH_DIFFUSE;
 }
 __host__ __device__ inline bool model_has_tex(int m) {
-  return m == TEXTURE_COLOR || m == LAMBERT || m == PHONG || m == GGX;
+  return m == TEXTURE_COLOR || m == LAMBERT || m == PHONG || m == GGX || m == PATH_TEST;
 }
+// Models whose samples trace several bounces (random walks of varying length).
+__host__ __device__ constexpr bool model_is_path(int m) { return m == PATH_DIFFUSE || m == PATH_TEST; }
 
 constexpr int kStackSize = 96;
 constexpr int kEmpty4 = (int)0x80000000;  // unused slot of a 4-wide node
@@ -116,6 +119,7 @@ struct JobDev {
   const float4* orig;    // untransformed positions
   const float4* col;
   const float4* nrm;
+  const float4* tan;     // tangents (PATH_TEST only, else null)
   const float2* tc;
   const int4* tri_v;     // per flattened triangle: global ids A,B,C and block index
   const BlockDev* blocks;
@@ -246,6 +250,7 @@ struct MeshSrc {
   const float* col;
   const float* nrm;
   const float* tc;
+  const float* tan;
 };
 
 // One differentiable mesh as the optimiser updates it.
@@ -272,7 +277,7 @@ struct JobAux {
   const MeshSrc* src;
   const float* const* tr_tab;
   float* block_tr;
-  float4 *pos, *orig, *col, *nrm;
+  float4 *pos, *orig, *col, *nrm, *tan;
   float2* tc;
   const int4* tri_v;
   const int* perm;

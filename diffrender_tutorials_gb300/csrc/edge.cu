@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(co
 static void launch_shade_job(const JobDev* d_jobs, int job, int mode, int grid, const int* order, bool det,
                              cudaStream_t s) {
   grid = std::max(1, grid);
-  const bool pairs = mode == PATH_DIFFUSE;
+  const bool pairs = model_is_path(mode);
   if (det) {
     if (pairs) k_edge_shade_job<true, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
     else k_edge_shade_job<true, false><<<grid, 256, 0, s>>>(d_jobs, job, order);

@@ -213,7 +213,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   for (int m = 0; m < nm; m++) {
     const MeshState& M = J.meshes[m];
     src[m] = MeshSrc{M.vertices.p, M.has_colors ? M.colors.p : nullptr, M.has_normals ? M.normals.p : nullptr,
-                     M.has_tc ? M.tc.p : nullptr};
+                     M.has_tc ? M.tc.p : nullptr, M.has_tangents ? M.tangents.p : nullptr};
     trs[m] = M.transforms.p;
   }
   J.src_tab.upload(src.data(), src.size(), s);
@@ -223,6 +223,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   J.orig.alloc(nv);
   J.col.alloc(nv);
   J.nrm.alloc(nv);
+  if (J.mode == PATH_TEST) J.tan.alloc(nv);  // the path model's shading frames
   J.tc.alloc(nv);
   J.block_tr.alloc(32 * (size_t)std::max(1, J.n_blocks));
   // inverse transforms of mesh 0 (Scene::get_transform_inv(0), kept from the
@@ -440,6 +441,7 @@ void sync_dev(Job& J) {
   d.orig = J.orig.p;
   d.col = J.col.p;
   d.nrm = J.nrm.p;
+  d.tan = J.tan.p;
   d.tc = J.tc.p;
   d.tri_v = J.tri_v.p;
   d.blocks = J.blocks.p;

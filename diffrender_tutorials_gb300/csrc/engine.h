@@ -178,6 +178,7 @@ struct Job {
   int n_vertices = 0, n_tris = 0, n_blocks = 0;
   std::vector<BlockDev> h_blocks;
   DevBuf<float4> pos, orig, col, nrm;
+  DevBuf<float4> tan;  // flattened tangents, PATH_TEST only
   DevBuf<float2> tc;
   DevBuf<int4> tri_v;
   DevBuf<BlockDev> blocks;

@@ -164,6 +164,7 @@ extern "C" int drgb_d_render_and_compare_noalloc(drgb_renderer* r, const drgb_ca
     d.orig = J.orig.p;
     d.col = J.col.p;
     d.nrm = J.nrm.p;
+    d.tan = J.tan.p;
     d.tc = J.tc.p;
     d.tri_v = J.tri_v.p;
     d.blocks = J.blocks.p;

@@ -250,7 +250,7 @@ constexpr int PX_MAX_SAMPLES = 64;
 #endif
 constexpr int px_min_blocks(int mode, bool det, bool hits) {
   (void)hits;  // the stored-hit variants get the same budget, for a like-for-like comparison
-  return mode == 0 ? 1 : det ? DRGB_PX_MIN_BLOCKS_DET : mode == PATH_DIFFUSE ? DRGB_PX_MIN_BLOCKS_PATH : DRGB_PX_MIN_BLOCKS;
+  return mode == 0 ? 1 : det ? DRGB_PX_MIN_BLOCKS_DET : model_is_path(mode) ? DRGB_PX_MIN_BLOCKS_PATH : DRGB_PX_MIN_BLOCKS;
 }
 template <int MODE, bool DET, bool HITS>
 __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_pixels(const JobDev* __restrict__ jobs, const int4* __restrict__ items,
@@ -551,6 +551,7 @@ static void launch_pixels_t(const JobDev* d_jobs, const int4* d_items, int n_ite
       k_pixels<LAMBERT_POINT_VCOLOR, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags);
       break;
     case PATH_DIFFUSE: k_pixels<PATH_DIFFUSE, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
+    case PATH_TEST: k_pixels<PATH_TEST, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
     default: k_pixels<0, DET, false><<<grid, PX_THREADS, 0, s>>>(d_jobs, d_items, n_items, d_counter, flags); break;
   }
 }
@@ -602,6 +603,7 @@ int pixel_blocks_resident(int mode) {
     case GGX: f = (const void*)k_pixels<GGX, false, false>; break;
     case LAMBERT_POINT_VCOLOR: f = (const void*)k_pixels<LAMBERT_POINT_VCOLOR, false, false>; break;
     case PATH_DIFFUSE: f = (const void*)k_pixels<PATH_DIFFUSE, false, false>; break;
+    case PATH_TEST: f = (const void*)k_pixels<PATH_TEST, false, false>; break;
     default: f = (const void*)k_pixels<0, false, false>; break;
   }
   DRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, PX_THREADS, 0));

@@ -113,6 +113,7 @@ int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_
   int64_t b = 0;
   b += V * 56 + T * 12 + tex * 4 + inst * 128;  // mesh arrays, transforms and inverses
   b += VF * (72 + 4 + 16 * nv);                 // flattened vertices, vertex blocks, projections
+  if (mode == PATH_TEST) b += VF * 16;          // flattened tangents
   b += TF * (16 + 272);                         // triangle ids, LBVH nodes (binary, 4-wide builds), leaves, sort buffers
   b += TF * (72 + 24 * nv);                     // edges (at most 3 per triangle), pmf/CDF per view
   b += px * (12 + 16 + 8 + 16 + 8);             // targets, adjoint, loss partials, edge queue, random table

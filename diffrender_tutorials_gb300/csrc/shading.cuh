@@ -381,15 +381,18 @@ __device__ __forceinline__ float rnd01(uint32_t a, uint32_t b, uint32_t c) {
 // order (no contraction): the oracle evaluates the same sequence, so both
 // sides draw bit-identical bounce directions, which the math library's
 // sinf/cosf (different on host and device) would not give.
+// sin and cos of a in [-pi/4, pi/4] by those two series.
+__device__ __forceinline__ void sincos_small(float a, float* ps, float* pc) {
+  const float a2 = a * a;
+  *ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f + a2 * 2.75573188e-6f))));
+  *pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
+                                                                                a2 * -2.75573188e-7f))));
+}
 __device__ __forceinline__ void sincos_turns(float x, float* s, float* c) {
   const float x4 = x * 4.0f;
   const float q = rintf(x4);
-  const float a = (x4 - q) * 1.57079633f;
-  const float a2 = a * a;
-  const float ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f +
-                                                                                   a2 * 2.75573188e-6f))));
-  const float pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
-                                                                                          a2 * -2.75573188e-7f))));
+  float ps, pc;
+  sincos_small((x4 - q) * 1.57079633f, &ps, &pc);
   switch (((int)q) & 3) {
     case 0: *s = ps; *c = pc; break;
     case 1: *s = pc; *c = -ps; break;
@@ -469,6 +472,123 @@ __device__ inline f3 path_diffuse_p(const JobDev& J, const Surf& first, uint32_t
   }
   if (d_alb0) *d_alb0 = dL0;
   return L;
+}
+
+// ConcentricSampleDisk (shade_path_test.cpp:77-95; Shirley and Chiu's
+// concentric map of the square onto the disk).  The angle of either wedge is
+// reduced to [-pi/4, pi/4] (cos(pi/2 - b) = sin b, sin(pi/2 - b) = cos b) and
+// evaluated by sincos_small, so the oracle draws the same directions.
+__device__ __forceinline__ float2 concentric_disk(float u0, float u1) {
+  const float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+  if (ox == 0.0f && oy == 0.0f) return make_float2(0.0f, 0.0f);
+  float sn, cs;
+  if (fabsf(ox) > fabsf(oy)) {
+    sincos_small(0.785398163f * (oy / ox), &sn, &cs);
+    return make_float2(ox * cs, ox * sn);
+  }
+  sincos_small(0.785398163f * (ox / oy), &sn, &cs);
+  return make_float2(oy * sn, oy * cs);
+}
+
+// Luminance of the throughput (intensity(), shade_path_test.cpp:75: double
+// weights, rounded to float).
+__device__ __forceinline__ float path_luminance(f3 c) {
+  return (float)(0.2126 * (double)c.x + 0.7152 * (double)c.y + 0.0722 * (double)c.z);
+}
+
+// shade<PATH_TEST> (shade_path_test.cpp:183-282): up to 8 bounces with
+// Russian roulette after the fourth, texture albedo, next-event estimation
+// toward the point light of colour normalize(1,0.8,0.5) x 2 (PointLight
+// normalises its colour, scene.h:77-82) at (0,0.7,0.7) jittered
+// by +-0.1 per axis, ambient 0.5 for rays that leave the scene.  The shading
+// frame is the interpolated (unnormalised) normal n and
+// e_x = normalize(n x tangent), e_y = normalize(n x e_x); bounces are
+// cosine-sampled in it and weighted by max(0, n_geom . dir) / pdf; a shadow
+// ray counts every hit along its whole line (GetNearestHit without a far
+// limit).  The reference draws from the shared rand(); here sample `key`,
+// bounce b and the job seed index a counter-based hash: draws 8b..8b+2
+// jitter the light, 8b+3 and 8b+4 pick the bounce, 8b+5 decides the
+// roulette.  A path whose throughput is exactly zero stops (its further
+// terms are all zero).  `alive` = the camera ray hit; every lane makes the
+// same traversal calls until the whole warp's paths have ended.
+template <bool WARP>
+__device__ inline f3 path_test_p(const JobDev& J, const Surf& first, uint32_t key, bool alive) {
+  constexpr float kPi = 3.14159265358979323846f;
+  f3 L = mk(0.0f, 0.0f, 0.0f), beta = mk(1.0f, 1.0f, 1.0f);
+  Surf sf = first;
+  f3 ro = first.ro, rd = first.rd;
+  for (int bounce = 0; bounce < 8; bounce++) {
+    bool hitb = alive;
+    if (bounce > 0) {
+      Hit hh;
+      hitb = trace_p<false, WARP>(J, ro, rd, 0.0f, 1e9f, alive, hh);
+      if (alive && !hitb) L = L + beta * 0.5f;
+      if (hitb) {
+        sf.h = hh;
+        const int4 tv = __ldg(J.tri_v + hh.tri);
+        sf.A = tv.x;
+        sf.B = tv.y;
+        sf.C = tv.z;
+        sf.block = tv.w;
+      }
+    }
+    f3 p = mk(0.0f, 0.0f, 0.0f), l = mk(0.0f, 0.0f, 1.0f), n = mk(0.0f, 0.0f, 1.0f), ng = n, alb = n;
+    f3 ex = mk(1.0f, 0.0f, 0.0f), ey = mk(0.0f, 1.0f, 0.0f);
+    float ld = 1.0f;
+    const uint32_t r0 = 8u * (uint32_t)bounce;
+    if (hitb) {
+      const float u = sf.h.u, v = sf.h.v;
+      const MeshDev& m = J.meshes[J.blocks[sf.block].mesh];
+      const float2 tc = interp_tc(J, sf);
+      n = interp(ld3(J.nrm, sf.A), ld3(J.nrm, sf.B), ld3(J.nrm, sf.C), u, v);
+      const f3 tg = interp(ld3(J.tan, sf.A), ld3(J.tan, sf.B), ld3(J.tan, sf.C), u, v);
+      const f3 pa = ld3(J.pos, sf.A);
+      ng = normalize(cross(ld3(J.pos, sf.B) - pa, ld3(J.pos, sf.C) - pa));
+      p = (ro + rd * sf.h.t) + ng * 1e-4f;
+      ex = normalize(cross(n, tg));
+      ey = normalize(cross(n, ex));
+      alb = sample_bilinear(tc.x, tc.y, m.tex_w, m.tex_h, m.tex);
+      const f3 jit = mk(2.0f * rnd01(key, r0, J.mp.seed) - 1.0f, 2.0f * rnd01(key, r0 + 1u, J.mp.seed) - 1.0f,
+                        2.0f * rnd01(key, r0 + 2u, J.mp.seed) - 1.0f);
+      const f3 lv = (mk(0.0f, 0.7f, 0.7f) + jit * 0.1f) - p;
+      ld = dot(lv, lv);
+      l = lv / sqrtf(ld);
+    }
+    Hit sh;
+    const bool occ = trace_p<true, WARP>(J, p, l, 0.0f, 1e9f, hitb, sh);
+    if (hitb && !occ) {
+      const f3 Li = (normalize(mk(1.0f, 0.8f, 0.5f)) * 2.0f) / ld;  // PointLight normalises its colour
+      L = L + beta * (Li * ((alb / kPi) * ref_max(0.0f, dot(n, l))));
+    }
+    if (hitb) {
+      const f3 wo = normalize(rd * -1.0f);
+      const float woz = dot(wo, n);
+      const float2 d = concentric_disk(rnd01(key, r0 + 3u, J.mp.seed), rnd01(key, r0 + 4u, J.mp.seed));
+      float wz = sqrtf(ref_max(0.0f, 1.0f - d.x * d.x - d.y * d.y));
+      if (woz < 0.0f) wz = -wz;
+      const float pdf = woz * wz > 0.0f ? fabsf(wz) / kPi : 1e9f;
+      const f3 nd = mk(ex.x * d.x + ey.x * d.y + n.x * wz, ex.y * d.x + ey.y * d.y + n.y * wz,
+                       ex.z * d.x + ey.z * d.y + n.z * wz);
+      beta = beta * (((alb / kPi) * ref_max(0.0f, dot(ng, nd))) / pdf);
+      rd = nd;
+      ro = p;
+      if (bounce > 3) {
+        const float q = ref_max(0.05f, 1.0f - path_luminance(beta));
+        if (rnd01(key, r0 + 5u, J.mp.seed) < q) hitb = false;
+        else beta = beta / (1.0f - q);
+      }
+      if (beta.x == 0.0f && beta.y == 0.0f && beta.z == 0.0f) hitb = false;
+    }
+    alive = hitb;
+    if (WARP ? !__any_sync(0xffffffffu, alive) : !alive) break;
+  }
+  return L;
+}
+
+// Out of line for the generic shader, whose other models would otherwise
+// share its register allocation.
+static __device__ __noinline__ f3 path_test_call(const JobDev& J, const Surf& first, uint32_t key, bool alive) {
+  return path_test_p<false>(J, first, key, alive);
 }
 
 // shade<M> for every model (shade_simple.cpp, shade_lambert.cpp).  MODE != 0
@@ -594,6 +714,10 @@ __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float 
     case PATH_DIFFUSE: {
       const f3 r = path_diffuse_p<WARP>(J, s, key, hit, nullptr);
       return hit ? r : mk(J.mp.ambient, J.mp.ambient, J.mp.ambient);
+    }
+    case PATH_TEST: {
+      const f3 r = (MODE == 0 && !WARP) ? path_test_call(J, s, key, hit) : path_test_p<WARP>(J, s, key, hit);
+      return hit ? r : mk(0.5f, 0.5f, 0.5f);
     }
     default:
       return mk(0.0f, 0.0f, 0.0f);

@@ -45,6 +45,7 @@ enum {
   DRGB_LAMBERT = 4,
   DRGB_PHONG = 5,                 /* shade_lambert.cpp:45-84 */
   DRGB_GGX = 6,                   /* shade_lambert.cpp:86-168 */
+  DRGB_PATH_TEST = 7,             /* shade_path_test.cpp:183-289: path tracer, counter-based RNG for rand() */
   DRGB_LAMBERT_POINT_VCOLOR = 16, /* point light, per-vertex albedo, ambient; no reference counterpart */
   DRGB_PATH_DIFFUSE = 17          /* fixed-depth diffuse path tracer with counter RNG; no reference counterpart */
 };
@@ -156,7 +157,9 @@ typedef struct drgb_scene_desc {
   const drgb_mesh_desc* meshes;
 } drgb_scene_desc;
 
-/* Constants of the two models without a reference counterpart. */
+/* Constants of the two models without a reference counterpart; of these,
+ * PATH_TEST (whose constants are the reference's) uses only `seed`, the
+ * key of its counter-based random numbers. */
 typedef struct drgb_model_params {
   float light_pos[3];
   float light_intensity;

@@ -648,15 +648,17 @@ static float lpv_factor(const ctx_t* c, const surf_t* sf) {
  * a^10 on a = (4x - q)*pi/2 in [-pi/4, pi/4] (error < 2e-9), rotated by the
  * quadrant.  The CUDA path evaluates the same operations in the same order,
  * so the bounce directions are bit-identical on both sides. */
+static void sincos_small(float a, float* ps, float* pc) {
+  const float a2 = a * a;
+  *ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f + a2 * 2.75573188e-6f))));
+  *pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
+                                                                                a2 * -2.75573188e-7f))));
+}
 static void sincos_turns(float x, float* s, float* c) {
   const float x4 = x * 4.0f;
   const float q = rintf(x4);
-  const float a = (x4 - q) * 1.57079633f;
-  const float a2 = a * a;
-  const float ps = a * (1.0f + a2 * (-1.66666672e-1f + a2 * (8.33333377e-3f + a2 * (-1.98412701e-4f +
-                                                                                   a2 * 2.75573188e-6f))));
-  const float pc = 1.0f + a2 * (-0.5f + a2 * (4.16666679e-2f + a2 * (-1.38888892e-3f + a2 * (2.48015876e-5f +
-                                                                                          a2 * -2.75573188e-7f))));
+  float ps, pc;
+  sincos_small((x4 - q) * 1.57079633f, &ps, &pc);
   switch (((int)q) & 3) {
     case 0: *s = ps; *c = pc; break;
     case 1: *s = pc; *c = -ps; break;
@@ -726,6 +728,97 @@ static f3 path_diffuse(const ctx_t* c, const surf_t* first, uint32_t sample_key,
     beta = mul3(beta, alb);
   }
   if (d_albedo0) *d_albedo0 = dL0;
+  return L;
+}
+
+/* ConcentricSampleDisk, shade_path_test.cpp:77-95 (Shirley and Chiu's
+ * concentric map): the angle of either wedge reduced to [-pi/4, pi/4]
+ * (cos(pi/2 - b) = sin b, sin(pi/2 - b) = cos b) for sincos_small. */
+static f2 concentric_disk(float u0, float u1) {
+  const float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+  float sn, cs;
+  if (ox == 0.0f && oy == 0.0f) return v2(0.0f, 0.0f);
+  if (fabsf(ox) > fabsf(oy)) {
+    sincos_small(0.785398163f * (oy / ox), &sn, &cs);
+    return v2(ox * cs, ox * sn);
+  }
+  sincos_small(0.785398163f * (ox / oy), &sn, &cs);
+  return v2(oy * sn, oy * cs);
+}
+
+/* intensity(), shade_path_test.cpp:75 (double weights) */
+static float path_luminance(f3 c) { return (float)(0.2126 * (double)c.x + 0.7152 * (double)c.y + 0.0722 * (double)c.z); }
+
+/* shade<PATH_TEST>, shade_path_test.cpp:133-282: at most MAX_DEPTH = 8
+ * bounces, Russian roulette for bounce > RR_DEPTH = 3, get_extended_surface_info
+ * (interpolated unnormalised normal n, tangent frame e_x = normalize(n x t),
+ * e_y = normalize(n x e_x), n_geom, position offset 1e-4 n_geom, texture
+ * albedo), direct_light/sample_light (light colour normalize(1,0.8,0.5)
+ * (scene.h:77-82) x 2 at (0,0.7,0.7)
+ * + 0.1 * [-1,1]^3, visibility = no hit on the whole line toward it),
+ * bsdf_sample_f_diffuse (cosine sample, flipped to wo's side, pdf |cos|/pi
+ * or 1e9), ambient 0.5 on leaving the scene.  The reference's rand() is
+ * replaced by rnd01(key, 8*bounce + j, seed): j = 0..2 light jitter, 3..4
+ * bounce direction, 5 roulette.  A path whose throughput is exactly zero
+ * stops (all its further terms are zero). */
+static f3 path_test(const ctx_t* c, const surf_t* first, uint32_t key) {
+  const prep_t* s = c->s;
+  const float PI_F = 3.14159265358979323846f;
+  const uint32_t seed = c->mp->seed;
+  f3 L = v3(0, 0, 0), beta = v3(1, 1, 1);
+  surf_t sf = *first;
+  f3 ro = first->ro, rd = first->rd;
+  for (int bounce = 0; bounce < 8; bounce++) {
+    if (bounce > 0) {
+      sf.h = nearest_hit(s, ro, rd, 0.0f, 1e9f);
+      if (sf.h.prim == 0xFFFFFFFFu) {
+        L = add3(L, scl3(beta, 0.5f));
+        break;
+      }
+      sf.A = get_index(s, (int)sf.h.geom, (int)sf.h.inst, (int)sf.h.prim * 3 + 0);
+      sf.B = get_index(s, (int)sf.h.geom, (int)sf.h.inst, (int)sf.h.prim * 3 + 1);
+      sf.C = get_index(s, (int)sf.h.geom, (int)sf.h.inst, (int)sf.h.prim * 3 + 2);
+    }
+    const uint32_t r0 = 8u * (uint32_t)bounce;
+    const float u = sf.h.u, v = sf.h.v;
+    const orc_mesh* m = s->meshes + sf.h.geom;
+    const f2 tc = interp2(s->tc[sf.A], s->tc[sf.B], s->tc[sf.C], u, v);
+    const f3 n = interp3(s->nrm[sf.A], s->nrm[sf.B], s->nrm[sf.C], u, v);
+    const f3 tg = interp3(s->tng[sf.A], s->tng[sf.B], s->tng[sf.C], u, v);
+    const f3 ng = norm3(cross3(sub3(s->pos[sf.B], s->pos[sf.A]), sub3(s->pos[sf.C], s->pos[sf.A])));
+    const f3 p = add3(add3(ro, scl3(rd, sf.h.t)), scl3(ng, 1e-4f));
+    const f3 ex = norm3(cross3(n, tg));
+    const f3 ey = norm3(cross3(n, ex));
+    const f3 alb = sample_bilinear(tc, m->tex_w, m->tex_h, m->texture);
+    /* direct light */
+    const f3 jit = v3(2.0f * rnd01(key, r0, seed) - 1.0f, 2.0f * rnd01(key, r0 + 1u, seed) - 1.0f,
+                      2.0f * rnd01(key, r0 + 2u, seed) - 1.0f);
+    const f3 lv = sub3(add3(v3(0.0f, 0.7f, 0.7f), scl3(jit, 0.1f)), p);
+    const float ld = dot3(lv, lv);
+    const f3 l = div3s(lv, sqrtf(ld));
+    if (!any_hit(s, p, l, 0.0f, 1e9f)) {
+      const f3 Li = div3s(scl3(norm3(v3(1.0f, 0.8f, 0.5f)), 2.0f), ld); /* PointLight normalises its colour */
+      L = add3(L, mul3(beta, mul3(Li, scl3(div3s(alb, PI_F), maxf_ref(0.0f, dot3(n, l))))));
+    }
+    /* next direction */
+    const f3 wo = norm3(scl3(rd, -1.0f));
+    const float woz = dot3(wo, n);
+    const f2 d = concentric_disk(rnd01(key, r0 + 3u, seed), rnd01(key, r0 + 4u, seed));
+    float wz = sqrtf(maxf_ref(0.0f, 1.0f - d.x * d.x - d.y * d.y));
+    if (woz < 0.0f) wz = -wz;
+    const float pdf = woz * wz > 0.0f ? fabsf(wz) / PI_F : 1e9f;
+    const f3 nd = v3(ex.x * d.x + ey.x * d.y + n.x * wz, ex.y * d.x + ey.y * d.y + n.y * wz,
+                     ex.z * d.x + ey.z * d.y + n.z * wz);
+    beta = mul3(beta, div3s(scl3(div3s(alb, PI_F), maxf_ref(0.0f, dot3(ng, nd))), pdf));
+    rd = nd;
+    ro = p;
+    if (bounce > 3) {
+      const float q = maxf_ref(0.05f, 1.0f - path_luminance(beta));
+      if (rnd01(key, r0 + 5u, seed) < q) break;
+      beta = div3s(beta, 1.0f - q);
+    }
+    if (beta.x == 0.0f && beta.y == 0.0f && beta.z == 0.0f) break;
+  }
   return L;
 }
 
@@ -833,7 +926,8 @@ typedef struct {
 
 static int mode_has_color(int mode) { return mode == ORC_VERTEX_COLOR || mode == ORC_LAMBERT_POINT_VCOLOR || mode == ORC_PATH_DIFFUSE; }
 static int mode_has_tex(int mode) {
-  return mode == ORC_TEXTURE_COLOR || mode == ORC_LAMBERT || mode == ORC_PHONG || mode == ORC_GGX;
+  return mode == ORC_TEXTURE_COLOR || mode == ORC_LAMBERT || mode == ORC_PHONG || mode == ORC_GGX ||
+         mode == ORC_PATH_TEST;
 }
 
 static dlayout_t make_layout(const orc_mesh* m, int mode) {
@@ -909,8 +1003,12 @@ static void static_block(int64_t n, int T, int k, int64_t* b, int64_t* e) {
  * Forward render (drender.h:98-141).
  * ------------------------------------------------------------------------- */
 static f3 shade_sample(const ctx_t* c, f2 sp, uint32_t key) {
-  if (c->mode != ORC_PATH_DIFFUSE) return shade(c, sp);
   surf_t sf;
+  if (c->mode == ORC_PATH_TEST) {
+    if (!cast(c, sp, &sf)) return v3(0.5f, 0.5f, 0.5f);
+    return path_test(c, &sf, key);
+  }
+  if (c->mode != ORC_PATH_DIFFUSE) return shade(c, sp);
   if (!cast(c, sp, &sf)) return v3(c->mp->ambient, c->mp->ambient, c->mp->ambient);
   return path_diffuse(c, &sf, key, NULL);
 }
@@ -997,7 +1095,7 @@ static void shade_grad(const ctx_t* c, const dmap_t* dm, f2 sp, f3 val, float* g
     col[3 * A + 0] += ca.x; col[3 * A + 1] += ca.y; col[3 * A + 2] += ca.z;
     col[3 * B + 0] += cb.x; col[3 * B + 1] += cb.y; col[3 * B + 2] += cb.z;
     col[3 * C + 0] += cc.x; col[3 * C + 1] += cc.y; col[3 * C + 2] += cc.z;
-  } else if (mode_has_tex(c->mode)) { /* PHONG, GGX: shade_lambert.cpp:80-84, 163-168 */
+  } else if (mode_has_tex(c->mode)) { /* PHONG, GGX: shade_lambert.cpp:80-84, 163-168; PATH_TEST: shade_path_test.cpp:284-289 */
     if (L->tex_off < 0) return;
     const f2 tc = interp2(s->tc[sf.A], s->tc[sf.B], s->tc[sf.C], u, v);
     sample_bilinear_grad(val, tc, m->tex_w, m->tex_h, g + L->tex_off);

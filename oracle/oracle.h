@@ -32,6 +32,7 @@ enum {
   ORC_LAMBERT = 4,
   ORC_PHONG = 5,
   ORC_GGX = 6,
+  ORC_PATH_TEST = 7,             /* shade_path_test.cpp:183-289, counter RNG in place of rand() */
   ORC_LAMBERT_POINT_VCOLOR = 16, /* point light + per-vertex albedo */
   ORC_PATH_DIFFUSE = 17          /* fixed-depth diffuse path tracer, counter RNG */
 };

@@ -15,6 +15,7 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 ORC_CAM_FLOATS = 82
 SILHOUETTE, VERTEX_COLOR, TEXTURE_COLOR, LAMBERT = 1, 2, 3, 4
+PATH_TEST = 7
 LAMBERT_POINT_VCOLOR, PATH_DIFFUSE = 16, 17
 
 

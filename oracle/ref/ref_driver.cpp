@@ -13,6 +13,7 @@
 //   CamInfo                           common_src/camera.h:6-44
 //   qmc::planeHammersley, prng::*     common_src/qmc.cpp:227-268
 //   mesh_utils::LoadMeshFromVSGF      common_src/cmesh.cpp:139-170
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <memory>
@@ -278,8 +279,37 @@ int main(int argc, char** argv) {
       std::vector<Img> imgs(cams.size());
       for (size_t i = 0; i < cams.size(); i++) imgs[i].resize((int)cams[i].width, (int)cams[i].height);
       dr->commit(scene);
-      dr->render(scene, cams.data(), imgs.data(), (int)cams.size());
-      images_out(out, "images", imgs);
+      // repeats > 1 (a random model such as PATH_TEST): the mean image of
+      // that many renders and the unbiased per-value variance across them
+      const int repeats = in.i("repeats", 1);
+      std::vector<double> sum, sum2;
+      for (int r = 0; r < repeats; r++) {
+        dr->render(scene, cams.data(), imgs.data(), (int)cams.size());
+        if (repeats == 1) break;
+        size_t k = 0;
+        for (auto& im : imgs) {
+          const float* p = (const float*)im.data();
+          const size_t n = 3 * (size_t)im.width() * im.height();
+          sum.resize(k + n, 0.0);
+          sum2.resize(k + n, 0.0);
+          for (size_t j = 0; j < n; j++, k++) {
+            sum[k] += p[j];
+            sum2[k] += (double)p[j] * p[j];
+          }
+        }
+      }
+      if (repeats == 1) {
+        images_out(out, "images", imgs);
+      } else {
+        std::vector<float> mean(sum.size()), var(sum.size());
+        for (size_t j = 0; j < sum.size(); j++) {
+          const double m = sum[j] / repeats;
+          mean[j] = (float)m;
+          var[j] = (float)std::max(0.0, (sum2[j] - repeats * m * m) / (repeats - 1));
+        }
+        out.put_f32("images", mean);
+        out.put_f32("images_var", var);
+      }
     } else {
       std::vector<int> ids;
       for (int32_t x : in.vec<int32_t>("dmesh_ids")) ids.push_back(x);

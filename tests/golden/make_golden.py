@@ -8,7 +8,9 @@ outputs as tests/golden/*.npz.  It needs the reference source tree and runs
 in the development container only; the fixtures it writes are committed and
 are all that the tests read.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # all but the long runs
+    python tests/golden/make_golden.py convergence  # 300-iteration optimiser runs
+    python tests/golden/make_golden.py path_test    # the PATH_TEST mean image
 """
 import math
 import os
@@ -50,6 +52,48 @@ def textured_sphere(sub=2, tex_size=16, seed=3):
     tex = rng.uniform(0.1, 0.9, size=(tex_size, tex_size, 3)).astype(np.float32)
     return TriangleMesh(m.vertices, m.indices, tc=np.stack([u, v], 1).astype(np.float32), normals=m.normals,
                         textures=[Texture(tex_size, tex_size, 3, tex.reshape(-1))])
+
+
+def path_test_scene():
+    """Scene for shade<PATH_TEST> (src/shade_path_test.cpp): a textured
+    sphere of radius 0.4 above a textured floor (y = -0.3), normals and
+    tangents given, both outward-wound; the model's point light (0,0.7,0.7)
+    lies outside the sphere.  Used with the camera PATH_TEST_CAM."""
+    sph = textured_sphere(2, tex_size=8, seed=7)
+    n = sph.normals.astype(np.float64)
+    t = np.cross(np.array([0.0, 1.0, 0.0]), n)
+    flat = np.linalg.norm(t, axis=1) < 1e-3
+    t[flat] = (1.0, 0.0, 0.0)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    sph.vertices = (sph.vertices * np.float32(0.4) + np.array([0.0, 0.1, 0.0], np.float32)).astype(np.float32)
+    sph.tangents = t.astype(np.float32)
+    y = -0.3
+    fv = np.array([[-2, y, -2], [2, y, -2], [2, y, 2], [-2, y, 2]], np.float32)
+    checker = np.array([[0.8, 0.75, 0.6] if (i + j) % 2 == 0 else [0.3, 0.35, 0.5] for j in range(4) for i in range(4)],
+                       np.float32)
+    floor = TriangleMesh(fv, np.array([0, 2, 1, 0, 3, 2], np.uint32),
+                         tc=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32),
+                         normals=np.tile(np.array([0, 1, 0], np.float32), (4, 1)),
+                         textures=[Texture(4, 4, 3, checker.reshape(-1))])
+    floor.tangents = np.tile(np.array([1, 0, 0], np.float32), (4, 1))
+    sc = Scene()
+    sc.add_mesh(sph)
+    sc.add_mesh(floor)
+    return sc
+
+
+PATH_TEST_CAM = dict(origin=(0.0, 0.7, 2.2), width=32, height=32)
+
+
+def path_test():
+    """The reference's PATH_TEST model (its shared rand() stream): mean
+    image of 16 renders at 64 spp and the per-value variance across them."""
+    build_ref.build(verbose=True)
+    sc = path_test_scene()
+    cam = Cam(PATH_TEST_CAM["origin"], PATH_TEST_CAM["width"], PATH_TEST_CAM["height"])
+    items = {"task": np.array([2], np.int32), "mode": np.array([7], np.int32), "spp": np.array([64], np.int32),
+             "repeats": np.array([16], np.int32), **scene_items(sc), **cam_items([cam])}
+    save("render_path_test", **items, **prefixed("out.", run(items)))
 
 
 def pyramid(seed=4):
@@ -275,6 +319,7 @@ def main():
              "dmesh_ids": np.array([0], np.int32)}
     out = run(items)
     save("optimize_cube_vc", **items, **prefixed("out.", out))
+    path_test()
 
 
 def _moved(mesh, m):
@@ -342,5 +387,7 @@ def convergence():
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "convergence":
         convergence()
+    elif len(sys.argv) > 1 and sys.argv[1] == "path_test":
+        path_test()
     else:
         main()
