@@ -662,6 +662,7 @@ def instances_arm(args, ws, rank, local, pg):
         for period in (0, 10):
             ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
             ro.set_option(N.OPT_BVH_BUILDER, builder)
+            ro.set_option(N.OPT_PRIMARY_RASTER, RASTER[args.raster])
             ro.set_option(N.OPT_BVH_REBUILD, period)
             opt = D.CreateSimpleOptimizer()
             opt.Init(isc, ro, cams, tgt, p)
@@ -757,6 +758,7 @@ def stress_arm(args, ws, rank, local, pg):
         ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
         ro.set_option(N.OPT_ADJOINT_HITS, hits)
         ro.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
+        ro.set_option(N.OPT_PRIMARY_RASTER, RASTER[args.raster])
         opt = D.CreateSimpleOptimizer()
         opt.Init(isc, ro, cams, tgt, p)
         stream = torch.cuda.ExternalStream(ro.stream(), device=local)
@@ -784,6 +786,7 @@ def stress_arm(args, ws, rank, local, pg):
     for period in (0, 100):
         ro = D.MakeDifferentialRenderer(D.DiffRenderSettings(S, spp), device=local)
         ro.set_option(N.OPT_BVH_BUILDER, BVH_BUILDERS[args.bvh])
+        ro.set_option(N.OPT_PRIMARY_RASTER, RASTER[args.raster])
         ro.set_option(N.OPT_BVH_REBUILD, period)
         opt = D.CreateSimpleOptimizer()
         opt.Init(isc, ro, cams, tgt, p)

@@ -319,6 +319,12 @@ void launch_loss_finalize(const JobDev* d_jobs, int n_jobs, cudaStream_t s);
 void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int nty, int tw, int th, cudaStream_t s);
 // Raster tile of tw x th pixels for S samples per pixel.
 void raster_tile(int S, int& tw, int& th);
+// The size rule of the raster pass (without autotuning): at least 2 M
+// forward camera samples per call, 64 triangles, and 32 forward samples per
+// (view, triangle).
+inline bool raster_pays(int64_t fwd_samples, int64_t n_views, int64_t n_tris) {
+  return fwd_samples >= (2 << 20) && n_tris >= 64 && fwd_samples >= 32 * n_views * n_tris;
+}
 // Light-space cells (G x G) of point-light shadow rays for the current geometry.
 void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s);
 int light_grid_size(int n_tris);

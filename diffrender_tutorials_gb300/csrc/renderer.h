@@ -184,10 +184,15 @@ struct drgb_renderer {
     // small calls: the raster pass's fixed cost (about 15 launches) outweighs
     // what it saves; measured on GB300, a 12-triangle cube at 256x256 x 16 spp
     // and 5,120 triangles at 512x512 x 4 spp x 2 views break even (1-2 M
-    // samples).  The optimiser's autotuner times both ways instead.
+    // samples).  Dense meshes: binning costs per (view, triangle) and the
+    // tile lists grow long, so fewer than about 32 forward samples per
+    // (view, triangle) trace (GB300, point light: 82k triangles x 4 views at
+    // 512x512 x 4 spp, 13 samples, 0.87x; 200k x 4 views x 16 spp, 21
+    // samples, 0.84x; from 51 samples on 1.13-1.58x).  The optimiser's
+    // autotuner times both ways instead.
     const size_t samples = (size_t)n_pixels() * J.S;
     const bool pays = J.raster == 2 ? true
-                      : J.raster_pick >= 0 ? J.raster_pick == 1 : (samples >= (2u << 20) && J.n_tris >= 64);
+                      : J.raster_pick >= 0 ? J.raster_pick == 1 : raster_pays(samples, J.n_views, J.n_tris);
     const bool on = J.raster && pays && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 &&
                     J.n_views > 0;
     if (on) {

@@ -124,8 +124,8 @@ int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_
   // the light-space cells of the point-light models (64 entries per triangle)
   const int64_t S = (int64_t)std::max(1, (int)std::sqrt((float)std::max(1, spp))) *
                     std::max(1, (int)std::sqrt((float)std::max(1, spp)));
-  // (the renderer's size rule: calls of fewer than 2 M camera samples trace)
-  if (px * S < (2 << 20) || TF < 64) return b;
+  // (the renderer's size rule)
+  if (!raster_pays(px * S, nv, TF)) return b;
   b += px * S * 32 + TF * nv * (64 + 128) + (int64_t)(1 << 16) * 4 + px * 8 + 64;
   if (mode == LAMBERT_POINT_VCOLOR || mode == PATH_DIFFUSE) {
     const int64_t G = light_grid_size((int)std::min<int64_t>(TF, 1 << 30));

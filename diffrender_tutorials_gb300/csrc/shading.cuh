@@ -183,11 +183,27 @@ __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, flo
   return true;
 }
 
-// Whether a camera ray of `view` at image position (x, y) can use the
-// raster pass's tile lists (built for this call's geometry; the footprints
-// are clipped to the image, so only positions inside it).
-__device__ __forceinline__ bool tiles_usable(const JobDev& J, const CamDev& cam, float x, float y) {
-  return J.ra_tiles && (*J.ra_state & 2u) && x >= 0.0f && x < cam.width && y >= 0.0f && y < cam.height;
+// Lists of at most this many entries are sorted by their distance bound
+// (k_sort_lists): a query stops at the first entry whose bound it beats.
+constexpr uint32_t kSortedList = 64;
+
+// Screen tile of image position (x, y) in `view` (index into ra_tiles).
+__device__ __forceinline__ int tile_of(const JobDev& J, int view, float x, float y) {
+  const int tx = min(J.ra_ntx - 1, (int)x / J.ra_tw), ty = min(J.ra_nty - 1, (int)y / J.ra_th);
+  return (view * J.ra_nty + ty) * J.ra_ntx + tx;
+}
+
+// Whether a camera ray of `view` at image position (x, y) uses the raster
+// pass's tile lists (built for this call's geometry; the footprints are
+// clipped to the image, so only positions inside it): only where the
+// tile's list is sorted.  A single query against a long unsorted list reads
+// every entry and costs more than the traversal (dense meshes: 200k
+// triangles at 512x512 doubled the edge pass).
+__device__ __forceinline__ bool tiles_usable(const JobDev& J, const CamDev& cam, int view, float x, float y) {
+  if (!(J.ra_tiles && (*J.ra_state & 2u) && x >= 0.0f && x < cam.width && y >= 0.0f && y < cam.height))
+    return false;
+  const int b = tile_of(J, view, x, y);
+  return __ldg(J.ra_tiles + b + 1) - __ldg(J.ra_tiles + b) <= kSortedList;
 }
 
 // The nearest hit of the camera ray of `view` at (x, y) among the triangles
@@ -203,17 +219,21 @@ __device__ __forceinline__ bool cast_tiles(const JobDev& J, const CamDev& cam, i
   s.A = s.B = s.C = 0;
   s.block = 0;
   if (!active) return false;
-  const int tx = min(J.ra_ntx - 1, (int)x / J.ra_tw), ty = min(J.ra_nty - 1, (int)y / J.ra_th);
-  const int b = (view * J.ra_nty + ty) * J.ra_ntx + tx;
+  const int b = tile_of(J, view, x, y);
   const uint32_t i0 = __ldg(J.ra_tiles + b), i1 = __ldg(J.ra_tiles + b + 1);
+  const bool sorted = i1 - i0 <= kSortedList;
   unsigned long long best = ~0ull;
   float bu = 0.0f, bv = 0.0f;
   unsigned n_tri = 0, n_fp = 0;
   for (uint32_t i = i0; i < i1; i++) {
     const int j = __ldg(J.ra_list + i);
     const float4 q0 = __ldg(J.ra_rec + 4 * j + 1);
-    // no hit on it can be nearer than the best so far (none yet: NaN compares false)
-    if (q0.w > __uint_as_float((uint32_t)(best >> 32))) continue;
+    // no hit on it can be nearer than the best so far (none yet: NaN
+    // compares false), nor on the entries after it in a sorted list
+    if (q0.w > __uint_as_float((uint32_t)(best >> 32))) {
+      if (sorted) break;
+      continue;
+    }
     n_fp++;
     const float4 box = __ldg(J.ra_rec + 4 * j);
     if (!(x >= box.x && x <= box.y && y >= box.z && y <= box.w)) continue;
@@ -311,12 +331,16 @@ __device__ __forceinline__ bool light_occluded(const JobDev& J, f3 p, f3 l, floa
   const int cx = min(g.G - 1, max(0, (int)a)), cy = min(g.G - 1, max(0, (int)b));
   const int c = cy * g.G + cx;
   const uint32_t i0 = __ldg(J.sh_cells + c), i1 = __ldg(J.sh_cells + c + 1);
+  const bool sorted = i1 - i0 <= kSortedList;
   unsigned n_tri = 0, n_fp = 0;
   bool occ = false;
   for (uint32_t i = i0; i < i1 && !occ; i++) {
     const int k = __ldg(J.sh_list + i);
     const float4 q0 = __ldg(J.sh_rec + 4 * k + 1);
-    if (q0.w >= tfar) continue;  // no nearer to the light than p: not between them
+    if (q0.w >= tfar) {  // no nearer to the light than p: not between them
+      if (sorted) break;  // nor is any later entry of a sorted list
+      continue;
+    }
     n_fp++;
     const float4 box = __ldg(J.sh_rec + 4 * k);
     if (!(a >= box.x && a <= box.y && b >= box.z && b <= box.w)) continue;
@@ -646,7 +670,7 @@ __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float 
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s)
-                   : (!WARP && view >= 0 && tiles_usable(J, cam, x, y)) ? cast_tiles(J, cam, view, x, y, active, s)
+                   : (!WARP && view >= 0 && tiles_usable(J, cam, view, x, y)) ? cast_tiles(J, cam, view, x, y, active, s)
                                                                        : cast_p<WARP>(J, cam, x, y, active, s);
   if (hit_tri) *hit_tri = hit ? s.h.tri : -1;
   const float u = s.h.u, v = s.h.v;
