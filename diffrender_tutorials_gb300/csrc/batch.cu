@@ -34,7 +34,7 @@ int64_t job_device_bytes(const Job& J) {
        J.loss_part.bytes() + J.loss_blk.bytes() + J.loss_out.bytes() + J.proj.bytes() + J.pmf.bytes() + J.cdf.bytes() + J.queue.bytes() +
        J.queue_count.bytes() + J.grad.bytes() + J.err.bytes();
   b += J.opt.m.bytes() + J.opt.G.bytes() + J.opt.lr.bytes() + J.opt.iter.bytes() + J.opt.losses.bytes();
-  b += J.vis[0].bytes() + J.vis[1].bytes() + J.ra_tiles.bytes() + J.ra_cursor.bytes() + J.ra_state.bytes() +
+  b += J.vis[0].bytes() + J.vis[1].bytes() + J.vis_uv[0].bytes() + J.vis_uv[1].bytes() + J.ra_tiles.bytes() + J.ra_cursor.bytes() + J.ra_state.bytes() +
        J.ra_list.bytes() + J.ra_rec.bytes();
   b += J.sh_grid.bytes() + J.sh_cells.bytes() + J.sh_cursor.bytes() + J.sh_list.bytes() + J.sh_rec.bytes();
   return b;

@@ -35,6 +35,11 @@ __host__ __device__ inline bool model_has_color(int m) {
 __host__ __device__ inline bool model_has_tex(int m) {
   return m == TEXTURE_COLOR || m == LAMBERT || m == PHONG || m == GGX || m == PATH_TEST;
 }
+// Whether a model's shader reads the camera ray (0: the generic shader, any
+// model); vertex colour, texture and silhouette interpolate by u, v alone.
+__host__ __device__ constexpr bool model_reads_ray(int m) {
+  return !(m == SILHOUETTE || m == VERTEX_COLOR || m == TEXTURE_COLOR);
+}
 // Models whose samples trace several bounces (random walks of varying length).
 __host__ __device__ constexpr bool model_is_path(int m) { return m == PATH_DIFFUSE || m == PATH_TEST; }
 
@@ -205,6 +210,11 @@ struct JobDev {
   // hit); null: the samples are traced through the hierarchy
   float4* vis_fwd;
   float4* vis_adj;
+  // point-light model: u, v of the hit per forward / adjoint sample, and the
+  // float4 record holds the shading point ro + rd * (t - 1e-5) in place of
+  // t (what the model uses of the ray; the pixel kernel then builds no ray)
+  float2* vis_uv_fwd;
+  float2* vis_uv_adj;
   const uint32_t* ra_state;  // bit 0: the raster pass wrote nothing this call; bit 1: its tile lists
                              // hold the current geometry (cleared by every refit)
   // the raster pass's screen tiles (tw x th pixels, ntx x nty per view): per

@@ -191,12 +191,21 @@ __device__ __forceinline__ void queue_append(int4* queue, int* count, int cap, b
   }
 }
 
+// One shading point of an edge sample: the generic shader (every model), or
+// the model MODE alone.
+template <int MODE>
+__device__ __forceinline__ f3 edge_point(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key,
+                                         int view) {
+  if (MODE == 0) return shade_generic(J, cam, x, y, key, view);
+  return shade_p<MODE, false>(J, cam, x, y, key, true, nullptr, false, float4{0.0f, 0.0f, 0.0f, 0.0f}, view);
+}
+
 // Shading and chain rule of queue entries [q0, q0+32) (one per lane).  DET:
 // the deterministic-mode variant (records for jobs that have record buffers).
 // PAIRS: two lanes per entry, the even one shading the inside point and the
 // odd one the outside point in the same traversal call (16 entries per
 // warp); else one lane per entry shades both points in turn.
-template <bool DET, bool PAIRS = false>
+template <bool DET, bool PAIRS = false, int MODE = 0>
 __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* queue, int n, int q0,
                                                 const int* order = nullptr) {
   const int lane = threadIdx.x & 31;
@@ -229,15 +238,15 @@ __device__ __forceinline__ void edge_shade_warp(const JobDev* jobs, const int4* 
     const uint32_t key_out = 0xA511E9B3u ^ ((uint32_t)(i * 2u + 1u) * 2654435761u);
     f3 color_in, color_out;
     if (PAIRS) {
-      const f3 mine = shade_generic(J, cam, side ? coutx : cinx, side ? couty : ciny, side ? key_out : key_in, view);
+      const f3 mine = edge_point<MODE>(J, cam, side ? coutx : cinx, side ? couty : ciny, side ? key_out : key_in, view);
       const unsigned pair = 3u << (lane & ~1);  // both lanes of an entry take this branch
       const f3 other = mk(__shfl_xor_sync(pair, mine.x, 1), __shfl_xor_sync(pair, mine.y, 1),
                           __shfl_xor_sync(pair, mine.z, 1));
       color_in = side ? other : mine;
       color_out = side ? mine : other;
     } else {
-      color_in = shade_generic(J, cam, cinx, ciny, key_in, view);
-      color_out = shade_generic(J, cam, coutx, couty, key_out, view);
+      color_in = edge_point<MODE>(J, cam, cinx, ciny, key_in, view);
+      color_out = edge_point<MODE>(J, cam, coutx, couty, key_out, view);
     }
     const float pdf = pm / sqrtf(dx0 * dx0 + dy0 * dy0);
     const float weight = 1.0f / (pdf * (float)J.edge_samples);
@@ -385,7 +394,7 @@ __global__ void k_edge_select(const JobDev* jobs, int job) {
 // the queue count), so warps that drew cheap samples take more and the launch
 // ends without a tail of idle SMs; -DDRGB_EDGE_STATIC strides statically.
 // `order` (may be null) is the shading order of the entries.
-template <bool DET, bool PAIRS = false>
+template <bool DET, bool PAIRS = false, int MODE = 0>
 __device__ __forceinline__ void edge_shade_loop(const JobDev* jobs, const int4* queue, int n, int* work,
                                                 const int* order) {
   constexpr int kPerWarp = PAIRS ? 16 : 32;
@@ -393,7 +402,7 @@ __device__ __forceinline__ void edge_shade_loop(const JobDev* jobs, const int4* 
   (void)work;
   const int stride = gridDim.x * blockDim.x / 32 * kPerWarp;
   for (int q0 = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * kPerWarp; q0 < n; q0 += stride)
-    edge_shade_warp<DET, PAIRS>(jobs, queue, n, q0, order);
+    edge_shade_warp<DET, PAIRS, MODE>(jobs, queue, n, q0, order);
 #else
   const int lane = threadIdx.x & 31;
   while (true) {
@@ -401,7 +410,7 @@ __device__ __forceinline__ void edge_shade_loop(const JobDev* jobs, const int4* 
     if (lane == 0) q0 = atomicAdd(work, kPerWarp);
     q0 = __shfl_sync(0xffffffffu, q0, 0);
     if (q0 >= n) break;
-    edge_shade_warp<DET, PAIRS>(jobs, queue, n, q0, order);
+    edge_shade_warp<DET, PAIRS, MODE>(jobs, queue, n, q0, order);
   }
 #endif
 }
@@ -428,12 +437,14 @@ __global__ void k_b_queue_keys(const JobDev* jobs, const int4* queue, const int*
 
 // Single job: the queue, its counter and its capacity are the job's own;
 // `order` (may be null) is the shading order of the queue entries.
-template <bool DET, bool PAIRS>
+// MODE != 0: the shader of that model alone (the point-light model of the
+// benchmark; fewer registers and spills than the generic shader).
+template <bool DET, bool PAIRS, int MODE = 0>
 __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(const JobDev* jobs, int job,
                                                                               const int* order) {
   const JobDev& J = jobs[job];
   stage_top_nodes(J);
-  edge_shade_loop<DET, PAIRS>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
+  edge_shade_loop<DET, PAIRS, MODE>(jobs, J.queue, min(J.queue_count[0], J.queue_cap), J.queue_count + 1, order);
 }
 
 // Lane pairs for the path model, whose two points cost alike but vary a lot
@@ -441,6 +452,11 @@ __global__ void __launch_bounds__(256, DRGB_EDGE_MIN_BLOCKS) k_edge_shade_job(co
 // 4.34 -> 4.03 ms); one lane per entry for the others, where the inside point
 // of a silhouette sample hits and casts a shadow ray and the outside point
 // misses (point-light icosphere: 1.50 ms against 2.10 ms with pairs).
+#ifdef DRGB_EDGE_GENERIC
+constexpr bool kEdgeSpecialised = false;
+#else
+constexpr bool kEdgeSpecialised = true;
+#endif
 static void launch_shade_job(const JobDev* d_jobs, int job, int mode, int grid, const int* order, bool det,
                              cudaStream_t s) {
   grid = std::max(1, grid);
@@ -448,9 +464,12 @@ static void launch_shade_job(const JobDev* d_jobs, int job, int mode, int grid, 
   if (det) {
     if (pairs) k_edge_shade_job<true, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
     else k_edge_shade_job<true, false><<<grid, 256, 0, s>>>(d_jobs, job, order);
+  } else if (pairs) {
+    k_edge_shade_job<false, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
+  } else if (mode == LAMBERT_POINT_VCOLOR && kEdgeSpecialised) {
+    k_edge_shade_job<false, false, LAMBERT_POINT_VCOLOR><<<grid, 256, 0, s>>>(d_jobs, job, order);
   } else {
-    if (pairs) k_edge_shade_job<false, true><<<grid, 256, 0, s>>>(d_jobs, job, order);
-    else k_edge_shade_job<false, false><<<grid, 256, 0, s>>>(d_jobs, job, order);
+    k_edge_shade_job<false, false><<<grid, 256, 0, s>>>(d_jobs, job, order);
   }
 }
 

@@ -491,6 +491,8 @@ void sync_dev(Job& J) {
   d.edge_sil = J.edge_sil;
   d.vis_fwd = J.raster_on ? J.vis[0].p : nullptr;
   d.vis_adj = J.raster_on ? J.vis[1].p : nullptr;
+  d.vis_uv_fwd = J.raster_on && vis_points(J.mode) ? J.vis_uv[0].p : nullptr;
+  d.vis_uv_adj = J.raster_on && vis_points(J.mode) ? J.vis_uv[1].p : nullptr;
   d.ra_state = J.ra_state.p;
   d.ra_tiles = J.raster_on ? J.ra_tiles.p : nullptr;
   d.ra_list = J.ra_list.p;

@@ -161,6 +161,7 @@ struct Job {
   int raster_pick = -1;       // the optimiser's autotuner's choice (-1: none, the size rule decides)
   bool raster_on = false;     // raster buffers set up for the current views (see renderer::raster_buffers)
   DevBuf<float4> vis[2];              // rasterised visibility of forward / adjoint samples
+  DevBuf<float2> vis_uv[2];           // their u, v where the records hold shading points
   DevBuf<uint32_t> ra_tiles;          // triangles per screen tile, then their offsets (scan)
   DevBuf<uint32_t> ra_cursor;         // per tile fill cursor
   DevBuf<uint32_t> ra_state;          // bit 0: the tile lists did not fit ra_list
@@ -325,6 +326,8 @@ void raster_tile(int S, int& tw, int& th);
 inline bool raster_pays(int64_t fwd_samples, int64_t n_views, int64_t n_tris) {
   return fwd_samples >= (2 << 20) && n_tris >= 64 && fwd_samples >= 32 * n_views * n_tris;
 }
+// Models whose raster records hold the shading point and u, v (JobDev::vis_uv_*).
+inline bool vis_points(int mode) { return mode == LAMBERT_POINT_VCOLOR; }
 // Light-space cells (G x G) of point-light shadow rays for the current geometry.
 void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s);
 int light_grid_size(int n_tris);

@@ -265,13 +265,34 @@ __device__ __forceinline__ float4 ra_hit(unsigned long long best, float u, float
   return make_float4(__uint_as_float((uint32_t)(best >> 32)), u, v, __int_as_float((int)(uint32_t)best));
 }
 
+// The point-light model's record: the shading point ro + rd * (t - 1e-5)
+// (lpv_factor_p's arithmetic on the sample's own camera ray), the triangle,
+// and u, v beside it.
+__device__ __forceinline__ void ra_point(unsigned long long best, float u, float v, f3 ro, f3 rd, float4* rec,
+                                         float2* uv) {
+  if (best == ~0ull) {
+    *rec = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+    *uv = make_float2(0.0f, 0.0f);
+    return;
+  }
+  const f3 p = ro + rd * (__uint_as_float((uint32_t)(best >> 32)) - 1e-5f);
+  *rec = make_float4(p.x, p.y, p.z, __int_as_float((int)(uint32_t)best));
+  *uv = make_float2(u, v);
+}
+
 // One block per (view, tile): the nearest hit of every forward (passes & 1)
 // and adjoint (passes & 2) sample of the tile's pixels.  The tile's
 // triangles are staged once per RA_STAGE for both passes; a thread holds
 // one forward and one adjoint sample (tiles of at most RA_THREADS samples),
 // whose two independent tests interleave.  Larger tiles (more than
 // RA_THREADS samples per pixel) take their samples RA_THREADS at a time.
-__global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int passes, int tw, int th, int ntx,
+// Four resident blocks (64 registers): the unconstrained allocation (94
+// registers, two blocks) ran the icosphere workload at 170.5 against 192.5
+// iterations/s on GB300.
+#ifndef DRGB_RESOLVE_MIN_BLOCKS
+#define DRGB_RESOLVE_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(RA_THREADS, DRGB_RESOLVE_MIN_BLOCKS) k_resolve(const JobDev* jobs, int passes, int tw, int th, int ntx,
                                                         int nty, const uint32_t* tiles, const int* list,
                                                         const uint32_t* state, const RaRec* rec) {
   __shared__ float4 s_a[RA_STAGE], s_e1[RA_STAGE], s_e2[RA_STAGE];  // A | id bits, e1, e2
@@ -287,6 +308,7 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
   const int S = J.S;
   const uint32_t l0 = tiles[b], l1 = tiles[b + 1];
   const int n_list = (int)(l1 - l0);
+  const bool sorted = n_list <= RA_STAGE;  // k_sort_lists orders lists of up to 64
   const int64_t vbase = J.img_off[view];
   const int tile_samples = tw * th * S;
   const bool fwd = passes & 1, adj = (passes >> 1) & 1;
@@ -317,13 +339,28 @@ __global__ void __launch_bounds__(RA_THREADS) k_resolve(const JobDev* jobs, int 
       }
       __syncthreads();
       for (int c = 0; c < nc; c++) {
+        // a sorted list (one stage): once both samples hold hits nearer than
+        // this entry's bound, no later entry can win either (no best yet:
+        // NaN, the comparison fails)
+        if (sorted) {
+          const float lb = s_rec[c].l0.w;
+          if ((!a0 || lb > __uint_as_float((uint32_t)(b0 >> 32))) &&
+              (!a1 || lb > __uint_as_float((uint32_t)(b1 >> 32))))
+            break;
+        }
         ra_test(s_a, s_e1, s_e2, s_rec, c, a0, x0, y0, ro0, rd0, b0, u0, v0, n_tests, n_fp);
         ra_test(s_a, s_e1, s_e2, s_rec, c, a1, x1, y1, ro1, rd1, b1, u1, v1, n_tests, n_fp);
       }
     }
     // every sample of the tile is written, a miss too
-    if (a0) J.vis_fwd[(vbase + (int64_t)py0 * W + px0) * S + k0] = ra_hit(b0, u0, v0);
-    if (a1) J.vis_adj[(vbase + (int64_t)py1 * W + px1) * S + k1] = ra_hit(b1, u1, v1);
+    const int64_t i0 = (vbase + (int64_t)py0 * W + px0) * S + k0, i1 = (vbase + (int64_t)py1 * W + px1) * S + k1;
+    if (J.vis_uv_fwd) {  // shading point + u, v (the same arithmetic as the shader's)
+      if (a0) ra_point(b0, u0, v0, ro0, rd0, J.vis_fwd + i0, J.vis_uv_fwd + i0);
+      if (a1) ra_point(b1, u1, v1, ro1, rd1, J.vis_adj + i1, J.vis_uv_adj + i1);
+    } else {
+      if (a0) J.vis_fwd[i0] = ra_hit(b0, u0, v0);
+      if (a1) J.vis_adj[i1] = ra_hit(b1, u1, v1);
+    }
     if (J.work && n_list > 0 && (a0 || a1)) {
       atomicAdd(J.work + 0, (unsigned long long)(a0 + a1));  // the samples' camera rays
       atomicAdd(J.work + 2, (unsigned long long)n_tests);

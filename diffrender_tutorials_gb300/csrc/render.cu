@@ -146,7 +146,8 @@ __device__ __forceinline__ void texture_grad(const JobDev& J, float* g, f3 val, 
 template <int MODE, bool DET, bool HITS>
 __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, bool active, float x, float y, f3 val,
                                            uint32_t key, float* wscr, int64_t rec_base, int& rec_n,
-                                           const float4* stored, int seed, bool use_vis, float4 vkey) {
+                                           const float4* stored, int seed, bool use_vis, float4 vkey,
+                                           const float2* vuv) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
   bool hit;
@@ -167,7 +168,9 @@ __device__ __forceinline__ void shade_grad(const JobDev& J, const CamDev& cam, b
       s.block = tv.w;
     }
   } else if (use_vis) {
-    hit = cast_vis(J, cam, x, y, active, vkey, s);
+    // the gradients of the vertex-colour and texture models read u, v only
+    hit = cast_vis(J, cam, x, y, active, vkey, s, vuv,
+                   MODE == 0 || mode == LAMBERT_POINT_VCOLOR || mode == PATH_DIFFUSE);
   } else {
     hit = cast_p<kPixelWarp>(J, cam, x, y, active, s, seed);
   }
@@ -334,9 +337,10 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         if (s < NS) s_hit[s] = act ? ht : -1;
 #else
         const bool use_vis = vis_ok && J.vis_fwd != nullptr;
-        const float4 vk = act && use_vis ? J.vis_fwd[(J.img_off[view] + (int64_t)py * W + px) * S + k]
-                                         : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
-        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, nullptr, use_vis, vk);
+        const int64_t vi = (J.img_off[view] + (int64_t)py * W + px) * S + k;
+        const float4 vk = act && use_vis ? J.vis_fwd[vi] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+        const float2* vuv = use_vis && J.vis_uv_fwd ? J.vis_uv_fwd + (act ? vi : 0) : nullptr;
+        const f3 sc = shade_p<MODE, kPixelWarp>(J, C, fx, fy, key, act, nullptr, use_vis, vk, -1, vuv);
 #endif
         if (act) c = sc / (float)S;
         if (s < NS) {
@@ -436,9 +440,11 @@ __global__ void __launch_bounds__(PX_THREADS, px_min_blocks(MODE, DET, HITS)) k_
         }
 #endif
         const bool use_vis = vis_ok && J.vis_adj != nullptr;
-        const float4 vk = act && use_vis ? J.vis_adj[(J.img_off[view] + (int64_t)py * W + px) * S + k]
-                                         : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
-        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed, use_vis, vk);
+        const int64_t vi = (J.img_off[view] + (int64_t)py * W + px) * S + k;
+        const float4 vk = act && use_vis ? J.vis_adj[vi] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+        const float2* vuv = use_vis && J.vis_uv_adj ? J.vis_uv_adj + (act ? vi : 0) : nullptr;
+        shade_grad<MODE, DET, HITS>(J, C, act, sx, sy, val, key, wscr, rec_base, rec_n, hslot, seed, use_vis, vk,
+                                    vuv);
       }
       if (DET && J.det && lane == 0 && !store_hits) J.rec_count[it - J.item_base] = rec_n;
     }

@@ -185,11 +185,11 @@ struct drgb_renderer {
     // what it saves; measured on GB300, a 12-triangle cube at 256x256 x 16 spp
     // and 5,120 triangles at 512x512 x 4 spp x 2 views break even (1-2 M
     // samples).  Dense meshes: binning costs per (view, triangle) and the
-    // tile lists grow long, so fewer than about 32 forward samples per
-    // (view, triangle) trace (GB300, point light: 82k triangles x 4 views at
-    // 512x512 x 4 spp, 13 samples, 0.87x; 200k x 4 views x 16 spp, 21
-    // samples, 0.84x; from 51 samples on 1.13-1.58x).  The optimiser's
-    // autotuner times both ways instead.
+    // tile lists grow long, so fewer than 32 forward samples per (view,
+    // triangle) trace (GB300: 64 instances of 5,120 triangles, 4 views at
+    // 512x512 x 16 spp, 13 samples, 0.88x; the 200k-triangle path-model
+    // stress scene, 21 samples, 0.94x; point light from 51 samples on
+    // 1.07-1.60x).  The optimiser's autotuner times both ways instead.
     const size_t samples = (size_t)n_pixels() * J.S;
     const bool pays = J.raster == 2 ? true
                       : J.raster_pick >= 0 ? J.raster_pick == 1 : raster_pays(samples, J.n_views, J.n_tris);
@@ -198,6 +198,10 @@ struct drgb_renderer {
     if (on) {
       J.vis[0].reserve(samples);
       J.vis[1].reserve(samples);
+      if (vis_points(J.mode)) {
+        J.vis_uv[0].reserve(samples);
+        J.vis_uv[1].reserve(samples);
+      }
       int tw, th, ntx, nty;
       raster_geometry(tw, th, ntx, nty);
       const size_t n_tiles = (size_t)J.n_views * ntx * nty;
@@ -238,7 +242,9 @@ struct drgb_renderer {
     const size_t n_tiles = (size_t)J.n_views * ntx * nty;
     if (J.dev.vis_fwd != J.vis[0].p || J.dev.vis_adj != J.vis[1].p || J.dev.ra_state != J.ra_state.p ||
         J.vis[0].n < samples || J.vis[1].n < samples || J.ra_tiles.n < scan_scratch(n_tiles + 1) ||
-        J.ra_cursor.n < n_tiles || !J.ra_list.p || J.ra_rec.n < (size_t)4 * J.n_views * J.n_tris) {
+        J.ra_cursor.n < n_tiles || !J.ra_list.p || J.ra_rec.n < (size_t)4 * J.n_views * J.n_tris ||
+        (vis_points(J.mode) && (J.dev.vis_uv_fwd != J.vis_uv[0].p || J.dev.vis_uv_adj != J.vis_uv[1].p ||
+                                J.vis_uv[0].n < samples || J.vis_uv[1].n < samples))) {
       // nothing built for this call: no stale hit or list may be read either
       // (state 0x01010101: bit 0 "wrote nothing" set, bit 1 "lists valid" clear)
       if (J.ra_state.p) DRGB_CUDA(cudaMemsetAsync(J.ra_state.p, 1, sizeof(uint32_t), st));

@@ -119,14 +119,15 @@ int64_t estimate_bytes(const drgb_scene_desc& s, const drgb_camera* cams, int n_
   b += px * (12 + 16 + 8 + 16 + 8);             // targets, adjoint, loss partials, edge queue, random table
   b += (V * 6 + tex + inst * 12) * 4 * 3;       // gradient, first and second moments
   b += 64 << 10;                                // tables, counters, loss history
-  // raster pass: a hit record per forward and adjoint sample, per (view,
+  // raster pass: a hit record per forward and adjoint sample (with u, v
+  // beside it for the point-light model), per (view,
   // triangle) a footprint and room for 32 tile-list entries, tile offsets;
   // the light-space cells of the point-light models (64 entries per triangle)
   const int64_t S = (int64_t)std::max(1, (int)std::sqrt((float)std::max(1, spp))) *
                     std::max(1, (int)std::sqrt((float)std::max(1, spp)));
   // (the renderer's size rule)
   if (!raster_pays(px * S, nv, TF)) return b;
-  b += px * S * 32 + TF * nv * (64 + 128) + (int64_t)(1 << 16) * 4 + px * 8 + 64;
+  b += px * S * (vis_points(mode) ? 48 : 32) + TF * nv * (64 + 128) + (int64_t)(1 << 16) * 4 + px * 8 + 64;
   if (mode == LAMBERT_POINT_VCOLOR || mode == PATH_DIFFUSE) {
     const int64_t G = light_grid_size((int)std::min<int64_t>(TF, 1 << 30));
     b += G * G * 8 + 16 + TF * (64 + 256) + (int64_t)(1 << 16) * 4 + 64;

@@ -155,10 +155,20 @@ __device__ __forceinline__ bool cast_p(const JobDev& J, const CamDev& cam, float
 
 // The camera ray of a sample whose nearest hit the raster pass found:
 // hit = {t, u, v, triangle bits} (triangle -1: none), the values the
-// reference's ray/triangle test computed for that ray.
+// reference's ray/triangle test computed for that ray.  uv != null: the
+// record is the point-light model's, hit = {shading point, triangle bits}
+// and *uv = {u, v}; the surface is then returned with ro = that point,
+// rd = 0 and t = 1e-5, so that ro + rd * (t - 1e-5), the shader's point,
+// is the stored point.  ray = false: the model reads no ray (its
+// interpolation uses u, v only) and none is built.
 __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, float x, float y, bool active,
-                                         float4 hit, Surf& s) {
-  camera_ray(cam, x, y, s.ro, s.rd);
+                                         float4 hit, Surf& s, const float2* uv = nullptr, bool ray = true) {
+  if (ray && !uv) {
+    camera_ray(cam, x, y, s.ro, s.rd);
+  } else {
+    s.ro = mk(hit.x, hit.y, hit.z);
+    s.rd = mk(0.0f, 0.0f, 0.0f);
+  }
   s.h.t = 1e9f;
   s.h.tri = -1;
   s.h.u = s.h.v = 0.0f;
@@ -171,9 +181,16 @@ __device__ __forceinline__ bool cast_vis(const JobDev& J, const CamDev& cam, flo
     atomicOr(J.err, ERR_VISIBILITY);
     return false;
   }
-  s.h.t = hit.x;
-  s.h.u = hit.y;
-  s.h.v = hit.z;
+  if (uv) {
+    const float2 q = *uv;
+    s.h.t = 1e-5f;
+    s.h.u = q.x;
+    s.h.v = q.y;
+  } else {
+    s.h.t = hit.x;
+    s.h.u = hit.y;
+    s.h.v = hit.z;
+  }
   s.h.tri = id;
   const int4 tv = __ldg(J.tri_v + id);
   s.A = tv.x;
@@ -666,10 +683,11 @@ __device__ __forceinline__ float ggx_term(f3 n, f3 ray_dir, f3 light_dir) {
 template <int MODE, bool WARP>
 __device__ inline f3 shade_p(const JobDev& J, const CamDev& cam, float x, float y, uint32_t key, bool active,
                              int* hit_tri = nullptr, bool use_vis = false,
-                             float4 vkey = float4{0.0f, 0.0f, 0.0f, 0.0f}, int view = -1) {
+                             float4 vkey = float4{0.0f, 0.0f, 0.0f, 0.0f}, int view = -1,
+                             const float2* vuv = nullptr) {
   const int mode = MODE ? MODE : J.mode;
   Surf s;
-  const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s)
+  const bool hit = use_vis ? cast_vis(J, cam, x, y, active, vkey, s, vuv, model_reads_ray(MODE))
                    : (!WARP && view >= 0 && tiles_usable(J, cam, view, x, y)) ? cast_tiles(J, cam, view, x, y, active, s)
                                                                        : cast_p<WARP>(J, cam, x, y, active, s);
   if (hit_tri) *hit_tri = hit ? s.h.tri : -1;

@@ -86,18 +86,19 @@ def test_server_job_same_alone_and_in_mix():
 def test_server_job_alone_and_in_mix_atomic_mode():
     """Float atomics: the first forward pass is identical; afterwards the
     summation order can flip the sign of near-zero gradient components, whose
-    step the reference's normalised update makes a full learning-rate step.
-    Measured relative loss deviation from the job alone, per step of 12:
-    mix 0, 0, 1e-6, 3e-6, 5e-6, 2.4e-4, ..., at most 2.9e-3; plain 0, 0, 0,
-    6e-4, ..., at most 5.4e-3.  Bounds: 1e-4 for the first three steps,
-    2e-2 for all."""
+    step the reference's normalised update makes a full learning-rate step,
+    and the trajectories drift apart at a rate that varies from run to run.
+    Measured relative loss deviation from the job alone over 12 steps: the
+    first three at most 1e-6; the last ones 3e-3 to 5e-3 in one run and up
+    to 4.9e-2 in another.  Bounds: 1e-4 for the first three steps, 0.1 for
+    all (the deterministic mode, above, gives the same bits)."""
     a, alone, plain, mixed = run_alone_plain_and_mix(False)
     assert alone[0][0] == mixed[0][0] == plain[0][0]
     assert alone[0].size == mixed[0].size == plain[0].size == 12
     for name, other in (("mix", mixed[0]), ("plain", plain[0])):
         print(name, "relative loss deviation per step", np.round(np.abs(other / alone[0] - 1), 6).tolist())
         np.testing.assert_allclose(other[:3], alone[0][:3], rtol=1e-4)
-        np.testing.assert_allclose(other, alone[0], rtol=2e-2)
+        np.testing.assert_allclose(other, alone[0], rtol=0.1)
 
 
 def test_server_budget_and_slots():
