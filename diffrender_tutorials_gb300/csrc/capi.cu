@@ -304,7 +304,8 @@ static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams,
   const cudaMemcpyKind h2d = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const cudaMemcpyKind d2h = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   J.targets.reserve(3 * npix);
-  DRGB_CUDA(cudaMemcpyAsync(J.targets.p, targets, sizeof(float) * 3 * npix, h2d, r->stream));
+  if (device_ptrs) DRGB_CUDA(cudaMemcpyAsync(J.targets.p, targets, sizeof(float) * 3 * npix, h2d, r->stream));
+  else r->upload_inputs(J.targets.p, targets, sizeof(float) * 3 * npix);
   if (out_images) J.images.reserve(3 * npix);
   r->push_dev();
   // images are only written when requested
@@ -312,6 +313,10 @@ static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams,
   if (!out_images) d.images = nullptr;
   DRGB_CUDA(cudaMemcpyAsync(r->d_job.p, &d, sizeof(JobDev), cudaMemcpyHostToDevice, r->stream));
   r->enqueue_iteration(out_images != nullptr);
+  if (r->pixels_wait) {  // a pass without pixel kernel (no views) still orders the copy
+    DRGB_CUDA(cudaStreamWaitEvent(r->stream, r->pixels_wait, 0));
+    r->pixels_wait = nullptr;
+  }
   if (J.grad_total > 0) DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, d2h, r->stream));
   if (out_images)
     DRGB_CUDA(cudaMemcpyAsync(out_images, J.images.p, sizeof(float) * 3 * npix, d2h, r->stream));

@@ -64,6 +64,11 @@ struct CamDev {
   float proj_inv[16];
   float wv_inv[16];
   float width, height;
+  // camera_ray's constants: the ray origin wv_inv * (0,0,0,1) (the same
+  // float operations, done once), and 1/width, 1/height when those are powers
+  // of two (x * 2^-k = x / 2^k exactly; 0 otherwise: divide)
+  float ro[3];
+  float inv_w, inv_h;
 };
 
 // A (mesh, instance) pair: where its vertices start in the flattened arrays.
@@ -456,7 +461,8 @@ __host__ __device__ inline void mat_inverse44(const float* m1, float* out) {
 // used by BruteForce3D::CastSingleRay (raytrace3d_bf.cpp:158-174).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void camera_ray(const CamDev& c, float x, float y, f3& ro, f3& rd) {
-  const float xn = x / c.width, yn = y / c.height;
+  const float xn = c.inv_w != 0.0f ? x * c.inv_w : x / c.width;
+  const float yn = c.inv_h != 0.0f ? y * c.inv_h : y / c.height;
   const float V0 = 2.0f * xn - 1.0f, V1 = -2.0f * yn + 1.0f, V2 = 0.0f, V3 = 1.0f;
   const float* B = c.proj_inv;
   float r0 = V0 * B[0] + V1 * B[4] + V2 * B[8] + V3 * B[12];
@@ -468,7 +474,7 @@ __device__ __forceinline__ void camera_ray(const CamDev& c, float x, float y, f3
   r2 /= r3;
   const f3 dir = normalize(mk(r0, r1, r2));
   const f3 p0 = mk(0.0f, 0.0f, 0.0f);
-  const f3 pos = mat_pt(c.wv_inv, p0);
+  const f3 pos = mk(c.ro[0], c.ro[1], c.ro[2]);  // mat_pt(c.wv_inv, p0)
   const f3 pos2 = mat_pt(c.wv_inv, p0 + dir * 100.0f);
   ro = pos;
   rd = normalize(pos2 - pos);

@@ -79,6 +79,17 @@ CamDev make_cam(const drgb_camera& c) {
   mat_inverse44(c.world_view, d.wv_inv);
   d.width = c.width;
   d.height = c.height;
+  // camera_ray's origin: mat_pt(wv_inv, (0,0,0)) in the device's operation
+  // order (host code is built without contraction, so the bits agree)
+  const float z = 0.0f, one = 1.0f;
+  for (int i = 0; i < 3; i++)
+    d.ro[i] = z * d.wv_inv[i] + z * d.wv_inv[4 + i] + z * d.wv_inv[8 + i] + one * d.wv_inv[12 + i];
+  auto pow2_inv = [](float w) {
+    int e = 0;
+    return (w > 0.0f && std::frexp(w, &e) == 0.5f) ? 1.0f / w : 0.0f;
+  };
+  d.inv_w = pow2_inv(c.width);
+  d.inv_h = pow2_inv(c.height);
   return d;
 }
 

@@ -63,12 +63,20 @@ struct drgb_renderer {
   // sequential chain per view).
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // Host-pointer calls copy the targets on `xfer` while the raster pass runs;
+  // pixels_wait (when set) is the event the pixel kernel waits for.
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t ev_xfer_fork = nullptr, ev_xfer = nullptr;
+  cudaEvent_t pixels_wait = nullptr;
   int px_resident = 0;  // pixel blocks per SM of the current model (0: not queried)
 
   ~drgb_renderer() {
     if (graph) cudaGraphExecDestroy(graph);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_xfer_fork) cudaEventDestroy(ev_xfer_fork);
+    if (ev_xfer) cudaEventDestroy(ev_xfer);
+    if (xfer) cudaStreamDestroy(xfer);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -300,9 +308,31 @@ struct drgb_renderer {
     const bool hits = J.store_hits && J.hit_buf.p && (flags & PX_ADJ);
     const int n = (int)J.h_pixel_items.size();
     flags |= raster_pass(flags);
+    wait_inputs();
     if (hits) launch_pixels(d_job.p, d_items.p, n, d_counter.p, PX_ADJ | PX_HIT_STORE, px_grid(), stream, J.mode, J.det);
     launch_pixels(d_job.p, d_items.p, n, d_counter.p, flags | (hits ? PX_HIT_LOAD : 0), px_grid(), stream, J.mode,
                   J.det);
+  }
+
+  // The pixel kernel reads the targets: wait for their copy (see xfer).
+  void wait_inputs() {
+    if (pixels_wait) DRGB_CUDA(cudaStreamWaitEvent(stream, pixels_wait, 0));
+  }
+
+  // Copies n bytes of host data to dst on the transfer stream, after the work
+  // already on the renderer's stream (which may still read dst); the next
+  // pixel pass waits for the copy, while the raster pass overlaps it.
+  void upload_inputs(void* dst, const void* src, size_t n) {
+    if (!xfer) {
+      DRGB_CUDA(cudaStreamCreateWithFlags(&xfer, cudaStreamNonBlocking));
+      DRGB_CUDA(cudaEventCreateWithFlags(&ev_xfer_fork, cudaEventDisableTiming));
+      DRGB_CUDA(cudaEventCreateWithFlags(&ev_xfer, cudaEventDisableTiming));
+    }
+    DRGB_CUDA(cudaEventRecord(ev_xfer_fork, stream));
+    DRGB_CUDA(cudaStreamWaitEvent(xfer, ev_xfer_fork, 0));
+    DRGB_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, xfer));
+    DRGB_CUDA(cudaEventRecord(ev_xfer, xfer));
+    pixels_wait = ev_xfer;
   }
 
   // Deterministic mode: clear the record counts before a gradient pass and
@@ -385,6 +415,7 @@ struct drgb_renderer {
       // one SM slot per CDF block stays free of the persistent pixel kernel
       const int grid = std::max(1, std::min(px_grid(), sm_count * px_resident - J.n_views));
       flags |= raster_pass(flags);
+      wait_inputs();
       launch_pixels(d_job.p, d_items.p, (int)J.h_pixel_items.size(), d_counter.p, flags, grid, stream, J.mode, J.det);
       launch_loss_finalize(d_job.p, 1, stream);
       DRGB_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
