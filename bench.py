@@ -363,14 +363,16 @@ def drgb_arm(args, w, ws, rank, local, pg):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     npix = w["res"] * w["res"] * w["views"]
     # algorithmic bytes of one pixel-kernel launch: targets read (12 B/px),
-    # adjoint written (16 B/px), the raster pass's hit record of every forward
-    # and adjoint camera sample read (16 B each), scene data read once
+    # adjoint written (16 B/px), the raster pass's record of every forward
+    # and adjoint camera sample read (16 B; 24 B for the point-light model,
+    # whose record adds u, v to the shading point), scene data read once
     # (pos/col/nrm/tc 56 B/vertex, triangles+indices 64 B/triangle, nodes
     # 64 B/node), gradients written
     n_tri = sum(m.face_count for m in isc.meshes)
     n_v = sum(m.vertex_count for m in isc.meshes)
     S_eff = int(math.isqrt(w["spp"])) ** 2
-    alg_bytes = npix * (12 + 16) + 2 * 16 * npix * S_eff + n_v * 56 + n_tri * (64 + 64) + n_v * 24
+    rec_bytes = 24 if w["mode"] == 16 else 16
+    alg_bytes = npix * (12 + 16) + 2 * rec_bytes * npix * S_eff + n_v * 56 + n_tri * (64 + 64) + n_v * 24
     px_s = prof["pixels"] / 1e3
     ach = alg_bytes / px_s / 1e9
     traffic = read_traffic()
