@@ -42,7 +42,7 @@ COMPILE = [
     "src/drender.cpp", "src/functions.cpp", "src/shade_simple.cpp", "src/shade_lambert.cpp",
     "src/shade_path_test.cpp", "src/shade_common.cpp", "src/utils.cpp", "src/optimizer_simple.cpp",
     "common_src/scene_utils.cpp", "common_src/qmc.cpp", "common_src/Image2d.cpp", "common_src/cmesh.cpp",
-    "raytrace_src/raytrace3d_bf.cpp",
+    "raytrace_src/raytrace3d_bf.cpp", "src/scenes.cpp",
 ]
 HEADER_DIRS = ["src", "common_src", "raytrace_src"]
 

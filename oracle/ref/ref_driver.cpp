@@ -27,6 +27,7 @@
 #include "raytrace.h"
 #include "kvio.h"
 #include "ref_pointlight.h"
+#include "scenes.h"
 #include "oracle.h"
 #ifdef DRGB_WITH_GPU
 #include "gpu_drender.h"  // the GPU IDiffRender / IOptimizer (diffrender_tutorials_gb300/cpp)
@@ -198,6 +199,53 @@ static void dscene_out(kv::File& out, DScene& ds) {
     k++;
   }
   out.put_i32("n_dmeshes", {k});
+}
+
+// The coordinates the reference's derivative tests draw
+// (random_unique_indices, src/tests.cpp:512-541): `cnt` of [from, to) --
+// all of them when the range is no larger; else one candidate per stride
+// of (to - from) / min(4 cnt, to - from), offset by rand() % stride, then
+// std::random_shuffle and the first `cnt`.  It draws from the C library's
+// rand() exactly as the test binary does, so called in the tests' order
+// from a fresh process it returns the tests' own coordinates.
+static std::vector<int> test_coordinates(int from, int to, int cnt) {
+  std::vector<int> all;
+  if (cnt <= 0) return all;
+  if (to - from <= cnt) {
+    for (int i = from; i < to; i++) all.push_back(i);
+    return all;
+  }
+  const int stride = (to - from) / std::min(4 * cnt, to - from);
+  for (int i = from; i < to; i += stride) all.push_back(stride == 1 ? i : i + std::rand() % stride);
+  std::random_shuffle(all.begin(), all.end());
+  all.resize(cnt);
+  return all;
+}
+
+// A mesh with every attribute it has (a prepared scene's mesh after
+// restore_meshes), under `prefix`.
+static void mesh_out(kv::File& out, const std::string& b, const TriangleMesh& mesh) {
+  auto put3 = [&](const char* name, const std::vector<float3>& a) {
+    if (a.empty()) return;
+    std::vector<float> v;
+    for (auto& p : a) { v.push_back(p.x); v.push_back(p.y); v.push_back(p.z); }
+    out.put_f32(b + name, v);
+  };
+  put3("vertices", mesh.vertices);
+  put3("colors", mesh.colors);
+  put3("normals", mesh.normals);
+  put3("tangents", mesh.tangents);
+  if (!mesh.tc.empty()) {
+    std::vector<float> v;
+    for (auto& p : mesh.tc) { v.push_back(p.x); v.push_back(p.y); }
+    out.put_f32(b + "tc", v);
+  }
+  out.put_u32(b + "indices", std::vector<uint32_t>(mesh.indices.begin(), mesh.indices.end()));
+  if (!mesh.textures.empty()) {
+    const CPUTexture& t = mesh.textures[0];
+    out.put_f32(b + "tex", t.m_data);
+    out.put_i32(b + "tex_shape", {t.w, t.h, t.channels});
+  }
 }
 
 static void scene_out(kv::File& out, const std::string& prefix, const Scene& s) {
@@ -389,6 +437,45 @@ int main(int argc, char** argv) {
     out.put_f32("norm4", flat(m.vNorm4f.data(), 4 * m.vNorm4f.size()));
     out.put_f32("tc2", flat(m.vTexCoord2f.data(), 2 * m.vTexCoord2f.size()));
     out.put_u32("indices", std::vector<uint32_t>(m.indices.begin(), m.indices.end()));
+  } else if (task == 9) {
+    // The scenes and camera of the reference's derivative tests 1.1-1.5
+    // (src/tests.cpp:31-107): initial and target meshes as the tests build
+    // them from src/scenes.cpp, after their transforms and restore_meshes.
+    CamInfo camera;
+    camera.width = 256.0f;
+    camera.height = 256.0f;
+    camera.mWorldView = LiteMath::translate4x4(float3(0, 0, -3));
+    camera.mProj = LiteMath::perspectiveMatrix(45.0f, camera.width / camera.height, 0.1f, 100.0f);
+    camera.commit();
+    out.put_f32("cam.worldview", mat_to_vec(camera.mWorldView));
+    out.put_f32("cam.proj", mat_to_vec(camera.mProj));
+    for (int k = 1; k <= 5; k++) {
+      TriangleMesh initialMesh, targetMesh;
+      Scene initialScene, targetScene;
+      if (k == 1) scn03_Triangle3D_White(initialMesh, targetMesh);
+      if (k == 2 || k == 4) scn05_Pyramid3D(initialMesh, targetMesh);
+      if (k == 3 || k == 5) scn09_Sphere3D_Textured(initialMesh, targetMesh);
+      if (k == 3) transform(initialMesh, LiteMath::translate4x4(float3(0, +0.2f, 0.0f)));
+      initialScene.add_mesh(initialMesh);
+      targetScene.add_mesh(targetMesh);
+      if (k == 3) {
+        initialScene.restore_meshes(false, false, true);
+        targetScene.restore_meshes(false, false, true);
+      }
+      const std::string b = "t1" + std::to_string(k) + ".";
+      mesh_out(out, b + "initial.", initialScene.get_mesh(0));
+      mesh_out(out, b + "target.", targetScene.get_mesh(0));
+      // the vertices (at most 100) and texels (1.5: 250) the test checks,
+      // drawn in the order test_base_derivatives draws them
+      const TriangleMesh& m = initialScene.get_mesh(0);
+      const int max_v = k == 5 ? 0 : 100, max_t = k == 5 ? 250 : 0;
+      auto verts = test_coordinates(0, m.vertex_count(), max_v);
+      out.put_i32(b + "test_vertices", std::vector<int32_t>(verts.begin(), verts.end()));
+      if (max_t > 0 && !m.textures.empty()) {
+        auto texels = test_coordinates(0, m.textures[0].w * m.textures[0].h, max_t);
+        out.put_i32(b + "test_texels", std::vector<int32_t>(texels.begin(), texels.end()));
+      }
+    }
   } else {
     std::fprintf(stderr, "unknown task %d\n", task);
     return 2;

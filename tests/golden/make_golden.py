@@ -11,6 +11,7 @@ are all that the tests read.
     python tests/golden/make_golden.py              # all but the long runs
     python tests/golden/make_golden.py convergence  # 300-iteration optimiser runs
     python tests/golden/make_golden.py path_test    # the PATH_TEST mean image
+    python tests/golden/make_golden.py fd_scenes    # scenes of the reference's derivative tests
 """
 import math
 import os
@@ -94,6 +95,13 @@ def path_test():
     items = {"task": np.array([2], np.int32), "mode": np.array([7], np.int32), "spp": np.array([64], np.int32),
              "repeats": np.array([16], np.int32), **scene_items(sc), **cam_items([cam])}
     save("render_path_test", **items, **prefixed("out.", run(items)))
+
+
+def reference_fd_scenes():
+    """The scenes and camera of the reference's derivative tests 1.1-1.5
+    (src/tests.cpp:31-107), built by the reference's own src/scenes.cpp."""
+    build_ref.build(verbose=True)
+    save("fd_tests1_scenes", **prefixed("out.", run({"task": np.array([9], np.int32)})))
 
 
 def pyramid(seed=4):
@@ -320,6 +328,7 @@ def main():
     out = run(items)
     save("optimize_cube_vc", **items, **prefixed("out.", out))
     path_test()
+    reference_fd_scenes()
 
 
 def _moved(mesh, m):
@@ -389,5 +398,7 @@ if __name__ == "__main__":
         convergence()
     elif len(sys.argv) > 1 and sys.argv[1] == "path_test":
         path_test()
+    elif len(sys.argv) > 1 and sys.argv[1] == "fd_scenes":
+        reference_fd_scenes()
     else:
         main()
