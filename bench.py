@@ -330,7 +330,7 @@ def drgb_arm(args, w, ws, rank, local, pg):
     deterministic = {"value": args.steps / (sum(det_ms) / 1e3), "unit": "iters/s",
                      "ms_per_step": sum(det_ms) / args.steps, "phases_ms": det_prof,
                      "how": "DRGB_OPT_DETERMINISTIC: gradient records sorted by index, fixed-order sums "
-                            "(every ray traced, as in the batched engine)"}
+                            "(tiles and cells by the size rule, as in the batched engine)"}
 
     # the same iteration sampling silhouette edges only (DRGB_OPT_EDGE_SET = 1)
     r.set_option(N.OPT_EDGE_SET, 1)

@@ -75,6 +75,10 @@ int32_t batch_attach(drgb_batch* b, std::unique_ptr<drgb_renderer> r) {
   require(r && r->device == b->device, "job prepared for another device");
   const int32_t id = b->next_id++;
   if (b->bvh_rebuild >= 0) r->bvh_rebuild = b->bvh_rebuild;
+  if (b->raster >= 0) {
+    const int rc = drgb_renderer_set_option(r.get(), DRGB_OPT_PRIMARY_RASTER, b->raster);
+    if (rc != DRGB_OK) throw CudaError(t_err_message(), rc);
+  }
   b->jobs[id] = std::move(r);
   b->order.push_back(id);
   b->dirty = true;
@@ -152,6 +156,16 @@ int drgb_batch_set_option(drgb_batch* b, int option, int64_t value) {
       require(value >= 0 && value <= (1 << 30), "hierarchy rebuild period: 0 (never) or iterations");
       b->bvh_rebuild = (int)value;
       for (auto& kv : b->jobs) kv.second->bvh_rebuild = b->bvh_rebuild;
+    } else if (option == DRGB_OPT_PRIMARY_RASTER) {
+      require(value >= 0 && value <= 2, "camera and shadow rays: 0, 1 or 2 (see drgb_renderer_set_option)");
+      DRGB_CUDA(cudaSetDevice(b->device));
+      DRGB_CUDA(cudaStreamSynchronize(b->stream));
+      b->raster = (int)value;
+      for (auto& kv : b->jobs) {
+        const int rc = drgb_renderer_set_option(kv.second.get(), DRGB_OPT_PRIMARY_RASTER, b->raster);
+        if (rc != DRGB_OK) throw CudaError(t_err_message(), rc);
+      }
+      b->dirty = true;
     } else if (option == DRGB_OPT_DETERMINISTIC) {
       DRGB_CUDA(cudaSetDevice(b->device));
       DRGB_CUDA(cudaStreamSynchronize(b->stream));

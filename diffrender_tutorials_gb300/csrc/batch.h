@@ -30,6 +30,7 @@ struct drgb_batch {
   int use_graph = 1;
   int det = 0;      // deterministic gradient reduction for every job added
   int bvh_rebuild = -1;  // hierarchy rebuild period for every job (-1: the jobs' own)
+  int raster = -1;       // DRGB_OPT_PRIMARY_RASTER for every job (-1: the jobs' own)
   bool det_any = false;  // some job of the current set reduces deterministically
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;

@@ -605,7 +605,8 @@ int drgb_optimizer_autotune(drgb_renderer* r, int trial_iters, int32_t* chosen, 
     float best = 1e30f;
     // 0. camera samples and point-light shadow rays by the raster pass or by
     //    traversal (the raster pass has a fixed cost that small calls do not
-    //    recover)
+    //    recover); deterministic mode keeps the size rule, which the job
+    //    follows alone, in a batch and in the server alike
     if (J.raster == 1 && !J.det && !J.trace_bruteforce && !J.store_hits) {
       int pick = 1;
       for (int k : {0, 1}) {

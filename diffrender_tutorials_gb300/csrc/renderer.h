@@ -185,11 +185,13 @@ struct drgb_renderer {
   }
   void raster_buffers() {
     Job& J = job;
-    // deterministic mode promises the same bits alone, in a batch and in the
-    // server, whose kernels trace: it traces too (the raster pass and the
-    // traversal find the same hits except the reference caster's
-    // clamped-determinant ones, which each finds only by chance)
-    // small calls: the raster pass's fixed cost (about 15 launches) outweighs
+    // Deterministic mode: a job runs its own raster pass alone, in a batch and
+    // in the server, under the same size rule (the autotuner leaves the
+    // choice to the rule), so the hits and the bits agree.  A call whose
+    // lists overflow traces (and the lists grow for the next): traversal and
+    // raster pass find the same hits except the reference caster's
+    // clamped-determinant ones, which each finds only by chance.
+    // Small calls: the raster pass's fixed cost (about 15 launches) outweighs
     // what it saves; measured on GB300, a 12-triangle cube at 256x256 x 16 spp
     // and 5,120 triangles at 512x512 x 4 spp x 2 views break even (1-2 M
     // samples).  Dense meshes: binning costs per (view, triangle) and the
@@ -201,8 +203,7 @@ struct drgb_renderer {
     const size_t samples = (size_t)n_pixels() * J.S;
     const bool pays = J.raster == 2 ? true
                       : J.raster_pick >= 0 ? J.raster_pick == 1 : raster_pays(samples, J.n_views, J.n_tris);
-    const bool on = J.raster && pays && !J.trace_bruteforce && !J.store_hits && !J.det && J.n_tris > 0 &&
-                    J.n_views > 0;
+    const bool on = J.raster && pays && !J.trace_bruteforce && !J.store_hits && J.n_tris > 0 && J.n_views > 0;
     if (on) {
       J.vis[0].reserve(samples);
       J.vis[1].reserve(samples);

@@ -112,8 +112,10 @@ enum {
                                     for every call (no size rule, not switched off by the autotuner); 0
                                     every ray through the hierarchy.  Same hits either way except the reference caster's
                                     clamped-determinant hits, which each method finds only by chance.  Off
-                                    for the brute-force caster, stored adjoint hits and deterministic mode.
-                                    Costs 32 bytes per camera sample of the views */
+                                    for the brute-force caster and stored adjoint hits.  In deterministic
+                                    mode the autotuner leaves the choice to the size rule, so a job makes
+                                    it alike alone, in a batch and in the server.  Costs 32 bytes per
+                                    camera sample of the views (48 for the point-light model) */
 };
 
 /* Camera (CamInfo, common_src/camera.h:6-44).  Matrices in LiteMath memory
@@ -302,7 +304,8 @@ int drgb_batch_add_job(drgb_batch* b, int shading_model, int spp, const drgb_mod
                        const drgb_opt_params* p, int32_t* job_id);
 int drgb_batch_remove_job(drgb_batch* b, int32_t job_id);
 int drgb_batch_size(drgb_batch* b);
-/* DRGB_OPT_USE_GRAPH, or DRGB_OPT_DETERMINISTIC / DRGB_OPT_BVH_REBUILD for every job, present and future */
+/* DRGB_OPT_USE_GRAPH, or DRGB_OPT_DETERMINISTIC / DRGB_OPT_BVH_REBUILD / DRGB_OPT_PRIMARY_RASTER for
+ * every job, present and future */
 int drgb_batch_set_option(drgb_batch* b, int option, int64_t value);
 /* n_iters iterations of every job: enqueue only / enqueue and wait. */
 int drgb_batch_run_async(drgb_batch* b, int64_t n_iters);

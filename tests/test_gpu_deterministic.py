@@ -130,6 +130,40 @@ def test_deterministic_plain_batch_and_server_agree_bit_for_bit():
     srv.close()
 
 
+def test_deterministic_with_tiles_and_cells():
+    """Tiles and cells forced (DRGB_OPT_PRIMARY_RASTER = 2): the plain
+    optimiser twice and the batch give the same bits, as with traversal."""
+    iters = 4
+    runs = []
+    setups = []
+    for name, mode, spp, ts, isc, cams in problems():
+        st = D.DiffRenderSettings(D.SHADING_MODEL(mode), spp)
+        r0 = D.MakeDifferentialRenderer(st)
+        r0.commit(ts)
+        tgt = r0.render(ts, cams)
+        setups.append((isc, cams, tgt, st, opt_params(mode)))
+        out = []
+        for _ in range(2):
+            r = D.MakeDifferentialRenderer(st)
+            r.set_option(N.OPT_DETERMINISTIC, 1)
+            r.set_option(N.OPT_PRIMARY_RASTER, 2)
+            opt = D.CreateSimpleOptimizer()
+            opt.Init(isc, r, cams, tgt, opt_params(mode))
+            opt.Run(iters)
+            out.append((np.array(opt.losses), opt.current_scene()))
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1].meshes[0].vertices, out[1][1].meshes[0].vertices)
+        runs.append(out[0])
+    b = D.BatchOptimizer()
+    b.set_option(N.OPT_DETERMINISTIC, 1)
+    b.set_option(N.OPT_PRIMARY_RASTER, 2)
+    ids = [b.add_job(*s) for s in setups]
+    b.run(iters)
+    for (losses, scene), jid in zip(runs, ids):
+        assert np.array_equal(b.losses(jid), losses)
+        assert np.array_equal(b.job_scene(jid).meshes[0].vertices, scene.meshes[0].vertices)
+
+
 def test_hierarchy_rebuilds_leave_the_trajectory_unchanged():
     """DRGB_OPT_BVH_REBUILD: a new topology every 2 iterations (plain and
     batched) gives the same losses as refitting one topology throughout and
