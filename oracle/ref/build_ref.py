@@ -19,7 +19,7 @@ Test infrastructure only.  Recipe:
 The reference's CMake build, Embree (missing binary) and Mitsuba (not
 installed) are not used.  Where the reference tree is absent, the patched copy under oracle/_ref/src
 (made earlier and shipped with the working tree) is compiled instead, so that
-the driver can be rebuilt on a machine of another architecture.
+ref_driver can be rebuilt on a machine of another architecture.
 """
 import os
 import platform
@@ -133,7 +133,7 @@ def _stale(exe, deps):
 
 
 def _oracle_object():
-    """oracle.c compiled for the driver (its TransformR Jacobian)."""
+    """oracle.c compiled for ref_driver (its TransformR Jacobian)."""
     src, hdr = os.path.join(ORACLE, "oracle.c"), os.path.join(ORACLE, "oracle.h")
     obj = os.path.join(BIN, "oracle.o")
     if _stale(obj, [src, hdr, __file__]):
@@ -144,7 +144,7 @@ def _oracle_object():
 
 
 def build(verbose=False):
-    """oracle/_ref/<arch>/ref_driver: the reference's CPU path behind the driver."""
+    """oracle/_ref/<arch>/ref_driver: the reference's CPU path behind ref_driver.cpp."""
     src_root = _source_tree(verbose)
     if src_root is None:
         return None

@@ -1,7 +1,7 @@
 """Inputs for the reference driver (oracle/ref/ref_driver.cpp) and a runner.
 
-Test infrastructure only.  Scenes and cameras are written in the driver's
-DRKV format (oracle/ref/kvio.py); `run` executes a driver binary built by
+Test infrastructure only.  Scenes and cameras are written in ref_driver's
+DRKV format (oracle/ref/kvio.py); `run` executes a ref_driver binary built by
 oracle/ref/build_ref.py and returns its outputs.
 """
 import os

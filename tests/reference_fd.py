@@ -4,7 +4,7 @@ src/tests.cpp:31-107 (test_base_derivatives), :491-637 (finDiff_param,
 test_fin_diff, test_derivatives) and :681-760 (PrintAndCompareGradients):
 
   * scenes and camera: the fixture `fd_tests1_scenes`, written by the
-    reference's own src/scenes.cpp through the driver (scn03 triangle,
+    reference's own src/scenes.cpp through ref_driver (scn03 triangle,
     scn05 pyramid, scn09 textured sphere; camera at z = 3, 45 degrees,
     256 x 256), 16 samples per pixel;
   * gradient: d_render of the initial scene with the adjoint 2(I - T) and
@@ -15,7 +15,7 @@ test_fin_diff, test_derivatives) and :681-760 (PrintAndCompareGradients):
   * coordinates: the test binary's own -- every vertex of meshes with at
     most 100; for the sphere of 1.3, 100 of its vertices, and for 1.5, 250
     texels with all channels, as the binary draws them from the C library's
-    rand() (recorded in the fixture by the driver);
+    rand() (recorded in the fixture by ref_driver);
   * error: sum |g - fd| / sum (|g| + |fd|) over the tested coordinates of a
     block; pass below 0.5 (positions, colours) and 0.01 (texture).
 

@@ -148,7 +148,7 @@ def test_restricted_transforms_behind_reference_interface():
 
 def test_adapter_builds_against_reference_headers():
     """CPU check: the adapter compiles with the reference's headers and links
-    to libdrgb (the driver is not run without a GPU)."""
+    to libdrgb (ref_driver_gpu is not run without a GPU)."""
     exe = build_ref.build_gpu_driver()
     if exe is None:
         pytest.skip("reference sources absent")
