@@ -38,7 +38,10 @@
 namespace drgb {
 
 constexpr float RA_MARGIN = 0.125f;  // pixels around the projected triangle
-constexpr int RA_THREADS = 256;
+#ifndef DRGB_RA_THREADS
+#define DRGB_RA_THREADS 256
+#endif
+constexpr int RA_THREADS = DRGB_RA_THREADS;  // threads of a resolve block, samples of a tile
 constexpr int RA_STAGE = 64;         // triangles staged in shared memory at a time
 
 struct RaTri {
