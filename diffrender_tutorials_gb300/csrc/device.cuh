@@ -193,6 +193,7 @@ struct JobDev {
   int queue_cap;
   int edge_samples;
   const float* rnd;         // 2 * edge_samples replayed random numbers
+  const int* rnd_order;     // sample indices by increasing first random number (may be null)
   int edge_exact;           // 1: full 2x3 screen Jacobian through the instance's own transform
   uint32_t edge_key_base;   // first queue-sort key of this job in a batch
   // optional work counters (rays, box tests, triangle tests, footprint tests); null normally

@@ -375,9 +375,13 @@ __global__ void __launch_bounds__(CDF_THREADS) k_edge_cdf(const JobDev* jobs, in
   edge_cdf_body(jobs[job], blockIdx.x, sbuf);
 }
 
+// Samples are taken in rnd_order when the job has it (consecutive entries
+// then fall on the same or neighbouring edges, the order the shading pass
+// wants) and in index order otherwise.
 __global__ void k_edge_select(const JobDev* jobs, int job) {
   const JobDev& J = jobs[job];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = J.rnd_order && j < J.edge_samples ? __ldg(J.rnd_order + j) : j;
   const int view = blockIdx.y;
   int edge_id;
   const bool keep = edge_select_test(J, view, i, edge_id);
@@ -522,7 +526,8 @@ __global__ void k_b_edge_select(const JobDev* jobs, const Seg* segs, int nseg, i
 // with -DDRGB_EDGE_NO_SORT shade in queue order.)
 static const int* sort_queue(const JobDev* d_jobs, int job, const Job& J, int grid, cudaStream_t s) {
 #ifndef DRGB_EDGE_NO_SORT
-  if (!J.qkey[0].p || J.n_edges <= 0) return nullptr;
+  // samples selected in rnd_order are already grouped by edge within a view
+  if (!J.qkey[0].p || J.n_edges <= 0 || J.dev.rnd_order) return nullptr;
   k_queue_keys<<<std::max(1, grid), 256, 0, s>>>(d_jobs, job, J.qkey[0].p, J.qidx[0].p, J.qn.p);
   count_launch();
   uint64_t top = (uint64_t)J.n_views * (uint64_t)J.n_edges;

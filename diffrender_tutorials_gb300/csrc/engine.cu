@@ -592,6 +592,27 @@ const float* edge_random_table(int n, cudaStream_t s) {
   return buf->p;
 }
 
+const int* edge_random_order(int n, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, DevBuf<int>*> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, n});
+  if (it != cache.end()) return it->second->p;
+  std::vector<float> h;
+  edge_random_host(n, h);
+  std::vector<int> order(std::max(n, 1));
+  for (int i = 0; i < (int)order.size(); i++) order[i] = i;
+  if (n > 0)
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h[2 * (size_t)a] < h[2 * (size_t)b]; });
+  auto* buf = new DevBuf<int>();
+  buf->upload(order.data(), order.size(), s);
+  DRGB_CUDA(cudaStreamSynchronize(s));
+  cache[{dev, n}] = buf;  // lives until process exit; shared by every renderer
+  return buf->p;
+}
+
 void init_job_model(Job& J, int mode, int spp) {
   J.mode = mode;
   J.spp = spp;

@@ -362,6 +362,10 @@ constexpr int kSortGrid = 512;  // blocks of sort_pairs_device (its histogram ha
 
 // edge random table shared by every job with the same sample count
 const float* edge_random_table(int n, cudaStream_t s);
+// The sample indices of that table ordered by their first number (the edge
+// choice): selected in this order, consecutive samples fall on the same or
+// neighbouring edges of the CDF.  Cached like the table.
+const int* edge_random_order(int n, cudaStream_t s);
 // The same 2n replayed random numbers in a host vector.
 void edge_random_host(int n, std::vector<float>& out);
 

@@ -162,6 +162,7 @@ struct drgb_renderer {
 #endif
     J.dev.edge_samples = edge_samples;
     J.dev.rnd = edge_samples > 0 ? edge_random_table(edge_samples, stream) : nullptr;
+    J.dev.rnd_order = edge_samples > 0 ? edge_random_order(edge_samples, stream) : nullptr;
     if (J.det) det_buffers(J, stream);
     if (J.store_hits) hit_buffers();
     raster_buffers();
@@ -352,6 +353,7 @@ struct drgb_renderer {
     job.dev.item_count = keep.item_count;
     job.dev.edge_samples = keep.edge_samples;
     job.dev.rnd = keep.rnd;
+    job.dev.rnd_order = keep.rnd_order;
     d_job.alloc(1);
     DRGB_CUDA(cudaMemcpyAsync(d_job.p, &job.dev, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
   }
