@@ -127,3 +127,40 @@ def test_path_test_optimizer_follows_the_oracle(scene):
     print("losses", got[[0, 5, 10, 19]], "oracle", ref[[0, 5, 10, 19]])
     assert np.allclose(got, ref, rtol=2e-2), np.abs(got / ref - 1).max()
     assert got[-1] < 0.1 * got[0]
+
+
+def test_path_test_in_a_batch_gives_the_plain_bits(scene):
+    """Deterministic mode: a PATH_TEST job alone and batched beside a
+    vertex-colour job (the batch's flattening writes its tangents, its
+    group runs the PATH_TEST pixel kernel and the generic edge shader)
+    gives the same losses and texture, bit for bit."""
+    _, sc, cams = scene
+    spp, iters = 16, 3
+    tgt = O.render(sc, cams, O.PATH_TEST, spp, mp=O.model_params(seed=11))
+    init = sc.copy()
+    init.meshes[0].textures[0].data[:] = np.float32(0.5)
+    p = D.OptimizerParameters(D.OptimizerParameters.GD_Adam, pos_lr=0.001, tex_lr=0.05)
+    st = D.DiffRenderSettings(D.SHADING_MODEL.PATH_TEST, spp)
+    mp = D.ModelParams(seed=11)
+    r = renderer(spp, 11)
+    r.set_option(N.OPT_DETERMINISTIC, 1)
+    opt = D.CreateSimpleOptimizer()
+    opt.Init(init, r, cams, tgt, p)
+    opt.Run(iters)
+    cube = D.make_cube(seed=1)
+    cs = D.Scene()
+    cs.add_mesh(cube)
+    vc = D.DiffRenderSettings(D.SHADING_MODEL.VERTEX_COLOR, 4)
+    rc = D.MakeDifferentialRenderer(vc)
+    rc.commit(cs)
+    ctgt = rc.render(cs, cams)
+    b = D.BatchOptimizer()
+    b.set_option(N.OPT_DETERMINISTIC, 1)
+    b.add_job(cs, cams, ctgt, vc, D.OptimizerParameters(D.OptimizerParameters.GD_Adam))
+    jid = b.add_job(init, cams, tgt, st, p, model_params=mp)
+    b.run(iters)
+    assert np.array_equal(b.losses(jid), np.asarray(opt.losses, np.float32))
+    got = b.job_scene(jid).meshes[0]
+    ref = opt.current_scene().meshes[0]
+    assert np.array_equal(got.textures[0].data, ref.textures[0].data)
+    assert np.array_equal(got.vertices, ref.vertices)
