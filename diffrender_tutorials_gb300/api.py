@@ -103,8 +103,45 @@ def _read_scene(template: Scene, get_mesh, get_restricted) -> Scene:
     return s
 
 
+_CAMERA_CACHE = {}  # camera parameters -> drgb_camera (the library's matrices)
+
+
+def _camera_key(cam: CamInfo, exact: bool = False):
+    """The parameters of a camera as a dictionary key: as given when they are
+    hashable (tuples of numbers), else converted to floats and bytes.  Equal
+    keys give equal cameras; one camera may have two keys."""
+    if cam.world_view is not None:
+        return (np.asarray(cam.world_view, np.float32).tobytes(), np.asarray(cam.proj, np.float32).tobytes(),
+                float(cam.width), float(cam.height))
+    if not exact:
+        return (cam.origin, cam.target, cam.up, cam.width, cam.height, cam.fov_rad, cam.znear, cam.zfar)
+    return (tuple(float(x) for x in cam.origin), tuple(float(x) for x in cam.target), tuple(float(x) for x in cam.up),
+            float(cam.width), float(cam.height), float(cam.fov_rad), float(cam.znear), float(cam.zfar))
+
+
+def _cached_camera(cam: CamInfo):
+    key = _camera_key(cam)
+    try:
+        return key, _CAMERA_CACHE.get(key)
+    except TypeError:  # arrays or lists among the parameters
+        key = _camera_key(cam, exact=True)
+        return key, _CAMERA_CACHE.get(key)
+
+
 def make_camera(cam: CamInfo) -> N.Camera:
-    """drgb_camera of a CamInfo (matrices computed by the library)."""
+    """drgb_camera of a CamInfo (matrices computed by the library; a camera
+    seen before is taken from a cache keyed by its parameters)."""
+    key, hit = _cached_camera(cam)
+    if hit is not None:
+        return N.Camera.from_buffer_copy(hit)
+    c = _make_camera(cam)
+    if len(_CAMERA_CACHE) >= 4096:
+        _CAMERA_CACHE.clear()
+    _CAMERA_CACHE[key] = N.Camera.from_buffer_copy(c)
+    return c
+
+
+def _make_camera(cam: CamInfo) -> N.Camera:
     c = N.Camera()
     if cam.world_view is not None:
         c.world_view[:] = [float(x) for x in np.asarray(cam.world_view, np.float32).reshape(16)]
@@ -122,7 +159,8 @@ def make_camera(cam: CamInfo) -> N.Camera:
 def make_cameras(cams: Sequence[CamInfo]):
     arr = (N.Camera * len(cams))()
     for i, c in enumerate(cams):
-        arr[i] = make_camera(c)
+        hit = _cached_camera(c)[1]
+        arr[i] = hit if hit is not None else make_camera(c)
     return arr
 
 

@@ -22,7 +22,7 @@ int64_t job_device_bytes(const Job& J) {
   int64_t b = 0;
   for (const MeshState& M : J.meshes)
     b += M.vertices.bytes() + M.colors.bytes() + M.tc.bytes() + M.normals.bytes() + M.tangents.bytes() +
-         M.transforms.bytes() + M.texture.bytes() + M.indices.bytes();
+         M.transforms.bytes() + M.texture.bytes() + M.rparams.bytes();
   b += J.pos.bytes() + J.orig.bytes() + J.col.bytes() + J.nrm.bytes() + J.tan.bytes() + J.tc.bytes() + J.tri_v.bytes() +
        J.blocks.bytes() + J.meshdev.bytes() + J.block_tr.bytes() + J.vblock.bytes() + J.src_tab.bytes() +
        J.tr_tab.bytes() + J.tr_inv0.bytes();

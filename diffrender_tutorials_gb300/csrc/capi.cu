@@ -207,6 +207,22 @@ int drgb_renderer_set_model_params(drgb_renderer* r, const drgb_model_params* p)
   });
 }
 
+// Whether a cudaMemcpyAsync from host pointer p may read p after it returns:
+// page-locked (and device) memory is read by the copy engine in stream
+// order, pageable memory is staged before the call returns.
+static bool read_after_return(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return true;
+  }
+  return a.type != cudaMemoryTypeUnregistered;
+}
+
+// Returns once the caller's arrays have been read: at once for pageable
+// memory (the flattening and refit run on in stream order, ahead of the next
+// call's work), after the stream has drained when an array is page-locked.
 int drgb_commit(drgb_renderer* r, const drgb_scene_desc* scene) {
   return guard([&] {
     check_renderer(r);
@@ -215,9 +231,17 @@ int drgb_commit(drgb_renderer* r, const drgb_scene_desc* scene) {
     upload_scene(J, scene, r->stream);
     J.opt.active = false;
     r->graph_valid = false;
-    set_dscene(J, nullptr, 0);
+    set_dscene(J, nullptr, 0, r->stream);
     commit_scene(J, r->stream);
-    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+    bool wait = false;
+    for (int m = 0; m < scene->n_meshes && !wait; m++) {
+      const drgb_mesh_desc& d = scene->meshes[m];
+      for (const void* p : {(const void*)d.vertices, (const void*)d.colors, (const void*)d.tc,
+                            (const void*)d.normals, (const void*)d.tangents, (const void*)d.indices,
+                            (const void*)d.restricted, (const void*)d.texture})
+        wait = wait || read_after_return(p);
+    }
+    if (wait) DRGB_CUDA(cudaStreamSynchronize(r->stream));
   });
 }
 
@@ -267,7 +291,7 @@ int drgb_d_render(drgb_renderer* r, const drgb_camera* cams, const float* adjoin
     r->set_device();
     Job& J = r->job;
     r->views(cams, n_views, true);
-    set_dscene(J, ids, n_ids);
+    set_dscene(J, ids, n_ids, r->stream);
     r->gradient_buffers(edge_samples_in_total);
     const size_t npix = (size_t)n_views * J.W * J.H;
     J.adj_in.reserve(3 * npix);
@@ -298,7 +322,7 @@ static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams,
   r->set_device();
   Job& J = r->job;
   r->views(cams, n_views, true);
-  set_dscene(J, ids, n_ids);
+  set_dscene(J, ids, n_ids, r->stream);
   r->gradient_buffers(edge_samples);
   const size_t npix = (size_t)n_views * J.W * J.H;
   const cudaMemcpyKind h2d = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -307,11 +331,7 @@ static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams,
   if (device_ptrs) DRGB_CUDA(cudaMemcpyAsync(J.targets.p, targets, sizeof(float) * 3 * npix, h2d, r->stream));
   else r->upload_inputs(J.targets.p, targets, sizeof(float) * 3 * npix);
   if (out_images) J.images.reserve(3 * npix);
-  r->push_dev();
-  // images are only written when requested
-  JobDev d = J.dev;
-  if (!out_images) d.images = nullptr;
-  DRGB_CUDA(cudaMemcpyAsync(r->d_job.p, &d, sizeof(JobDev), cudaMemcpyHostToDevice, r->stream));
+  r->push_dev(out_images != nullptr);  // images are only written when requested
   r->enqueue_iteration(out_images != nullptr);
   if (r->pixels_wait) {  // a pass without pixel kernel (no views) still orders the copy
     DRGB_CUDA(cudaStreamWaitEvent(r->stream, r->pixels_wait, 0));
@@ -320,9 +340,12 @@ static void d_render_and_compare_impl(drgb_renderer* r, const drgb_camera* cams,
   if (J.grad_total > 0) DRGB_CUDA(cudaMemcpyAsync(dscene, J.grad.p, sizeof(float) * J.grad_total, d2h, r->stream));
   if (out_images)
     DRGB_CUDA(cudaMemcpyAsync(out_images, J.images.p, sizeof(float) * 3 * npix, d2h, r->stream));
-  if (loss) DRGB_CUDA(cudaMemcpyAsync(loss, J.loss_out.p, sizeof(float), d2h, r->stream));
-  if (!device_ptrs) r->check_flags();
-  else DRGB_CUDA(cudaStreamSynchronize(r->stream));  // the JobDev staging copy above reads host memory
+  if (device_ptrs) {
+    if (loss) DRGB_CUDA(cudaMemcpyAsync(loss, J.loss_out.p, sizeof(float), d2h, r->stream));
+    DRGB_CUDA(cudaStreamSynchronize(r->stream));
+  } else {
+    r->check_flags(loss);  // the loss comes back with the status words, in the call's one wait
+  }
 }
 
 int drgb_d_render_and_compare(drgb_renderer* r, const drgb_camera* cams, const float* targets, int n_views,
@@ -395,7 +418,7 @@ int drgb_optimizer_init(drgb_renderer* r, const drgb_scene_desc* scene, const dr
     r->set_device();
     Job& J = r->job;
     upload_scene(J, scene, r->stream);
-    set_dscene(J, p->dmesh_ids, p->n_dmesh_ids);
+    set_dscene(J, p->dmesh_ids, p->n_dmesh_ids, r->stream);
     commit_scene(J, r->stream);
     r->views(cams, n_views, true);
     const size_t npix = (size_t)n_views * J.W * J.H;

@@ -136,9 +136,31 @@ static void hammersley(int n, float* out) {
 void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   if (!scene || scene->n_meshes < 0 || (scene->n_meshes > 0 && !scene->meshes))
     throw CudaError("scene descriptor is null or malformed", DRGB_ERR_INVALID);
-  rebuild_bvh_discard(J);  // a host build in progress reads the triangle lists replaced here
   const int nm = scene->n_meshes;
-  J.meshes.clear();
+  // every mesh is checked before anything of the committed scene changes
+  for (int m = 0; m < nm; m++) {
+    const drgb_mesh_desc& d = scene->meshes[m];
+    if (d.n_vertices < 0 || d.n_indices < 0 || d.n_indices % 3 != 0 || (d.n_vertices > 0 && !d.vertices) ||
+        (d.n_indices > 0 && !d.indices))
+      throw CudaError("mesh " + std::to_string(m) + ": bad vertex/index arrays", DRGB_ERR_INVALID);
+    if (d.n_instances > 1 && !d.transforms && !d.restricted)
+      throw CudaError("mesh " + std::to_string(m) + ": several instances need transforms", DRGB_ERR_INVALID);
+    for (int i = 0; i < d.n_indices; i++)
+      if (d.indices[i] >= (uint32_t)d.n_vertices)
+        throw CudaError("mesh " + std::to_string(m) + ": index out of range", DRGB_ERR_INVALID);
+    const bool tex = d.texture && d.tex_w > 0 && d.tex_h > 0;
+    if (tex && d.tex_channels != 3) throw CudaError("textures must have 3 channels", DRGB_ERR_INVALID);
+    if (model_has_tex(J.mode) && !tex)
+      throw CudaError("mesh " + std::to_string(m) + ": the shading model needs a texture", DRGB_ERR_INVALID);
+    if (model_has_tex(J.mode) && !d.tc)
+      throw CudaError("mesh " + std::to_string(m) + ": the shading model needs texture coordinates", DRGB_ERR_INVALID);
+  }
+  rebuild_bvh_discard(J);  // a host build in progress reads the triangle lists replaced here
+  // The meshes' device buffers are kept from the last commit and reused where
+  // the sizes agree: a commit of the same meshes (the reference commits the
+  // scene on every d_render_and_compare, drender.h:176) frees and allocates
+  // nothing (cudaFree waits for the whole device).  Uploads are ordered on
+  // the renderer's stream behind any work that still reads them.
   J.meshes.resize(nm);
   J.h_blocks.clear();
   std::vector<int> vblock;
@@ -147,15 +169,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   for (int m = 0; m < nm; m++) {
     const drgb_mesh_desc& d = scene->meshes[m];
     MeshState& M = J.meshes[m];
-    if (d.n_vertices < 0 || d.n_indices < 0 || d.n_indices % 3 != 0 || (d.n_vertices > 0 && !d.vertices) ||
-        (d.n_indices > 0 && !d.indices))
-      throw CudaError("mesh " + std::to_string(m) + ": bad vertex/index arrays", DRGB_ERR_INVALID);
     const int ninst = d.n_instances <= 0 ? 1 : d.n_instances;
-    if (d.n_instances > 1 && !d.transforms && !d.restricted)
-      throw CudaError("mesh " + std::to_string(m) + ": several instances need transforms", DRGB_ERR_INVALID);
-    for (int i = 0; i < d.n_indices; i++)
-      if (d.indices[i] >= (uint32_t)d.n_vertices)
-        throw CudaError("mesh " + std::to_string(m) + ": index out of range", DRGB_ERR_INVALID);
     M.nv = d.n_vertices;
     M.ni = d.n_indices;
     M.n_inst = ninst;
@@ -165,11 +179,14 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     M.has_normals = d.normals != nullptr;
     M.has_tangents = d.tangents != nullptr;
     if (M.has_colors) M.colors.upload(d.colors, 3 * (size_t)d.n_vertices, s);
+    else M.colors.reset();
     if (M.has_tc) M.tc.upload(d.tc, 2 * (size_t)d.n_vertices, s);
+    else M.tc.reset();
     if (M.has_normals) M.normals.upload(d.normals, 3 * (size_t)d.n_vertices, s);
+    else M.normals.reset();
     if (M.has_tangents) M.tangents.upload(d.tangents, 3 * (size_t)d.n_vertices, s);
-    M.h_indices.assign(d.indices, d.indices + d.n_indices);
-    M.indices.upload(d.indices, d.n_indices, s);
+    else M.tangents.reset();
+    M.h_indices.assign(d.indices, d.indices + d.n_indices);  // the triangles reach the device as tri_v
     std::vector<float> tr(16 * (size_t)ninst, 0.0f);
     M.restricted = d.restricted != nullptr;
     if (M.restricted) {
@@ -184,7 +201,6 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     M.h_transforms = tr;
     M.transforms.upload(tr.data(), tr.size(), s);
     if (d.texture && d.tex_w > 0 && d.tex_h > 0) {
-      if (d.tex_channels != 3) throw CudaError("textures must have 3 channels", DRGB_ERR_INVALID);
       M.tex_w = d.tex_w;
       M.tex_h = d.tex_h;
       M.tex_c = d.tex_channels;
@@ -193,10 +209,6 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
       M.tex_w = M.tex_h = M.tex_c = 0;
       M.texture.reset();
     }
-    if (model_has_tex(J.mode) && !M.texture.p)
-      throw CudaError("mesh " + std::to_string(m) + ": the shading model needs a texture", DRGB_ERR_INVALID);
-    if (model_has_tex(J.mode) && !M.has_tc)
-      throw CudaError("mesh " + std::to_string(m) + ": the shading model needs texture coordinates", DRGB_ERR_INVALID);
     for (int j = 0; j < ninst; j++) {
       const int b = (int)J.h_blocks.size();
       J.h_blocks.push_back(BlockDev{voff, toff, m, j});
@@ -211,13 +223,13 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   J.n_vertices = voff;
   J.n_tris = toff;
   J.n_blocks = (int)J.h_blocks.size();
-  J.blocks.upload(J.h_blocks.data(), J.h_blocks.size(), s);
-  J.vblock.upload(vblock.data(), vblock.size(), s);
-  J.tri_v.upload(tri_v.data(), tri_v.size(), s);
+  upload_changed(J.blocks, J.up_blocks, J.h_blocks.data(), J.h_blocks.size(), s);
+  upload_changed(J.vblock, J.up_vblock, vblock.data(), vblock.size(), s);
   // the same triangles (global vertex ids and blocks) keep the edge list
   const bool same_topology = tri_v.size() == J.h_tri_v.size() &&
                              (tri_v.empty() || std::memcmp(tri_v.data(), J.h_tri_v.data(),
                                                            sizeof(int4) * tri_v.size()) == 0);
+  if (!same_topology || !J.tri_v.p || J.tri_v.n != tri_v.size()) J.tri_v.upload(tri_v.data(), tri_v.size(), s);
   J.h_tri_v.swap(tri_v);  // kept for the hierarchy builders and their topology cache
   std::vector<MeshSrc> src(nm);
   std::vector<const float*> trs(nm);
@@ -227,8 +239,8 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
                      M.has_tc ? M.tc.p : nullptr, M.has_tangents ? M.tangents.p : nullptr};
     trs[m] = M.transforms.p;
   }
-  J.src_tab.upload(src.data(), src.size(), s);
-  J.tr_tab.upload(trs.data(), trs.size(), s);
+  upload_changed(J.src_tab, J.up_src_tab, src.data(), src.size(), s);
+  upload_changed(J.tr_tab, J.up_tr_tab, trs.data(), trs.size(), s);
   const size_t nv = std::max(1, J.n_vertices);
   J.pos.alloc(nv);
   J.orig.alloc(nv);
@@ -252,7 +264,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
       else tr[16 * j] = tr[16 * j + 5] = tr[16 * j + 10] = tr[16 * j + 15] = 1.0f;
       mat_inverse44(&tr[16 * j], &inv[16 * j]);
     }
-    J.tr_inv0.upload(inv.data(), inv.size(), s);
+    upload_changed(J.tr_inv0, J.up_tr_inv0, inv.data(), inv.size(), s);
   }
   if (!same_topology) {
     J.edge_ids_key.clear();
@@ -389,11 +401,11 @@ int first_block(const Job& J, int mesh) {
   return 0;
 }
 
-void set_dscene(Job& J, const int32_t* ids, int n_ids) {
+void set_dscene(Job& J, const int32_t* ids, int n_ids, cudaStream_t s) {
   J.grad_total = compute_layout(J, ids, n_ids, J.dlay, &J.grad_alloc);
   J.dmesh_ids.assign(ids, ids + n_ids);
   J.grad.reserve(std::max<int64_t>(1, J.grad_alloc));
-  std::vector<MeshDev> md(J.meshes.size());
+  std::vector<MeshDev> md(J.meshes.size(), MeshDev{});
   for (size_t m = 0; m < J.meshes.size(); m++) {
     const MeshState& M = J.meshes[m];
     MeshDev& d = md[m];
@@ -420,8 +432,14 @@ void set_dscene(Job& J, const int32_t* ids, int n_ids) {
     d.tex_off = L.tex_off;
     d.tr_off = L.tr_off;
   }
-  J.meshdev.upload(md.data(), md.size(), 0);
-  DRGB_CUDA(cudaStreamSynchronize(0));
+  // the table changes when the meshes or the differentiated set do: repeated
+  // calls on one scene upload nothing; an upload is ordered on the stream
+  // behind the work that still reads the previous table
+  if (J.meshdev.p && J.meshdev.n == md.size() && J.h_meshdev.size() == md.size() &&
+      std::memcmp(J.h_meshdev.data(), md.data(), sizeof(MeshDev) * md.size()) == 0)
+    return;
+  J.meshdev.upload(md.data(), md.size(), s);
+  J.h_meshdev = md;
 }
 
 // Pixel tile of one warp: at most 32 samples (one pixel when a pixel has

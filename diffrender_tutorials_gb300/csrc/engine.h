@@ -71,6 +71,16 @@ struct DevBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// Uploads count values from h unless the device buffer holds exactly them
+// already (`last`: the host copy of its previous upload); a commit of an
+// unchanged scene copies none of the tables derived from it.
+template <class T>
+void upload_changed(DevBuf<T>& d, std::vector<T>& last, const T* h, size_t count, cudaStream_t s) {
+  if (d.p && d.n == count && last.size() == count && std::memcmp(last.data(), h, sizeof(T) * count) == 0) return;
+  d.upload(h, count, s);
+  last.assign(h, h + count);
+}
+
 // Page-locked host buffer: copies to and from it run asynchronously.
 template <class T>
 struct HostBuf {
@@ -132,7 +142,6 @@ struct MeshState {
   bool restricted = false;  // TransformR instances: rparams drive transforms
   DevBuf<float> vertices, colors, tc, normals, tangents, transforms, texture, rparams;
   std::vector<float> h_transforms;  // instance matrices as committed (column major)
-  DevBuf<uint32_t> indices;
   int tex_w = 0, tex_h = 0, tex_c = 0;
   bool has_colors = false, has_tc = false, has_normals = false, has_tangents = false;
   std::vector<uint32_t> h_indices;
@@ -184,11 +193,18 @@ struct Job {
   DevBuf<int4> tri_v;
   DevBuf<BlockDev> blocks;
   DevBuf<MeshDev> meshdev;
+  std::vector<MeshDev> h_meshdev;  // the table as last uploaded
   DevBuf<float> block_tr;  // 32 floats per block: transform, inverse-transpose
   DevBuf<int> vblock;      // block of each flattened vertex
   DevBuf<MeshSrc> src_tab;
   DevBuf<const float*> tr_tab;
   DevBuf<float> tr_inv0;   // inverse transforms of mesh 0 at the first commit
+  // host copies of the tables above as last uploaded (upload_changed)
+  std::vector<BlockDev> up_blocks;
+  std::vector<int> up_vblock;
+  std::vector<MeshSrc> up_src_tab;
+  std::vector<const float*> up_tr_tab;
+  std::vector<float> up_tr_inv0;
   // BVH
   DevBuf<float4> nodes, tri;
   DevBuf<float4> nodes4;   // 4-wide view of the binary hierarchy, refreshed after each refit
@@ -275,7 +291,7 @@ void build_bvh(Job& J, cudaStream_t s);                // topology (Morton, sort
 void refit_bvh(Job& J, cudaStream_t s);
 void setup_views(Job& J, const drgb_camera* cams, int n_views);
 void sync_dev(Job& J);
-void set_dscene(Job& J, const int32_t* ids, int n_ids);
+void set_dscene(Job& J, const int32_t* ids, int n_ids, cudaStream_t s);
 void build_edges(Job& J);
 // Flattened block of instance 0 of a mesh (its instances' blocks follow).
 int first_block(const Job& J, int mesh);

@@ -2,6 +2,7 @@
 // shared by the C-ABI translation units.
 #pragma once
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -69,6 +70,10 @@ struct drgb_renderer {
   cudaEvent_t ev_xfer_fork = nullptr, ev_xfer = nullptr;
   cudaEvent_t pixels_wait = nullptr;
   int px_resident = 0;  // pixel blocks per SM of the current model (0: not queried)
+  // Page-locked words a call reads back at its end in one wait: the kernels'
+  // error flags, the tile lists' state, the light cells' overflow flag and
+  // the loss.
+  HostBuf<uint32_t> h_status;
 
   ~drgb_renderer() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -271,28 +276,22 @@ struct drgb_renderer {
     return PX_VIS;
   }
 
-  // After a synchronised call: lists that did not fit double their room for
-  // the next call (that call traced its camera rays instead).
-  void raster_grow() {
+  // After a synchronised call: lists that did not fit (state bit 0 of the
+  // tile lists, the light cells' overflow flag, as check_flags read them
+  // back) double their room for the next call (that call traced instead).
+  void raster_grow(uint32_t tiles_state, uint32_t cells_overflow) {
     Job& J = job;
-    if (!J.raster_on || !J.ra_state.p) return;
-    uint32_t st = 0;
-    DRGB_CUDA(cudaMemcpy(&st, J.ra_state.p, sizeof(st), cudaMemcpyDeviceToHost));
-    if (st & 1u) {
+    if (tiles_state & 1u) {
       J.ra_list.alloc(2 * J.ra_list.n);
-      DRGB_CUDA(cudaMemset(J.ra_state.p, 0, sizeof(uint32_t)));
+      DRGB_CUDA(cudaMemsetAsync(J.ra_state.p, 0, sizeof(uint32_t), stream));
       graph_valid = false;
       push_dev();
     }
-    if (J.shadow_on && J.sh_grid.p) {
-      LightGrid g;
-      DRGB_CUDA(cudaMemcpy(&g, J.sh_grid.p, sizeof(g), cudaMemcpyDeviceToHost));
-      if (g.overflow) {
-        J.sh_list.alloc(2 * J.sh_list.n);
-        DRGB_CUDA(cudaMemset(J.sh_grid.p, 0, sizeof(LightGrid)));
-        graph_valid = false;
-        push_dev();
-      }
+    if (cells_overflow) {
+      J.sh_list.alloc(2 * J.sh_list.n);
+      DRGB_CUDA(cudaMemsetAsync(J.sh_grid.p, 0, sizeof(LightGrid), stream));
+      graph_valid = false;
+      push_dev();
     }
   }
 
@@ -346,7 +345,9 @@ struct drgb_renderer {
     if (job.det && job.rec_key.p) launch_det_reduce(job, sm_count, stream);
   }
 
-  void push_dev() {
+  // images = false: the device copy writes no images (a call that returns
+  // none), the host copy keeps the buffer.
+  void push_dev(bool images = true) {
     JobDev keep = job.dev;
     sync_dev(job);
     job.dev.item_base = keep.item_base;
@@ -355,14 +356,30 @@ struct drgb_renderer {
     job.dev.rnd = keep.rnd;
     job.dev.rnd_order = keep.rnd_order;
     d_job.alloc(1);
-    DRGB_CUDA(cudaMemcpyAsync(d_job.p, &job.dev, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
+    JobDev d = job.dev;
+    if (!images) d.images = nullptr;
+    DRGB_CUDA(cudaMemcpyAsync(d_job.p, &d, sizeof(JobDev), cudaMemcpyHostToDevice, stream));
   }
 
-  void check_flags() {
-    uint32_t f = 0;
-    DRGB_CUDA(cudaMemcpyAsync(&f, job.err.p, sizeof(f), cudaMemcpyDeviceToHost, stream));
+  // The end of a call: one wait for the stream, then the kernels' error
+  // flags (an error throws), the lists' overflow state, and (loss non-null)
+  // the loss of the call copied to host memory.
+  void check_flags(float* loss = nullptr) {
+    Job& J = job;
+    h_status.reserve(4);
+    uint32_t* h = h_status.p;
+    h[1] = h[2] = 0;
+    DRGB_CUDA(cudaMemcpyAsync(h, J.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    if (J.raster_on && J.ra_state.p)
+      DRGB_CUDA(cudaMemcpyAsync(h + 1, J.ra_state.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    if (J.shadow_on && J.sh_grid.p)
+      DRGB_CUDA(cudaMemcpyAsync(h + 2, reinterpret_cast<const char*>(J.sh_grid.p) + offsetof(LightGrid, overflow),
+                                sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    if (loss) DRGB_CUDA(cudaMemcpyAsync(h + 3, J.loss_out.p, sizeof(float), cudaMemcpyDeviceToHost, stream));
     DRGB_CUDA(cudaStreamSynchronize(stream));
-    raster_grow();
+    if (loss) std::memcpy(loss, h + 3, sizeof(float));
+    const uint32_t f = h[0];
+    raster_grow(h[1], h[2]);
     if (f) {
       DRGB_CUDA(cudaMemsetAsync(job.err.p, 0, sizeof(uint32_t), stream));
       DRGB_CUDA(cudaStreamSynchronize(stream));

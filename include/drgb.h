@@ -207,7 +207,12 @@ int drgb_renderer_set_model_params(drgb_renderer* r, const drgb_model_params* p)
 void* drgb_renderer_stream(drgb_renderer* r);
 
 /* IDiffRender::commit (src/drender.h:91-96): uploads the scene, flattens it
- * and builds the LBVH on the device. */
+ * and builds the ray-tracing hierarchy (a scene with the same triangles keeps
+ * its topology and refits it; the device buffers of same-sized meshes are
+ * reused).  Returns once the scene's arrays have been read: at once for
+ * pageable host memory, with the flattening and refit left running on the
+ * renderer stream ahead of the next call; after that stream has finished
+ * when an array is page-locked. */
 int drgb_commit(drgb_renderer* r, const drgb_scene_desc* scene);
 
 /* IDiffRender::render (src/drender.h:98-141): images are width*height*3
@@ -234,7 +239,10 @@ int drgb_d_render_and_compare(drgb_renderer* r, const drgb_camera* cams, const f
                               float* out_images, float* loss);
 
 /* Same with device pointers (targets, dscene, out_images, loss may be device
- * memory the caller owns); enqueued on the renderer stream, no host sync. */
+ * memory the caller owns): no copies through host memory.  The work is
+ * enqueued on the renderer stream and the call returns when that stream has
+ * finished it; kernel error flags are left for the next host-pointer call
+ * to report. */
 int drgb_d_render_and_compare_device(drgb_renderer* r, const drgb_camera* cams, const float* d_targets, int n_views,
                                      int edge_samples_in_total, const int32_t* dmesh_ids, int n_ids, float* d_dscene,
                                      float* d_out_images, float* d_loss);
