@@ -126,23 +126,37 @@ __device__ __forceinline__ float dist_lower_bound(const f3 P[3], float ox, float
 
 // Orders each list (lengths 2..64; longer ones stay unsorted) by the lower
 // bound in rec[4 * entry + 1].w, nearest first, so the queries meet the
-// triangles that can win first and skip the rest by one comparison.
+// triangles that can win first and skip the rest by one comparison.  One
+// warp per list, two entries per lane: an entry's place is the number of
+// entries before it in the order (key, position in the list), counted
+// against every key broadcast by shuffle; the keys compare as their bits
+// mapped to an unsigned order (a total order, NaN included, so the places
+// are distinct).  The queries' results do not depend on how equal keys are
+// ordered.
+__device__ __forceinline__ uint32_t key_order(float k) {
+  const uint32_t u = __float_as_uint(k);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 __global__ void k_sort_lists(const uint32_t* offs, int n_lists, int* list, const float4* rec, uint32_t cap) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= n_lists || offs[n_lists] > cap) return;  // lists that did not fit were not filled
-  const uint32_t i0 = offs[b], n = offs[b + 1] - i0;
-  if (n < 2 || n > 64) return;
+  const int w = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (w >= n_lists || offs[n_lists] > cap) return;  // lists that did not fit were not filled
+  const uint32_t i0 = offs[w], n = offs[w + 1] - i0;
+  if (n < 2 || n > kSortedList) return;  // warp-uniform
   int* L = list + i0;
-  for (uint32_t i = 1; i < n; i++) {
-    const int e = L[i];
-    const float key = rec[4 * e + 1].w;
-    int j = (int)i - 1;
-    while (j >= 0 && rec[4 * L[j] + 1].w > key) {
-      L[j + 1] = L[j];
-      j--;
-    }
-    L[j + 1] = e;
+  const uint32_t ia = lane, ib = lane + 32;
+  const int ea = ia < n ? L[ia] : 0, eb = ib < n ? L[ib] : 0;
+  const uint32_t ka = ia < n ? key_order(rec[4 * ea + 1].w) : 0u;
+  const uint32_t kb = ib < n ? key_order(rec[4 * eb + 1].w) : 0u;
+  uint32_t ra = 0, rb = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    const uint32_t kj = __shfl_sync(0xffffffffu, j < 32 ? ka : kb, (int)(j & 31));
+    ra += (kj < ka || (kj == ka && j < ia)) ? 1u : 0u;
+    rb += (kj < kb || (kj == kb && j < ib)) ? 1u : 0u;
   }
+  __syncwarp();  // every lane has read its entries before any is moved
+  if (ia < n) L[ra] = ea;
+  if (ib < n) L[rb] = eb;
 }
 
 // Tile range of a footprint (tiles of tw x th pixels, ntx x nty per view).
@@ -526,7 +540,7 @@ void launch_light_grid(const JobDev* d_job, const Job& J, int G, cudaStream_t s)
   launch_rs_scan(J.sh_cells.p, n_cells + 1, s);
   k_light_bin<1><<<grid, 256, 0, s>>>(d_job, g, J.sh_cells.p, J.sh_cursor.p, J.sh_list.p, (uint32_t)J.sh_list.n,
                                       J.sh_rec.p);
-  k_sort_lists<<<(n_cells + 255) / 256, 256, 0, s>>>(J.sh_cells.p, n_cells, J.sh_list.p, J.sh_rec.p,
+  k_sort_lists<<<(int)(((int64_t)n_cells * 32 + 255) / 256), 256, 0, s>>>(J.sh_cells.p, n_cells, J.sh_list.p, J.sh_rec.p,
                                                       (uint32_t)J.sh_list.n);
   k_light_valid<<<1, 1, 0, s>>>(g);
   count_launch(5);
@@ -567,7 +581,7 @@ void launch_raster(const JobDev* d_job, const Job& J, int passes, int ntx, int n
   launch_rs_scan(tiles, n_tiles + 1, s);
   k_bin<1><<<grid, 256, 0, s>>>(d_job, tw, th, ntx, nty, tiles, cursor, J.ra_list.p, (uint32_t)J.ra_list.n, state,
                                 rec);
-  k_sort_lists<<<(n_tiles + 255) / 256, 256, 0, s>>>(tiles, n_tiles, J.ra_list.p, J.ra_rec.p,
+  k_sort_lists<<<(int)(((int64_t)n_tiles * 32 + 255) / 256), 256, 0, s>>>(tiles, n_tiles, J.ra_list.p, J.ra_rec.p,
                                                      (uint32_t)J.ra_list.n);
   k_resolve<<<n_tiles, RA_THREADS, 0, s>>>(d_job, passes, tw, th, ntx, nty, tiles, J.ra_list.p, state, rec);
   k_tiles_valid<<<1, 1, 0, s>>>(state);
