@@ -145,9 +145,6 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
       throw CudaError("mesh " + std::to_string(m) + ": bad vertex/index arrays", DRGB_ERR_INVALID);
     if (d.n_instances > 1 && !d.transforms && !d.restricted)
       throw CudaError("mesh " + std::to_string(m) + ": several instances need transforms", DRGB_ERR_INVALID);
-    for (int i = 0; i < d.n_indices; i++)
-      if (d.indices[i] >= (uint32_t)d.n_vertices)
-        throw CudaError("mesh " + std::to_string(m) + ": index out of range", DRGB_ERR_INVALID);
     const bool tex = d.texture && d.tex_w > 0 && d.tex_h > 0;
     if (tex && d.tex_channels != 3) throw CudaError("textures must have 3 channels", DRGB_ERR_INVALID);
     if (model_has_tex(J.mode) && !tex)
@@ -155,6 +152,27 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     if (model_has_tex(J.mode) && !d.tc)
       throw CudaError("mesh " + std::to_string(m) + ": the shading model needs texture coordinates", DRGB_ERR_INVALID);
   }
+  // The same meshes with the same vertex and instance counts and the same
+  // index arrays as the committed scene (an optimiser moving vertices): the
+  // index check and the triangle tables (blocks, vertex blocks, triangle
+  // list) carry over.
+  bool same_structure = J.committed && (int)J.meshes.size() == nm;
+  for (int m = 0; m < nm && same_structure; m++) {
+    const drgb_mesh_desc& d = scene->meshes[m];
+    const MeshState& M = J.meshes[m];
+    same_structure = M.nv == d.n_vertices && M.ni == d.n_indices &&
+                     M.n_inst == (d.n_instances <= 0 ? 1 : d.n_instances) &&
+                     (int)M.h_indices.size() == d.n_indices &&
+                     (d.n_indices == 0 ||
+                      std::memcmp(M.h_indices.data(), d.indices, sizeof(uint32_t) * (size_t)d.n_indices) == 0);
+  }
+  if (!same_structure)
+    for (int m = 0; m < nm; m++) {
+      const drgb_mesh_desc& d = scene->meshes[m];
+      for (int i = 0; i < d.n_indices; i++)
+        if (d.indices[i] >= (uint32_t)d.n_vertices)
+          throw CudaError("mesh " + std::to_string(m) + ": index out of range", DRGB_ERR_INVALID);
+    }
   rebuild_bvh_discard(J);  // a host build in progress reads the triangle lists replaced here
   // The meshes' device buffers are kept from the last commit and reused where
   // the sizes agree: a commit of the same meshes (the reference commits the
@@ -162,7 +180,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
   // nothing (cudaFree waits for the whole device).  Uploads are ordered on
   // the renderer's stream behind any work that still reads them.
   J.meshes.resize(nm);
-  J.h_blocks.clear();
+  if (!same_structure) J.h_blocks.clear();
   std::vector<int> vblock;
   std::vector<int4> tri_v;
   int voff = 0, toff = 0;
@@ -186,7 +204,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
     else M.normals.reset();
     if (M.has_tangents) M.tangents.upload(d.tangents, 3 * (size_t)d.n_vertices, s);
     else M.tangents.reset();
-    M.h_indices.assign(d.indices, d.indices + d.n_indices);  // the triangles reach the device as tri_v
+    if (!same_structure) M.h_indices.assign(d.indices, d.indices + d.n_indices);  // on the device as tri_v
     std::vector<float> tr(16 * (size_t)ninst, 0.0f);
     M.restricted = d.restricted != nullptr;
     if (M.restricted) {
@@ -209,7 +227,7 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
       M.tex_w = M.tex_h = M.tex_c = 0;
       M.texture.reset();
     }
-    for (int j = 0; j < ninst; j++) {
+    for (int j = 0; j < ninst && !same_structure; j++) {
       const int b = (int)J.h_blocks.size();
       J.h_blocks.push_back(BlockDev{voff, toff, m, j});
       for (int k = 0; k < d.n_vertices; k++) vblock.push_back(b);
@@ -220,17 +238,19 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
       toff += d.n_indices / 3;
     }
   }
-  J.n_vertices = voff;
-  J.n_tris = toff;
-  J.n_blocks = (int)J.h_blocks.size();
-  upload_changed(J.blocks, J.up_blocks, J.h_blocks.data(), J.h_blocks.size(), s);
-  upload_changed(J.vblock, J.up_vblock, vblock.data(), vblock.size(), s);
-  // the same triangles (global vertex ids and blocks) keep the edge list
-  const bool same_topology = tri_v.size() == J.h_tri_v.size() &&
-                             (tri_v.empty() || std::memcmp(tri_v.data(), J.h_tri_v.data(),
-                                                           sizeof(int4) * tri_v.size()) == 0);
-  if (!same_topology || !J.tri_v.p || J.tri_v.n != tri_v.size()) J.tri_v.upload(tri_v.data(), tri_v.size(), s);
-  J.h_tri_v.swap(tri_v);  // kept for the hierarchy builders and their topology cache
+  bool same_topology = true;
+  if (!same_structure) {
+    J.n_vertices = voff;
+    J.n_tris = toff;
+    J.n_blocks = (int)J.h_blocks.size();
+    upload_changed(J.blocks, J.up_blocks, J.h_blocks.data(), J.h_blocks.size(), s);
+    upload_changed(J.vblock, J.up_vblock, vblock.data(), vblock.size(), s);
+    // the same triangles (global vertex ids and blocks) keep the edge list
+    same_topology = tri_v.size() == J.h_tri_v.size() &&
+                    (tri_v.empty() || std::memcmp(tri_v.data(), J.h_tri_v.data(), sizeof(int4) * tri_v.size()) == 0);
+    if (!same_topology || !J.tri_v.p || J.tri_v.n != tri_v.size()) J.tri_v.upload(tri_v.data(), tri_v.size(), s);
+    J.h_tri_v.swap(tri_v);  // kept for the hierarchy builders and their topology cache
+  }
   std::vector<MeshSrc> src(nm);
   std::vector<const float*> trs(nm);
   for (int m = 0; m < nm; m++) {
