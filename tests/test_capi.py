@@ -57,3 +57,33 @@ def test_opt_params_default(lib):
     assert abs(p.position_lr - 0.1) < 1e-7 and p.flags == 15
     assert lib.drgb_opt_params_default(1, C.byref(p)) == 0
     assert p.decay_period == 25
+
+
+def test_camera_cache_is_keyed_by_value(lib):
+    """make_camera keeps the library's matrices per camera: a camera built
+    from equal parameters (tuples, lists or arrays) gets the same matrices
+    as a fresh computation, and a changed camera gets its own."""
+    from diffrender_tutorials_gb300 import api
+    from diffrender_tutorials_gb300.scene import CamInfo
+
+    def fresh(cam):
+        c = api._make_camera(cam)
+        return np.array(c.world_view[:] + c.proj[:] + [c.width, c.height], np.float32)
+
+    def cached(cam):
+        c = make_camera(cam)
+        return np.array(c.world_view[:] + c.proj[:] + [c.width, c.height], np.float32)
+
+    a = CamInfo(origin=(0.5, 1.0, 3.0), width=64, height=48)
+    assert np.array_equal(cached(a), fresh(a))
+    assert np.array_equal(cached(a), fresh(a))  # second call: from the cache
+    for same in (CamInfo(origin=[0.5, 1.0, 3.0], width=64, height=48),
+                 CamInfo(origin=np.array([0.5, 1.0, 3.0], np.float32), width=64, height=48)):
+        assert np.array_equal(cached(same), fresh(a))
+    a.origin = (0.5, 1.25, 3.0)  # a changed camera is not served the old matrices
+    assert np.array_equal(cached(a), fresh(a))
+    b = CamInfo(origin=(0.5, 1.0, 3.0), width=64, height=48, fov_rad=0.5)
+    assert not np.array_equal(cached(b), cached(CamInfo(origin=(0.5, 1.0, 3.0), width=64, height=48)))
+    arr = api.make_cameras([a, b, a])
+    assert np.array_equal(np.array(arr[0].world_view[:]), np.array(arr[2].world_view[:]))
+    assert np.array_equal(np.array(arr[1].proj[:], np.float32), fresh(b)[16:32])
