@@ -174,6 +174,9 @@ void upload_scene(Job& J, const drgb_scene_desc* scene, cudaStream_t s) {
           throw CudaError("mesh " + std::to_string(m) + ": index out of range", DRGB_ERR_INVALID);
     }
   rebuild_bvh_discard(J);  // a host build in progress reads the triangle lists replaced here
+  // from here on the committed scene changes: a failure part-way (a device
+  // error) leaves no scene committed, and the next commit rebuilds everything
+  J.committed = false;
   // The meshes' device buffers are kept from the last commit and reused where
   // the sizes agree: a commit of the same meshes (the reference commits the
   // scene on every d_render_and_compare, drender.h:176) frees and allocates
